@@ -1,0 +1,60 @@
+// isp_kernels.h - host-visible launchers of the CUDA kernels (no device code).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "isp_common.h"
+
+namespace imop {
+
+// nominal fused tile (the last tile of a row / column absorbs a remainder below 4)
+constexpr int kTileW = 64;
+constexpr int kTileH = 32;
+
+// device scratch of the defect-chain fix-up
+struct FixupScratch {
+    int* heap;
+    int* ov_idx;
+    int* ov_val;
+    int* n_ov;
+    int cap;
+};
+
+// map-mode defect plan (built on the host from the defect list, uploaded once)
+struct MapPlan {
+    int n_comp;
+    const int* comp_slot_ptr;  // n_comp + 1
+    const int* comp_slots;     // unique slots of each component
+    const int* comp_ent_ptr;   // n_comp + 1
+    const int* comp_entries;   // slot of each map entry, in map order
+    const int2* slot_xy;       // pixel of each slot
+};
+
+int fused_tile_grid(int w, int h, int& ntx, int& nty);
+cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots, int bd, uint8_t* d_out,
+                              cudaStream_t st);
+// map-mode defect values of one frame (before the kernels that read them)
+cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st);
+// map resolve (map mode) + seed reset + fused tiles + fix-up, in stream order
+cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st);
+
+// plain per-operator form: one kernel per stage over full frames in device memory.
+// Buffers: bayer_a/bayer_b are w*h u16, rgb is w*h*3 u16.
+struct PlainBuffers {
+    uint16_t* bayer_a;
+    uint16_t* bayer_b;
+    uint16_t* rgb;
+};
+struct PlainDumps {  // device pointers, may be null
+    uint16_t* unpacked;
+    uint16_t* black_level;
+    uint16_t* defect;
+    uint16_t* lens_shading;
+    uint16_t* white_balance;
+    uint16_t* demosaic;
+    uint16_t* ccm;
+};
+cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, const PlainBuffers& b,
+                         const PlainDumps* dumps, cudaStream_t st);
+
+}  // namespace imop

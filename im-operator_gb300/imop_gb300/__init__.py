@@ -1,0 +1,185 @@
+"""imop_gb300 - Python host mirror of the GB300 RAW->RGB ISP library (libimop_isp.so).
+
+Thin ctypes layer over the C ABI declared in include/imop_isp.h.  Device buffers are passed as
+raw addresses (for example torch.Tensor.data_ptr()), streams as raw cudaStream_t handles.  The
+library is required: importing `lib()` raises when libimop_isp.so has not been built, so no
+caller can silently fall back to a CPU path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import *  # noqa: F401,F403
+from .params import Pipeline  # noqa: F401
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libimop_isp.so")
+_lib = None
+
+
+class IspError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"imop status {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        i, vp, sz = C.c_int, C.c_void_p, C.c_size_t
+        PP = C.POINTER(abi.IspParams)
+        sig = {
+            "imop_isp_params_default": (None, [PP, i, i, i, i]),
+            "imop_isp_input_bytes": (sz, [PP]),
+            "imop_isp_output_bytes": (sz, [PP]),
+            "imop_isp_create": (i, [C.POINTER(vp)]),
+            "imop_isp_destroy": (i, [vp]),
+            "imop_isp_set_params": (i, [vp, PP]),
+            "imop_isp_run_host": (i, [vp, vp, sz, vp, sz]),
+            "imop_isp_run_device": (i, [vp, vp, vp, vp]),
+            "imop_isp_run_device_plain": (i, [vp, vp, vp, vp]),
+            "imop_isp_dump_stages": (i, [vp, vp, sz, C.POINTER(abi.StageDumps)]),
+            "imop_isp_set_tile": (i, [vp, i, i]),
+            "imop_isp_last_stats": (i, [vp, C.POINTER(i), C.POINTER(i)]),
+            "imop_scene_render": (i, [i, i, i, i, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float, vp]),
+            "imop_scene_defects": (i, [i, i, C.c_uint64, i, C.POINTER(abi.DefectPoint)]),
+            "imop_scene_apply_defects": (i, [vp, i, i, i, C.POINTER(abi.DefectPoint), i]),
+            "imop_packed_bytes": (sz, [i, i, i]),
+            "imop_pack_mipi": (i, [vp, i, i, i, vp]),
+            "imop_last_error_string": (C.c_char_p, []),
+            "imop_abi_version": (i, []),
+            "imop_has_cuda": (i, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != 0:
+        raise IspError(code, lib().imop_last_error_string().decode(errors="replace"))
+    return code
+
+
+def _addr(x):
+    """device / host address of a tensor, ndarray or integer"""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(type(x))
+
+
+class Isp:
+    """One pipeline context (imop_isp_t)."""
+
+    def __init__(self, pipeline=None):
+        h = C.c_void_p()
+        check(lib().imop_isp_create(C.byref(h)))
+        self.h = h
+        self.pipeline = None
+        self._cparams = None
+        if pipeline is not None:
+            self.set_params(pipeline)
+
+    def close(self):
+        if self.h:
+            lib().imop_isp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, pl):
+        cp = pl.to_c()
+        check(lib().imop_isp_set_params(self.h, C.byref(cp)))
+        self.pipeline = pl
+        self._cparams = cp
+
+    def run_host(self, raw):
+        pl = self.pipeline
+        raw = np.ascontiguousarray(raw).view(np.uint8).reshape(-1)
+        out = np.empty(pl.output_shape(), dtype=pl.output_dtype())
+        check(lib().imop_isp_run_host(self.h, raw.ctypes.data, raw.nbytes, out.ctypes.data, out.nbytes))
+        return out
+
+    def run_device(self, d_in, d_out, stream=0):
+        check(lib().imop_isp_run_device(self.h, _addr(d_in), _addr(d_out), stream))
+
+    def run_device_plain(self, d_in, d_out, stream=0):
+        check(lib().imop_isp_run_device_plain(self.h, _addr(d_in), _addr(d_out), stream))
+
+    def dump_stages(self, raw):
+        pl = self.pipeline
+        raw = np.ascontiguousarray(raw).view(np.uint8).reshape(-1)
+        h, w = pl.height, pl.width
+        rgb_wb = pl.stage_order == abi.ORDER_RGB_WB
+        d = {
+            "unpacked": np.zeros((h, w), np.uint16),
+            "black_level": np.zeros((h, w), np.uint16),
+            "defect": np.zeros((h, w), np.uint16),
+            "lens_shading": np.zeros((h, w), np.uint16),
+            "white_balance": np.zeros((h, w, 3) if rgb_wb else (h, w), np.uint16),
+            "demosaic": np.zeros((h, w, 3), np.uint16),
+            "ccm": np.zeros((h, w, 3), np.uint16),
+            "output": np.zeros(pl.output_shape(), pl.output_dtype()),
+        }
+        sd = abi.StageDumps(*[d[k].ctypes.data for k in ("unpacked", "black_level", "defect", "lens_shading",
+                                                         "white_balance", "demosaic", "ccm", "output")])
+        check(lib().imop_isp_dump_stages(self.h, raw.ctypes.data, raw.nbytes, C.byref(sd)))
+        return d
+
+    def last_stats(self):
+        s, o = C.c_int(), C.c_int()
+        check(lib().imop_isp_last_stats(self.h, C.byref(s), C.byref(o)))
+        return s.value, o.value
+
+
+# ---- synthetic scenes ---------------------------------------------------------------------------
+def scene(width, height, bit_depth, pattern=abi.RGGB, seed=20261203, lo=None, hi=None, gain=0.5,
+          read_sigma=2.0):
+    """Seeded Bayer frame (uint8 for bd <= 8, uint16 otherwise) as an (h, w) array."""
+    mv = (1 << bit_depth) - 1
+    lo = float(lo if lo is not None else 0.0625 * (mv + 1))
+    hi = float(hi if hi is not None else mv)
+    out = np.empty((height, width), np.uint8 if bit_depth <= 8 else np.uint16)
+    check(lib().imop_scene_render(width, height, bit_depth, pattern, seed, lo, hi, gain, read_sigma,
+                                  out.ctypes.data))
+    return out
+
+
+def defects(width, height, count, seed=20261203):
+    pts = (abi.DefectPoint * max(1, count))()
+    check(lib().imop_scene_defects(width, height, seed, count, pts))
+    return np.array([(pts[i].x, pts[i].y) for i in range(count)], np.int32).reshape(-1, 2)
+
+
+def apply_defects(frame, pts, bit_depth):
+    pts = np.ascontiguousarray(pts, np.int32).reshape(-1, 2)
+    h, w = frame.shape
+    check(lib().imop_scene_apply_defects(frame.ctypes.data, w, h, bit_depth,
+                                         pts.ctypes.data_as(C.POINTER(abi.DefectPoint)), pts.shape[0]))
+    return frame
+
+
+def pack_mipi(frame, bit_depth):
+    h, w = frame.shape
+    f = np.ascontiguousarray(frame, np.uint16)
+    out = np.empty(lib().imop_packed_bytes(w, h, bit_depth), np.uint8)
+    check(lib().imop_pack_mipi(f.ctypes.data, w, h, bit_depth, out.ctypes.data))
+    return out

@@ -1,0 +1,214 @@
+/*
+ * imop_isp.h - C ABI of the GB300-native RAW->RGB ISP hot path.
+ *
+ * One fused sm_103a kernel runs
+ *   unpack -> black_level -> defect_correct -> lens_shading -> white_balance
+ *   -> Bayer demosaic (HQLI / AMAZE / MG) -> ccm -> tone LUT -> RGB8
+ * over one frame or over a batch of frames of uneven sizes and formats.
+ *
+ * Every entry point takes plain pointers and sizes; no C++ or torch types cross
+ * this boundary.  Status codes 0..6 are numerically equal to the reference's
+ * imop::DemosaicError (include/imop/types.hpp:31-39 of im-operator) and to the
+ * per-module error enums (e.g. include/black_level/types.hpp:13-21), so a
+ * caller that maps "non-zero" to "fall back" keeps the reference's contract.
+ *
+ * Reference interfaces replaced (paths are relative to the im-operator tree):
+ *   imop_isp_run_host      : the host-side composition of
+ *                            black_level::process_black_level   (src/black_level/dispatch.cpp:44-63)
+ *                            defect_correct::process_defect_correct (src/defect_correct/dispatch.cpp:44-63)
+ *                            lens_shading::process_lens_shading  (src/lens_shading/dispatch.cpp:41-60)
+ *                            imop::demosaic                      (src/algorithms/dispatch.cpp:89-113)
+ *                            white_balance::process_white_balance (src/white_balance/dispatch.cpp:196-219)
+ *                            ccm::process_ccm                    (src/ccm/dispatch.cpp:167-191)
+ *                            tone::process_tone                  (src/tone/dispatch.cpp:66-86)
+ *                            with their GPU glue in src/gpu_dispatch.cpp:292-571
+ *   imop_isp_batch_*       : imop::demosaic_cuda_batch           (src/algorithms/cuda_dispatch.cpp:150-209)
+ *   imop_op_*              : the per-operator *_cuda entry points of src/gpu_dispatch.cpp
+ *                            and imop::demosaic_cuda (src/algorithms/cuda_dispatch.cpp:68-141)
+ */
+#ifndef IMOP_ISP_H
+#define IMOP_ISP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMOP_ISP_ABI_VERSION 1
+
+/* ---- status codes (0..6 == imop::DemosaicError) ---------------------------------- */
+enum {
+    IMOP_OK = 0,
+    IMOP_ERR_NULL_INPUT = 1,
+    IMOP_ERR_INVALID_DIMENSIONS = 2,
+    IMOP_ERR_INVALID_BIT_DEPTH = 3,
+    IMOP_ERR_INVALID_PATTERN = 4,
+    IMOP_ERR_IMAGE_TOO_SMALL = 5,
+    IMOP_ERR_INTERNAL = 6,
+    /* codes beyond the reference enum; a DemosaicError-typed caller sees them as InternalError */
+    IMOP_ERR_INVALID_ARGUMENT = 100, /* a parameter outside its documented range          */
+    IMOP_ERR_UNSUPPORTED = 101,      /* format / algorithm combination not on this path     */
+    IMOP_ERR_CUDA = 102,             /* a CUDA runtime call failed                          */
+    IMOP_ERR_TIMEOUT = 103,          /* a bounded device-side wait expired                  */
+    IMOP_ERR_CAPACITY = 104,         /* a device-side list (defect chain, queue) overflowed */
+    IMOP_ERR_NO_DEVICE = 105         /* no CUDA device visible                              */
+};
+
+/* imop::BayerPattern (include/imop/types.hpp:12-17) */
+enum { IMOP_RGGB = 0, IMOP_BGGR = 1, IMOP_GRBG = 2, IMOP_GBRG = 3 };
+
+/* imop::DemosaicAlgorithm values (include/imop/types.hpp:19-29) served by this path */
+enum { IMOP_DEMOSAIC_HQLI = 1, IMOP_DEMOSAIC_MG = 2, IMOP_DEMOSAIC_AMAZE = 6 };
+
+/* stage bits */
+enum {
+    IMOP_STAGE_BLACK_LEVEL = 1u << 0,
+    IMOP_STAGE_DEFECT = 1u << 1,
+    IMOP_STAGE_LENS_SHADING = 1u << 2,
+    IMOP_STAGE_WHITE_BALANCE = 1u << 3,
+    IMOP_STAGE_CCM = 1u << 4,
+    IMOP_STAGE_ALL = 0x1Fu
+};
+
+/* where white balance runs */
+enum {
+    IMOP_ORDER_BAYER_WB = 0, /* WB on the Bayer mosaic before demosaic (fused spec order)  */
+    IMOP_ORDER_RGB_WB = 1    /* WB on RGB after demosaic (the order the reference's calls compose) */
+};
+
+/* black_level::BlackLevelAlgorithm (include/black_level/types.hpp:8-11) */
+enum { IMOP_BL_PER_CHANNEL = 0, IMOP_BL_GLOBAL = 1 };
+/* defect_correct::DefectCorrectAlgorithm (include/defect_correct/types.hpp:8-11) */
+enum { IMOP_DPC_ADAPTIVE = 0, IMOP_DPC_MAP_BASED = 1 };
+/* lens shading modes */
+enum {
+    IMOP_LSC_GRID = 0,       /* explicit gw x gh x 4 FP32 gain grid, bilinear (flat_field.cpp:78-107)  */
+    IMOP_LSC_POLYNOMIAL = 1, /* lens_shading::process_polynomial (polynomial.cpp:13-52)                 */
+    IMOP_LSC_FLAT_FIELD = 2  /* 32x24 grid derived from a flat-field frame (flat_field.cpp:30-76)       */
+};
+/* tone modes: every mode ends in an 8-bit value (int)(f(v)*255+0.5) clamped to [0,255] */
+enum {
+    IMOP_TONE_LINEAR = 0, /* f(v) = v / max                                         */
+    IMOP_TONE_LUT = 1,    /* f(v) = lut[v], 2^bit_depth FP32 entries in [0,1]        */
+    IMOP_TONE_KNOTS = 2   /* 33-knot piecewise-linear curve (curves_3point.cpp:114-135 rule) */
+};
+/* output format */
+enum {
+    IMOP_OUT_RGB8 = 0,  /* interleaved RGB, 3 bytes per pixel, after the tone stage            */
+    IMOP_OUT_NATIVE = 1 /* interleaved RGB at the input bit depth (u8, or u16 when bd > 8); no tone */
+};
+
+/* defect_correct::DefectPoint (include/defect_correct/types.hpp:41-43): same layout */
+typedef struct ImopDefectPoint {
+    int x, y;
+} ImopDefectPoint;
+
+typedef struct ImopIspParams {
+    int width, height;
+    int bit_depth;   /* 8, 10 or 12 (packed: 10 or 12; unpacked u16 accepts 9..16) */
+    int packed;      /* 0: u8 (bd<=8) or u16 LSB-aligned; 1: MIPI RAW10 (4 px / 5 B) or RAW12 (2 px / 3 B) */
+    int pattern;     /* IMOP_RGGB ... */
+    int demosaic;    /* IMOP_DEMOSAIC_* */
+    unsigned stages; /* IMOP_STAGE_* bits */
+    int stage_order; /* IMOP_ORDER_* */
+
+    int bl_mode;          /* IMOP_BL_* */
+    float bl_offset[4];   /* R, Gr, Gb, B (GLOBAL uses [0]) */
+
+    int dpc_mode;         /* IMOP_DPC_* */
+    float dpc_threshold;  /* adaptive: relative threshold, clamped to [0.05, 1] */
+    const ImopDefectPoint* dpc_map; /* map-based: copied by imop_isp_set_params */
+    int dpc_map_count;
+
+    int lsc_mode;         /* IMOP_LSC_* */
+    const float* lsc_grid;        /* [grid_h][grid_w][4] (R, Gr, Gb, B); copied */
+    int lsc_grid_w, lsc_grid_h;   /* >= 2 each */
+    float lsc_poly[4][3];         /* per channel a2, a4, a6 */
+    float lsc_center[2];          /* optical centre, normalised */
+    const void* lsc_flat_field;   /* flat-field frame, same storage as an unpacked input; copied */
+    int lsc_flat_w, lsc_flat_h;
+
+    float wb_gain[3];     /* R, G, B */
+    float ccm[9];         /* row-major 3x3, out = M * in */
+
+    int tone_mode;        /* IMOP_TONE_* */
+    const float* tone_lut; int tone_lut_len; /* copied; tone_lut_len == 2^bit_depth */
+    float tone_knots[33];
+
+    int out_format;       /* IMOP_OUT_* */
+} ImopIspParams;
+
+/* Fill *p with the identity pipeline for a w x h frame: all stages off, HQLI, linear tone, RGB8. */
+void imop_isp_params_default(ImopIspParams* p, int width, int height, int bit_depth, int packed);
+
+/* Byte sizes of one input frame and one output frame for the given parameters. */
+size_t imop_isp_input_bytes(const ImopIspParams* p);
+size_t imop_isp_output_bytes(const ImopIspParams* p);
+
+/* ---- context ----------------------------------------------------------------------- */
+typedef struct imop_isp_ctx* imop_isp_t;
+
+int imop_isp_create(imop_isp_t* out_ctx);
+int imop_isp_destroy(imop_isp_t ctx);
+/* Validates and uploads parameters (grid, LUT, defect map are copied to the device).
+ * Same validation order and codes as the reference dispatchers. */
+int imop_isp_set_params(imop_isp_t ctx, const ImopIspParams* p);
+
+/* Drop-in semantics: host buffers, H2D + fused kernel + D2H, synchronous (the reference's
+ * gpu_dispatch.cpp call shape).  in_bytes / out_bytes must be at least the frame sizes. */
+int imop_isp_run_host(imop_isp_t ctx, const void* in, size_t in_bytes, void* out, size_t out_bytes);
+
+/* Device pointers, asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream). */
+int imop_isp_run_device(imop_isp_t ctx, const void* d_in, void* d_out, void* stream);
+
+/* Plain per-operator form: the same pipeline as one kernel per stage over full frames kept
+ * in device memory (the comparator for the fused kernel).  Asynchronous on `stream`. */
+int imop_isp_run_device_plain(imop_isp_t ctx, const void* d_in, void* d_out, void* stream);
+
+/* Per-stage dumps through the plain per-operator kernels.  Each non-NULL host pointer receives
+ * one full frame: Bayer stages as u16 per pixel (w*h*2 bytes), RGB stages as u16 x 3 per pixel
+ * (w*h*6 bytes), the final output in the context's output format. Synchronous. */
+typedef struct ImopStageDumps {
+    uint16_t* unpacked;     /* raw values after unpack                  */
+    uint16_t* black_level;  /* after black level                        */
+    uint16_t* defect;       /* after defect correction                  */
+    uint16_t* lens_shading; /* after lens shading                       */
+    uint16_t* white_balance;/* after Bayer WB (ORDER_BAYER_WB) or RGB WB (ORDER_RGB_WB, 3 ch) */
+    uint16_t* demosaic;     /* RGB at bit depth after demosaic          */
+    uint16_t* ccm;          /* RGB at bit depth after CCM               */
+    uint8_t* output;        /* final output                             */
+} ImopStageDumps;
+int imop_isp_dump_stages(imop_isp_t ctx, const void* in, size_t in_bytes, ImopStageDumps* dumps);
+
+/* Tile shape of the fused kernel (0 = autotuned / default). */
+int imop_isp_set_tile(imop_isp_t ctx, int tile_w, int tile_h);
+
+/* Device-side defect-chain statistics of the last run (seeds re-resolved in raster order). */
+int imop_isp_last_stats(imop_isp_t ctx, int* dpc_seeds, int* dpc_overrides);
+
+/* ---- synthetic scene (seeded, bit-identical on every host) --------------------------- */
+/* Per CFA channel: 4 random 2-D sinusoids mapped to [lo, hi], shot noise (gain DN/e-) and
+ * Gaussian read noise, rounded and clamped; written as u8 (bd <= 8) or u16 LSB-aligned. */
+int imop_scene_render(int width, int height, int bit_depth, int pattern, uint64_t seed, float lo,
+                      float hi, float gain_dn_per_e, float read_sigma_dn, void* out);
+/* Seeded distinct defect positions inside [2,w-2)x[2,h-2): first half hot, second half dead. */
+int imop_scene_defects(int width, int height, uint64_t seed, int count, ImopDefectPoint* out);
+/* Write hot (max) / dead (0) values at the listed positions of an unpacked frame. */
+int imop_scene_apply_defects(void* frame, int width, int height, int bit_depth,
+                             const ImopDefectPoint* pts, int count);
+/* MIPI pack an unpacked u16 frame (10 or 12 bit); out must hold imop_packed_bytes(). */
+size_t imop_packed_bytes(int width, int height, int bit_depth);
+int imop_pack_mipi(const uint16_t* in, int width, int height, int bit_depth, uint8_t* out);
+
+/* ---- misc --------------------------------------------------------------------------- */
+const char* imop_last_error_string(void);
+int imop_abi_version(void);
+/* 1 when a CUDA device is visible (cached, like has_cuda_shared in src/gpu_dispatch.cpp:37-43). */
+int imop_has_cuda(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMOP_ISP_H */

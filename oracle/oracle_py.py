@@ -1,0 +1,129 @@
+"""ctypes binding of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker
+and the timed CPU baseline; never by the product package.
+
+  liboracle_isp.so        the C restatement (oracle/isp_oracle.c), built by `make -C oracle`
+  _ref/libimop_ref.so     the reference's own CPU functions compiled from its sources
+                          (`make -C oracle ref`); present only where the reference tree is
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "im-operator_gb300"))
+
+from imop_gb300 import abi  # noqa: E402  (struct layouts only)
+
+_lib = None
+_ref = None
+
+U16P = C.POINTER(C.c_uint16)
+U8P = C.POINTER(C.c_uint8)
+F32P = C.POINTER(C.c_float)
+
+
+def _p(a, t=C.c_void_p):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class OracleDumps(C.Structure):
+    _fields_ = [(n, U16P) for n in ("unpacked", "black_level", "defect", "lens_shading",
+                                    "white_balance", "demosaic", "ccm")]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle_isp.so")
+        if not os.path.exists(path):
+            raise RuntimeError("oracle not built: run `make -C oracle`")
+        _lib = C.CDLL(path)
+        _lib.or_pipeline.argtypes = [C.POINTER(abi.IspParams), C.c_void_p, C.c_void_p, C.POINTER(OracleDumps)]
+        _lib.or_pipeline.restype = C.c_int
+        _lib.or_get_packed_raw.argtypes = [U8P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        _lib.or_get_packed_raw.restype = C.c_int
+        _lib.or_tone_value.argtypes = [C.c_int, F32P, F32P, C.c_int, C.c_int]
+        _lib.or_tone_value.restype = C.c_float
+        _lib.or_tone_to_u8.argtypes = [C.c_float]
+        _lib.or_tone_to_u8.restype = C.c_uint8
+        _lib.or_lsc_flat_field_grid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, F32P]
+        _lib.or_lsc_flat_field_grid.restype = C.c_int
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(os.path.join(HERE, "_ref", "libimop_ref.so"))
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        path = os.path.join(HERE, "_ref", "libimop_ref.so")
+        if not os.path.exists(path):
+            raise RuntimeError("reference library not built: run `make -C oracle ref`")
+        _ref = C.CDLL(path)
+        i = C.c_int
+        _ref.ref_get_packed_raw.argtypes = [U8P, i, i, i, i, i]
+        _ref.ref_get_raw.argtypes = [U8P, i, i, i, i, i, i]
+        _ref.ref_black_level.argtypes = [U16P, i, i, i, i, i, F32P]
+        _ref.ref_dpc.argtypes = [U16P, i, i, i, i, i, C.c_float, C.POINTER(C.c_int), i]
+        _ref.ref_lsc_poly.argtypes = [U16P, i, i, i, i, F32P, C.c_float, C.c_float]
+        _ref.ref_lsc_flat_field.argtypes = [U16P, i, i, i, i, U8P, i, i]
+        _ref.ref_demosaic.argtypes = [U16P, U16P, i, i, i, i, i]
+        _ref.ref_demosaic_raw.argtypes = [U8P, U16P, i, i, i, i, i, i]
+        _ref.ref_wb_rgb.argtypes = [U16P, i, i, i, F32P]
+        _ref.ref_ccm.argtypes = [U16P, i, i, i, F32P]
+    return _ref
+
+
+# ---- oracle ---------------------------------------------------------------------------------
+STAGES = ("unpacked", "black_level", "defect", "lens_shading", "white_balance", "demosaic", "ccm")
+
+
+def pipeline(pl, raw, dumps=False):
+    """Run the oracle chain for a `Pipeline` on one input frame (bytes as np.uint8).
+    Returns (output ndarray, dict of stage dumps or None)."""
+    p = pl.to_c()
+    raw = np.ascontiguousarray(raw, dtype=np.uint8)
+    if raw.size < pl.input_bytes():
+        raise ValueError("input smaller than one frame")
+    out = np.zeros(pl.output_shape(), dtype=pl.output_dtype())
+    d = None
+    dd = None
+    if dumps:
+        n = pl.pixels
+        wb_rgb = pl.stage_order == abi.ORDER_RGB_WB
+        d = {
+            "unpacked": np.zeros((pl.height, pl.width), np.uint16),
+            "black_level": np.zeros((pl.height, pl.width), np.uint16),
+            "defect": np.zeros((pl.height, pl.width), np.uint16),
+            "lens_shading": np.zeros((pl.height, pl.width), np.uint16),
+            "white_balance": np.zeros((pl.height, pl.width, 3) if wb_rgb else (pl.height, pl.width), np.uint16),
+            "demosaic": np.zeros((pl.height, pl.width, 3), np.uint16),
+            "ccm": np.zeros((pl.height, pl.width, 3), np.uint16),
+        }
+        del n
+        dd = OracleDumps(*[d[k].ctypes.data_as(U16P) for k in STAGES])
+    st = lib().or_pipeline(C.byref(p), raw.ctypes.data, out.ctypes.data, C.byref(dd) if dd else None)
+    if st != 0:
+        raise RuntimeError(f"oracle pipeline failed with status {st}")
+    return out, d
+
+
+def get_packed_raw(buf, x, y, w, h, bd):
+    buf = np.ascontiguousarray(buf, dtype=np.uint8)
+    return lib().or_get_packed_raw(_p(buf, U8P), x, y, w, h, bd)
+
+
+def flat_field_grid(ff, pattern, bd):
+    ff = np.ascontiguousarray(ff)
+    g = np.zeros((24, 32, 4), np.float32)
+    st = lib().or_lsc_flat_field_grid(ff.ctypes.data, ff.shape[1], ff.shape[0], pattern, bd, _p(g, F32P))
+    if st:
+        raise RuntimeError(f"flat field grid failed: {st}")
+    return g
