@@ -196,6 +196,8 @@ int validate_params(const ImopIspParams* p) {
     if (p->bit_depth < 1 || p->bit_depth > 16) return fail(IMOP_ERR_INVALID_BIT_DEPTH, "bit depth must be 1-16");
     if (p->pattern < 0 || p->pattern > 3) return fail(IMOP_ERR_INVALID_PATTERN, "invalid Bayer pattern");
     if (p->width < 6 || p->height < 6) return fail(IMOP_ERR_IMAGE_TOO_SMALL, "image too small for the pipeline (min 6x6)");
+    if ((long long)p->width * p->height * 6 >= (1LL << 31))
+        return fail(IMOP_ERR_UNSUPPORTED, "frame larger than 2^31 output bytes");
     if (p->packed && p->bit_depth != 10 && p->bit_depth != 12)
         return fail(IMOP_ERR_UNSUPPORTED, "packed input must be MIPI RAW10 or RAW12");
     if (p->demosaic != IMOP_DEMOSAIC_HQLI && p->demosaic != IMOP_DEMOSAIC_AMAZE && p->demosaic != IMOP_DEMOSAIC_MG)
@@ -272,10 +274,25 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
         float v = (p->bl_mode == IMOP_BL_GLOBAL) ? p->bl_offset[0] : p->bl_offset[c];
         fp.bl[c] = std::max(0.0f, v);
     }
+    // integral offsets: (int)((float)v - off) == v - off exactly, a saturating u16 subtract
+    fp.bl_int = 1;
+    for (int c = 0; c < 4; c++)
+        if (!(fp.bl[c] == std::floor(fp.bl[c]) && fp.bl[c] <= 65535.0f)) fp.bl_int = 0;
+    {
+        PatternOffsets po = pattern_offsets(p->pattern);
+        for (int par = 0; par < 2; par++) {
+            uint32_t lo = (uint32_t)fp.bl[bayer_color(par, 0, po)], hi = (uint32_t)fp.bl[bayer_color(par, 1, po)];
+            fp.bl2[par] = fp.bl_int ? (lo | (hi << 16)) : 0u;
+            fp.bl_i[par][0] = fp.bl_int ? (int)lo : 0;
+            fp.bl_i[par][1] = fp.bl_int ? (int)hi : 0;
+        }
+    }
+    fp.mv2 = (uint32_t)fp.mv | ((uint32_t)fp.mv << 16);
     fp.dpc_mode = p->dpc_mode;
     {
         float t = std::max(0.05f, std::min(1.0f, p->dpc_threshold));
         fp.dpc_thr = (int)(t * (float)fp.mv);
+        fp.thr2 = (uint32_t)fp.dpc_thr | ((uint32_t)fp.dpc_thr << 16);
     }
     cudaError_t e;
     if ((p->stages & IMOP_STAGE_DEFECT) && p->dpc_mode == IMOP_DPC_MAP_BASED) {
@@ -330,8 +347,17 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
     fp.wb_cfa[3] = p->wb_gain[2];
     for (int i = 0; i < 3; i++) fp.wb_rgb[i] = p->wb_gain[i];
     for (int i = 0; i < 9; i++) fp.ccm[i] = p->ccm[i];
-    // tone table
-    if ((e = tabs.tone8.ensure((size_t)fp.mv + 1))) return cuda_fail(e, "alloc tone table");
+    // AMAZE reciprocal table 1/(1+k), k = 0 .. 3*mv (the largest gradient sum)
+    if (p->demosaic == IMOP_DEMOSAIC_AMAZE) {
+        if ((e = tabs.rtab.ensure((size_t)(3 * fp.mv + 1) * sizeof(float)))) return cuda_fail(e, "alloc rtab");
+        if ((e = launch_recip_table((float*)tabs.rtab.ptr, 3 * fp.mv + 1, st))) return cuda_fail(e, "rtab kernel");
+        fp.rtab = (const float*)tabs.rtab.ptr;
+    }
+    fp.need_align = (fp.bd > 8 && fp.bd < 16 &&
+                     !(p->stages & (IMOP_STAGE_BLACK_LEVEL | IMOP_STAGE_LENS_SHADING)) &&
+                     !((p->stages & IMOP_STAGE_WHITE_BALANCE) && p->stage_order == IMOP_ORDER_BAYER_WB)) ? 1 : 0;
+    // tone table (padded: the kernel reads it in 4-byte words)
+    if ((e = tabs.tone8.ensure(std::max<size_t>((size_t)fp.mv + 1, 4096) + 16))) return cuda_fail(e, "alloc tone table");
     fp.tone8 = (const uint8_t*)tabs.tone8.ptr;
     if (p->out_format == IMOP_OUT_RGB8) {
         const float* d_lut = nullptr;

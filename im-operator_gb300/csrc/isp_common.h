@@ -76,9 +76,14 @@ struct FrameParams {
     size_t in_bytes;     // size of the input buffer (packed tail rule)
     // black level: per CFA colour (R, Gr, Gb, B), already max(0, .)
     float bl[4];
+    int bl_int;          // all offsets integral and < 65536: exact as a saturating u16 subtract
+    uint32_t bl2[2];     // packed (x even, x odd) offsets for even / odd rows
+    int bl_i[2][2];      // integral offsets [row parity][column parity]
+    uint32_t mv2;        // (mv, mv)
     // defect correction
     int dpc_mode;        // 0 adaptive, 1 map
     int dpc_thr;         // absolute threshold
+    uint32_t thr2;       // (thr, thr)
     const int* map_row_ptr;   // h+1 offsets into map_ent (map mode)
     const int2* map_ent;      // (x, value slot) per unique map pixel, sorted by row then x
     const int* map_val;       // resolved value per slot (written by the resolve kernel)
@@ -95,6 +100,10 @@ struct FrameParams {
     float ccm[9];
     // tone: 2^bd-entry u8 table
     const uint8_t* tone8;
+    // AMAZE: rtab[k] = 1/(1+k) correctly rounded, k in [0, 3*mv]
+    const float* rtab;
+    // the demosaic's u16 read shifts MSB-aligned samples (no earlier stage clamped them)
+    int need_align;
     // data
     const uint8_t* in;
     uint8_t* out;

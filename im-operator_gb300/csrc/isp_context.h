@@ -25,7 +25,7 @@ struct DevBuf {
 
 // device copies of one frame's parameter tables
 struct FrameTables {
-    DevBuf grid, lut, knots, tone8;
+    DevBuf grid, lut, knots, tone8, rtab;
     DevBuf map_row_ptr, map_ent, map_val, slot_xy, comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
     MapPlan plan{};
 };

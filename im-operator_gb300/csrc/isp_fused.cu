@@ -45,27 +45,38 @@ __global__ void tone_table_kernel(int mode, const float* lut, const float* knots
     out[v] = (uint8_t)dev::clampi(q, 0, 255);
 }
 
+// rtab[k] = 1 / (1 + k), correctly rounded (the AMAZE weights 1.0f / (1.0f + gradient))
+__global__ void recip_table_kernel(float* out, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = __frcp_rn((float)(1 + k));
+}
+
 // ---------------------------------------------------------------------------------------------
 // one CTA per tile, tiles in raster order
-template <int TW, int TH>
+template <int TW, int TH, int OUTB>
 __global__ void __launch_bounds__(kThreads) fused_frame_kernel(const __grid_constant__ FrameParams fp, int ntx,
                                                                int nty) {
-    __shared__ TileSmem<TW, TH> sm;
+    extern __shared__ __align__(16) uint8_t dsm[];
+    auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
+    tile_init(sm);
+    uint32_t parity = 0;
     int t = blockIdx.x;
     int tx = t % ntx, ty = t / ntx;
     int x0, tw, y0, th;
     tile_span(fp.w, TW, ntx, tx, x0, tw);
     tile_span(fp.h, TH, nty, ty, y0, th);
-    process_tile<TW, TH>(fp, x0, y0, tw, th, sm, Overrides{nullptr, nullptr, 0}, true);
+    process_tile<TW, TH, OUTB>(fp, x0, y0, tw, th, sm, Overrides{nullptr, nullptr, 0}, true, parity);
 }
 
 // defect-chain fix-up (adaptive mode), one CTA per frame
-template <int TW, int TH>
+template <int TW, int TH, int OUTB>
 __global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_constant__ FrameParams fp,
                                                              FixupScratch fs) {
-    __shared__ TileSmem<TW, TH> sm;
+    extern __shared__ __align__(16) uint8_t dsm[];
+    auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
     __shared__ int s_nov;
     if (*fp.seed_count == 0) return;
+    tile_init(sm);
     if (threadIdx.x == 0) {
         GlobalOrig orig{&fp, pattern_offsets(fp.pattern)};
         s_nov = resolve_chains(fp, orig, fs);
@@ -74,14 +85,15 @@ __global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_consta
     __syncthreads();
     const int n_ov = s_nov;
     Overrides ov{fs.ov_idx, fs.ov_val, n_ov};
-    // re-render the 11x11 output window around each changed pixel (radius 3 of demosaic
-    // support plus 2 of border copies)
+    uint32_t parity = 0;
+    // re-render the output window around each changed pixel: radius 3 of demosaic support plus
+    // 2 of border copies, started on an even column
     for (int k = 0; k < n_ov; k++) {
         int p = fs.ov_idx[k];
         int x = p % fp.w, y = p / fp.w;
-        int wx0 = max(0, x - 5), wx1 = min(fp.w, x + 6);
+        int wx0 = max(0, (x - 5) & ~1), wx1 = min(fp.w, x + 6);
         int wy0 = max(0, y - 5), wy1 = min(fp.h, y + 6);
-        process_tile<TW, TH>(fp, wx0, wy0, wx1 - wx0, wy1 - wy0, sm, ov, false);
+        if (!process_tile<TW, TH, OUTB>(fp, wx0, wy0, wx1 - wx0, wy1 - wy0, sm, ov, false, parity)) return;
     }
 }
 
@@ -137,22 +149,43 @@ cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots
     return cudaGetLastError();
 }
 
+cudaError_t launch_recip_table(float* d_out, int n, cudaStream_t st) {
+    recip_table_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_out, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st) {
     if (plan.n_comp > 0) dpc_map_resolve_kernel<<<(plan.n_comp + 127) / 128, 128, 0, st>>>(fp, plan);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st) {
+template <int OUTB>
+static cudaError_t launch_fused_t(const FrameParams& fp, const FixupScratch& fs, cudaStream_t st) {
+    constexpr size_t smem = sizeof(TileSmem<kTileW, kTileH, OUTB>);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(fused_frame_kernel<kTileW, kTileH, OUTB>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dpc_fixup_kernel<kTileW, kTileH, OUTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     int ntx, nty;
     int n = fused_tile_grid(fp.w, fp.h, ntx, nty);
+    fused_frame_kernel<kTileW, kTileH, OUTB><<<n, kThreads, smem, st>>>(fp, ntx, nty);
+    if ((fp.stages & 2u) && fp.dpc_mode == 0) dpc_fixup_kernel<kTileW, kTileH, OUTB><<<1, kThreads, smem, st>>>(fp, fs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st) {
     if ((fp.stages & 2u) && fp.dpc_mode == 1 && plan) launch_map_resolve(fp, *plan, st);
     if ((fp.stages & 2u) && fp.dpc_mode == 0) {
         cudaError_t e = cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st);
         if (e != cudaSuccess) return e;
     }
-    fused_frame_kernel<kTileW, kTileH><<<n, kThreads, 0, st>>>(fp, ntx, nty);
-    if ((fp.stages & 2u) && fp.dpc_mode == 0) dpc_fixup_kernel<kTileW, kTileH><<<1, kThreads, 0, st>>>(fp, fs);
-    return cudaGetLastError();
+    return fp.out_bpc == 2 ? launch_fused_t<6>(fp, fs, st) : launch_fused_t<3>(fp, fs, st);
 }
 
 }  // namespace imop

@@ -1,48 +1,30 @@
-// isp_tile.cuh - one output tile of the fused RAW->RGB pipeline.
+// isp_tile.cuh - one output tile of the fused RAW->RGB pipeline (sm_103a).
 //
-// A CTA owns a tw x th tile of output pixels.  It stages the tile plus a 5-pixel apron of the
-// unpacked, black-levelled mosaic in shared memory, corrects defects and applies lens shading
-// and white balance on a 3-pixel apron, interpolates green on a 1-pixel apron, then produces
-// demosaic -> CCM -> tone for its own pixels and writes them out.  Each pixel reads its RAW bytes
-// from global memory once per CTA that needs it (aprons are L2 hits) and each RGB byte is
-// written once.
+// A CTA of 256 threads owns a tw x th tile of output pixels and works on horizontal pixel pairs
+// (x even, x+1): one 32-bit word of two u16 samples.  In every Bayer row a pair holds exactly one
+// green and one red/blue site, so the demosaic code is the same for every thread (no CFA-colour
+// divergence), and the integer stages run as 16-bit SIMD on the pair word.
 //
-// Apron radii: output (x,y) needs demosaic inputs within 1 (HQLI) or, through green, 3 pixels
-// (AMAZE / MG); the defect kernel reads 2 more.  Border pixels copy from pixels at most 2 away
-// (border_source), which lie inside the same tile because tiles are at least 4 pixels wide.
+//   stage   region (radius around the tile)   storage
+//   raw     rows +-5, columns +-6            bytes, one 1-D TMA bulk copy per row (mbarrier)
+//   orig    rows +-5, columns +-6            u16x2: unpacked, black-levelled
+//   bay     rows +-3, columns +-4            u16x2: defect-corrected (Jacobi), lens shading, WB
+//   green   rows +-1, columns +-2            f32 per pair: green at the pair's red/blue site
+//   out     the tile                         bytes, shifted to the output's 16-byte phase
+//
+// Output (x,y) needs demosaic inputs within 1 (HQLI) or, through green, 3 pixels (AMAZE, MG);
+// defect correction reads 2 more.  Border pixels copy from pixels at most 2 away (border_source),
+// which lie in the same tile because every tile is at least 4 pixels wide and high.
 #pragma once
 
 #include "isp_device.cuh"
+#include "isp_ptx.cuh"
 
 namespace imop {
 
 constexpr int kThreads = 256;
-constexpr int kHaloRaw = 5;
-constexpr int kHaloBay = 3;
-constexpr int kHaloG = 1;
 
-// The nominal tile is TW x TH; the last tile of a row/column absorbs a remainder below 4.
-template <int TW, int TH>
-struct TileGeom {
-    static constexpr int TWM = TW + 3, THM = TH + 3;
-    static constexpr int OR_W = TWM + 2 * kHaloRaw, OR_H = THM + 2 * kHaloRaw;
-    static constexpr int DP_W = TWM + 2 * kHaloBay, DP_H = THM + 2 * kHaloBay;
-    static constexpr int GG_W = TWM + 2 * kHaloG, GG_H = THM + 2 * kHaloG;
-    static constexpr int OUT_PITCH = TWM * 6;
-};
-
-template <int TW, int TH>
-struct TileSmem {
-    using G = TileGeom<TW, TH>;
-    uint16_t orig[G::OR_H * G::OR_W];
-    uint16_t dpc[G::DP_H * G::DP_W];
-    uint16_t bay[G::DP_H * G::DP_W];
-    float green[G::GG_H * G::GG_W];
-    uint8_t out[G::THM * G::OUT_PITCH];
-};
-
-// tile grid of one frame along one axis: n tiles of `t` pixels, the last one absorbing a
-// remainder smaller than 4
+// tile grid along one axis: n tiles of `t` pixels, the last absorbing a remainder below 4
 __host__ __device__ inline int tiles_along(int extent, int t) {
     int n = (extent + t - 1) / t;
     int rem = extent - (n - 1) * t;
@@ -86,163 +68,536 @@ struct Overrides {
     int n;
 };
 
-template <int TW, int TH>
-__device__ void process_tile(const FrameParams& fp, int x0, int y0, int tw, int th, TileSmem<TW, TH>& sm,
-                             Overrides ov, bool detect_seeds) {
-    using G = TileGeom<TW, TH>;
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int round16(int a) { return (a + 15) / 16 * 16; }
+
+template <int TW, int TH, int OUTB>
+struct TileGeom {
+    static_assert(TW % 2 == 0, "tile width must be even");
+    static constexpr int TWM = TW + 3, THM = TH + 3;  // a merged last tile
+    static constexpr int TWP = (TWM + 1) / 2;         // pairs of own pixels
+    static constexpr int OPW = TWP + 6, ORH = THM + 10, OW = 2 * OPW;
+    static constexpr int BPW = TWP + 4, BRH = THM + 6, BW = 2 * BPW;
+    static constexpr int GPW = TWP + 2, GRH = THM + 2;
+    static constexpr int RAW_PITCH = round16(4 * OPW + 32);
+    static constexpr int OUT_PITCH = round16(TWM * OUTB + 16);
+    static constexpr int A_BYTES = cmax(ORH * RAW_PITCH, GRH * GPW * 4);
+    static constexpr int B_BYTES = cmax(ORH * OW * 4, THM * OUT_PITCH);
+};
+
+template <int TW, int TH, int OUTB>
+struct TileSmem {
+    using G = TileGeom<TW, TH, OUTB>;
+    alignas(16) uint8_t regA[G::A_BYTES];   // raw staging, then green at red/blue sites
+    alignas(16) uint8_t regB[G::B_BYTES];   // orig samples (int per pixel), then output staging
+    alignas(16) int bay[G::BRH * G::BW];    // samples after defect correction, lens shading, WB
+    alignas(16) uint8_t tone8[4096];        // tone table (bit depth <= 12)
+    uint8_t mod[G::BRH * G::BPW];           // bit h: pixel h of the pair was corrected
+    int row_a0[G::ORH];                     // staged byte window [a0, a0 + len) of each raw row
+    int row_len[G::ORH];
+    int row_base[G::ORH];                   // staged offset of the region's first pair, or -1
+    int col_gx[2 * G::BPW];
+    float col_fx[2 * G::BPW];
+    int row_gy[G::BRH];
+    float row_fy[G::BRH];
+    alignas(8) uint64_t bar;
+};
+
+// ---- helpers on pair words --------------------------------------------------------------------
+__device__ __forceinline__ int half_of(uint32_t w, int h) { return h ? (int)(w >> 16) : (int)(w & 0xFFFFu); }
+__device__ __forceinline__ int lo16(uint32_t w) { return (int)(w & 0xFFFFu); }
+__device__ __forceinline__ int hi16(uint32_t w) { return (int)(w >> 16); }
+__device__ __forceinline__ uint32_t pack2(int lo, int hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+
+// byte range [b0, b1) of pixels [i0, i1) (pixel indices) in the input stream
+__device__ __forceinline__ void pixel_bytes(int fmt, int i0, int i1, int& b0, int& b1) {
+    switch (fmt) {
+        case FMT_U8: b0 = i0; b1 = i1; break;
+        case FMT_U16: b0 = 2 * i0; b1 = 2 * i1; break;
+        case FMT_P12: b0 = 3 * (i0 >> 1); b1 = 3 * ((i1 - 1) >> 1) + 3; break;
+        default: b0 = 5 * (i0 >> 2); b1 = 5 * ((i1 - 1) >> 2) + 5; break;
+    }
+}
+
+// one raw byte of the staged row (or of global memory past the staged window)
+template <class SM>
+__device__ __forceinline__ int staged_byte(const FrameParams& fp, const SM& sm, const uint8_t* row, int r, int off) {
+    int rel = off - sm.row_a0[r];
+    if (rel >= 0 && rel < sm.row_len[r]) return row[rel];
+    return __ldg(fp.in + off);
+}
+
+// unpacked sample of pixel index i (row r of the staged window); the packed-tail rule of
+// pixel::get_packed_raw (a group ending at or past the buffer end reads 0) is kept
+template <class SM>
+__device__ __forceinline__ int staged_raw(const FrameParams& fp, const SM& sm, const uint8_t* row, int r, int i) {
+    switch (fp.fmt) {
+        case FMT_U8: return staged_byte(fp, sm, row, r, i);
+        case FMT_U16: return staged_byte(fp, sm, row, r, 2 * i) | (staged_byte(fp, sm, row, r, 2 * i + 1) << 8);
+        case FMT_P12: {
+            int off = (i >> 1) * 3;
+            if (off + 2 >= (int)fp.in_bytes) return 0;
+            int b1 = staged_byte(fp, sm, row, r, off + 1);
+            if ((i & 1) == 0) return ((staged_byte(fp, sm, row, r, off) << 4) | (b1 & 0xF)) & fp.mv;
+            return ((staged_byte(fp, sm, row, r, off + 2) << 4) | (b1 >> 4)) & fp.mv;
+        }
+        default: {
+            int off = (i >> 2) * 5;
+            int sub = i & 3;
+            if (off + 4 >= (int)fp.in_bytes) return 0;
+            int b = staged_byte(fp, sm, row, r, off + sub), b4 = staged_byte(fp, sm, row, r, off + 4);
+            return ((b << 2) | ((b4 >> (2 * sub)) & 3)) & fp.mv;
+        }
+    }
+}
+
+// MIPI RAW12 pair from its three bytes (b0 | b1 << 8 | b2 << 16): p0 = b0<<4 | b1&15, p1 = b2<<4 | b1>>4
+__device__ __forceinline__ uint32_t unpack12_pair(uint32_t v) {
+    uint32_t hi8 = __byte_perm(v, 0u, 0x4240u);           // b0 | b2 << 16
+    uint32_t b1 = __byte_perm(v, 0u, 0x4141u);            // b1 | b1 << 16
+    return (hi8 << 4) | (b1 & 0x0000000Fu) | ((b1 >> 4) & 0x000F0000u);
+}
+
+// scalar defect kernel on the orig plane (edges and the rare non-fast pixels)
+template <class OrigAt>
+__device__ __forceinline__ int dpc_scalar(const FrameParams& fp, OrigAt orig, int x, int y) {
+    unsigned m = dev::dpc_valid_mask(x, y, fp.w, fp.h);
+    int nb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (m & 1u) nb[0] = orig(x - 2, y - 2);
+    if (m & 2u) nb[1] = orig(x, y - 2);
+    if (m & 4u) nb[2] = orig(x + 2, y - 2);
+    if (m & 8u) nb[3] = orig(x - 2, y);
+    if (m & 16u) nb[4] = orig(x + 2, y);
+    if (m & 32u) nb[5] = orig(x - 2, y + 2);
+    if (m & 64u) nb[6] = orig(x, y + 2);
+    if (m & 128u) nb[7] = orig(x + 2, y + 2);
+    return dev::dpc_apply(orig(x, y), nb, m, fp.dpc_thr);
+}
+
+// bounded wait on the staging barrier; on expiry the tile is abandoned with IMOP_ERR_TIMEOUT
+__device__ __forceinline__ bool wait_stage(const FrameParams& fp, uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); it++)
+        if (ptx::mbar_try_wait(bar, parity)) return true;
+    atomicExch(fp.status, 103 /* IMOP_ERR_TIMEOUT */);
+    return false;
+}
+
+template <int TW, int TH, int OUTB>
+__device__ void tile_init(TileSmem<TW, TH, OUTB>& sm) {
+    if (threadIdx.x == 0) {
+        ptx::mbar_init(&sm.bar, 1);
+        ptx::fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// green value of a pixel inside the green region: the stored red/blue-site green, or the
+// green-site sample (AMAZE only inside the interior; MG everywhere)
+struct GreenAt {
+    const float* green;
+    const int* bay;
+    int xg0, yg0, xb, yb, gpitch, bpitch, W, H, r_row, r_col, b_col, mg;
+    __device__ __forceinline__ float operator()(int x, int y) const {
+        int rbh = ((y & 1) == r_row) ? r_col : b_col;
+        if ((x & 1) == rbh) return green[(y - yg0) * gpitch + ((x - xg0) >> 1)];
+        bool interior = x >= 2 && x < W - 2 && y >= 2 && y < H - 2;
+        if (!(interior || mg)) return -1.0f;
+        return (float)bay[(y - yb) * bpitch + (x - xb)];
+    }
+};
+
+__device__ __forceinline__ int u16q(float t, int mv) { return (int)min(__float2uint_rz(t), (unsigned)mv); }
+
+// Process one tile. `parity` is the staging barrier's phase, flipped once per tile.
+template <int TW, int TH, int OUTB>
+__device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int th, TileSmem<TW, TH, OUTB>& sm,
+                             Overrides ov, bool detect_seeds, uint32_t& parity) {
+    using G = TileGeom<TW, TH, OUTB>;
     const int W = fp.w, H = fp.h, mv = fp.mv;
     const PatternOffsets po = pattern_offsets(fp.pattern);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool dpc_on = (fp.stages & 2u) != 0;
     const bool adaptive = dpc_on && fp.dpc_mode == 0;
+    const int xo = x0 - 6, yo = y0 - 5;              // orig region origin (xo even)
+    const int opw = (tw + 13) / 2, oh = th + 10;      // orig region in pairs / rows
+    const int xb = x0 - 4, yb = y0 - 3;               // bay region origin
+    const int bpw = (tw + 9) / 2, bh = th + 6;
+    const int xg0 = x0 - 2, yg0 = y0 - 1;             // green region origin
+    const int gpw = (tw + 5) / 2, gh = th + 2;
+    const int tpw = (tw + 1) / 2;                     // own pairs
+    const bool tone_smem = fp.out_format == 0 && fp.bd <= 12;
 
-    // ---- 1. unpack + black level over the tile and a 5-pixel apron ----------------------
-    const int ow = tw + 2 * kHaloRaw, oh = th + 2 * kHaloRaw;
-    for (int i = tid; i < ow * oh; i += kThreads) {
-        int r = i / ow, c = i - r * ow;
-        int gx = x0 - kHaloRaw + c, gy = y0 - kHaloRaw + r;
-        int v = 0;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = dev::orig_value(fp, gx, gy, po);
-        sm.orig[r * G::OR_W + c] = (uint16_t)v;
-    }
-    __syncthreads();
-
-    auto ORIG = [&](int gx, int gy) -> int {
-        return sm.orig[(gy - y0 + kHaloRaw) * G::OR_W + (gx - x0 + kHaloRaw)];
-    };
-    auto DPC = [&](int gx, int gy) -> int { return sm.dpc[(gy - y0 + kHaloBay) * G::DP_W + (gx - x0 + kHaloBay)]; };
-    auto BAY = [&](int gx, int gy) -> int { return sm.bay[(gy - y0 + kHaloBay) * G::DP_W + (gx - x0 + kHaloBay)]; };
-
-    // ---- 2. defect correction (Jacobi), lens shading, Bayer white balance, 3-pixel apron ---
-    const int dw = tw + 2 * kHaloBay, dh = th + 2 * kHaloBay;
-    for (int i = tid; i < dw * dh; i += kThreads) {
-        int r = i / dw, c = i - r * dw;
-        int gx = x0 - kHaloBay + c, gy = y0 - kHaloBay + r;
-        int o = ORIG(gx, gy);
-        int j = o, b = 0;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-            if (adaptive && gx >= 2 && gx < W - 2 && gy >= 2 && gy < H - 2) {
-                int nb[8] = {ORIG(gx - 2, gy - 2), ORIG(gx, gy - 2), ORIG(gx + 2, gy - 2), ORIG(gx - 2, gy),
-                             ORIG(gx + 2, gy), ORIG(gx - 2, gy + 2), ORIG(gx, gy + 2), ORIG(gx + 2, gy + 2)};
-                j = dev::dpc_apply(o, nb, dev::dpc_valid_mask(gx, gy, W, H), fp.dpc_thr);
-                if (ov.n > 0) {
-                    int s = find_override(ov.idx, ov.val, ov.n, gy * W + gx);
-                    if (s >= 0) j = s;
+    // ---- 1. stage raw rows: one 1-D bulk copy per row on a 16-byte aligned window ----------
+    const int in16 = (int)(fp.in_bytes & ~(size_t)15);
+    const bool bulk_ok = ((reinterpret_cast<uintptr_t>(fp.in) & 15) == 0);
+    if (warp == 0) {
+        uint32_t bytes = 0;
+        for (int r = lane; r < oh; r += 32) {
+            int y = yo + r;
+            int a0 = 0, len = 0, base = -1;
+            if (y >= 0 && y < H) {
+                int xs = max(0, xo), xe = min(W, xo + 2 * opw);
+                int b0, b1;
+                pixel_bytes(fp.fmt, y * W + xs, y * W + xe, b0, b1);
+                b1 = min(b1, (int)fp.in_bytes);
+                a0 = b0 & ~15;
+                int a1 = min((b1 + 15) & ~15, in16);
+                len = max(a1 - a0, 0);
+                int i = y * W + xo;  // pixel index of the region's first pair (may lie left of the frame)
+                switch (fp.fmt) {
+                    case FMT_U8: base = i - a0; break;
+                    case FMT_U16: base = 2 * i - a0; break;
+                    case FMT_P12: base = ((i & 1) == 0) ? 3 * (i >> 1) - a0 : -1; break;
+                    default: base = -1; break;
                 }
-            } else if (dpc_on && fp.dpc_mode == 1 && gx >= 2 && gx < W - 2 && gy >= 2 && gy < H - 2) {
-                int s = map_lookup(fp, gx, gy);
-                if (s >= 0) j = s;
             }
-            b = dev::bayer_tail(fp, j, gx, gy, bayer_color(gy, gx, po));
+            sm.row_a0[r] = a0;
+            sm.row_len[r] = len;
+            sm.row_base[r] = base;
+            if (bulk_ok) bytes += (uint32_t)len;
         }
-        sm.dpc[r * G::DP_W + c] = (uint16_t)j;
-        sm.bay[r * G::DP_W + c] = (uint16_t)b;
+        if (bulk_ok) {
+            for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+            ptx::fence_proxy_async_smem();
+            if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.bar, bytes);
+            __syncwarp();
+            for (int r = lane; r < oh; r += 32) {
+                int n = sm.row_len[r];
+                if (n > 0) ptx::bulk_g2s(sm.regA + r * G::RAW_PITCH, fp.in + sm.row_a0[r], (uint32_t)n, &sm.bar);
+            }
+        }
+    }
+    // tone table and lens-shading tables (overlap the copies)
+    if (tone_smem) {
+        int n = fp.mv + 1;
+        for (int k = tid * 4; k < n; k += kThreads * 4)
+            *reinterpret_cast<uint32_t*>(sm.tone8 + k) = __ldg(reinterpret_cast<const uint32_t*>(fp.tone8 + k));
+    }
+    if ((fp.stages & 4u) && fp.lsc_mode == 0) {
+        for (int c = tid; c < 2 * bpw; c += kThreads) {
+            int x = min(max(xb + c, 0), W - 1);
+            float gx_f = __fdiv_rn(dev::fmul((float)x, (float)(fp.gw - 1)), (float)(W - 1));
+            int gx_i = dev::clampi(dev::ftoi(gx_f), 0, fp.gw - 2);
+            sm.col_gx[c] = gx_i;
+            sm.col_fx[c] = dev::fsub(gx_f, (float)gx_i);
+        }
+        for (int r = tid; r < bh; r += kThreads) {
+            int y = min(max(yb + r, 0), H - 1);
+            float gy_f = __fdiv_rn(dev::fmul((float)y, (float)(fp.gh - 1)), (float)(H - 1));
+            int gy_i = dev::clampi(dev::ftoi(gy_f), 0, fp.gh - 2);
+            sm.row_gy[r] = gy_i;
+            sm.row_fy[r] = dev::fsub(gy_f, (float)gy_i);
+        }
     }
     __syncthreads();
-
-    // ---- 3. defect-chain seeds: own pixels whose raster-earlier neighbour was corrected and
-    //         whose value changes when those corrections are seen (sequential semantics) ----
-    if (detect_seeds && adaptive) {
-        for (int i = tid; i < tw * th; i += kThreads) {
-            int r = i / tw, c = i - r * tw;
-            int gx = x0 + c, gy = y0 + r;
-            if (gx < 2 || gx >= W - 2 || gy < 2 || gy >= H - 2) continue;
-            unsigned valid = dev::dpc_valid_mask(gx, gy, W, H);
-            const int ex[4] = {gx - 2, gx, gx + 2, gx - 2}, ey[4] = {gy - 2, gy - 2, gy - 2, gy};
-            bool any = false;
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if ((valid >> k) & 1u) any |= DPC(ex[k], ey[k]) != ORIG(ex[k], ey[k]);
-            if (!any) continue;
-            int nb[8] = {DPC(gx - 2, gy - 2), DPC(gx, gy - 2), DPC(gx + 2, gy - 2), DPC(gx - 2, gy),
-                         ORIG(gx + 2, gy), ORIG(gx - 2, gy + 2), ORIG(gx, gy + 2), ORIG(gx + 2, gy + 2)};
-            int s1 = dev::dpc_apply(ORIG(gx, gy), nb, valid, fp.dpc_thr);
-            if (s1 != DPC(gx, gy)) {
-                int slot = atomicAdd(fp.seed_count, 1);
-                if (slot < fp.seed_cap) fp.seeds[slot] = gy * W + gx;
-                else atomicExch(fp.status, 104 /* IMOP_ERR_CAPACITY */);
-            }
+    if (bulk_ok) {
+        if (!wait_stage(fp, &sm.bar, parity)) return false;
+        parity ^= 1u;
+    } else {
+        // unaligned input pointer: threads copy the same windows byte by byte
+        for (int r = 0; r < oh; r++) {
+            int n = sm.row_len[r];
+            for (int k = tid; k < n; k += kThreads) sm.regA[r * G::RAW_PITCH + k] = __ldg(fp.in + sm.row_a0[r] + k);
         }
+        __syncthreads();
     }
 
-    // ---- 4. green plane on a 1-pixel apron (AMAZE, MG) ------------------------------------
-    const int gwid = tw + 2 * kHaloG, ghgt = th + 2 * kHaloG;
-    if (fp.demosaic != DM_HQLI) {
-        for (int i = tid; i < gwid * ghgt; i += kThreads) {
-            int r = i / gwid, c = i - r * gwid;
-            int gx = x0 - kHaloG + c, gy = y0 - kHaloG + r;
-            float g = -1.0f;
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-                bool at_r = ((gy & 1) == po.r_row) && ((gx & 1) == po.r_col);
-                bool at_b = ((gy & 1) == po.b_row) && ((gx & 1) == po.b_col);
-                bool interior = gx >= 2 && gx < W - 2 && gy >= 2 && gy < H - 2;
-                if (!at_r && !at_b) {
-                    // AMAZE sets green only inside the interior; MG at every green site
-                    if (interior || fp.demosaic == DM_MG) g = (float)BAY(gx, gy);
-                } else if (interior) {
-                    int cc = BAY(gx, gy);
-                    if (fp.demosaic == DM_AMAZE) {
-                        g = dev::amaze_green(cc, BAY(gx - 1, gy), BAY(gx + 1, gy), BAY(gx - 2, gy), BAY(gx + 2, gy),
-                                             BAY(gx, gy - 1), BAY(gx, gy + 1), BAY(gx, gy - 2), BAY(gx, gy + 2));
-                    } else {
-                        int n1 = BAY(gx, gy - 1) + BAY(gx, gy + 1) + BAY(gx + 1, gy) + BAY(gx - 1, gy);
-                        int n2 = BAY(gx, gy - 2) + BAY(gx, gy + 2) + BAY(gx + 2, gy) + BAY(gx - 2, gy);
-                        if (fp.bd <= 8) {
-                            // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler)
-                            g = (float)dev::clampi((4 * cc + 2 * n1 - n2 + 4) >> 3, 0, mv);
-                        } else {
-                            // src/algorithms/mg.cpp:187-196: (4c + 2*(n+s+e+w) - (n2+s2+e2+w2)) / 8
-                            float t = dev::fsub(dev::fadd(dev::fmul(4.0f, (float)cc), dev::fmul(2.0f, (float)n1)),
-                                                (float)n2);
-                            g = __fdiv_rn(t, 8.0f);
-                        }
+    // ---- 2. unpack + black level -> orig samples (one int per pixel) ------------------------
+    int* orig = reinterpret_cast<int*>(sm.regB);
+    const bool bl_on = (fp.stages & 1u) != 0;
+    for (int s = tid; s < G::ORH * G::OPW; s += kThreads) {
+        int r = s / G::OPW, pc = s - r * G::OPW;
+        if (r >= oh || pc >= opw) continue;
+        int y = yo + r, x = xo + 2 * pc;
+        int v0 = 0, v1 = 0;
+        if (y >= 0 && y < H) {
+            const uint8_t* row = sm.regA + r * G::RAW_PITCH;
+            const int base = sm.row_base[r], len = sm.row_len[r];
+            const bool in0 = x >= 0 && x < W, in1 = x + 1 >= 0 && x + 1 < W;
+            bool done = false;
+            if (in0 && in1 && base >= 0) {
+                if (fp.fmt == FMT_P12) {
+                    int off = base + 3 * pc;
+                    if (off >= 0 && off + 3 <= len) {
+                        int o4 = off & ~3;
+                        uint32_t w0 = *reinterpret_cast<const uint32_t*>(row + o4);
+                        uint32_t w1 = *reinterpret_cast<const uint32_t*>(row + o4 + 4);
+                        uint32_t w = unpack12_pair(__funnelshift_r(w0, w1, 8 * (off & 3)));
+                        v0 = (int)(w & 0xFFFFu);
+                        v1 = (int)(w >> 16);
+                        done = true;
+                    }
+                } else if (fp.fmt == FMT_U16) {
+                    int off = base + 4 * pc;
+                    if (off >= 0 && off + 4 <= len) {
+                        uint32_t w = ((off & 3) == 0) ? *reinterpret_cast<const uint32_t*>(row + off)
+                                                      : (uint32_t)*reinterpret_cast<const uint16_t*>(row + off) |
+                                                            ((uint32_t)*reinterpret_cast<const uint16_t*>(row + off + 2) << 16);
+                        v0 = (int)(w & 0xFFFFu);
+                        v1 = (int)(w >> 16);
+                        done = true;
+                    }
+                } else if (fp.fmt == FMT_U8) {
+                    int off = base + 2 * pc;
+                    if (off >= 0 && off + 2 <= len) {
+                        v0 = row[off];
+                        v1 = row[off + 1];
+                        done = true;
                     }
                 }
             }
-            sm.green[r * G::GG_W + c] = g;
+            if (!done) {
+                int i = y * W + x;
+                if (in0) v0 = staged_raw(fp, sm, row, r, i);
+                if (in1) v1 = staged_raw(fp, sm, row, r, i + 1);
+            }
+            if (bl_on) {
+                if (fp.bl_int) {
+                    // (int)((float)v - off) == v - off for an integral offset
+                    const int p = y & 1;
+                    v0 = min(max(v0 - fp.bl_i[p][0], 0), mv);
+                    v1 = min(max(v1 - fp.bl_i[p][1], 0), mv);
+                } else {
+                    v0 = dev::black_level(fp, v0, bayer_color(y, x, po));
+                    v1 = dev::black_level(fp, v1, bayer_color(y, x + 1, po));
+                }
+            }
+            if (!in0) v0 = 0;
+            if (!in1) v1 = 0;
+        }
+        *reinterpret_cast<int2*>(orig + r * G::OW + 2 * pc) = make_int2(v0, v1);
+    }
+    __syncthreads();
+
+    auto ORIGV = [&](int x, int y) -> int { return orig[(y - yo) * G::OW + (x - xo)]; };
+
+    // ---- 3. defect correction (Jacobi), lens shading, Bayer WB -> bay samples ---------------
+    // warp-rows: a warp takes 32 pair columns of one row; with two column blocks every warp
+    // keeps one row parity and one column pair, so its colour constants stay in registers
+    int local_mod = 0;
+    const bool lsc_grid = (fp.stages & 4u) && fp.lsc_mode == 0;
+    const bool lsc_poly = (fp.stages & 4u) && fp.lsc_mode == 1;
+    const bool wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
+    const float2 h5 = make_float2(0.5f, 0.5f);
+    {
+        const int nbk = (bpw + 31) >> 5;
+        int cache_key = -1;
+        float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f, WB0 = 1.f, WB1 = 1.f;
+        for (int item = warp; item < nbk * bh; item += 8) {
+            int blk, r;
+            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+            int pc = blk * 32 + lane;
+            if (pc >= bpw) continue;
+            int y = yb + r, x = xb + 2 * pc;
+            const int* o = orig + (r + 2) * G::OW + (x - xo);
+            int2 c = *reinterpret_cast<const int2*>(o);
+            int j0 = c.x, j1 = c.y;
+            bool yin = y >= 0 && y < H;
+            if (yin && adaptive) {
+                bool fast = x >= 4 && x + 1 < W - 4 && y >= 4 && y < H - 4;
+                if (fast) {
+                    int2 n0 = *reinterpret_cast<const int2*>(o - 2 * G::OW - 2);
+                    int2 n1 = *reinterpret_cast<const int2*>(o - 2 * G::OW);
+                    int2 n2 = *reinterpret_cast<const int2*>(o - 2 * G::OW + 2);
+                    int2 n3 = *reinterpret_cast<const int2*>(o - 2);
+                    int2 n4 = *reinterpret_cast<const int2*>(o + 2);
+                    int2 n5 = *reinterpret_cast<const int2*>(o + 2 * G::OW - 2);
+                    int2 n6 = *reinterpret_cast<const int2*>(o + 2 * G::OW);
+                    int2 n7 = *reinterpret_cast<const int2*>(o + 2 * G::OW + 2);
+                    int mn0 = min(min(min(n0.x, n1.x), min(n2.x, n3.x)), min(min(n4.x, n5.x), min(n6.x, n7.x)));
+                    int mx0 = max(max(max(n0.x, n1.x), max(n2.x, n3.x)), max(max(n4.x, n5.x), max(n6.x, n7.x)));
+                    int mn1 = min(min(min(n0.y, n1.y), min(n2.y, n3.y)), min(min(n4.y, n5.y), min(n6.y, n7.y)));
+                    int mx1 = max(max(max(n0.y, n1.y), max(n2.y, n3.y)), max(max(n4.y, n5.y), max(n6.y, n7.y)));
+                    // |c - median| <= thr is certain when c - min <= thr and max - c <= thr
+                    const int thr = fp.dpc_thr;
+                    if (max(c.x - mn0, mx0 - c.x) > thr) {
+                        int nb[8] = {n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x};
+                        j0 = dev::dpc_apply(c.x, nb, 0xFFu, thr);
+                    }
+                    if (max(c.y - mn1, mx1 - c.y) > thr) {
+                        int nb[8] = {n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y};
+                        j1 = dev::dpc_apply(c.y, nb, 0xFFu, thr);
+                    }
+                } else {
+                    if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) j0 = dpc_scalar(fp, ORIGV, x, y);
+                    if (x + 1 >= 2 && x + 1 < W - 2 && y >= 2 && y < H - 2) j1 = dpc_scalar(fp, ORIGV, x + 1, y);
+                }
+                if (ov.n > 0 && y >= 2 && y < H - 2) {
+                    if (x >= 2 && x < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x); if (sv >= 0) j0 = sv; }
+                    if (x + 1 >= 2 && x + 1 < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x + 1); if (sv >= 0) j1 = sv; }
+                }
+            } else if (yin && dpc_on && fp.dpc_mode == 1 && y >= 2 && y < H - 2 &&
+                       __ldg(fp.map_row_ptr + y + 1) > __ldg(fp.map_row_ptr + y)) {
+                if (x >= 2 && x < W - 2) { int sv = map_lookup(fp, x, y); if (sv >= 0) j0 = sv; }
+                if (x + 1 >= 2 && x + 1 < W - 2) { int sv = map_lookup(fp, x + 1, y); if (sv >= 0) j1 = sv; }
+            }
+            int m = (j0 != c.x) | ((j1 != c.y) << 1);
+            local_mod |= m;
+            sm.mod[r * G::BPW + pc] = (uint8_t)m;
+            // lens shading + white balance: scalar products (packed FP32 multiply-add pairs would be
+            // fused into one rounding), packed sums
+            int u0 = 0, u1 = 0;
+            if (yin) {
+                const int p = y & 1;
+                const int c0 = bayer_color(p, 0, po), c1 = bayer_color(p, 1, po);
+                u0 = j0;
+                u1 = j1;
+                if (lsc_grid) {
+                    int gy_i = sm.row_gy[r];
+                    int key = (gy_i * 2 + p) * 1024 + pc;
+                    if (key != cache_key) {
+                        // g00*(1-fx), g10*fx, g01*(1-fx), g11*fx of both samples for this cell row
+                        cache_key = key;
+                        float f0 = sm.col_fx[2 * pc], f1 = sm.col_fx[2 * pc + 1];
+                        const float* g0 = fp.grid + (gy_i * fp.gw + sm.col_gx[2 * pc]) * 4 + c0;
+                        const float* g1 = fp.grid + (gy_i * fp.gw + sm.col_gx[2 * pc + 1]) * 4 + c1;
+                        float of0 = dev::fsub(1.0f, f0), of1 = dev::fsub(1.0f, f1);
+                        A0 = dev::fmul(__ldg(g0), of0); A1 = dev::fmul(__ldg(g1), of1);
+                        B0 = dev::fmul(__ldg(g0 + 4), f0); B1 = dev::fmul(__ldg(g1 + 4), f1);
+                        C0 = dev::fmul(__ldg(g0 + 4 * fp.gw), of0); C1 = dev::fmul(__ldg(g1 + 4 * fp.gw), of1);
+                        D0 = dev::fmul(__ldg(g0 + 4 * fp.gw + 4), f0); D1 = dev::fmul(__ldg(g1 + 4 * fp.gw + 4), f1);
+                        WB0 = fp.wb_cfa[c0]; WB1 = fp.wb_cfa[c1];
+                    }
+                    float fy = sm.row_fy[r], ofy = dev::fsub(1.0f, fy);
+                    float2 pa = make_float2(dev::fmul(A0, ofy), dev::fmul(A1, ofy));
+                    float2 pb = make_float2(dev::fmul(B0, ofy), dev::fmul(B1, ofy));
+                    float2 pcc = make_float2(dev::fmul(C0, fy), dev::fmul(C1, fy));
+                    float2 pd = make_float2(dev::fmul(D0, fy), dev::fmul(D1, fy));
+                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(pa, pb), pcc), pd);
+                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, gain.x), dev::fmul((float)u1, gain.y)), h5);
+                    u0 = u16q(t.x, mv);
+                    u1 = u16q(t.y, mv);
+                } else {
+                    if (lsc_poly) {
+                        u0 = dev::lsc_poly(fp, u0, x, y, c0);
+                        u1 = dev::lsc_poly(fp, u1, x + 1, y, c1);
+                    }
+                    WB0 = fp.wb_cfa[c0];
+                    WB1 = fp.wb_cfa[c1];
+                }
+                if (wb_bayer) {
+                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, WB0), dev::fmul((float)u1, WB1)), h5);
+                    u0 = u16q(t.x, mv);
+                    u1 = u16q(t.y, mv);
+                }
+                if (fp.need_align) {
+                    if (u0 > mv) u0 >>= (16 - fp.bd);
+                    if (u1 > mv) u1 >>= (16 - fp.bd);
+                }
+                if (x < 0 || x >= W) u0 = 0;
+                if (x + 1 < 0 || x + 1 >= W) u1 = 0;
+            }
+            *reinterpret_cast<int2*>(sm.bay + r * G::BW + 2 * pc) = make_int2(u0, u1);
+        }
+    }
+    const int any_mod = __syncthreads_or(local_mod);
+
+    auto BAYV = [&](int x, int y) -> int { return sm.bay[(y - yb) * G::BW + (x - xb)]; };
+    float* green = reinterpret_cast<float*>(sm.regA);  // one float per pair row: the R/B site
+
+    // ---- 4a. defect-chain seeds among own pixels (only tiles with a corrected pixel) ---------
+    if (detect_seeds && adaptive && any_mod) {
+        for (int s = tid; s < G::THM * G::TWP; s += kThreads) {
+            int r = s / G::TWP, pc = s - r * G::TWP;
+            if (r >= th || pc >= tpw) continue;
+            int y = y0 + r;
+            // quick reject: no corrected pixel among the earlier neighbours of either sample
+            const uint8_t* mr = sm.mod + (r + 1) * G::BPW + (pc + 2);  // row y-2, pair of x
+            const uint8_t* m0 = sm.mod + (r + 3) * G::BPW + (pc + 2);  // row y
+            if ((mr[-1] | mr[0] | mr[1] | m0[-1]) == 0) continue;
+            for (int h = 0; h < 2; h++) {
+                int x = x0 + 2 * pc + h;
+                if (x >= x0 + tw || x < 2 || x >= W - 2 || y < 2 || y >= H - 2) continue;
+                unsigned valid = dev::dpc_valid_mask(x, y, W, H);
+                auto MOD = [&](int xx, int yy) { return (sm.mod[(yy - yb) * G::BPW + ((xx - xb) >> 1)] >> ((xx - xb) & 1)) & 1; };
+                bool any = ((valid & 1u) && MOD(x - 2, y - 2)) || ((valid & 2u) && MOD(x, y - 2)) ||
+                           ((valid & 4u) && MOD(x + 2, y - 2)) || ((valid & 8u) && MOD(x - 2, y));
+                if (!any) continue;
+                int nb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                const int ex[4] = {x - 2, x, x + 2, x - 2}, ey[4] = {y - 2, y - 2, y - 2, y};
+                for (int k = 0; k < 4; k++)
+                    if ((valid >> k) & 1u) nb[k] = MOD(ex[k], ey[k]) ? dpc_scalar(fp, ORIGV, ex[k], ey[k]) : ORIGV(ex[k], ey[k]);
+                if (valid & 16u) nb[4] = ORIGV(x + 2, y);
+                if (valid & 32u) nb[5] = ORIGV(x - 2, y + 2);
+                if (valid & 64u) nb[6] = ORIGV(x, y + 2);
+                if (valid & 128u) nb[7] = ORIGV(x + 2, y + 2);
+                int s1 = dev::dpc_apply(ORIGV(x, y), nb, valid, fp.dpc_thr);
+                int jp = MOD(x, y) ? dpc_scalar(fp, ORIGV, x, y) : ORIGV(x, y);
+                if (s1 != jp) {
+                    int slot = atomicAdd(fp.seed_count, 1);
+                    if (slot < fp.seed_cap) fp.seeds[slot] = y * W + x;
+                    else atomicExch(fp.status, 104 /* IMOP_ERR_CAPACITY */);
+                }
+            }
+        }
+    }
+
+    // ---- 4b. green at the red/blue site of each pair (AMAZE, MG) ---------------------------
+    if (fp.demosaic != DM_HQLI) {
+        const int nbk = (gpw + 31) >> 5;
+        for (int item = warp; item < nbk * gh; item += 8) {
+            int blk, r;
+            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+            int pc = blk * 32 + lane;
+            if (pc >= gpw) continue;
+            int y = yg0 + r;
+            int rbh = ((y & 1) == po.r_row) ? po.r_col : po.b_col;
+            int x = xg0 + 2 * pc + rbh;
+            float g = -1.0f;
+            if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) {
+                const int* b = sm.bay + (r + 2) * G::BW + (x - xb);
+                int cc = b[0], hm1 = b[-1], hp1 = b[1], hm2 = b[-2], hp2 = b[2];
+                int vm1 = b[-G::BW], vp1 = b[G::BW], vm2 = b[-2 * G::BW], vp2 = b[2 * G::BW];
+                if (fp.demosaic == DM_AMAZE) {
+                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fp.rtab);
+                } else if (fp.bd <= 8) {
+                    // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
+                    g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
+                } else {
+                    // src/algorithms/mg.cpp:187-196, exact in FP32 for integer samples
+                    float t = dev::fsub(dev::fadd(dev::fmul(4.0f, (float)cc), dev::fmul(2.0f, (float)(vm1 + vp1 + hp1 + hm1))),
+                                        (float)(vm2 + vp2 + hp2 + hm2));
+                    g = __fdiv_rn(t, 8.0f);
+                }
+            }
+            green[r * G::GPW + pc] = g;
         }
     }
     __syncthreads();
-    auto GRN = [&](int gx, int gy) -> float { return sm.green[(gy - y0 + kHaloG) * G::GG_W + (gx - x0 + kHaloG)]; };
 
-    // ---- 5. demosaic + RGB tail + tone for own pixels --------------------------------------
-    const int bpc = fp.out_bpc;
-    for (int i = tid; i < tw * th; i += kThreads) {
-        int r = i / tw, c = i - r * tw;
-        int gx = x0 + c, gy = y0 + r;
-        int sx, sy;
-        dev::border_source(gx, gy, W, H, fp.border_mode, sx, sy);
+    const GreenAt GRNV{green, sm.bay, xg0, yg0, xb, yb, G::GPW, G::BW, W, H, po.r_row, po.r_col, po.b_col,
+                       fp.demosaic == DM_MG};
+
+    // demosaic of one pixel at (sx, sy) (generic path: border tiles, MG and fix-up windows)
+    auto demosaic_at = [&](int sx, int sy, int& R, int& Gv, int& B) {
         bool at_r = ((sy & 1) == po.r_row) && ((sx & 1) == po.r_col);
         bool at_b = ((sy & 1) == po.b_row) && ((sx & 1) == po.b_col);
-        int R = 0, Gv = 0, B = 0;
+        R = Gv = B = 0;
         if (fp.demosaic == DM_HQLI) {
-            // detail::hqli_core (src/algorithms/interp_core.hpp:39-65); outside the interior the
-            // reference leaves the zeroed output untouched
+            // detail::hqli_core (src/algorithms/interp_core.hpp:39-65)
             if (sx >= 2 && sx < W - 2 && sy >= 2 && sy < H - 2) {
-                int n4 = BAY(sx - 1, sy) + BAY(sx + 1, sy) + BAY(sx, sy - 1) + BAY(sx, sy + 1);
-                int d4 = BAY(sx - 1, sy - 1) + BAY(sx + 1, sy - 1) + BAY(sx - 1, sy + 1) + BAY(sx + 1, sy + 1);
-                if (at_r) {
-                    R = BAY(sx, sy); Gv = (n4 + 2) / 4; B = (d4 + 2) / 4;
-                } else if (at_b) {
-                    R = (d4 + 2) / 4; Gv = (n4 + 2) / 4; B = BAY(sx, sy);
-                } else {
-                    Gv = BAY(sx, sy);
-                    int hz = (BAY(sx - 1, sy) + BAY(sx + 1, sy) + 1) / 2;
-                    int vt = (BAY(sx, sy - 1) + BAY(sx, sy + 1) + 1) / 2;
+                int n4 = BAYV(sx - 1, sy) + BAYV(sx + 1, sy) + BAYV(sx, sy - 1) + BAYV(sx, sy + 1);
+                int d4 = BAYV(sx - 1, sy - 1) + BAYV(sx + 1, sy - 1) + BAYV(sx - 1, sy + 1) + BAYV(sx + 1, sy + 1);
+                if (at_r) { R = BAYV(sx, sy); Gv = (n4 + 2) / 4; B = (d4 + 2) / 4; }
+                else if (at_b) { R = (d4 + 2) / 4; Gv = (n4 + 2) / 4; B = BAYV(sx, sy); }
+                else {
+                    Gv = BAYV(sx, sy);
+                    int hz = (BAYV(sx - 1, sy) + BAYV(sx + 1, sy) + 1) / 2;
+                    int vt = (BAYV(sx, sy - 1) + BAYV(sx, sy + 1) + 1) / 2;
                     if ((sy & 1) == po.r_row) { R = hz; B = vt; } else { B = hz; R = vt; }
                 }
                 R = min(R, mv); Gv = min(Gv, mv); B = min(B, mv);
             }
         } else if (fp.demosaic == DM_MG && fp.bd <= 8) {
             // integer colour differences (src/algorithms/mg.cpp:74-146)
-            int g = (int)GRN(sx, sy);
-            int Ri = 0, Bi = 0, Gi = g;
+            int g = (int)GRNV(sx, sy);
+            int Ri = 0, Bi = 0;
             if (sx >= 1 && sx < W - 1 && sy >= 1 && sy < H - 1) {
-                auto cdi = [&](int x, int y) { return BAY(x, y) - (int)GRN(x, y); };
+                auto cdi = [&](int x, int y) { return BAYV(x, y) - (int)GRNV(x, y); };
                 if (at_r || at_b) {
-                    int s = cdi(sx - 1, sy - 1) + cdi(sx + 1, sy - 1) + cdi(sx - 1, sy + 1) + cdi(sx + 1, sy + 1);
-                    int other = g + (s + 2) / 4;
-                    if (at_r) { Ri = BAY(sx, sy); Bi = other; } else { Bi = BAY(sx, sy); Ri = other; }
+                    int sum = cdi(sx - 1, sy - 1) + cdi(sx + 1, sy - 1) + cdi(sx - 1, sy + 1) + cdi(sx + 1, sy + 1);
+                    int other = g + (sum + 2) / 4;
+                    if (at_r) { Ri = BAYV(sx, sy); Bi = other; } else { Bi = BAYV(sx, sy); Ri = other; }
                 } else {
                     int hz = cdi(sx - 1, sy) + cdi(sx + 1, sy), vt = cdi(sx, sy - 1) + cdi(sx, sy + 1);
                     int rc = ((sy & 1) == po.r_row) ? hz : vt, bc = ((sy & 1) == po.r_row) ? vt : hz;
@@ -250,17 +605,17 @@ __device__ void process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                     Bi = g + (bc + 1) / 2;
                 }
             }
-            R = dev::clampi(Ri, 0, mv); Gv = dev::clampi(Gi, 0, mv); B = dev::clampi(Bi, 0, mv);
+            R = dev::clampi(Ri, 0, mv); Gv = dev::clampi(g, 0, mv); B = dev::clampi(Bi, 0, mv);
         } else {
             // float colour differences (src/algorithms/common.hpp:142-199, amaze.cpp:62-114)
-            float g = GRN(sx, sy), Rf = 0.0f, Bf = 0.0f;
+            float g = GRNV(sx, sy), Rf = 0.0f, Bf = 0.0f;
             if (sx >= 1 && sx < W - 1 && sy >= 1 && sy < H - 1) {
-                auto cd = [&](int x, int y) { return dev::fsub((float)BAY(x, y), GRN(x, y)); };
+                auto cd = [&](int x, int y) { return dev::fsub((float)BAYV(x, y), GRNV(x, y)); };
                 if (at_r || at_b) {
-                    float s = dev::fadd(dev::fadd(dev::fadd(cd(sx - 1, sy - 1), cd(sx + 1, sy - 1)), cd(sx - 1, sy + 1)),
-                                        cd(sx + 1, sy + 1));
-                    float other = dev::fadd(g, dev::fmul(s, 0.25f));
-                    if (at_r) { Rf = (float)BAY(sx, sy); Bf = other; } else { Bf = (float)BAY(sx, sy); Rf = other; }
+                    float sum = dev::fadd(dev::fadd(dev::fadd(cd(sx - 1, sy - 1), cd(sx + 1, sy - 1)), cd(sx - 1, sy + 1)),
+                                          cd(sx + 1, sy + 1));
+                    float other = dev::fadd(g, dev::fmul(sum, 0.25f));
+                    if (at_r) { Rf = (float)BAYV(sx, sy); Bf = other; } else { Bf = (float)BAYV(sx, sy); Rf = other; }
                 } else {
                     float hz = dev::fadd(cd(sx - 1, sy), cd(sx + 1, sy));
                     float vt = dev::fadd(cd(sx, sy - 1), cd(sx, sy + 1));
@@ -271,27 +626,156 @@ __device__ void process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             }
             R = dev::round_plane(Rf, mv); Gv = dev::round_plane(g, mv); B = dev::round_plane(Bf, mv);
         }
-        dev::rgb_tail(fp, R, Gv, B);
-        uint8_t* o = sm.out + r * G::OUT_PITCH + c * 3 * bpc;
-        if (fp.out_format == 0) {
-            o[0] = __ldg(fp.tone8 + R); o[1] = __ldg(fp.tone8 + Gv); o[2] = __ldg(fp.tone8 + B);
-        } else if (bpc == 1) {
-            o[0] = (uint8_t)R; o[1] = (uint8_t)Gv; o[2] = (uint8_t)B;
-        } else {
-            o[0] = (uint8_t)R; o[1] = (uint8_t)(R >> 8); o[2] = (uint8_t)Gv;
-            o[3] = (uint8_t)(Gv >> 8); o[4] = (uint8_t)B; o[5] = (uint8_t)(B >> 8);
+    };
+
+    // ---- 5. demosaic + RGB WB/CCM + tone for own pairs -> output staging ---------------------
+    uint8_t* outs = sm.regB;
+    const int bpc = fp.out_bpc;
+    const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
+    const bool border_tile = x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2;
+    const bool ccm_on = (fp.stages & 16u) != 0;
+    const bool wb_rgb = (fp.stages & 8u) && fp.stage_order == 1;
+    {
+        const int nbk = (tpw + 31) >> 5;
+        for (int item = warp; item < nbk * th; item += 8) {
+            int blk, r;
+            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+            int pc = blk * 32 + lane;
+            if (pc >= tpw) continue;
+            int y = y0 + r, x = x0 + 2 * pc;
+            int R0, G0, B0, R1, G1, B1;
+            if (!border_tile && fp.demosaic != DM_MG) {
+                const bool rrow = (y & 1) == po.r_row;
+                const int rbh = rrow ? po.r_col : po.b_col;  // sample of the pair at the red/blue site
+                const int xr = x + rbh, xg = x + 1 - rbh;
+                const int* br = sm.bay + (r + 3) * G::BW + (xr - xb);  // red/blue site
+                const int* bg = sm.bay + (r + 3) * G::BW + (xg - xb);  // green site
+                int own, gq, oq, gg, hz, vt;  // R/B site: own, green, other; G site: green, horizontal, vertical
+                if (fp.demosaic == DM_HQLI) {
+                    // detail::hqli_core (src/algorithms/interp_core.hpp:39-65)
+                    int n4 = br[-1] + br[1] + br[-G::BW] + br[G::BW];
+                    int d4 = br[-G::BW - 1] + br[-G::BW + 1] + br[G::BW - 1] + br[G::BW + 1];
+                    own = min(br[0], mv);
+                    gq = min((n4 + 2) / 4, mv);
+                    oq = min((d4 + 2) / 4, mv);
+                    gg = min(bg[0], mv);
+                    hz = min((bg[-1] + bg[1] + 1) / 2, mv);
+                    vt = min((bg[-G::BW] + bg[G::BW] + 1) / 2, mv);
+                } else {
+                    // AMAZE colour differences (src/algorithms/common.hpp:142-199, amaze.cpp:62-114).
+                    // Red/blue site xr: the other colour from the four diagonals, the red/blue sites of
+                    // rows y-1, y+1 at columns xr-1, xr+1.  Green site xg: horizontal neighbours are
+                    // this row's red/blue sites, vertical ones those of rows y-1, y+1.
+                    const float* gr = green + (r + 1) * G::GPW + (pc + 1);  // this pair row's R/B green
+                    // pair offsets of columns xr-1 / xr+1 (diagonals) and xg-1 / xg+1 (horizontal)
+                    const int pa = rbh ? 0 : -1, pl = rbh ? -1 : 0;
+                    float g_rb = gr[0];
+                    float c00 = dev::fsub((float)br[-G::BW - 1], gr[-G::GPW + pa]);
+                    float c01 = dev::fsub((float)br[-G::BW + 1], gr[-G::GPW + pa + 1]);
+                    float c10 = dev::fsub((float)br[G::BW - 1], gr[G::GPW + pa]);
+                    float c11 = dev::fsub((float)br[G::BW + 1], gr[G::GPW + pa + 1]);
+                    float sum = dev::fadd(dev::fadd(dev::fadd(c00, c01), c10), c11);
+                    float fown = (float)br[0], fgq = (float)bg[0];
+                    float2 hv = dev::fadd2(make_float2(dev::fsub((float)bg[-1], gr[pl]), dev::fsub((float)bg[-G::BW], gr[-G::GPW])),
+                                           make_float2(dev::fsub((float)bg[1], gr[pl + 1]), dev::fsub((float)bg[G::BW], gr[G::GPW])));
+                    // x*0.5 and x*0.25 are exact, so these multiply-adds round once either way
+                    float other = dev::fadd(g_rb, dev::fmul(sum, 0.25f));
+                    float2 rb2 = dev::fadd2(make_float2(fgq, fgq), make_float2(dev::fmul(hv.x, 0.5f), dev::fmul(hv.y, 0.5f)));
+                    own = dev::round_plane(fown, mv);
+                    oq = dev::round_plane(other, mv);
+                    gq = dev::round_plane(g_rb, mv);
+                    gg = dev::round_plane(fgq, mv);
+                    hz = dev::round_plane(rb2.x, mv);
+                    vt = dev::round_plane(rb2.y, mv);
+                }
+                // red/blue site: R,B = own/other by row; green site: R,B = horizontal/vertical by row
+                int rr_rb = rrow ? own : oq, bb_rb = rrow ? oq : own;
+                int rr_g = rrow ? hz : vt, bb_g = rrow ? vt : hz;
+                if (rbh == 0) { R0 = rr_rb; G0 = gq; B0 = bb_rb; R1 = rr_g; G1 = gg; B1 = bb_g; }
+                else { R1 = rr_rb; G1 = gq; B1 = bb_rb; R0 = rr_g; G0 = gg; B0 = bb_g; }
+            } else {
+                int sx, sy;
+                dev::border_source(x, y, W, H, fp.border_mode, sx, sy);
+                demosaic_at(sx, sy, R0, G0, B0);
+                dev::border_source(x + 1, y, W, H, fp.border_mode, sx, sy);
+                demosaic_at(sx, sy, R1, G1, B1);
+            }
+            // RGB-domain white balance (reference call order), CCM: scalar products, packed sums
+            if (wb_rgb) {
+                float2 t;
+                t = dev::fadd2(make_float2(dev::fmul((float)R0, fp.wb_rgb[0]), dev::fmul((float)R1, fp.wb_rgb[0])), h5);
+                R0 = u16q(t.x, mv); R1 = u16q(t.y, mv);
+                t = dev::fadd2(make_float2(dev::fmul((float)G0, fp.wb_rgb[1]), dev::fmul((float)G1, fp.wb_rgb[1])), h5);
+                G0 = u16q(t.x, mv); G1 = u16q(t.y, mv);
+                t = dev::fadd2(make_float2(dev::fmul((float)B0, fp.wb_rgb[2]), dev::fmul((float)B1, fp.wb_rgb[2])), h5);
+                B0 = u16q(t.x, mv); B1 = u16q(t.y, mv);
+            }
+            if (ccm_on) {
+                const float* m = fp.ccm;
+                const float r0 = (float)R0, r1 = (float)R1, g0 = (float)G0, g1 = (float)G1, b0 = (float)B0, b1 = (float)B1;
+                // ((m0*r + m1*g) + m2*b) + 0.5 for both samples, each product rounded on its own
+                float2 ro = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[0], r0), dev::fmul(m[0], r1)),
+                                                             make_float2(dev::fmul(m[1], g0), dev::fmul(m[1], g1))),
+                                                  make_float2(dev::fmul(m[2], b0), dev::fmul(m[2], b1))), h5);
+                float2 go = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[3], r0), dev::fmul(m[3], r1)),
+                                                             make_float2(dev::fmul(m[4], g0), dev::fmul(m[4], g1))),
+                                                  make_float2(dev::fmul(m[5], b0), dev::fmul(m[5], b1))), h5);
+                float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[6], r0), dev::fmul(m[6], r1)),
+                                                             make_float2(dev::fmul(m[7], g0), dev::fmul(m[7], g1))),
+                                                  make_float2(dev::fmul(m[8], b0), dev::fmul(m[8], b1))), h5);
+                // (int)(v + 0.5) clamped to [0, mv]: truncation saturating at 0, then min
+                R0 = u16q(ro.x, mv); R1 = u16q(ro.y, mv);
+                G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
+                B0 = u16q(bo.x, mv); B1 = u16q(bo.y, mv);
+            }
+            int g0 = (y * W + x0) * 3 * bpc;
+            int shift = (int)((out_base + (uintptr_t)g0) & 15);
+            uint8_t* q = outs + r * G::OUT_PITCH + shift + 2 * pc * 3 * bpc;
+            const bool has1 = x + 1 < x0 + tw;
+            if (fp.out_format == 0) {
+                const uint8_t* tt = tone_smem ? sm.tone8 : fp.tone8;
+                int t0 = tt[R0], t1 = tt[G0], t2 = tt[B0];
+                if (((shift & 1) == 0) && has1) {
+                    int t3 = tt[R1], t4 = tt[G1], t5 = tt[B1];
+                    uint16_t* q16 = reinterpret_cast<uint16_t*>(q);
+                    q16[0] = (uint16_t)(t0 | (t1 << 8));
+                    q16[1] = (uint16_t)(t2 | (t3 << 8));
+                    q16[2] = (uint16_t)(t4 | (t5 << 8));
+                } else {
+                    q[0] = (uint8_t)t0; q[1] = (uint8_t)t1; q[2] = (uint8_t)t2;
+                    if (has1) { q[3] = tt[R1]; q[4] = tt[G1]; q[5] = tt[B1]; }
+                }
+            } else if (bpc == 1) {
+                q[0] = (uint8_t)R0; q[1] = (uint8_t)G0; q[2] = (uint8_t)B0;
+                if (has1) { q[3] = (uint8_t)R1; q[4] = (uint8_t)G1; q[5] = (uint8_t)B1; }
+            } else {
+                int v[6] = {R0, G0, B0, R1, G1, B1};
+                for (int k = 0; k < (has1 ? 6 : 3); k++) { q[2 * k] = (uint8_t)v[k]; q[2 * k + 1] = (uint8_t)(v[k] >> 8); }
+            }
         }
     }
     __syncthreads();
 
-    // ---- 6. write the tile rows (3*bpc*tw contiguous bytes per row) ------------------------
-    const int rowbytes = tw * 3 * bpc;
-    for (int i = tid; i < rowbytes * th; i += kThreads) {
-        int r = i / rowbytes, b = i - r * rowbytes;
-        size_t goff = ((size_t)(y0 + r) * W + x0) * 3 * bpc + b;
-        fp.out[goff] = sm.out[r * G::OUT_PITCH + b];
+    // ---- 6. store: 16-byte vector stores on the output's own 16-byte grid --------------------
+    const int len = tw * 3 * bpc;
+    constexpr int CH = G::OUT_PITCH / 16;
+    for (int s = tid; s < G::THM * CH; s += kThreads) {
+        int r = s / CH, k = s - r * CH;
+        if (r >= th) continue;
+        int g0 = ((y0 + r) * W + x0) * 3 * bpc;
+        int shift = (int)((out_base + (uintptr_t)g0) & 15);
+        int lo = 16 * k, hi = lo + 16;  // staging bytes [lo, hi) <-> output bytes g0 - shift + [lo, hi)
+        if (hi <= shift || lo >= shift + len) continue;
+        const uint8_t* src = outs + r * G::OUT_PITCH;
+        uint8_t* dst = fp.out + g0 - shift;
+        if (lo >= shift && hi <= shift + len) {
+            ptx::st_global_v4(dst + lo, *reinterpret_cast<const uint4*>(src + lo));
+        } else {
+            for (int qq = max(lo, shift); qq < min(hi, shift + len); qq++) dst[qq] = src[qq];
+        }
     }
     __syncthreads();
+    return true;
 }
 
 }  // namespace imop
