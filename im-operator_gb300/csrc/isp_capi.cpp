@@ -252,10 +252,9 @@ int device_ready() {
 }
 
 // Expand validated ImopIspParams into a FrameParams whose table pointers refer to `tabs`.
-int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp, cudaStream_t st) {
-    int rc = validate_params(p);
-    if (rc) return rc;
-    if (!device_ready()) return fail(IMOP_ERR_NO_DEVICE, "no CUDA device");
+// Scalar expansion of validated parameters into FrameParams (no device or host allocation);
+// table pointers are left null for the caller to fill.
+void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
     std::memset(&fp, 0, sizeof(fp));
     fp.w = p->width;
     fp.h = p->height;
@@ -294,6 +293,31 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
         fp.dpc_thr = (int)(t * (float)fp.mv);
         fp.thr2 = (uint32_t)fp.dpc_thr | ((uint32_t)fp.dpc_thr << 16);
     }
+    fp.lsc_mode = (p->lsc_mode == IMOP_LSC_POLYNOMIAL) ? 1 : 0;
+    if ((p->stages & IMOP_STAGE_LENS_SHADING) && p->lsc_mode == IMOP_LSC_POLYNOMIAL) {
+        for (int c = 0; c < 4; c++)
+            for (int k = 0; k < 3; k++) fp.poly[c][k] = p->lsc_poly[c][k];
+        // src/lens_shading/polynomial.cpp:25-27
+        fp.lsc_cx = p->lsc_center[0] * (float)fp.w;
+        fp.lsc_cy = p->lsc_center[1] * (float)fp.h;
+        fp.lsc_max_r = std::sqrt(fp.lsc_cx * fp.lsc_cx + fp.lsc_cy * fp.lsc_cy);
+    }
+    fp.wb_cfa[0] = p->wb_gain[0];
+    fp.wb_cfa[1] = p->wb_gain[1];
+    fp.wb_cfa[2] = p->wb_gain[1];
+    fp.wb_cfa[3] = p->wb_gain[2];
+    for (int i = 0; i < 3; i++) fp.wb_rgb[i] = p->wb_gain[i];
+    for (int i = 0; i < 9; i++) fp.ccm[i] = p->ccm[i];
+    fp.need_align = (fp.bd > 8 && fp.bd < 16 &&
+                     !(p->stages & (IMOP_STAGE_BLACK_LEVEL | IMOP_STAGE_LENS_SHADING)) &&
+                     !((p->stages & IMOP_STAGE_WHITE_BALANCE) && p->stage_order == IMOP_ORDER_BAYER_WB)) ? 1 : 0;
+}
+
+int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp, cudaStream_t st) {
+    int rc = validate_params(p);
+    if (rc) return rc;
+    if (!device_ready()) return fail(IMOP_ERR_NO_DEVICE, "no CUDA device");
+    expand_frame_params(p, fp);
     cudaError_t e;
     if ((p->stages & IMOP_STAGE_DEFECT) && p->dpc_mode == IMOP_DPC_MAP_BASED) {
         HostMapPlan P;
@@ -316,16 +340,8 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
     } else {
         tabs.plan.n_comp = 0;
     }
-    fp.lsc_mode = (p->lsc_mode == IMOP_LSC_POLYNOMIAL) ? 1 : 0;
     if (p->stages & IMOP_STAGE_LENS_SHADING) {
-        if (p->lsc_mode == IMOP_LSC_POLYNOMIAL) {
-            for (int c = 0; c < 4; c++)
-                for (int k = 0; k < 3; k++) fp.poly[c][k] = p->lsc_poly[c][k];
-            // src/lens_shading/polynomial.cpp:25-27
-            fp.lsc_cx = p->lsc_center[0] * (float)fp.w;
-            fp.lsc_cy = p->lsc_center[1] * (float)fp.h;
-            fp.lsc_max_r = std::sqrt(fp.lsc_cx * fp.lsc_cx + fp.lsc_cy * fp.lsc_cy);
-        } else {
+        if (p->lsc_mode != IMOP_LSC_POLYNOMIAL) {
             std::vector<float> g;
             if (p->lsc_mode == IMOP_LSC_FLAT_FIELD) {
                 rc = flat_field_grid(p->lsc_flat_field, p->lsc_flat_w, p->lsc_flat_h, p->pattern, p->bit_depth, g);
@@ -341,21 +357,12 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
             fp.grid = (const float*)tabs.grid.ptr;
         }
     }
-    fp.wb_cfa[0] = p->wb_gain[0];
-    fp.wb_cfa[1] = p->wb_gain[1];
-    fp.wb_cfa[2] = p->wb_gain[1];
-    fp.wb_cfa[3] = p->wb_gain[2];
-    for (int i = 0; i < 3; i++) fp.wb_rgb[i] = p->wb_gain[i];
-    for (int i = 0; i < 9; i++) fp.ccm[i] = p->ccm[i];
     // AMAZE reciprocal table 1/(1+k), k = 0 .. 3*mv (the largest gradient sum)
     if (p->demosaic == IMOP_DEMOSAIC_AMAZE) {
         if ((e = tabs.rtab.ensure((size_t)(3 * fp.mv + 1) * sizeof(float)))) return cuda_fail(e, "alloc rtab");
         if ((e = launch_recip_table((float*)tabs.rtab.ptr, 3 * fp.mv + 1, st))) return cuda_fail(e, "rtab kernel");
         fp.rtab = (const float*)tabs.rtab.ptr;
     }
-    fp.need_align = (fp.bd > 8 && fp.bd < 16 &&
-                     !(p->stages & (IMOP_STAGE_BLACK_LEVEL | IMOP_STAGE_LENS_SHADING)) &&
-                     !((p->stages & IMOP_STAGE_WHITE_BALANCE) && p->stage_order == IMOP_ORDER_BAYER_WB)) ? 1 : 0;
     // tone table (padded: the kernel reads it in 4-byte words)
     if ((e = tabs.tone8.ensure(std::max<size_t>((size_t)fp.mv + 1, 4096) + 16))) return cuda_fail(e, "alloc tone table");
     fp.tone8 = (const uint8_t*)tabs.tone8.ptr;

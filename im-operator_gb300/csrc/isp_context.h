@@ -40,6 +40,7 @@ int set_error(int code, const char* msg);
 int cuda_fail(cudaError_t e, const char* what);
 int validate_params(const ImopIspParams* p);
 int device_ready();
+void expand_frame_params(const ImopIspParams* p, FrameParams& fp);
 int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp, cudaStream_t st);
 int ensure_fixup(FixupState& fx, int cap);
 void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs);

@@ -188,6 +188,24 @@ int imop_isp_set_tile(imop_isp_t ctx, int tile_w, int tile_h);
 /* Device-side defect-chain statistics of the last run (seeds re-resolved in raster order). */
 int imop_isp_last_stats(imop_isp_t ctx, int* dpc_seeds, int* dpc_overrides);
 
+/* ---- no device allocation ----------------------------------------------------------- */
+/* No counterpart in the reference: the reference's GPU glue allocates per call
+ * (src/gpu_dispatch.cpp:433) or through per-thread workspaces.  This entry point is for callers
+ * that cannot let a library allocate device memory - a loop that owns all device memory through
+ * its own pool, or a real-time loop that cannot afford cudaMalloc / cudaFree stalling the device.
+ * It runs the same fused pipeline as imop_isp_run_device on the caller's device frames and
+ * allocates nothing: its parameter tables and defect-chain scratch live in one file-scope device
+ * array of about 390 KB that every GPU loading the library keeps until exit.  The first call on
+ * each device looks up that array's address (cudaGetSymbolAddress, with the device current); make
+ * that first call before any stream capture begins.  Limits: bit depth <= 12, lens shading by an
+ * explicit grid of at most 64x64 nodes or by polynomial, adaptive defect correction only (no
+ * defect map), and at most 16384 defect-chain seeds per call (IMOP_ERR_CAPACITY beyond).  Other
+ * parameters return IMOP_ERR_UNSUPPORTED before any work.  All calls share the array and each
+ * call resets what must start at zero, so calls that overlap on the GPU (two streams or host
+ * threads at once) race.  The call enqueues on `stream`, waits for it, and returns the device
+ * status. */
+int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d_in, void* d_out, void* stream);
+
 /* ---- synthetic scene (seeded, bit-identical on every host) --------------------------- */
 /* Per CFA channel: 4 random 2-D sinusoids mapped to [lo, hi], shot noise (gain DN/e-) and
  * Gaussian read noise, rounded and clamped; written as u8 (bd <= 8) or u16 LSB-aligned. */
