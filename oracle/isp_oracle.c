@@ -741,6 +741,13 @@ int or_pipeline(const ImopIspParams* p, const void* in, void* out, OracleDumps* 
         or_wb_bayer(bay, w, h, p->pattern, bd, p->wb_gain);
         rgb_copy_fill(dumps->white_balance, bay, n);
     }
+    /* the demosaic reads u16 samples through align_raw_value (include/imop/pixel_utils.hpp:129-137):
+     * a sample above max is taken as MSB-aligned; a no-op once any Bayer stage has clamped */
+    if (bd > 8 && bd < 16) {
+        int mv = or_max_val(bd);
+        for (size_t i = 0; i < n; i++)
+            if (bay[i] > mv) bay[i] = (uint16_t)(bay[i] >> (16 - bd));
+    }
     if (p->demosaic == IMOP_DEMOSAIC_AMAZE) or_demosaic_amaze(bay, rgb, w, h, p->pattern, bd);
     else if (p->demosaic == IMOP_DEMOSAIC_MG) or_demosaic_mg(bay, rgb, w, h, p->pattern, bd);
     else or_demosaic_hqli(bay, rgb, w, h, p->pattern, bd);

@@ -127,3 +127,32 @@ def flat_field_grid(ff, pattern, bd):
     if st:
         raise RuntimeError(f"flat field grid failed: {st}")
     return g
+
+
+# ---- per-stage bindings (the tests pin each restated stage) ------------------------------------
+def stages():
+    """ctypes handles of the oracle's per-stage functions."""
+    L = lib()
+    i = C.c_int
+    L.or_black_level.argtypes = [U16P, i, i, i, i, i, F32P]
+    L.or_dpc_adaptive.argtypes = [U16P, i, i, i, i, C.c_float]
+    L.or_dpc_map.argtypes = [U16P, i, i, i, i, C.c_void_p, i]
+    L.or_lsc_poly.argtypes = [U16P, i, i, i, i, F32P, C.c_float, C.c_float]
+    L.or_lsc_grid.argtypes = [U16P, i, i, i, i, F32P, i, i]
+    L.or_wb_bayer.argtypes = [U16P, i, i, i, i, F32P]
+    for f in (L.or_demosaic_hqli, L.or_demosaic_amaze, L.or_demosaic_mg):
+        f.argtypes = [U16P, U16P, i, i, i, i]
+    L.or_wb_rgb.argtypes = [U16P, i, i, i, F32P]
+    L.or_ccm.argtypes = [U16P, i, i, i, F32P]
+    L.or_unpack.argtypes = [U8P, i, i, i, i, U16P]
+    return L
+
+
+def demosaic(bay, pattern, algo, bd):
+    L = stages()
+    h, w = bay.shape
+    bay = np.ascontiguousarray(bay, np.uint16)
+    out = np.zeros((h, w, 3), np.uint16)
+    fn = {1: L.or_demosaic_hqli, 6: L.or_demosaic_amaze, 2: L.or_demosaic_mg}[algo]
+    fn(bay.ctypes.data_as(U16P), out.ctypes.data_as(U16P), w, h, pattern, bd)
+    return out
