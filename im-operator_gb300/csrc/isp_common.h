@@ -112,6 +112,13 @@ struct FrameParams {
     int* seeds;
     int seed_cap;
     int* status;         // sticky error word (IMOP_ERR_*), 0 when fine
+    // defect-chain fix-up scratch of this frame (heap, sorted override list)
+    int* fix_heap;
+    int* fix_ov_idx;
+    int* fix_ov_val;
+    int* fix_n_ov;
+    int fix_cap;         // entries of fix_heap / fix_ov_*
+    int tiles_x, tiles_y;  // tile grid of this frame
 };
 
 }  // namespace imop

@@ -52,34 +52,86 @@ __global__ void recip_table_kernel(float* out, int n) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// one CTA per tile, tiles in raster order
-template <int TW, int TH, int OUTB>
-__global__ void __launch_bounds__(kThreads) fused_frame_kernel(const __grid_constant__ FrameParams fp, int ntx,
-                                                               int nty) {
-    extern __shared__ __align__(16) uint8_t dsm[];
-    auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
-    tile_init(sm);
-    uint32_t parity = 0;
-    int t = blockIdx.x;
-    int tx = t % ntx, ty = t / ntx;
-    int x0, tw, y0, th;
-    tile_span(fp.w, TW, ntx, tx, x0, tw);
-    tile_span(fp.h, TH, nty, ty, y0, th);
-    process_tile<TW, TH, OUTB>(fp, x0, y0, tw, th, sm, Overrides{nullptr, nullptr, 0}, true, parity);
+// Persistent fused kernel: CTA c takes items c, c + gridDim.x, ... of the launch's (frame, tile)
+// list.  Warp 0 stages the next item into the other raw buffer before the CTA computes the
+// current one, so the copy of tile k+1 overlaps the arithmetic of tile k.
+
+// frame of item `item` (a handful of frames per launch: a linear scan)
+__device__ __forceinline__ int item_frame(const BatchLaunch& bl, int item) {
+    int f = 0;
+    while (f + 1 < bl.n_frames && item >= bl.item_start[f + 1]) f++;
+    return f;
 }
 
-// defect-chain fix-up (adaptive mode), one CTA per frame
+// warp 0: copy the item's frame parameters into slot b and start staging its raw rows
 template <int TW, int TH, int OUTB>
-__global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_constant__ FrameParams fp,
-                                                             FixupScratch fs) {
+__device__ void stage_item(TileSmem<TW, TH, OUTB>& sm, const BatchLaunch& bl, int item, int b) {
+    const int lane = threadIdx.x & 31;
+    const int f = item_frame(bl, item);
+    const FrameParams& src = bl.frames[f];
+    static_assert(sizeof(FrameParams) % 4 == 0, "frame parameters copy as words");
+    const int* s = reinterpret_cast<const int*>(&src);
+    int* d = reinterpret_cast<int*>(&sm.fp[b]);
+    for (int k = lane; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
+    int t = item - bl.item_start[f];
+    int ty = t / src.tiles_x, tx = t - ty * src.tiles_x;
+    int x0, tw, y0, th;
+    tile_span(src.w, TW, src.tiles_x, tx, x0, tw);
+    tile_span(src.h, TH, src.tiles_y, ty, y0, th);
+    __syncwarp();
+    stage_tile(sm, b, x0, y0, tw, th);
+}
+
+template <int TW, int TH, int OUTB>
+__global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_constant__ BatchLaunch bl) {
+    extern __shared__ __align__(16) uint8_t dsm[];
+    auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
+    int item = blockIdx.x;
+    if (item >= bl.n_items) return;
+    tile_init(sm);
+    uint32_t par0 = 0, par1 = 0;
+    const Overrides none{nullptr, nullptr, 0};
+    if (threadIdx.x < 32) stage_item(sm, bl, item, 0);
+    __syncthreads();
+    int b = 0;
+    while (true) {
+        const int next = item + gridDim.x;
+        if (next < bl.n_items && threadIdx.x < 32) stage_item(sm, bl, next, b ^ 1);
+        const FrameParams& fp = sm.fp[b];
+        const bool full = tile_is_full<TW, TH>(fp, sm.tile[b][0], sm.tile[b][1], sm.tile[b][2], sm.tile[b][3]);
+        uint32_t& par = b ? par1 : par0;
+        bool ok = full ? compute_tile<TW, TH, OUTB, true>(sm, b, none, true, par)
+                       : compute_tile<TW, TH, OUTB, false>(sm, b, none, true, par);
+        if (!ok) {
+            // leave no bulk copy in flight into this CTA's shared memory
+            if (next < bl.n_items && (reinterpret_cast<uintptr_t>(sm.fp[b ^ 1].in) & 15) == 0)
+                wait_bar(&sm.bar[b ^ 1], b ? par0 : par1);
+            return;
+        }
+        if (next >= bl.n_items) return;
+        item = next;
+        b ^= 1;
+    }
+}
+
+// defect-chain fix-up (adaptive mode), one CTA per frame of the launch
+template <int TW, int TH, int OUTB>
+__global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
     __shared__ int s_nov;
-    if (*fp.seed_count == 0) return;
+    const FrameParams& gfp = bl.frames[blockIdx.x];
+    if (!((gfp.stages & 2u) && gfp.dpc_mode == 0) || *gfp.seed_count == 0) return;
     tile_init(sm);
+    if (threadIdx.x < 32) {
+        const int* s = reinterpret_cast<const int*>(&gfp);
+        int* d = reinterpret_cast<int*>(&sm.fp[0]);
+        for (int k = threadIdx.x; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
+    }
+    const FixupScratch fs{gfp.fix_heap, gfp.fix_ov_idx, gfp.fix_ov_val, gfp.fix_n_ov, gfp.fix_cap};
     if (threadIdx.x == 0) {
-        GlobalOrig orig{&fp, pattern_offsets(fp.pattern)};
-        s_nov = resolve_chains(fp, orig, fs);
+        GlobalOrig orig{&gfp, pattern_offsets(gfp.pattern)};
+        s_nov = resolve_chains(gfp, orig, fs);
         *fs.n_ov = s_nov;
     }
     __syncthreads();
@@ -90,10 +142,10 @@ __global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_consta
     // 2 of border copies, started on an even column
     for (int k = 0; k < n_ov; k++) {
         int p = fs.ov_idx[k];
-        int x = p % fp.w, y = p / fp.w;
-        int wx0 = max(0, (x - 5) & ~1), wx1 = min(fp.w, x + 6);
-        int wy0 = max(0, y - 5), wy1 = min(fp.h, y + 6);
-        if (!process_tile<TW, TH, OUTB>(fp, wx0, wy0, wx1 - wx0, wy1 - wy0, sm, ov, false, parity)) return;
+        int x = p % gfp.w, y = p / gfp.w;
+        int wx0 = max(0, (x - 5) & ~1), wx1 = min(gfp.w, x + 6);
+        int wy0 = max(0, y - 5), wy1 = min(gfp.h, y + 6);
+        if (!process_tile_sync<TW, TH, OUTB>(sm, wx0, wy0, wx1 - wx0, wy1 - wy0, ov, parity)) return;
     }
 }
 
@@ -159,33 +211,108 @@ cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaS
     return cudaGetLastError();
 }
 
+namespace {
+
+constexpr int kMaxDevices = 64;
+
 template <int OUTB>
-static cudaError_t launch_fused_t(const FrameParams& fp, const FixupScratch& fs, cudaStream_t st) {
-    constexpr size_t smem = sizeof(TileSmem<kTileW, kTileH, OUTB>);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(fused_frame_kernel<kTileW, kTileH, OUTB>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(dpc_fixup_kernel<kTileW, kTileH, OUTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+struct FusedKernels {
+    static constexpr size_t smem = sizeof(TileSmem<kTileW, kTileH, OUTB>);
+    // dynamic shared memory opt-in and resident CTAs per SM, once per device
+    static int ctas_per_sm[kMaxDevices];
+    static int sms[kMaxDevices];
+    static cudaError_t setup(int& grid_limit) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        if (!ctas_per_sm[dev]) {
+            e = cudaFuncSetAttribute(fused_batch_kernel<kTileW, kTileH, OUTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(dpc_fixup_kernel<kTileW, kTileH, OUTB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int n = 0, m = 0;
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_batch_kernel<kTileW, kTileH, OUTB>, kThreads,
+                                                                  smem);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            sms[dev] = m;
+            ctas_per_sm[dev] = n > 0 ? n : 1;
+        }
+        grid_limit = sms[dev] * ctas_per_sm[dev];
+        return cudaSuccess;
     }
-    int ntx, nty;
-    int n = fused_tile_grid(fp.w, fp.h, ntx, nty);
-    fused_frame_kernel<kTileW, kTileH, OUTB><<<n, kThreads, smem, st>>>(fp, ntx, nty);
-    if ((fp.stages & 2u) && fp.dpc_mode == 0) dpc_fixup_kernel<kTileW, kTileH, OUTB><<<1, kThreads, smem, st>>>(fp, fs);
-    return cudaGetLastError();
+    static cudaError_t launch(const BatchLaunch& bl, bool fixup, cudaStream_t st) {
+        int limit = 0;
+        cudaError_t e = setup(limit);
+        if (e != cudaSuccess) return e;
+        int grid = bl.n_items < limit ? bl.n_items : limit;
+        if (grid > 0) fused_batch_kernel<kTileW, kTileH, OUTB><<<grid, kThreads, smem, st>>>(bl);
+        if (fixup) dpc_fixup_kernel<kTileW, kTileH, OUTB><<<bl.n_frames, kThreads, smem, st>>>(bl);
+        return cudaGetLastError();
+    }
+};
+template <int OUTB> int FusedKernels<OUTB>::ctas_per_sm[kMaxDevices] = {};
+template <int OUTB> int FusedKernels<OUTB>::sms[kMaxDevices] = {};
+
+cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st) {
+    BatchLaunch bl;
+    bl.n_frames = n;
+    int items = 0;
+    bool fixup = false;
+    for (int f = 0; f < n; f++) {
+        FrameParams& fp = frames[f];
+        fp.tiles_x = tiles_along(fp.w, kTileW);
+        fp.tiles_y = tiles_along(fp.h, kTileH);
+        bl.item_start[f] = items;
+        items += fp.tiles_x * fp.tiles_y;
+        bl.frames[f] = fp;
+        fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
+    }
+    bl.item_start[n] = items;
+    bl.n_items = items;
+    return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st) : FusedKernels<3>::launch(bl, fixup, st);
 }
 
-cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st) {
-    if ((fp.stages & 2u) && fp.dpc_mode == 1 && plan) launch_map_resolve(fp, *plan, st);
+}  // namespace
+
+int fused_grid_limit(int out_bpc) {
+    int limit = 0;
+    cudaError_t e = out_bpc == 2 ? FusedKernels<6>::setup(limit) : FusedKernels<3>::setup(limit);
+    return e == cudaSuccess ? limit : 0;
+}
+
+cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st) {
+    // one launch per run of at most kBatchInline frames sharing an output channel width
+    int i = 0;
+    while (i < n) {
+        int j = i + 1;
+        while (j < n && j - i < kBatchInline && frames[j].out_bpc == frames[i].out_bpc) j++;
+        cudaError_t e = launch_batch_group(frames + i, j - i, st);
+        if (e != cudaSuccess) return e;
+        i = j;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_fused(const FrameParams& fp_in, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st) {
+    FrameParams fp = fp_in;
+    fp.fix_heap = fs.heap;
+    fp.fix_ov_idx = fs.ov_idx;
+    fp.fix_ov_val = fs.ov_val;
+    fp.fix_n_ov = fs.n_ov;
+    fp.fix_cap = fs.cap;
+    if ((fp.stages & 2u) && fp.dpc_mode == 1 && plan) {
+        cudaError_t e = launch_map_resolve(fp, *plan, st);
+        if (e != cudaSuccess) return e;
+    }
     if ((fp.stages & 2u) && fp.dpc_mode == 0) {
         cudaError_t e = cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st);
         if (e != cudaSuccess) return e;
     }
-    return fp.out_bpc == 2 ? launch_fused_t<6>(fp, fs, st) : launch_fused_t<3>(fp, fs, st);
+    return launch_batch_group(&fp, 1, st);
 }
 
 }  // namespace imop

@@ -9,7 +9,17 @@ namespace imop {
 
 // nominal fused tile (the last tile of a row / column absorbs a remainder below 4)
 constexpr int kTileW = 120;
-constexpr int kTileH = 32;
+constexpr int kTileH = 24;
+
+// Frames of one fused launch, passed by value as the kernel's parameter block: the persistent
+// kernel walks the (frame, tile) items of all frames, frame after frame, tiles in raster order.
+constexpr int kBatchInline = 16;
+struct BatchLaunch {
+    int n_frames;
+    int n_items;
+    int item_start[kBatchInline + 1];  // first item of each frame; item_start[n_frames] = n_items
+    FrameParams frames[kBatchInline];
+};
 
 // device scratch of the defect-chain fix-up
 struct FixupScratch {
@@ -38,6 +48,12 @@ cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots
 cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st);
 // map resolve (map mode) + seed reset + fused tiles + fix-up, in stream order
 cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st);
+// Up to kBatchInline frames in one persistent launch plus one fix-up launch.  Each frame carries
+// its own seed counter, seed list and fix-up scratch (FrameParams::fix_*); its seed counter must be
+// zero and its map-mode values resolved when the launch runs.  tiles_x / tiles_y are filled in.
+cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st);
+// CTAs of the persistent fused kernel on the current device (SMs x resident CTAs per SM)
+int fused_grid_limit(int out_bpc);
 
 // plain per-operator form: one kernel per stage over full frames in device memory.
 // Buffers: bayer_a/bayer_b are w*h u16, rgb is w*h*3 u16.

@@ -1,20 +1,27 @@
 // isp_tile.cuh - one output tile of the fused RAW->RGB pipeline (sm_103a).
 //
 // A CTA of 256 threads owns a tw x th tile of output pixels and works on horizontal pixel pairs
-// (x even, x+1): one 32-bit word of two u16 samples.  In every Bayer row a pair holds exactly one
-// green and one red/blue site, so the demosaic code is the same for every thread (no CFA-colour
-// divergence), and the integer stages run as 16-bit SIMD on the pair word.
+// (x even, x+1).  In every Bayer row a pair holds exactly one green and one red/blue site, so the
+// demosaic code is the same for every thread (no CFA-colour divergence).
 //
 //   stage   region (radius around the tile)   storage
-//   raw     rows +-5, columns +-6            bytes, one 1-D TMA bulk copy per row (mbarrier)
-//   orig    rows +-5, columns +-6            u16x2: unpacked, black-levelled
-//   bay     rows +-3, columns +-4            u16x2: defect-corrected (Jacobi), lens shading, WB
+//   raw     rows +-5, columns +-6            bytes, one 1-D TMA bulk copy per row (mbarrier);
+//                                            two buffers, so the next tile is staged while this
+//                                            one is computed
+//   orig    rows +-5, columns +-6            int per pixel: unpacked, black-levelled
+//   bay     rows +-3, columns +-4            int per pixel: defect-corrected (Jacobi), LSC, WB
 //   green   rows +-1, columns +-2            f32 per pair: green at the pair's red/blue site
+//                                            (in the tile's raw buffer, free after unpacking)
 //   out     the tile                         bytes, shifted to the output's 16-byte phase
+//                                            (in the orig plane, free after the seed check)
 //
 // Output (x,y) needs demosaic inputs within 1 (HQLI) or, through green, 3 pixels (AMAZE, MG);
 // defect correction reads 2 more.  Border pixels copy from pixels at most 2 away (border_source),
 // which lie in the same tile because every tile is at least 4 pixels wide and high.
+//
+// Tiles whose whole apron lies inside the frame with margin take a specialisation (FULL) with
+// compile-time extents and no bounds checks; frame-edge tiles, ragged last tiles and the defect
+// fix-up windows take the general path.
 #pragma once
 
 #include "isp_device.cuh"
@@ -81,34 +88,37 @@ struct TileGeom {
     static constexpr int GPW = TWP + 2, GRH = THM + 2;
     static constexpr int RAW_PITCH = round16(4 * OPW + 32);
     static constexpr int OUT_PITCH = round16(TWM * OUTB + 16);
-    static constexpr int A_BYTES = cmax(ORH * RAW_PITCH, GRH * GPW * 4);
+    static constexpr int RAW_BYTES = cmax(ORH * RAW_PITCH, GRH * GPW * 4);
     static constexpr int B_BYTES = cmax(ORH * OW * 4, THM * OUT_PITCH);
+    // region extents of a full (nominal) tile, in pairs / rows
+    static constexpr int F_OPW = (TW + 13) / 2, F_OH = TH + 10;
+    static constexpr int F_BPW = (TW + 9) / 2, F_BH = TH + 6;
+    static constexpr int F_GPW = (TW + 5) / 2, F_GH = TH + 2;
+    static constexpr int F_TPW = (TW + 1) / 2;
 };
 
 template <int TW, int TH, int OUTB>
 struct TileSmem {
     using G = TileGeom<TW, TH, OUTB>;
-    alignas(16) uint8_t regA[G::A_BYTES];   // raw staging, then green at red/blue sites
-    alignas(16) uint8_t regB[G::B_BYTES];   // orig samples (int per pixel), then output staging
-    alignas(16) int bay[G::BRH * G::BW];    // samples after defect correction, lens shading, WB
-    alignas(16) uint8_t tone8[4096];        // tone table (bit depth <= 12)
-    uint8_t mod[G::BRH * G::BPW];           // bit h: pixel h of the pair was corrected
-    int row_a0[G::ORH];                     // staged byte window [a0, a0 + len) of each raw row
-    int row_len[G::ORH];
-    int row_base[G::ORH];                   // staged offset of the region's first pair, or -1
+    alignas(16) uint8_t raw[2][G::RAW_BYTES];  // raw staging; green of the computed tile reuses it
+    alignas(16) uint8_t regB[G::B_BYTES];      // orig samples (int per pixel), then output staging
+    alignas(16) int bay[G::BRH * G::BW];       // samples after defect correction, lens shading, WB
+    alignas(16) uint8_t tone8[4096];           // tone table (bit depth <= 12)
+    alignas(16) FrameParams fp[2];             // parameters of the frame of each staged tile
+    uint8_t mod[G::BRH * G::BPW];              // bit h: pixel h of the pair was corrected
+    int row_a0[2][G::ORH];                     // staged byte window [a0, a0 + len) of each raw row
+    int row_len[2][G::ORH];
+    int row_base[2][G::ORH];                   // staged offset of the region's first pair, or -1
     int col_gx[2 * G::BPW];
     float col_fx[2 * G::BPW];
     int row_gy[G::BRH];
     float row_fy[G::BRH];
-    alignas(8) uint64_t bar;
+    int tile[2][4];                            // x0, y0, tw, th of each staged tile
+    const uint8_t* tone_src;                   // the tone table held in tone8
+    alignas(8) uint64_t bar[2];
 };
 
-// ---- helpers on pair words --------------------------------------------------------------------
-__device__ __forceinline__ int half_of(uint32_t w, int h) { return h ? (int)(w >> 16) : (int)(w & 0xFFFFu); }
-__device__ __forceinline__ int lo16(uint32_t w) { return (int)(w & 0xFFFFu); }
-__device__ __forceinline__ int hi16(uint32_t w) { return (int)(w >> 16); }
-__device__ __forceinline__ uint32_t pack2(int lo, int hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
-
+// ---- small helpers -----------------------------------------------------------------------------
 // byte range [b0, b1) of pixels [i0, i1) (pixel indices) in the input stream
 __device__ __forceinline__ void pixel_bytes(int fmt, int i0, int i1, int& b0, int& b1) {
     switch (fmt) {
@@ -120,32 +130,30 @@ __device__ __forceinline__ void pixel_bytes(int fmt, int i0, int i1, int& b0, in
 }
 
 // one raw byte of the staged row (or of global memory past the staged window)
-template <class SM>
-__device__ __forceinline__ int staged_byte(const FrameParams& fp, const SM& sm, const uint8_t* row, int r, int off) {
-    int rel = off - sm.row_a0[r];
-    if (rel >= 0 && rel < sm.row_len[r]) return row[rel];
+__device__ __forceinline__ int staged_byte(const FrameParams& fp, int a0, int len, const uint8_t* row, int off) {
+    int rel = off - a0;
+    if (rel >= 0 && rel < len) return row[rel];
     return __ldg(fp.in + off);
 }
 
-// unpacked sample of pixel index i (row r of the staged window); the packed-tail rule of
+// unpacked sample of pixel index i of a staged row; the packed-tail rule of
 // pixel::get_packed_raw (a group ending at or past the buffer end reads 0) is kept
-template <class SM>
-__device__ __forceinline__ int staged_raw(const FrameParams& fp, const SM& sm, const uint8_t* row, int r, int i) {
+__device__ __forceinline__ int staged_raw(const FrameParams& fp, int a0, int len, const uint8_t* row, int i) {
     switch (fp.fmt) {
-        case FMT_U8: return staged_byte(fp, sm, row, r, i);
-        case FMT_U16: return staged_byte(fp, sm, row, r, 2 * i) | (staged_byte(fp, sm, row, r, 2 * i + 1) << 8);
+        case FMT_U8: return staged_byte(fp, a0, len, row, i);
+        case FMT_U16: return staged_byte(fp, a0, len, row, 2 * i) | (staged_byte(fp, a0, len, row, 2 * i + 1) << 8);
         case FMT_P12: {
             int off = (i >> 1) * 3;
             if (off + 2 >= (int)fp.in_bytes) return 0;
-            int b1 = staged_byte(fp, sm, row, r, off + 1);
-            if ((i & 1) == 0) return ((staged_byte(fp, sm, row, r, off) << 4) | (b1 & 0xF)) & fp.mv;
-            return ((staged_byte(fp, sm, row, r, off + 2) << 4) | (b1 >> 4)) & fp.mv;
+            int b1 = staged_byte(fp, a0, len, row, off + 1);
+            if ((i & 1) == 0) return ((staged_byte(fp, a0, len, row, off) << 4) | (b1 & 0xF)) & fp.mv;
+            return ((staged_byte(fp, a0, len, row, off + 2) << 4) | (b1 >> 4)) & fp.mv;
         }
         default: {
             int off = (i >> 2) * 5;
             int sub = i & 3;
             if (off + 4 >= (int)fp.in_bytes) return 0;
-            int b = staged_byte(fp, sm, row, r, off + sub), b4 = staged_byte(fp, sm, row, r, off + 4);
+            int b = staged_byte(fp, a0, len, row, off + sub), b4 = staged_byte(fp, a0, len, row, off + 4);
             return ((b << 2) | ((b4 >> (2 * sub)) & 3)) & fp.mv;
         }
     }
@@ -174,21 +182,30 @@ __device__ __forceinline__ int dpc_scalar(const FrameParams& fp, OrigAt orig, in
     return dev::dpc_apply(orig(x, y), nb, m, fp.dpc_thr);
 }
 
-// bounded wait on the staging barrier; on expiry the tile is abandoned with IMOP_ERR_TIMEOUT
-__device__ __forceinline__ bool wait_stage(const FrameParams& fp, uint64_t* bar, uint32_t parity) {
+// bounded wait on a staging barrier (about a second at most); false when it gave up
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
     for (uint32_t it = 0; it < (1u << 22); it++)
         if (ptx::mbar_try_wait(bar, parity)) return true;
-    atomicExch(fp.status, 103 /* IMOP_ERR_TIMEOUT */);
     return false;
 }
 
 template <int TW, int TH, int OUTB>
 __device__ void tile_init(TileSmem<TW, TH, OUTB>& sm) {
     if (threadIdx.x == 0) {
-        ptx::mbar_init(&sm.bar, 1);
+        ptx::mbar_init(&sm.bar[0], 1);
+        ptx::mbar_init(&sm.bar[1], 1);
         ptx::fence_mbar_init();
+        sm.tone_src = nullptr;
     }
     __syncthreads();
+}
+
+// A tile with the nominal extents whose raw apron, defect apron and demosaic support lie inside
+// the frame with margin (and whose packed rows start on a pair boundary): no bounds checks.
+template <int TW, int TH>
+__device__ __forceinline__ bool tile_is_full(const FrameParams& fp, int x0, int y0, int tw, int th) {
+    const bool even_rows = fp.fmt == FMT_U8 || fp.fmt == FMT_U16 || (fp.w & 1) == 0;
+    return tw == TW && th == TH && x0 >= 8 && y0 >= 8 && x0 + TW + 8 <= fp.w && y0 + TH + 8 <= fp.h && even_rows;
 }
 
 // green value of a pixel inside the green region: the stored red/blue-site green, or the
@@ -208,72 +225,93 @@ struct GreenAt {
 
 __device__ __forceinline__ int u16q(float t, int mv) { return (int)min(__float2uint_rz(t), (unsigned)mv); }
 
-// Process one tile. `parity` is the staging barrier's phase, flipped once per tile.
+// ---- staging (warp 0): row windows of buffer b, bulk copies completing on bar[b] ----------------
+// sm.fp[b] holds the tile's frame parameters.  With an input pointer that is not 16-byte aligned
+// nothing is copied here: compute_tile copies the same windows with plain loads.
 template <int TW, int TH, int OUTB>
-__device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int th, TileSmem<TW, TH, OUTB>& sm,
-                             Overrides ov, bool detect_seeds, uint32_t& parity) {
+__device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, int tw, int th) {
     using G = TileGeom<TW, TH, OUTB>;
+    const FrameParams& fp = sm.fp[b];
+    const int lane = threadIdx.x & 31;
+    const int W = fp.w, H = fp.h;
+    const int xo = x0 - 6, yo = y0 - 5;
+    const int opw = (tw + 13) / 2, oh = th + 10;
+    const int in16 = (int)(fp.in_bytes & ~(size_t)15);
+    const bool bulk_ok = ((reinterpret_cast<uintptr_t>(fp.in) & 15) == 0);
+    uint32_t bytes = 0;
+    for (int r = lane; r < oh; r += 32) {
+        int y = yo + r;
+        int a0 = 0, len = 0, base = -1;
+        if (y >= 0 && y < H) {
+            int xs = max(0, xo), xe = min(W, xo + 2 * opw);
+            int b0, b1;
+            pixel_bytes(fp.fmt, y * W + xs, y * W + xe, b0, b1);
+            b1 = min(b1, (int)fp.in_bytes);
+            a0 = b0 & ~15;
+            int a1 = min((b1 + 15) & ~15, in16);
+            len = max(a1 - a0, 0);
+            int i = y * W + xo;  // pixel index of the region's first pair (may lie left of the frame)
+            switch (fp.fmt) {
+                case FMT_U8: base = i - a0; break;
+                case FMT_U16: base = 2 * i - a0; break;
+                case FMT_P12: base = ((i & 1) == 0) ? 3 * (i >> 1) - a0 : -1; break;
+                default: base = ((i & 1) == 0) ? 5 * (i >> 2) - a0 : -1; break;
+            }
+        }
+        sm.row_a0[b][r] = a0;
+        sm.row_len[b][r] = len;
+        sm.row_base[b][r] = base;
+        bytes += (uint32_t)len;
+    }
+    if (lane == 0) {
+        sm.tile[b][0] = x0;
+        sm.tile[b][1] = y0;
+        sm.tile[b][2] = tw;
+        sm.tile[b][3] = th;
+    }
+    if (!bulk_ok) return;
+    for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+    if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.bar[b], bytes);
+    __syncwarp();
+    for (int r = lane; r < oh; r += 32) {
+        int n = sm.row_len[b][r];
+        if (n > 0) ptx::bulk_g2s(sm.raw[b] + r * G::RAW_PITCH, fp.in + sm.row_a0[b][r], (uint32_t)n, &sm.bar[b]);
+    }
+}
+
+// ---- compute one staged tile (all threads) ------------------------------------------------------
+// `parity` is buffer b's barrier phase, flipped when its bytes are consumed.  Returns false, the
+// same on every thread, when the staged bytes never arrived (the status word is set).
+template <int TW, int TH, int OUTB, bool FULL>
+__device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bool detect_seeds, uint32_t& parity) {
+    using G = TileGeom<TW, TH, OUTB>;
+    const FrameParams& fp = sm.fp[b];
+    const int x0 = sm.tile[b][0], y0 = sm.tile[b][1];
+    const int tw = FULL ? TW : sm.tile[b][2], th = FULL ? TH : sm.tile[b][3];
     const int W = fp.w, H = fp.h, mv = fp.mv;
     const PatternOffsets po = pattern_offsets(fp.pattern);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool dpc_on = (fp.stages & 2u) != 0;
+    const unsigned stages = fp.stages;
+    const bool dpc_on = (stages & 2u) != 0;
     const bool adaptive = dpc_on && fp.dpc_mode == 0;
-    const int xo = x0 - 6, yo = y0 - 5;              // orig region origin (xo even)
-    const int opw = (tw + 13) / 2, oh = th + 10;      // orig region in pairs / rows
-    const int xb = x0 - 4, yb = y0 - 3;               // bay region origin
-    const int bpw = (tw + 9) / 2, bh = th + 6;
-    const int xg0 = x0 - 2, yg0 = y0 - 1;             // green region origin
-    const int gpw = (tw + 5) / 2, gh = th + 2;
-    const int tpw = (tw + 1) / 2;                     // own pairs
+    const int demosaic = fp.demosaic;
+    const int xo = x0 - 6, yo = y0 - 5;  // orig region origin (xo even)
+    const int opw = FULL ? G::F_OPW : (tw + 13) / 2, oh = FULL ? G::F_OH : th + 10;
+    const int xb = x0 - 4, yb = y0 - 3;  // bay region origin
+    const int bpw = FULL ? G::F_BPW : (tw + 9) / 2, bh = FULL ? G::F_BH : th + 6;
+    const int xg0 = x0 - 2, yg0 = y0 - 1;  // green region origin
+    const int gpw = FULL ? G::F_GPW : (tw + 5) / 2, gh = FULL ? G::F_GH : th + 2;
+    const int tpw = FULL ? G::F_TPW : (tw + 1) / 2;  // own pairs
     const bool tone_smem = fp.out_format == 0 && fp.bd <= 12;
+    uint8_t* raw = sm.raw[b];
 
-    // ---- 1. stage raw rows: one 1-D bulk copy per row on a 16-byte aligned window ----------
-    const int in16 = (int)(fp.in_bytes & ~(size_t)15);
-    const bool bulk_ok = ((reinterpret_cast<uintptr_t>(fp.in) & 15) == 0);
-    if (warp == 0) {
-        uint32_t bytes = 0;
-        for (int r = lane; r < oh; r += 32) {
-            int y = yo + r;
-            int a0 = 0, len = 0, base = -1;
-            if (y >= 0 && y < H) {
-                int xs = max(0, xo), xe = min(W, xo + 2 * opw);
-                int b0, b1;
-                pixel_bytes(fp.fmt, y * W + xs, y * W + xe, b0, b1);
-                b1 = min(b1, (int)fp.in_bytes);
-                a0 = b0 & ~15;
-                int a1 = min((b1 + 15) & ~15, in16);
-                len = max(a1 - a0, 0);
-                int i = y * W + xo;  // pixel index of the region's first pair (may lie left of the frame)
-                switch (fp.fmt) {
-                    case FMT_U8: base = i - a0; break;
-                    case FMT_U16: base = 2 * i - a0; break;
-                    case FMT_P12: base = ((i & 1) == 0) ? 3 * (i >> 1) - a0 : -1; break;
-                    default: base = -1; break;
-                }
-            }
-            sm.row_a0[r] = a0;
-            sm.row_len[r] = len;
-            sm.row_base[r] = base;
-            if (bulk_ok) bytes += (uint32_t)len;
-        }
-        if (bulk_ok) {
-            for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
-            ptx::fence_proxy_async_smem();
-            if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.bar, bytes);
-            __syncwarp();
-            for (int r = lane; r < oh; r += 32) {
-                int n = sm.row_len[r];
-                if (n > 0) ptx::bulk_g2s(sm.regA + r * G::RAW_PITCH, fp.in + sm.row_a0[r], (uint32_t)n, &sm.bar);
-            }
-        }
-    }
-    // tone table and lens-shading tables (overlap the copies)
-    if (tone_smem) {
-        int n = fp.mv + 1;
+    // tone table (when the frame's table changed) and lens-shading tables, then the staged bytes
+    if (tone_smem && sm.tone_src != fp.tone8) {
+        int n = mv + 1;
         for (int k = tid * 4; k < n; k += kThreads * 4)
             *reinterpret_cast<uint32_t*>(sm.tone8 + k) = __ldg(reinterpret_cast<const uint32_t*>(fp.tone8 + k));
     }
-    if ((fp.stages & 4u) && fp.lsc_mode == 0) {
+    if ((stages & 4u) && fp.lsc_mode == 0) {
         for (int c = tid; c < 2 * bpw; c += kThreads) {
             int x = min(max(xb + c, 0), W - 1);
             float gx_f = __fdiv_rn(dev::fmul((float)x, (float)(fp.gw - 1)), (float)(W - 1));
@@ -289,36 +327,45 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             sm.row_fy[r] = dev::fsub(gy_f, (float)gy_i);
         }
     }
-    __syncthreads();
-    if (bulk_ok) {
-        if (!wait_stage(fp, &sm.bar, parity)) return false;
+    bool arrived = true;
+    if ((reinterpret_cast<uintptr_t>(fp.in) & 15) == 0) {
+        arrived = wait_bar(&sm.bar[b], parity);
         parity ^= 1u;
     } else {
-        // unaligned input pointer: threads copy the same windows byte by byte
-        for (int r = 0; r < oh; r++) {
-            int n = sm.row_len[r];
-            for (int k = tid; k < n; k += kThreads) sm.regA[r * G::RAW_PITCH + k] = __ldg(fp.in + sm.row_a0[r] + k);
-        }
+        // unaligned input pointer: threads copy the staged windows byte by byte
         __syncthreads();
+        for (int r = 0; r < oh; r++) {
+            int n = sm.row_len[b][r];
+            for (int k = tid; k < n; k += kThreads) raw[r * G::RAW_PITCH + k] = __ldg(fp.in + sm.row_a0[b][r] + k);
+        }
     }
+    if (__syncthreads_or(!arrived)) {
+        if (tid == 0) atomicExch(fp.status, 103 /* IMOP_ERR_TIMEOUT */);
+        return false;
+    }
+    if (tid == 0 && tone_smem) sm.tone_src = fp.tone8;
 
     // ---- 2. unpack + black level -> orig samples (one int per pixel) ------------------------
     int* orig = reinterpret_cast<int*>(sm.regB);
-    const bool bl_on = (fp.stages & 1u) != 0;
-    for (int s = tid; s < G::ORH * G::OPW; s += kThreads) {
-        int r = s / G::OPW, pc = s - r * G::OPW;
-        if (r >= oh || pc >= opw) continue;
+    const bool bl_on = (stages & 1u) != 0;
+    const bool bl_int = fp.bl_int != 0;
+    const int fmt = fp.fmt;
+    constexpr int OPW_LOOP = FULL ? G::F_OPW : G::OPW;
+    constexpr int OH_LOOP = FULL ? G::F_OH : G::ORH;
+    for (int s = tid; s < OH_LOOP * OPW_LOOP; s += kThreads) {
+        int r = s / OPW_LOOP, pc = s - r * OPW_LOOP;
+        if (!FULL && (r >= oh || pc >= opw)) continue;
         int y = yo + r, x = xo + 2 * pc;
         int v0 = 0, v1 = 0;
-        if (y >= 0 && y < H) {
-            const uint8_t* row = sm.regA + r * G::RAW_PITCH;
-            const int base = sm.row_base[r], len = sm.row_len[r];
-            const bool in0 = x >= 0 && x < W, in1 = x + 1 >= 0 && x + 1 < W;
+        if (FULL || (y >= 0 && y < H)) {
+            const uint8_t* row = raw + r * G::RAW_PITCH;
+            const int base = sm.row_base[b][r], len = sm.row_len[b][r];
+            const bool in0 = FULL || (x >= 0 && x < W), in1 = FULL || (x + 1 >= 0 && x + 1 < W);
             bool done = false;
-            if (in0 && in1 && base >= 0) {
-                if (fp.fmt == FMT_P12) {
+            if (FULL || (in0 && in1 && base >= 0)) {
+                if (fmt == FMT_P12) {
                     int off = base + 3 * pc;
-                    if (off >= 0 && off + 3 <= len) {
+                    if (FULL || (off >= 0 && off + 3 <= len)) {
                         int o4 = off & ~3;
                         uint32_t w0 = *reinterpret_cast<const uint32_t*>(row + o4);
                         uint32_t w1 = *reinterpret_cast<const uint32_t*>(row + o4 + 4);
@@ -327,9 +374,9 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                         v1 = (int)(w >> 16);
                         done = true;
                     }
-                } else if (fp.fmt == FMT_U16) {
+                } else if (fmt == FMT_U16) {
                     int off = base + 4 * pc;
-                    if (off >= 0 && off + 4 <= len) {
+                    if (FULL || (off >= 0 && off + 4 <= len)) {
                         uint32_t w = ((off & 3) == 0) ? *reinterpret_cast<const uint32_t*>(row + off)
                                                       : (uint32_t)*reinterpret_cast<const uint16_t*>(row + off) |
                                                             ((uint32_t)*reinterpret_cast<const uint16_t*>(row + off + 2) << 16);
@@ -337,22 +384,33 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                         v1 = (int)(w >> 16);
                         done = true;
                     }
-                } else if (fp.fmt == FMT_U8) {
+                } else if (fmt == FMT_U8) {
                     int off = base + 2 * pc;
-                    if (off >= 0 && off + 2 <= len) {
+                    if (FULL || (off >= 0 && off + 2 <= len)) {
                         v0 = row[off];
                         v1 = row[off + 1];
                         done = true;
                     }
+                } else {
+                    // MIPI RAW10: the pair is sample 0-1 or 2-3 of its 5-byte group
+                    const int i = y * W + x;
+                    const int goff = base + 5 * ((i >> 2) - ((y * W + xo) >> 2));
+                    const int sub = i & 2;
+                    if (FULL || (goff >= 0 && goff + 5 <= len)) {
+                        const int b4 = row[goff + 4];
+                        v0 = (row[goff + sub] << 2) | ((b4 >> (2 * sub)) & 3);
+                        v1 = (row[goff + sub + 1] << 2) | ((b4 >> (2 * sub + 2)) & 3);
+                        done = true;
+                    }
                 }
             }
-            if (!done) {
-                int i = y * W + x;
-                if (in0) v0 = staged_raw(fp, sm, row, r, i);
-                if (in1) v1 = staged_raw(fp, sm, row, r, i + 1);
+            if (!FULL && !done) {
+                const int i = y * W + x, a0 = sm.row_a0[b][r];
+                if (in0) v0 = staged_raw(fp, a0, len, row, i);
+                if (in1) v1 = staged_raw(fp, a0, len, row, i + 1);
             }
             if (bl_on) {
-                if (fp.bl_int) {
+                if (bl_int) {
                     // (int)((float)v - off) == v - off for an integral offset
                     const int p = y & 1;
                     v0 = min(max(v0 - fp.bl_i[p][0], 0), mv);
@@ -362,8 +420,10 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                     v1 = dev::black_level(fp, v1, bayer_color(y, x + 1, po));
                 }
             }
-            if (!in0) v0 = 0;
-            if (!in1) v1 = 0;
+            if (!FULL) {
+                if (!in0) v0 = 0;
+                if (!in1) v1 = 0;
+            }
         }
         *reinterpret_cast<int2*>(orig + r * G::OW + 2 * pc) = make_int2(v0, v1);
     }
@@ -375,12 +435,14 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
     // warp-rows: a warp takes 32 pair columns of one row; with two column blocks every warp
     // keeps one row parity and one column pair, so its colour constants stay in registers
     int local_mod = 0;
-    const bool lsc_grid = (fp.stages & 4u) && fp.lsc_mode == 0;
-    const bool lsc_poly = (fp.stages & 4u) && fp.lsc_mode == 1;
-    const bool wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
+    const bool lsc_grid = (stages & 4u) && fp.lsc_mode == 0;
+    const bool lsc_poly = (stages & 4u) && fp.lsc_mode == 1;
+    const bool wb_bayer = (stages & 8u) && fp.stage_order == 0;
+    const bool need_align = fp.need_align != 0;
+    const int thr = fp.dpc_thr;
     const float2 h5 = make_float2(0.5f, 0.5f);
     {
-        const int nbk = (bpw + 31) >> 5;
+        const int nbk = FULL ? (G::F_BPW + 31) / 32 : (bpw + 31) >> 5;
         int cache_key = -1;
         float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f, WB0 = 1.f, WB1 = 1.f;
         for (int item = warp; item < nbk * bh; item += 8) {
@@ -392,9 +454,9 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             const int* o = orig + (r + 2) * G::OW + (x - xo);
             int2 c = *reinterpret_cast<const int2*>(o);
             int j0 = c.x, j1 = c.y;
-            bool yin = y >= 0 && y < H;
+            const bool yin = FULL || (y >= 0 && y < H);
             if (yin && adaptive) {
-                bool fast = x >= 4 && x + 1 < W - 4 && y >= 4 && y < H - 4;
+                const bool fast = FULL || (x >= 4 && x + 1 < W - 4 && y >= 4 && y < H - 4);
                 if (fast) {
                     int2 n0 = *reinterpret_cast<const int2*>(o - 2 * G::OW - 2);
                     int2 n1 = *reinterpret_cast<const int2*>(o - 2 * G::OW);
@@ -409,7 +471,6 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                     int mn1 = min(min(min(n0.y, n1.y), min(n2.y, n3.y)), min(min(n4.y, n5.y), min(n6.y, n7.y)));
                     int mx1 = max(max(max(n0.y, n1.y), max(n2.y, n3.y)), max(max(n4.y, n5.y), max(n6.y, n7.y)));
                     // |c - median| <= thr is certain when c - min <= thr and max - c <= thr
-                    const int thr = fp.dpc_thr;
                     if (max(c.x - mn0, mx0 - c.x) > thr) {
                         int nb[8] = {n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x};
                         j0 = dev::dpc_apply(c.x, nb, 0xFFu, thr);
@@ -422,7 +483,7 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                     if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) j0 = dpc_scalar(fp, ORIGV, x, y);
                     if (x + 1 >= 2 && x + 1 < W - 2 && y >= 2 && y < H - 2) j1 = dpc_scalar(fp, ORIGV, x + 1, y);
                 }
-                if (ov.n > 0 && y >= 2 && y < H - 2) {
+                if (!FULL && ov.n > 0 && y >= 2 && y < H - 2) {
                     if (x >= 2 && x < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x); if (sv >= 0) j0 = sv; }
                     if (x + 1 >= 2 && x + 1 < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x + 1); if (sv >= 0) j1 = sv; }
                 }
@@ -480,12 +541,14 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                     u0 = u16q(t.x, mv);
                     u1 = u16q(t.y, mv);
                 }
-                if (fp.need_align) {
+                if (need_align) {
                     if (u0 > mv) u0 >>= (16 - fp.bd);
                     if (u1 > mv) u1 >>= (16 - fp.bd);
                 }
-                if (x < 0 || x >= W) u0 = 0;
-                if (x + 1 < 0 || x + 1 >= W) u1 = 0;
+                if (!FULL) {
+                    if (x < 0 || x >= W) u0 = 0;
+                    if (x + 1 < 0 || x + 1 >= W) u1 = 0;
+                }
             }
             *reinterpret_cast<int2*>(sm.bay + r * G::BW + 2 * pc) = make_int2(u0, u1);
         }
@@ -493,7 +556,7 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
     const int any_mod = __syncthreads_or(local_mod);
 
     auto BAYV = [&](int x, int y) -> int { return sm.bay[(y - yb) * G::BW + (x - xb)]; };
-    float* green = reinterpret_cast<float*>(sm.regA);  // one float per pair row: the R/B site
+    float* green = reinterpret_cast<float*>(raw);  // one float per pair row: the R/B site
 
     // ---- 4a. defect-chain seeds among own pixels (only tiles with a corrected pixel) ---------
     if (detect_seeds && adaptive && any_mod) {
@@ -533,8 +596,9 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
     }
 
     // ---- 4b. green at the red/blue site of each pair (AMAZE, MG) ---------------------------
-    if (fp.demosaic != DM_HQLI) {
-        const int nbk = (gpw + 31) >> 5;
+    if (demosaic != DM_HQLI) {
+        const int nbk = FULL ? (G::F_GPW + 31) / 32 : (gpw + 31) >> 5;
+        const float* rtab = fp.rtab;
         for (int item = warp; item < nbk * gh; item += 8) {
             int blk, r;
             if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
@@ -544,12 +608,12 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             int rbh = ((y & 1) == po.r_row) ? po.r_col : po.b_col;
             int x = xg0 + 2 * pc + rbh;
             float g = -1.0f;
-            if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) {
-                const int* b = sm.bay + (r + 2) * G::BW + (x - xb);
-                int cc = b[0], hm1 = b[-1], hp1 = b[1], hm2 = b[-2], hp2 = b[2];
-                int vm1 = b[-G::BW], vp1 = b[G::BW], vm2 = b[-2 * G::BW], vp2 = b[2 * G::BW];
-                if (fp.demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fp.rtab);
+            if (FULL || (x >= 2 && x < W - 2 && y >= 2 && y < H - 2)) {
+                const int* bp = sm.bay + (r + 2) * G::BW + (x - xb);
+                int cc = bp[0], hm1 = bp[-1], hp1 = bp[1], hm2 = bp[-2], hp2 = bp[2];
+                int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
+                if (demosaic == DM_AMAZE) {
+                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
@@ -566,14 +630,14 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
     __syncthreads();
 
     const GreenAt GRNV{green, sm.bay, xg0, yg0, xb, yb, G::GPW, G::BW, W, H, po.r_row, po.r_col, po.b_col,
-                       fp.demosaic == DM_MG};
+                       demosaic == DM_MG};
 
-    // demosaic of one pixel at (sx, sy) (generic path: border tiles, MG and fix-up windows)
+    // demosaic of one pixel at (sx, sy) (general path: border tiles, MG and fix-up windows)
     auto demosaic_at = [&](int sx, int sy, int& R, int& Gv, int& B) {
         bool at_r = ((sy & 1) == po.r_row) && ((sx & 1) == po.r_col);
         bool at_b = ((sy & 1) == po.b_row) && ((sx & 1) == po.b_col);
         R = Gv = B = 0;
-        if (fp.demosaic == DM_HQLI) {
+        if (demosaic == DM_HQLI) {
             // detail::hqli_core (src/algorithms/interp_core.hpp:39-65)
             if (sx >= 2 && sx < W - 2 && sy >= 2 && sy < H - 2) {
                 int n4 = BAYV(sx - 1, sy) + BAYV(sx + 1, sy) + BAYV(sx, sy - 1) + BAYV(sx, sy + 1);
@@ -588,7 +652,7 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
                 }
                 R = min(R, mv); Gv = min(Gv, mv); B = min(B, mv);
             }
-        } else if (fp.demosaic == DM_MG && fp.bd <= 8) {
+        } else if (demosaic == DM_MG && fp.bd <= 8) {
             // integer colour differences (src/algorithms/mg.cpp:74-146)
             int g = (int)GRNV(sx, sy);
             int Ri = 0, Bi = 0;
@@ -632,11 +696,13 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
     uint8_t* outs = sm.regB;
     const int bpc = fp.out_bpc;
     const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
-    const bool border_tile = x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2;
-    const bool ccm_on = (fp.stages & 16u) != 0;
-    const bool wb_rgb = (fp.stages & 8u) && fp.stage_order == 1;
+    const int out_format = fp.out_format;
+    const bool border_tile = !FULL && (x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2);
+    const bool ccm_on = (stages & 16u) != 0;
+    const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
     {
-        const int nbk = (tpw + 31) >> 5;
+        const int nbk = FULL ? (G::F_TPW + 31) / 32 : (tpw + 31) >> 5;
+        const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
         for (int item = warp; item < nbk * th; item += 8) {
             int blk, r;
             if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
@@ -644,14 +710,14 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             if (pc >= tpw) continue;
             int y = y0 + r, x = x0 + 2 * pc;
             int R0, G0, B0, R1, G1, B1;
-            if (!border_tile && fp.demosaic != DM_MG) {
+            if (!border_tile && demosaic != DM_MG) {
                 const bool rrow = (y & 1) == po.r_row;
                 const int rbh = rrow ? po.r_col : po.b_col;  // sample of the pair at the red/blue site
                 const int xr = x + rbh, xg = x + 1 - rbh;
                 const int* br = sm.bay + (r + 3) * G::BW + (xr - xb);  // red/blue site
                 const int* bg = sm.bay + (r + 3) * G::BW + (xg - xb);  // green site
                 int own, gq, oq, gg, hz, vt;  // R/B site: own, green, other; G site: green, horizontal, vertical
-                if (fp.demosaic == DM_HQLI) {
+                if (demosaic == DM_HQLI) {
                     // detail::hqli_core (src/algorithms/interp_core.hpp:39-65)
                     int n4 = br[-1] + br[1] + br[-G::BW] + br[G::BW];
                     int d4 = br[-G::BW - 1] + br[-G::BW + 1] + br[G::BW - 1] + br[G::BW + 1];
@@ -703,11 +769,11 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             // RGB-domain white balance (reference call order), CCM: scalar products, packed sums
             if (wb_rgb) {
                 float2 t;
-                t = dev::fadd2(make_float2(dev::fmul((float)R0, fp.wb_rgb[0]), dev::fmul((float)R1, fp.wb_rgb[0])), h5);
+                t = dev::fadd2(make_float2(dev::fmul((float)R0, wr), dev::fmul((float)R1, wr)), h5);
                 R0 = u16q(t.x, mv); R1 = u16q(t.y, mv);
-                t = dev::fadd2(make_float2(dev::fmul((float)G0, fp.wb_rgb[1]), dev::fmul((float)G1, fp.wb_rgb[1])), h5);
+                t = dev::fadd2(make_float2(dev::fmul((float)G0, wg), dev::fmul((float)G1, wg)), h5);
                 G0 = u16q(t.x, mv); G1 = u16q(t.y, mv);
-                t = dev::fadd2(make_float2(dev::fmul((float)B0, fp.wb_rgb[2]), dev::fmul((float)B1, fp.wb_rgb[2])), h5);
+                t = dev::fadd2(make_float2(dev::fmul((float)B0, wbl), dev::fmul((float)B1, wbl)), h5);
                 B0 = u16q(t.x, mv); B1 = u16q(t.y, mv);
             }
             if (ccm_on) {
@@ -731,8 +797,8 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             int g0 = (y * W + x0) * 3 * bpc;
             int shift = (int)((out_base + (uintptr_t)g0) & 15);
             uint8_t* q = outs + r * G::OUT_PITCH + shift + 2 * pc * 3 * bpc;
-            const bool has1 = x + 1 < x0 + tw;
-            if (fp.out_format == 0) {
+            const bool has1 = FULL || x + 1 < x0 + tw;
+            if (out_format == 0) {
                 const uint8_t* tt = tone_smem ? sm.tone8 : fp.tone8;
                 int t0 = tt[R0], t1 = tt[G0], t2 = tt[B0];
                 if (((shift & 1) == 0) && has1) {
@@ -774,8 +840,20 @@ __device__ bool process_tile(const FrameParams& fp, int x0, int y0, int tw, int 
             for (int qq = max(lo, shift); qq < min(hi, shift + len); qq++) dst[qq] = src[qq];
         }
     }
+    // this tile's generic reads and writes of its raw buffer come before the bulk copy that
+    // stages a later tile into it
+    ptx::fence_proxy_async_smem();
     __syncthreads();
     return true;
+}
+
+// One tile of frame sm.fp[0] through buffer 0, staged and computed in turn (fix-up windows).
+template <int TW, int TH, int OUTB>
+__device__ bool process_tile_sync(TileSmem<TW, TH, OUTB>& sm, int x0, int y0, int tw, int th, Overrides ov,
+                                  uint32_t& parity) {
+    if (threadIdx.x < 32) stage_tile(sm, 0, x0, y0, tw, th);
+    __syncthreads();
+    return compute_tile<TW, TH, OUTB, false>(sm, 0, ov, false, parity);
 }
 
 }  // namespace imop
