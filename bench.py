@@ -6,8 +6,10 @@ pipeline (BL 256, 0.01 % defects + adaptive correction, 17x13 lens-shading grid,
 CCM, 4096-entry gamma LUT -> RGB8).  The batch is larger than L2 (FRAMES x 55 MB), so no L2 flush
 is needed between steps.
 
-  value       Mpix/s of the fused path with inputs resident in HBM (whole job, all ranks)
-  e2e         the same through the host-buffer API: pinned H2D of each frame, fused kernel, D2H
+  value       Mpix/s of the fused path with inputs resident in HBM (whole job, all ranks): one
+              recorded batch per step (one persistent launch over all frames' tiles)
+  e2e         the same through the host-buffer batch API: pinned frames, copies in / kernels /
+              copies out pipelined over three streams
   roofline    dominant kernel: algorithmic bytes per launch / CUDA-event launch time vs the
               measured HBM copy bandwidth
   plain       the same batch through the plain per-operator kernels (one kernel per stage)
@@ -41,7 +43,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--frames", type=int, default=8, help="frames per step (batch)")
     ap.add_argument("--cpu-sample-frames", type=int, default=4)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operator leg")
     return ap.parse_args()
 
 
@@ -173,14 +177,13 @@ def main():
         run_reference(args)
         return
     world, rank, local = dist_init()
-    import numpy as np
     import torch
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import imop_gb300 as I
-    from imop_gb300 import workloads
+    from imop_gb300 import abi, workloads
 
     pl = workloads.c2_pipeline()
     B = args.frames
@@ -195,86 +198,90 @@ def main():
     isp = I.Isp(pl)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
+    dev_frames = [(None, d_in[i].data_ptr(), d_out[i].data_ptr()) for i in range(B)]
+    host_batch = [(None, h_in[i].data_ptr(), h_out[i].data_ptr()) for i in range(B)]
 
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(B)]
-
-    def step_device(timed_kernels=False):
-        for i in range(B):
-            if timed_kernels:
-                kev[i][0].record(stream)
-            isp.run_device(d_in[i].data_ptr(), d_out[i].data_ptr(), sh)
-            if timed_kernels:
-                kev[i][1].record(stream)
+    def step_device():
+        # one recorded graph per step: seed-counter reset, one persistent launch over all B
+        # frames' tiles, one defect-chain fix-up launch
+        isp.batch_submit(dev_frames, flags=abi.BATCH_GRAPH, stream=sh)
 
     def step_plain():
-        for i in range(B):
-            isp.run_device_plain(d_in[i].data_ptr(), d_out[i].data_ptr(), sh)
-
-    def step_e2e():
-        for i in range(B):
-            d_in[i].copy_(h_in[i], non_blocking=True)
-            isp.run_device(d_in[i].data_ptr(), d_out[i].data_ptr(), sh)
-            h_out[i].copy_(d_out[i], non_blocking=True)
+        isp.batch_submit(dev_frames, flags=abi.BATCH_PLAIN, stream=sh)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    def timed(fn, steps, **kw):
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        kernel_ms = []
-        for _ in range(steps):
-            fn(**kw)
-            if kw.get("timed_kernels"):
-                # per-launch kernel times (events on the launching stream)
-                pass
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        ms = ev0.elapsed_time(ev1)
+    def max_over_ranks(ms):
         if world > 1:
             t = torch.tensor([ms], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             ms = float(t.item())
-        return ms, kernel_ms
+        return ms
 
-    # correctness gate before timing: fused == plain on the batch's first frame
+    def timed(fn, steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(steps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return max_over_ranks(ev0.elapsed_time(ev1))
+
+    # correctness gate before timing: the fused batch equals the plain per-operator batch
     step_device()
-    ref = d_out[0].clone()
-    isp.run_device_plain(d_in[0].data_ptr(), d_out[0].data_ptr(), sh)
+    fused = d_out.clone()
+    step_plain()
     torch.cuda.synchronize()
-    parity_ok = bool(torch.equal(ref, d_out[0]))
+    parity_ok = bool(torch.equal(fused, d_out))
+    isp.sync_status(sh)
 
     for _ in range(args.warmup):
         step_device()
     torch.cuda.synchronize()
-
     with ClockSampler(local) as clk:
-        ms, _ = timed(step_device, args.steps)
-    # per-launch kernel durations (same launches, events bracketing each frame's launch)
+        ms = timed(step_device, args.steps)
+    isp.sync_status(sh)
+    # duration of the dominant launch: the batch without the graph (seed reset, persistent
+    # kernel, fix-up), CUDA events on the launching stream
     launch_ms = []
-    for _ in range(max(1, min(args.steps, 3))):
-        step_device(timed_kernels=True)
+    for _ in range(max(1, min(args.steps, 5))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        isp.batch_submit(dev_frames, stream=sh)
+        e1.record(stream)
         torch.cuda.synchronize()
-        launch_ms += [a.elapsed_time(b) for a, b in kev]
+        launch_ms.append(e0.elapsed_time(e1))
 
-    for _ in range(max(1, args.warmup // 2)):
-        step_e2e()
-    ms_e2e, _ = timed(step_e2e, args.steps)
-    for _ in range(max(1, args.warmup // 2)):
-        step_plain()
-    ms_plain, _ = timed(step_plain, args.steps)
+    ms_e2e = None
+    if not args.no_e2e:
+        # end to end through the host-buffer batch call: pinned frames, copies in, kernels and
+        # copies out pipelined over three device slots; synchronous, so wall-clock timed
+        for _ in range(max(1, args.warmup // 2)):
+            isp.run_host_batch(host_batch)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            isp.run_host_batch(host_batch)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3)
+        barrier()
+    ms_plain = None
+    if not args.no_plain:
+        for _ in range(max(1, args.warmup // 2)):
+            step_plain()
+        ms_plain = timed(step_plain, args.steps)
 
     px_step = B * pl.pixels
     mpix = world * args.steps * px_step / (ms / 1e3) / 1e6
-    mpix_e2e = world * args.steps * px_step / (ms_e2e / 1e3) / 1e6
-    mpix_plain = world * args.steps * px_step / (ms_plain / 1e3) / 1e6
     alg_bytes = in_b + out_b + 4096 * 4 + 17 * 13 * 4 * 4  # per frame: RAW12P in, RGB8 out, LUT, grid
-    per_launch_ms = statistics.mean(launch_ms)
-    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    per_launch_ms = statistics.median(launch_ms)
+    achieved = B * alg_bytes / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
     line = {
@@ -289,17 +296,22 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "gbs_algorithmic": round(world * args.steps * B * alg_bytes / (ms / 1e3) / 1e9, 1),
         "hbm_frac": round(world * args.steps * B * alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
-        "e2e": {"value": round(mpix_e2e, 2), "unit": "Mpix/s", "h2d_bytes_per_step": B * in_b,
-                "d2h_bytes_per_step": B * out_b},
-        "plain": {"value": round(mpix_plain, 2), "unit": "Mpix/s", "ms_per_step": round(ms_plain / args.steps, 4)},
         "fused_equals_plain": parity_ok,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "fused_frame_kernel (+ seed reset and defect-chain fix-up of the same launch)",
-                     "bytes_per_launch": alg_bytes, "launch_ms": round(per_launch_ms, 4)},
-        "gpu_launches": 2 * B * args.steps,
+                     "kernel": "fused_batch_kernel: one persistent launch over the step's frames "
+                               "(timed with its seed reset and defect fix-up launch)",
+                     "bytes_per_launch": B * alg_bytes, "launch_ms": round(per_launch_ms, 4)},
+        "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
+    if ms_e2e is not None:
+        line["e2e"] = {"value": round(world * args.steps * px_step / (ms_e2e / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                       "h2d_bytes_per_step": B * in_b, "d2h_bytes_per_step": B * out_b,
+                       "api": "imop_isp_run_host_batch (pinned host frames)"}
+    if ms_plain is not None:
+        line["plain"] = {"value": round(world * args.steps * px_step / (ms_plain / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                         "ms_per_step": round(ms_plain / args.steps, 4)}
     if rank == 0 and not args.no_cpu:
         rate, done, dt = cpu_oracle_rate(pl, host_frames[: max(1, args.cpu_sample_frames)])
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",

@@ -62,14 +62,7 @@ cudaError_t DevBuf::ensure(size_t bytes) {
 // Unique defect pixels inside [2,w-2)x[2,h-2) become slots (sorted by row, then column); slots
 // that are same-colour neighbours at step 2 (or repeated entries) form components that the
 // device resolves serially in map order.
-struct HostMapPlan {
-    std::vector<int> row_ptr;
-    std::vector<int2> ent;  // (x, slot)
-    std::vector<int2> slot_xy;
-    std::vector<int> comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
-};
-
-static void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan& P) {
+void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan& P) {
     std::vector<std::pair<int, int>> keys;  // (y, x) of entries inside the interior
     std::vector<int> entry_key;             // per map entry: raster index or -1
     for (int i = 0; i < n; i++) {
@@ -139,16 +132,9 @@ static void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, Host
     }
 }
 
-template <class T>
-static cudaError_t upload(DevBuf& b, const std::vector<T>& v) {
-    cudaError_t e = b.ensure(std::max<size_t>(1, v.size()) * sizeof(T));
-    if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-}
-
 // Grid construction of lens_shading::process_flat_field (src/lens_shading/flat_field.cpp:30-76):
 // a parameter derivation done once per set_params, 32 x 24 x 4 gains.
-static int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm) {
+int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm) {
     if (!ff) return fail(IMOP_ERR_NULL_INPUT, "flat-field frame is null");
     if (ffw <= 0 || ffh <= 0) return fail(IMOP_ERR_INVALID_DIMENSIONS, "flat-field dimensions");
     auto rd = [&](int x, int y) -> int {
@@ -313,6 +299,29 @@ void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
                      !((p->stages & IMOP_STAGE_WHITE_BALANCE) && p->stage_order == IMOP_ORDER_BAYER_WB)) ? 1 : 0;
 }
 
+int upload_map_plan(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp) {
+    HostMapPlan P;
+    build_map_plan(p->dpc_map, p->dpc_map_count, p->width, p->height, P);
+    cudaError_t e;
+    if ((e = upload(tabs.map_row_ptr, P.row_ptr)) || (e = upload(tabs.map_ent, P.ent)) ||
+        (e = upload(tabs.slot_xy, P.slot_xy)) || (e = upload(tabs.comp_slot_ptr, P.comp_slot_ptr)) ||
+        (e = upload(tabs.comp_slots, P.comp_slots)) || (e = upload(tabs.comp_ent_ptr, P.comp_ent_ptr)) ||
+        (e = upload(tabs.comp_entries, P.comp_entries)) ||
+        (e = tabs.map_val.ensure(std::max<size_t>(1, P.slot_xy.size()) * sizeof(int))))
+        return cuda_fail(e, "upload defect map");
+    fp.map_row_ptr = (const int*)tabs.map_row_ptr.ptr;
+    fp.map_ent = (const int2*)tabs.map_ent.ptr;
+    fp.map_val = (const int*)tabs.map_val.ptr;
+    tabs.n_slots = (int)P.slot_xy.size();
+    tabs.plan.n_comp = (int)P.comp_slot_ptr.size() - 1;
+    tabs.plan.comp_slot_ptr = (const int*)tabs.comp_slot_ptr.ptr;
+    tabs.plan.comp_slots = (const int*)tabs.comp_slots.ptr;
+    tabs.plan.comp_ent_ptr = (const int*)tabs.comp_ent_ptr.ptr;
+    tabs.plan.comp_entries = (const int*)tabs.comp_entries.ptr;
+    tabs.plan.slot_xy = (const int2*)tabs.slot_xy.ptr;
+    return IMOP_OK;
+}
+
 int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp, cudaStream_t st) {
     int rc = validate_params(p);
     if (rc) return rc;
@@ -320,23 +329,7 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
     expand_frame_params(p, fp);
     cudaError_t e;
     if ((p->stages & IMOP_STAGE_DEFECT) && p->dpc_mode == IMOP_DPC_MAP_BASED) {
-        HostMapPlan P;
-        build_map_plan(p->dpc_map, p->dpc_map_count, fp.w, fp.h, P);
-        if ((e = upload(tabs.map_row_ptr, P.row_ptr)) || (e = upload(tabs.map_ent, P.ent)) ||
-            (e = upload(tabs.slot_xy, P.slot_xy)) || (e = upload(tabs.comp_slot_ptr, P.comp_slot_ptr)) ||
-            (e = upload(tabs.comp_slots, P.comp_slots)) || (e = upload(tabs.comp_ent_ptr, P.comp_ent_ptr)) ||
-            (e = upload(tabs.comp_entries, P.comp_entries)) ||
-            (e = tabs.map_val.ensure(std::max<size_t>(1, P.slot_xy.size()) * sizeof(int))))
-            return cuda_fail(e, "upload defect map");
-        fp.map_row_ptr = (const int*)tabs.map_row_ptr.ptr;
-        fp.map_ent = (const int2*)tabs.map_ent.ptr;
-        fp.map_val = (const int*)tabs.map_val.ptr;
-        tabs.plan.n_comp = (int)P.comp_slot_ptr.size() - 1;
-        tabs.plan.comp_slot_ptr = (const int*)tabs.comp_slot_ptr.ptr;
-        tabs.plan.comp_slots = (const int*)tabs.comp_slots.ptr;
-        tabs.plan.comp_ent_ptr = (const int*)tabs.comp_ent_ptr.ptr;
-        tabs.plan.comp_entries = (const int*)tabs.comp_entries.ptr;
-        tabs.plan.slot_xy = (const int2*)tabs.slot_xy.ptr;
+        if ((rc = upload_map_plan(p, tabs, fp))) return rc;
     } else {
         tabs.plan.n_comp = 0;
     }

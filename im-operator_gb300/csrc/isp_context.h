@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/imop_isp.h"
@@ -28,6 +30,53 @@ struct FrameTables {
     DevBuf grid, lut, knots, tone8, rtab;
     DevBuf map_row_ptr, map_ent, map_val, slot_xy, comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
     MapPlan plan{};
+    int n_slots = 0;  // unique map pixels (entries of map_val)
+};
+
+// map-mode plan built on the host from a defect list
+struct HostMapPlan {
+    std::vector<int> row_ptr;
+    std::vector<int2> ent;  // (x, slot)
+    std::vector<int2> slot_xy;
+    std::vector<int> comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
+};
+
+template <class T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v) {
+    cudaError_t e = b.ensure((v.empty() ? 1 : v.size()) * sizeof(T));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Parameter tables of many parameter sets, one device copy per distinct content (batches).
+struct TableCache {
+    std::unordered_map<uint64_t, std::unique_ptr<DevBuf>> grids, tones;
+    std::unordered_map<uint64_t, std::unique_ptr<FrameTables>> maps;
+    std::unique_ptr<DevBuf> rtab[17];
+    size_t entries() const { return grids.size() + tones.size() + maps.size(); }
+};
+
+// per-frame defect-chain scratch and map values of a batch
+struct BatchScratch {
+    DevBuf seed_count, n_ov, seeds, heap, ov_idx, ov_val, map_val;
+    int frames = 0, cap = 0, map_cap = 0;
+};
+
+// device slots, streams and events of the pipelined host batch
+struct HostPipeline {
+    static constexpr int kSlots = 3;
+    DevBuf d_in[kSlots], d_out[kSlots];
+    cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+    cudaEvent_t in_done[kSlots] = {}, comp_done[kSlots] = {}, out_done[kSlots] = {};
+    bool ready = false;
+    ~HostPipeline();
+};
+
+// a recorded batch and its key
+struct BatchGraph {
+    uint64_t key = 0;
+    cudaGraphExec_t exec = nullptr;
+    ~BatchGraph();
 };
 
 // defect-chain scratch (seeds, heap, overrides) and the sticky status word
@@ -42,6 +91,9 @@ int validate_params(const ImopIspParams* p);
 int device_ready();
 void expand_frame_params(const ImopIspParams* p, FrameParams& fp);
 int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp, cudaStream_t st);
+int upload_map_plan(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp);
+void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan& P);
+int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm);
 int ensure_fixup(FixupState& fx, int cap);
 void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs);
 int take_status(FixupState& fx);
@@ -56,4 +108,10 @@ struct imop_isp_ctx {
     imop::FixupState fix;
     imop::DevBuf d_in, d_out;                      // run_host staging frames
     imop::DevBuf plain_a, plain_b, plain_rgb;      // plain per-operator intermediates
+    imop::TableCache cache;                        // batch parameter tables
+    imop::BatchScratch batch;                      // batch defect-chain scratch
+    imop::HostPipeline pipe;                       // run_host_batch slots and streams
+    imop::BatchGraph graph;                        // last recorded batch
+    cudaStream_t aux = nullptr;                    // table builds and graph capture
+    ~imop_isp_ctx();
 };

@@ -46,6 +46,9 @@ def lib():
             "imop_isp_dump_stages": (i, [vp, vp, sz, C.POINTER(abi.StageDumps)]),
             "imop_isp_set_tile": (i, [vp, i, i]),
             "imop_isp_last_stats": (i, [vp, C.POINTER(i), C.POINTER(i)]),
+            "imop_isp_sync_status": (i, [vp, vp]),
+            "imop_isp_batch_submit": (i, [vp, C.POINTER(abi.FrameDesc), i, C.c_uint, vp]),
+            "imop_isp_run_host_batch": (i, [vp, C.POINTER(abi.FrameDesc), i]),
             "imop_scene_render": (i, [i, i, i, i, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float, vp]),
             "imop_scene_defects": (i, [i, i, C.c_uint64, i, C.POINTER(abi.DefectPoint)]),
             "imop_scene_apply_defects": (i, [vp, i, i, i, C.POINTER(abi.DefectPoint), i]),
@@ -148,6 +151,36 @@ class Isp:
         s, o = C.c_int(), C.c_int()
         check(lib().imop_isp_last_stats(self.h, C.byref(s), C.byref(o)))
         return s.value, o.value
+
+    def sync_status(self, stream=0):
+        check(lib().imop_isp_sync_status(self.h, stream))
+
+    @staticmethod
+    def _descs(frames):
+        """frames: list of (Pipeline or None, input, output); returns the C array and its keep-alive"""
+        keep = []
+        arr = (abi.FrameDesc * max(1, len(frames)))()
+        for k, (pl, inp, out) in enumerate(frames):
+            cp = None
+            if pl is not None:
+                cp = pl.to_c()
+                keep.append(cp)
+            arr[k].params = C.pointer(cp) if cp is not None else None
+            arr[k].inp = _addr(inp)
+            arr[k].out = _addr(out)
+        return arr, keep
+
+    def batch_submit(self, frames, flags=0, stream=0):
+        """Device frames: list of (Pipeline or None, d_in, d_out); asynchronous on `stream`."""
+        arr, keep = self._descs(frames)
+        check(lib().imop_isp_batch_submit(self.h, arr, len(frames), flags, stream))
+        del keep
+
+    def run_host_batch(self, frames):
+        """Host frames: list of (Pipeline or None, input ndarray, output ndarray); synchronous."""
+        arr, keep = self._descs(frames)
+        check(lib().imop_isp_run_host_batch(self.h, arr, len(frames)))
+        del keep
 
 
 # ---- synthetic scenes ---------------------------------------------------------------------------

@@ -72,4 +72,8 @@ class StageDumps(C.Structure):
 
 
 class FrameDesc(C.Structure):
-    _fields_ = [("params", C.POINTER(IspParams)), ("d_in", C.c_void_p), ("d_out", C.c_void_p)]
+    _fields_ = [("params", C.POINTER(IspParams)), ("inp", C.c_void_p), ("out", C.c_void_p)]
+
+
+BATCH_GRAPH = 1
+BATCH_PLAIN = 2

@@ -188,6 +188,39 @@ int imop_isp_set_tile(imop_isp_t ctx, int tile_w, int tile_h);
 /* Device-side defect-chain statistics of the last run (seeds re-resolved in raster order). */
 int imop_isp_last_stats(imop_isp_t ctx, int* dpc_seeds, int* dpc_overrides);
 
+/* Wait for the work this context enqueued on `stream`, then return and clear the sticky device
+ * status (IMOP_ERR_CAPACITY when a defect-chain list overflowed, IMOP_ERR_TIMEOUT when a staging
+ * wait gave up).  The asynchronous entry points do not read it themselves. */
+int imop_isp_sync_status(imop_isp_t ctx, void* stream);
+
+/* ---- batches -------------------------------------------------------------------------- */
+/* Replaces imop::demosaic_cuda_batch (src/algorithms/cuda_dispatch.cpp:150-209), which takes
+ * one size, one format and host pointers; a batch here mixes frame sizes, formats and
+ * parameter sets. */
+typedef struct ImopFrameDesc {
+    const ImopIspParams* params; /* this frame's parameters; NULL = the context's (set_params) */
+    const void* in;              /* input frame  (device memory for batch_submit, host for run_host_batch) */
+    void* out;                   /* output frame (same) */
+} ImopFrameDesc;
+
+enum {
+    IMOP_BATCH_GRAPH = 1, /* record the batch's launches into a CUDA graph once and replay it while
+                             the descriptors (pointers and parameter contents) stay the same */
+    IMOP_BATCH_PLAIN = 2  /* one plain per-operator pipeline per frame (the comparator) */
+};
+
+/* All frames through the persistent fused kernel: one launch per run of up to 16 frames with
+ * the same output channel width, tiles of every frame pulled by the same CTAs, and one defect
+ * fix-up launch.  Parameter tables are uploaded once per distinct content and cached in the
+ * context.  Asynchronous on `stream`; device frames must stay valid until it completes. */
+int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames, int n, unsigned flags, void* stream);
+
+/* Host frames (the drop-in call shape of demosaic_cuda_batch): copies in, fused kernel and
+ * copies out are pipelined over three device slots and three streams, so the transfers of one
+ * frame overlap the kernels of its neighbours.  Page-locked host buffers overlap fully; pageable
+ * ones are copied synchronously by the CUDA runtime.  Synchronous; returns the device status. */
+int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
+
 /* ---- no device allocation ----------------------------------------------------------- */
 /* No counterpart in the reference: the reference's GPU glue allocates per call
  * (src/gpu_dispatch.cpp:433) or through per-thread workspaces.  This entry point is for callers
