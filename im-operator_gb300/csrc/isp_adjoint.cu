@@ -1,0 +1,530 @@
+// isp_adjoint.cu - the differentiable calibration chain on sm_103a: forward render and adjoint.
+//
+// Chain (per pixel, FP32, no rounding between stages; the reference's stage formulas):
+//   b = clamp(raw - bl[c], 0, mv)      l = clamp(b * gain(x, y, c), 0, mv)     u = clamp(l * wb[c], 0, mv)
+//   demosaic(u) -> clamp(., 0, mv) -> o = clamp(M . rgb, 0, mv) -> t = knots lerp at o / mv
+// Demosaic is HQLI or AMAZE (gradient-weighted green at red/blue sites, colour differences with
+// the -1 green sentinel outside [2,w-2)x[2,h-2), border copies from rows / columns 2 and -3).
+//
+// The adjoint recomputes the forward per tile (64 x 16 output pixels; the last tile of a row or
+// column absorbs a remainder below 4 so that every border copy source lies inside its tile) into
+// shared planes: u with a 3-pixel apron, green with a 1-pixel apron.  It back-propagates dL/dt
+// of the tile's own pixels into gradient planes of the same extent (shared atomics), then the
+// green plane into u, then u into the per-pixel parameters.  A u or green sample in the apron
+// holds only the contributions of this tile's outputs; its parameter terms are linear in those
+// contributions, so each tile adds its share and no tile needs another tile's gradients.
+//
+// Parameter gradients: BL, WB, CCM and the loss in registers, tone knots and the lens-shading grid
+// in shared accumulators; each CTA of the persistent grid writes one partial vector and a second
+// kernel adds the partials in CTA order.
+
+#include <cuda_runtime.h>
+
+#include "isp_adjoint.h"
+#include "isp_device.cuh"
+#include "isp_tile.cuh"
+
+namespace imop {
+namespace {
+
+constexpr int kAdjThreads = 256;
+constexpr int kTX = 64, kTY = 16;
+constexpr int kUW = kTX + 3 + 6, kUH = kTY + 3 + 6;  // u region: tile (merged) +- 3
+constexpr int kGW = kTX + 3 + 2, kGH = kTY + 3 + 2;  // green region: tile +- 1
+constexpr int kMaxParams = 16 + 4 * kAdjMaxGridNodes + 33;
+
+struct AdjSmem {
+    float th[kMaxParams];
+    float acc_grid[4 * kAdjMaxGridNodes];
+    float acc_knots[33];
+    float raw[kUH * kUW];
+    float u[kUH * kUW];
+    float gu[kUH * kUW];
+    float G[kGH * kGW];
+    float gG[kGH * kGW];
+    int col_gx[kUW];
+    float col_fx[kUW];
+    int row_gy[kUH];
+    float row_fy[kUH];
+    float red[kAdjThreads / 32][18];
+};
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+__device__ __forceinline__ float inside(float v, float lo, float hi) { return (v > lo && v < hi) ? 1.0f : 0.0f; }
+__device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : (v < 0.0f ? -1.0f : 0.0f); }
+
+struct TileCtx {
+    const AdjFrame* f;
+    PatternOffsets po;
+    int x0, y0, tw, th;
+    int xu, yu;  // u region origin (x0 - 3, y0 - 3)
+    int xg, yg;  // green region origin (x0 - 1, y0 - 1)
+    __device__ int cfa(int x, int y) const { return bayer_color(y, x, po); }
+    __device__ bool at_r(int x, int y) const { return ((y & 1) == po.r_row) && ((x & 1) == po.r_col); }
+    __device__ bool at_b(int x, int y) const { return ((y & 1) == po.b_row) && ((x & 1) == po.b_col); }
+    __device__ bool rb(int x, int y) const { return at_r(x, y) || at_b(x, y); }
+    __device__ int ui(int x, int y) const { return (y - yu) * kUW + (x - xu); }
+    __device__ int gi(int x, int y) const { return (y - yg) * kGW + (x - xg); }
+};
+
+__device__ __forceinline__ float wb_of(const float* th, int c) { return th[4 + (c == 0 ? 0 : (c == 3 ? 2 : 1))]; }
+
+// AMAZE green at a red/blue site from the u plane; parts receive the terms the adjoint needs
+__device__ float amaze_df(const AdjSmem& sm, const TileCtx& t, int x, int y, float* parts) {
+    const float* u = sm.u;
+    int i = t.ui(x, y);
+    float c = u[i], hm1 = u[i - 1], hp1 = u[i + 1], hm2 = u[i - 2], hp2 = u[i + 2];
+    float vm1 = u[i - kUW], vp1 = u[i + kUW], vm2 = u[i - 2 * kUW], vp2 = u[i + 2 * kUW];
+    float lapH = 2.0f * c - hm2 - hp2, lapV = 2.0f * c - vm2 - vp2;
+    float gH = fabsf(hm1 - hp1) + fabsf(lapH), gV = fabsf(vm1 - vp1) + fabsf(lapV);
+    float a = 1.0f / (1.0f + gH), b = 1.0f / (1.0f + gV);
+    float s = a + b;
+    float wh = a / s, wv = b / s;
+    float gh = (hm1 + hp1) * 0.5f + lapH * 0.25f, gv = (vm1 + vp1) * 0.5f + lapV * 0.25f;
+    if (parts) {
+        parts[0] = a; parts[1] = b; parts[2] = wh; parts[3] = wv; parts[4] = gh; parts[5] = gv;
+        parts[6] = sgnf(hm1 - hp1); parts[7] = sgnf(lapH); parts[8] = sgnf(vm1 - vp1); parts[9] = sgnf(lapV);
+    }
+    return wh * gh + wv * gv;
+}
+
+__device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, float v[3]) {
+    const AdjFrame& f = *t.f;
+    const float* u = sm.u;
+    v[0] = v[1] = v[2] = 0.0f;
+    const bool ar = t.at_r(x, y), ab = t.at_b(x, y), rrow = (y & 1) == t.po.r_row;
+    const int i = t.ui(x, y);
+    if (f.demosaic == DM_HQLI) {
+        if (x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) return;
+        float n4 = u[i - 1] + u[i + 1] + u[i - kUW] + u[i + kUW];
+        float d4 = u[i - kUW - 1] + u[i - kUW + 1] + u[i + kUW - 1] + u[i + kUW + 1];
+        if (ar) { v[0] = u[i]; v[1] = n4 * 0.25f; v[2] = d4 * 0.25f; }
+        else if (ab) { v[0] = d4 * 0.25f; v[1] = n4 * 0.25f; v[2] = u[i]; }
+        else {
+            float hz = (u[i - 1] + u[i + 1]) * 0.5f, vt = (u[i - kUW] + u[i + kUW]) * 0.5f;
+            v[1] = u[i];
+            v[0] = rrow ? hz : vt;
+            v[2] = rrow ? vt : hz;
+        }
+        return;
+    }
+    const float* G = sm.G;
+    const int j = t.gi(x, y);
+    float g = G[j];
+    v[1] = g;
+    if (x < 1 || x >= f.w - 1 || y < 1 || y >= f.h - 1) return;
+    if (ar || ab) {
+        float s = (u[i - kUW - 1] - G[j - kGW - 1]) + (u[i - kUW + 1] - G[j - kGW + 1]) +
+                  (u[i + kUW - 1] - G[j + kGW - 1]) + (u[i + kUW + 1] - G[j + kGW + 1]);
+        float other = g + s * 0.25f;
+        if (ar) { v[0] = u[i]; v[2] = other; } else { v[2] = u[i]; v[0] = other; }
+    } else {
+        float hz = (u[i - 1] - G[j - 1]) + (u[i + 1] - G[j + 1]);
+        float vt = (u[i - kUW] - G[j - kGW]) + (u[i + kUW] - G[j + kGW]);
+        v[0] = g + (rrow ? hz : vt) * 0.5f;
+        v[2] = g + (rrow ? vt : hz) * 0.5f;
+    }
+}
+
+__device__ void demosaic_df_back(AdjSmem& sm, const TileCtx& t, int x, int y, const float gv[3]) {
+    const AdjFrame& f = *t.f;
+    float* gu = sm.gu;
+    const bool ar = t.at_r(x, y), ab = t.at_b(x, y), rrow = (y & 1) == t.po.r_row;
+    const int i = t.ui(x, y);
+    if (f.demosaic == DM_HQLI) {
+        if (x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) return;
+        if (ar || ab) {
+            float gown = ar ? gv[0] : gv[2], goth = (ar ? gv[2] : gv[0]) * 0.25f, gg = gv[1] * 0.25f;
+            atomicAdd(&gu[i], gown);
+            atomicAdd(&gu[i - 1], gg); atomicAdd(&gu[i + 1], gg); atomicAdd(&gu[i - kUW], gg); atomicAdd(&gu[i + kUW], gg);
+            atomicAdd(&gu[i - kUW - 1], goth); atomicAdd(&gu[i - kUW + 1], goth);
+            atomicAdd(&gu[i + kUW - 1], goth); atomicAdd(&gu[i + kUW + 1], goth);
+        } else {
+            float ghz = (rrow ? gv[0] : gv[2]) * 0.5f, gvt = (rrow ? gv[2] : gv[0]) * 0.5f;
+            atomicAdd(&gu[i], gv[1]);
+            atomicAdd(&gu[i - 1], ghz); atomicAdd(&gu[i + 1], ghz);
+            atomicAdd(&gu[i - kUW], gvt); atomicAdd(&gu[i + kUW], gvt);
+        }
+        return;
+    }
+    float* gG = sm.gG;
+    const int j = t.gi(x, y);
+    if (x < 1 || x >= f.w - 1 || y < 1 || y >= f.h - 1) {
+        atomicAdd(&gG[j], gv[1]);
+        return;
+    }
+    if (ar || ab) {
+        float goth = ar ? gv[2] : gv[0];
+        atomicAdd(&gu[i], ar ? gv[0] : gv[2]);
+        atomicAdd(&gG[j], gv[1] + goth);
+        float q = goth * 0.25f;
+        atomicAdd(&gu[i - kUW - 1], q); atomicAdd(&gG[j - kGW - 1], -q);
+        atomicAdd(&gu[i - kUW + 1], q); atomicAdd(&gG[j - kGW + 1], -q);
+        atomicAdd(&gu[i + kUW - 1], q); atomicAdd(&gG[j + kGW - 1], -q);
+        atomicAdd(&gu[i + kUW + 1], q); atomicAdd(&gG[j + kGW + 1], -q);
+    } else {
+        float ghz = (rrow ? gv[0] : gv[2]) * 0.5f, gvt = (rrow ? gv[2] : gv[0]) * 0.5f;
+        atomicAdd(&gG[j], gv[0] + gv[1] + gv[2]);
+        atomicAdd(&gu[i - 1], ghz); atomicAdd(&gG[j - 1], -ghz);
+        atomicAdd(&gu[i + 1], ghz); atomicAdd(&gG[j + 1], -ghz);
+        atomicAdd(&gu[i - kUW], gvt); atomicAdd(&gG[j - kGW], -gvt);
+        atomicAdd(&gu[i + kUW], gvt); atomicAdd(&gG[j + kGW], -gvt);
+    }
+}
+
+__device__ __forceinline__ void tile_of(const AdjLaunch& L, int item, int& fi, TileCtx& t) {
+    const AdjFrame& f = L.f;
+    const int per = f.tiles_x * f.tiles_y;
+    fi = item / per;
+    int k = item - fi * per;
+    int ty = k / f.tiles_x, tx = k - ty * f.tiles_x;
+    t.f = &L.f;
+    t.po = pattern_offsets(f.pattern);
+    tile_span(f.w, kTX, f.tiles_x, tx, t.x0, t.tw);
+    tile_span(f.h, kTY, f.tiles_y, ty, t.y0, t.th);
+    t.xu = t.x0 - 3;
+    t.yu = t.y0 - 3;
+    t.xg = t.x0 - 1;
+    t.yg = t.y0 - 1;
+}
+
+// one raw sample of frame f (pixel formats of the product path)
+__device__ __forceinline__ int adj_raw(const AdjFrame& f, const uint8_t* in, int x, int y) {
+    FrameParams fp;
+    fp.w = f.w;
+    fp.mv = f.mv;
+    fp.fmt = f.fmt;
+    fp.in = in;
+    fp.in_bytes = f.in_bytes;
+    return dev::load_raw(fp, x, y);
+}
+
+// forward planes of one tile: raw, u (apron 3), green (apron 1); gradient planes cleared
+template <bool BACKWARD>
+__device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
+    const AdjFrame& f = *t.f;
+    const int tid = threadIdx.x;
+    const float mvf = (float)f.mv;
+    const int uw = t.tw + 6, uh = t.th + 6;
+    for (int c = tid; c < uw; c += kAdjThreads) {
+        int x = min(max(t.xu + c, 0), f.w - 1);
+        // gx = x (gw-1) / (w-1), the apply loop's grid position
+        float gxf = (float)x * (float)(f.gw - 1) / (float)(f.w - 1);
+        int gi = min(max((int)gxf, 0), f.gw - 2);
+        sm.col_gx[c] = gi;
+        sm.col_fx[c] = gxf - (float)gi;
+    }
+    for (int r = tid; r < uh; r += kAdjThreads) {
+        int y = min(max(t.yu + r, 0), f.h - 1);
+        float gyf = (float)y * (float)(f.gh - 1) / (float)(f.h - 1);
+        int gi = min(max((int)gyf, 0), f.gh - 2);
+        sm.row_gy[r] = gi;
+        sm.row_fy[r] = gyf - (float)gi;
+    }
+    __syncthreads();
+    const float* grid = sm.th + 16;
+    for (int s = tid; s < uw * uh; s += kAdjThreads) {
+        int r = s / uw, c = s - r * uw;
+        int x = t.xu + c, y = t.yu + r;
+        int i = r * kUW + c;
+        float rv = 0.0f, uv = 0.0f;
+        if (x >= 0 && x < f.w && y >= 0 && y < f.h) {
+            int cc = t.cfa(x, y);
+            rv = (float)adj_raw(f, in, x, y);
+            float b = clampf(rv - sm.th[cc], 0.0f, mvf);
+            int gx = sm.col_gx[c], gy = sm.row_gy[r];
+            float fx = sm.col_fx[c], fy = sm.row_fy[r];
+            const float* g0 = grid + (gy * f.gw + gx) * 4 + cc;
+            float gain = g0[0] * (1.0f - fx) * (1.0f - fy) + g0[4] * fx * (1.0f - fy) +
+                         g0[4 * f.gw] * (1.0f - fx) * fy + g0[4 * f.gw + 4] * fx * fy;
+            float l = clampf(b * gain, 0.0f, mvf);
+            uv = clampf(l * wb_of(sm.th, cc), 0.0f, mvf);
+        }
+        sm.raw[i] = rv;
+        sm.u[i] = uv;
+        if (BACKWARD) sm.gu[i] = 0.0f;
+    }
+    __syncthreads();
+    if (f.demosaic == DM_AMAZE || BACKWARD) {
+        const int gw = t.tw + 2, gh = t.th + 2;
+        for (int s = tid; s < gw * gh; s += kAdjThreads) {
+            int r = s / gw, c = s - r * gw;
+            int x = t.xg + c, y = t.yg + r;
+            int j = r * kGW + c;
+            float g = -1.0f;
+            if (f.demosaic == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
+                g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
+            sm.G[j] = g;
+            if (BACKWARD) sm.gG[j] = 0.0f;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void tone_df(const float* knots, float o, float mvf, float& t, int& idx, float& frac) {
+    float fi = o / mvf * 32.0f;
+    int k = (int)fi;
+    float fr = fi - (float)k;
+    if (k > 31) { k = 31; fr = 1.0f; }
+    if (k < 0) { k = 0; fr = 0.0f; }
+    idx = k;
+    frac = fr;
+    t = knots[k] * (1.0f - fr) + knots[k + 1] * fr;
+}
+
+struct RegAcc {
+    float bl[4], wb[3], ccm[9], loss;
+};
+
+// forward (+ adjoint) of the tile's own pixels
+template <bool BACKWARD>
+__device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaunch& L, RegAcc& acc) {
+    const AdjFrame& f = *t.f;
+    const float mvf = (float)f.mv;
+    const float* M = sm.th + 7;
+    const float* knots = sm.th + 16 + 4 * f.gw * f.gh;
+    const size_t frame_px = (size_t)f.w * f.h;
+    for (int s = threadIdx.x; s < t.tw * t.th; s += kAdjThreads) {
+        int r = s / t.tw, c = s - r * t.tw;
+        int x = t.x0 + c, y = t.y0 + r;
+        int sx, sy;
+        dev::border_source(x, y, f.w, f.h, f.border_mode, sx, sy);
+        float v[3], rgb[3], pre[3], o[3], tt[3], fr[3];
+        int idx[3];
+        demosaic_df(sm, t, sx, sy, v);
+#pragma unroll
+        for (int k = 0; k < 3; k++) rgb[k] = clampf(v[k], 0.0f, mvf);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            pre[q] = M[3 * q] * rgb[0] + M[3 * q + 1] * rgb[1] + M[3 * q + 2] * rgb[2];
+            o[q] = clampf(pre[q], 0.0f, mvf);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) tone_df(knots, o[k], mvf, tt[k], idx[k], fr[k]);
+        const size_t pi = ((size_t)fi * frame_px + (size_t)y * f.w + x) * 3;
+        if constexpr (!BACKWARD) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) L.rgb_out[pi + k] = tt[k];
+        } else {
+        float gt[3], go[3], grgb[3] = {0.0f, 0.0f, 0.0f}, gv[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float rv = L.ref[pi + k];
+            if (L.mode == 0) {
+                float e = tt[k] - rv;
+                acc.loss += e * e;
+                gt[k] = 2.0f * e;
+            } else {
+                gt[k] = rv;
+                acc.loss += tt[k] * rv;
+            }
+            atomicAdd(&sm.acc_knots[idx[k]], gt[k] * (1.0f - fr[k]));
+            atomicAdd(&sm.acc_knots[idx[k] + 1], gt[k] * fr[k]);
+            go[k] = gt[k] * (knots[idx[k] + 1] - knots[idx[k]]) * 32.0f / mvf;
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            float gp = go[q] * inside(pre[q], 0.0f, mvf);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                acc.ccm[3 * q + j] += gp * rgb[j];
+                grgb[j] += M[3 * q + j] * gp;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) gv[k] = grgb[k] * inside(v[k], 0.0f, mvf);
+        demosaic_df_back(sm, t, sx, sy, gv);
+        }
+    }
+}
+
+// adjoint of the green plane into u, then of u into the per-pixel parameters
+__device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
+    const AdjFrame& f = *t.f;
+    const int tid = threadIdx.x;
+    const float mvf = (float)f.mv;
+    __syncthreads();
+    if (f.demosaic == DM_AMAZE) {
+        const int gw = t.tw + 2, gh = t.th + 2;
+        for (int s = tid; s < gw * gh; s += kAdjThreads) {
+            int r = s / gw, c = s - r * gw;
+            int x = t.xg + c, y = t.yg + r;
+            float g = sm.gG[r * kGW + c];
+            if (g == 0.0f || x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) continue;
+            int i = t.ui(x, y);
+            if (!t.rb(x, y)) {
+                atomicAdd(&sm.gu[i], g);
+                continue;
+            }
+            float P[10];
+            amaze_df(sm, t, x, y, P);
+            float a = P[0], b = P[1], wh = P[2], wv = P[3], gh_ = P[4], gv_ = P[5];
+            float s2 = (a + b) * (a + b);
+            float dgH = -a * a * b * (gh_ - gv_) / s2;
+            float dgV = -b * b * a * (gv_ - gh_) / s2;
+            float tH = g * (wh * 0.25f + dgH * P[7]);
+            float tV = g * (wv * 0.25f + dgV * P[9]);
+            atomicAdd(&sm.gu[i - 1], g * (wh * 0.5f + dgH * P[6]));
+            atomicAdd(&sm.gu[i + 1], g * (wh * 0.5f - dgH * P[6]));
+            atomicAdd(&sm.gu[i - 2], -tH);
+            atomicAdd(&sm.gu[i + 2], -tH);
+            atomicAdd(&sm.gu[i - kUW], g * (wv * 0.5f + dgV * P[8]));
+            atomicAdd(&sm.gu[i + kUW], g * (wv * 0.5f - dgV * P[8]));
+            atomicAdd(&sm.gu[i - 2 * kUW], -tV);
+            atomicAdd(&sm.gu[i + 2 * kUW], -tV);
+            atomicAdd(&sm.gu[i], 2.0f * (tH + tV));
+        }
+        __syncthreads();
+    }
+    const int uw = t.tw + 6, uh = t.th + 6;
+    const float* grid = sm.th + 16;
+    for (int s = tid; s < uw * uh; s += kAdjThreads) {
+        int r = s / uw, c = s - r * uw;
+        int i = r * kUW + c;
+        float g = sm.gu[i];
+        if (g == 0.0f) continue;
+        int x = t.xu + c, y = t.yu + r;
+        if (x < 0 || x >= f.w || y < 0 || y >= f.h) continue;
+        int cc = t.cfa(x, y);
+        float rv = sm.raw[i];
+        float b = clampf(rv - sm.th[cc], 0.0f, mvf);
+        int gx = sm.col_gx[c], gy = sm.row_gy[r];
+        float fx = sm.col_fx[c], fy = sm.row_fy[r];
+        int n0 = (gy * f.gw + gx) * 4 + cc;
+        const float* g0 = grid + n0;
+        float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
+        float gain = g0[0] * w00 + g0[4] * w10 + g0[4 * f.gw] * w01 + g0[4 * f.gw + 4] * w11;
+        float l = clampf(b * gain, 0.0f, mvf);
+        float wb = wb_of(sm.th, cc);
+        if (!(l * wb > 0.0f && l * wb < mvf)) continue;
+        float gwb = g * l;
+        if (cc == 0) acc.wb[0] += gwb; else if (cc == 3) acc.wb[2] += gwb; else acc.wb[1] += gwb;
+        float gl = g * wb;
+        if (!(b * gain > 0.0f && b * gain < mvf)) continue;
+        float ggain = gl * b;
+        atomicAdd(&sm.acc_grid[n0], ggain * w00);
+        atomicAdd(&sm.acc_grid[n0 + 4], ggain * w10);
+        atomicAdd(&sm.acc_grid[n0 + 4 * f.gw], ggain * w01);
+        atomicAdd(&sm.acc_grid[n0 + 4 * f.gw + 4], ggain * w11);
+        float v = rv - sm.th[cc];
+        if (v > 0.0f && v < mvf) {
+            float gb = -gl * gain;
+            if (cc == 0) acc.bl[0] += gb; else if (cc == 1) acc.bl[1] += gb; else if (cc == 2) acc.bl[2] += gb; else acc.bl[3] += gb;
+        }
+    }
+    __syncthreads();
+}
+
+template <bool BACKWARD>
+__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
+    extern __shared__ __align__(16) uint8_t dsm[];
+    AdjSmem& sm = *reinterpret_cast<AdjSmem*>(dsm);
+    const int tid = threadIdx.x;
+    for (int k = tid; k < L.n_params; k += kAdjThreads) sm.th[k] = L.theta[k];
+    if (BACKWARD) {
+        for (int k = tid; k < 4 * kAdjMaxGridNodes; k += kAdjThreads) sm.acc_grid[k] = 0.0f;
+        for (int k = tid; k < 33; k += kAdjThreads) sm.acc_knots[k] = 0.0f;
+    }
+    __syncthreads();
+    RegAcc acc;
+#pragma unroll
+    for (int k = 0; k < 4; k++) acc.bl[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) acc.wb[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc.ccm[k] = 0.0f;
+    acc.loss = 0.0f;
+    for (int item = blockIdx.x; item < L.n_items; item += gridDim.x) {
+        int fi;
+        TileCtx t;
+        tile_of(L, item, fi, t);
+        const uint8_t* in = L.raw + (size_t)fi * L.f.in_bytes;
+        tile_forward<BACKWARD>(sm, t, in);
+        tile_pixels<BACKWARD>(sm, t, fi, L, acc);
+        if (BACKWARD) tile_back_planes(sm, t, acc);
+        else __syncthreads();
+    }
+    if (!BACKWARD) return;
+    // block reduction of the register accumulators, warps in order
+    float vals[17];
+#pragma unroll
+    for (int k = 0; k < 4; k++) vals[k] = acc.bl[k];
+#pragma unroll
+    for (int k = 0; k < 3; k++) vals[4 + k] = acc.wb[k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) vals[7 + k] = acc.ccm[k];
+    vals[16] = acc.loss;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < 17; k++) {
+        float v = vals[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sm.red[warp][k] = v;
+    }
+    __syncthreads();
+    float* part = L.partials + (size_t)blockIdx.x * (L.n_params + 1);
+    if (tid < 17) {
+        float v = 0.0f;
+        for (int w = 0; w < kAdjThreads / 32; w++) v += sm.red[w][tid];
+        if (tid < 16) part[tid] = v;
+        else part[L.n_params] = v;
+    }
+    const int ng = 4 * L.f.gw * L.f.gh;
+    for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = sm.acc_grid[k];
+    for (int k = tid; k < 33; k += kAdjThreads) part[16 + ng + k] = sm.acc_knots[k];
+}
+
+// grad[k] = sum over CTAs of partial[cta][k], in CTA order; loss likewise
+__global__ void reduce_partials_kernel(const float* partials, int n_parts, int n_params, float* grad, float* loss) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > n_params) return;
+    float s = 0.0f;
+    for (int c = 0; c < n_parts; c++) s += partials[(size_t)c * (n_params + 1) + k];
+    if (k < n_params) grad[k] = s;
+    else if (loss) *loss = s;
+}
+
+}  // namespace
+
+int adj_tile_grid(int w, int h, int& tx, int& ty) {
+    tx = tiles_along(w, kTX);
+    ty = tiles_along(h, kTY);
+    return tx * ty;
+}
+
+size_t adj_smem_bytes() { return sizeof(AdjSmem); }
+
+cudaError_t adj_grid_limit(int& limit) {
+    static int cached[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!cached[dev]) {
+        const int smem = (int)sizeof(AdjSmem);
+        if ((e = cudaFuncSetAttribute(adjoint_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+            (e = cudaFuncSetAttribute(adjoint_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+            return e;
+        int n = 0, sms = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel<true>, kAdjThreads, smem)) ||
+            (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+            return e;
+        cached[dev] = sms * (n > 0 ? n : 1);
+    }
+    limit = cached[dev];
+    return cudaSuccess;
+}
+
+cudaError_t launch_adjoint(const AdjLaunch& L, bool backward, int grid, float* d_grad, float* d_loss, cudaStream_t st) {
+    const size_t smem = sizeof(AdjSmem);
+    if (backward) {
+        adjoint_kernel<true><<<grid, kAdjThreads, smem, st>>>(L);
+        reduce_partials_kernel<<<(L.n_params + 1 + 255) / 256, 256, 0, st>>>(L.partials, grid, L.n_params, d_grad,
+                                                                            d_loss);
+    } else {
+        adjoint_kernel<false><<<grid, kAdjThreads, smem, st>>>(L);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace imop

@@ -113,5 +113,6 @@ struct imop_isp_ctx {
     imop::HostPipeline pipe;                       // run_host_batch slots and streams
     imop::BatchGraph graph;                        // last recorded batch
     cudaStream_t aux = nullptr;                    // table builds and graph capture
+    imop::DevBuf adj_partials;                     // adjoint per-CTA partial sums
     ~imop_isp_ctx();
 };

@@ -49,6 +49,9 @@ def lib():
             "imop_isp_sync_status": (i, [vp, vp]),
             "imop_isp_batch_submit": (i, [vp, C.POINTER(abi.FrameDesc), i, C.c_uint, vp]),
             "imop_isp_run_host_batch": (i, [vp, C.POINTER(abi.FrameDesc), i]),
+            "imop_adjoint_param_count": (i, [C.POINTER(abi.AdjointDesc)]),
+            "imop_isp_render_device": (i, [vp, C.POINTER(abi.AdjointDesc), vp, vp, vp, vp]),
+            "imop_isp_backward_device": (i, [vp, C.POINTER(abi.AdjointDesc), vp, vp, vp, i, vp, vp, vp]),
             "imop_scene_render": (i, [i, i, i, i, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float, vp]),
             "imop_scene_defects": (i, [i, i, C.c_uint64, i, C.POINTER(abi.DefectPoint)]),
             "imop_scene_apply_defects": (i, [vp, i, i, i, C.POINTER(abi.DefectPoint), i]),

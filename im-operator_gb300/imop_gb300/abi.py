@@ -77,3 +77,13 @@ class FrameDesc(C.Structure):
 
 BATCH_GRAPH = 1
 BATCH_PLAIN = 2
+
+
+class AdjointDesc(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("bit_depth", C.c_int), ("packed", C.c_int),
+                ("pattern", C.c_int), ("demosaic", C.c_int), ("grid_w", C.c_int), ("grid_h", C.c_int),
+                ("n_frames", C.c_int)]
+
+
+ADJ_TARGET = 0
+ADJ_UPSTREAM = 1

@@ -83,3 +83,40 @@ def c2_frame(pl, index=0):
 
 def c3_pipelines():
     return [c1_pipeline(5320, 4600, 8), c1_pipeline(5320, 4600, 12)]
+
+
+# ---- C5: calibration of the differentiable chain ------------------------------------------------
+# 16 x 1006x758 RGGB 12-bit frames (u16 unpacked), 933 parameters (BL 4, WB 3, CCM 9, 17x13x4
+# lens-shading grid, 33 tone knots); the target is the FP64 forward at the true parameters, the
+# start point the true parameters scaled by 1 + U(-0.2, 0.2).
+C5_SCENE = (256, 1400)  # scene range: the true gains keep nearly every sample below 2^12 - 1
+
+
+def c5_desc(n_frames=16, width=1006, height=758, demosaic=abi.AMAZE, grid=(17, 13)):
+    return abi.AdjointDesc(width, height, 12, 0, abi.RGGB, demosaic, grid[0], grid[1], n_frames)
+
+
+def c5_theta_true(desc):
+    gw, gh = desc.grid_w, desc.grid_h
+    knots = (np.arange(33) / 32.0) ** (1.0 / 2.2)
+    th = np.concatenate([
+        np.array([240.0, 256.0, 256.0, 272.0]),
+        np.array([1.9, 1.0, 1.6]),
+        np.array(random_ccm(BASE_SEED + 5)),
+        radial_grid(desc.width, desc.height, gw, gh, 1.8).reshape(-1).astype(np.float64),
+        knots,
+    ])
+    return th.astype(np.float32)
+
+
+def c5_theta_init(theta_true, seed=BASE_SEED + 7, spread=0.2):
+    rng = np.random.default_rng(seed)
+    return (theta_true * (1.0 + rng.uniform(-spread, spread, theta_true.shape))).astype(np.float32)
+
+
+def c5_frames(desc, first=0):
+    """Raw bytes of desc.n_frames frames back to back (u16 LSB-aligned)."""
+    from . import scene
+    out = [scene(desc.width, desc.height, 12, desc.pattern, BASE_SEED + 500 + first + k, lo=C5_SCENE[0],
+                 hi=C5_SCENE[1]).view(np.uint8).reshape(-1) for k in range(desc.n_frames)]
+    return np.concatenate(out)

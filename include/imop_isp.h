@@ -221,6 +221,47 @@ int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames, int n, un
  * ones are copied synchronously by the CUDA runtime.  Synchronous; returns the device status. */
 int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
 
+/* ---- differentiable pipeline (calibration) ------------------------------------------- */
+/* No counterpart in the reference, which has no parameter gradients.  The differentiable
+ * forward is the calibration chain
+ *     unpack -> black level -> lens-shading grid -> Bayer WB -> demosaic -> CCM -> 33-knot tone
+ * with every stage's formula and clamp kept and the integer rounding between stages dropped;
+ * its output is the tone value t in FP32 (the RGB8 path would store (int)(255 t + 0.5)).
+ * Demosaic HQLI or AMAZE (AMAZE's gradient weights are differentiated, |.| with sign(0) = 0);
+ * clamps pass gradient strictly inside their range.  Defect correction has no parameters and is
+ * not part of this chain.
+ *
+ * Parameter vector theta (FP32), in this order:
+ *     bl[4]                 black level per CFA colour (R, Gr, Gb, B), in DN
+ *     wb[3]                 Bayer WB gain R, G (both greens), B
+ *     ccm[9]                row-major 3x3
+ *     grid[grid_h][grid_w][4]  lens-shading gains per node and CFA colour
+ *     knots[33]             tone curve at v/max = k/32, linear in between
+ * 16 + 4*grid_w*grid_h + 33 values (933 for a 17x13 grid). */
+typedef struct ImopAdjointDesc {
+    int width, height, bit_depth, packed, pattern;
+    int demosaic;          /* IMOP_DEMOSAIC_HQLI or IMOP_DEMOSAIC_AMAZE */
+    int grid_w, grid_h;    /* 2..32 nodes per side, grid_w * grid_h <= 256 */
+    int n_frames;          /* frames stored back to back (input bytes of one frame apart) */
+} ImopAdjointDesc;
+
+enum {
+    IMOP_ADJ_TARGET = 0,   /* ref = target t (FP32 x 3 per pixel); loss = sum (t - target)^2 */
+    IMOP_ADJ_UPSTREAM = 1  /* ref = dL/dt (FP32 x 3 per pixel); loss receives sum t * dL/dt */
+};
+
+int imop_adjoint_param_count(const ImopAdjointDesc* d);
+
+/* Differentiable forward: t for every pixel of every frame (n_frames * h * w * 3 FP32). */
+int imop_isp_render_device(imop_isp_t ctx, const ImopAdjointDesc* d, const float* d_theta, const void* d_raw,
+                           float* d_rgb, void* stream);
+
+/* Adjoint: recomputes the forward per tile, back-propagates dL/dt and writes dL/dtheta
+ * (param_count FP32) and the loss (one FP32).  Per-CTA partial sums are added in a fixed order
+ * by a second kernel. Asynchronous on `stream`. */
+int imop_isp_backward_device(imop_isp_t ctx, const ImopAdjointDesc* d, const float* d_theta, const void* d_raw,
+                             const float* d_ref, int mode, float* d_loss, float* d_grad, void* stream);
+
 /* ---- no device allocation ----------------------------------------------------------- */
 /* No counterpart in the reference: the reference's GPU glue allocates per call
  * (src/gpu_dispatch.cpp:433) or through per-thread workspaces.  This entry point is for callers

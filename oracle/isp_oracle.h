@@ -79,6 +79,15 @@ void or_render_f64(const uint16_t* raw, int w, int h, int bd, int pattern, int g
 double or_adjoint_f64(const uint16_t* raw, const float* target, int w, int h, int bd, int pattern,
                       int gw, int gh, const double* theta, double* grad);
 
+/* FP64 differentiable calibration chain (isp_oracle_grad.c): parameter layout as
+ * ImopAdjointDesc in include/imop_isp.h; raw frames back to back; rgb / ref are n_frames*h*w*3. */
+int or_adj_param_count(const ImopAdjointDesc* d);
+int or_adj_forward(const ImopAdjointDesc* d, const double* theta, const uint8_t* raw, double* rgb_out);
+int or_adj_loss_grad(const ImopAdjointDesc* d, const double* theta, const uint8_t* raw, const float* ref, int mode,
+                     double* loss, double* grad);
+int or_adj_loss(const ImopAdjointDesc* d, const double* theta, const uint8_t* raw, const float* ref, int mode,
+                double* loss);
+
 #ifdef __cplusplus
 }
 #endif

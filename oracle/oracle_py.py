@@ -156,3 +156,57 @@ def demosaic(bay, pattern, algo, bd):
     fn = {1: L.or_demosaic_hqli, 6: L.or_demosaic_amaze, 2: L.or_demosaic_mg}[algo]
     fn(bay.ctypes.data_as(U16P), out.ctypes.data_as(U16P), w, h, pattern, bd)
     return out
+
+
+# ---- FP64 differentiable calibration chain ------------------------------------------------------
+def _adj_lib():
+    L = lib()
+    D = C.POINTER(abi.AdjointDesc)
+    DP = C.POINTER(C.c_double)
+    L.or_adj_param_count.argtypes = [D]
+    L.or_adj_param_count.restype = C.c_int
+    L.or_adj_forward.argtypes = [D, DP, U8P, DP]
+    L.or_adj_loss_grad.argtypes = [D, DP, U8P, F32P, C.c_int, DP, DP]
+    L.or_adj_loss.argtypes = [D, DP, U8P, F32P, C.c_int, DP]
+    return L
+
+
+def adj_forward(desc, theta, raw):
+    """t of every pixel (n_frames, h, w, 3) in FP64."""
+    L = _adj_lib()
+    th = np.ascontiguousarray(theta, np.float64)
+    raw = np.ascontiguousarray(raw, np.uint8)
+    out = np.zeros((desc.n_frames, desc.height, desc.width, 3), np.float64)
+    st = L.or_adj_forward(C.byref(desc), th.ctypes.data_as(C.POINTER(C.c_double)), _p(raw, U8P),
+                          out.ctypes.data_as(C.POINTER(C.c_double)))
+    if st:
+        raise RuntimeError(f"or_adj_forward: {st}")
+    return out
+
+
+def adj_loss_grad(desc, theta, raw, ref, mode=0):
+    """(loss, dL/dtheta) in FP64 against a target (mode 0) or an upstream gradient (mode 1)."""
+    L = _adj_lib()
+    th = np.ascontiguousarray(theta, np.float64)
+    raw = np.ascontiguousarray(raw, np.uint8)
+    ref = np.ascontiguousarray(ref, np.float32)
+    g = np.zeros(L.or_adj_param_count(C.byref(desc)), np.float64)
+    loss = C.c_double()
+    st = L.or_adj_loss_grad(C.byref(desc), th.ctypes.data_as(C.POINTER(C.c_double)), _p(raw, U8P), _p(ref, F32P),
+                            mode, C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_double)))
+    if st:
+        raise RuntimeError(f"or_adj_loss_grad: {st}")
+    return loss.value, g
+
+
+def adj_loss(desc, theta, raw, ref, mode=0):
+    L = _adj_lib()
+    th = np.ascontiguousarray(theta, np.float64)
+    raw = np.ascontiguousarray(raw, np.uint8)
+    ref = np.ascontiguousarray(ref, np.float32)
+    loss = C.c_double()
+    st = L.or_adj_loss(C.byref(desc), th.ctypes.data_as(C.POINTER(C.c_double)), _p(raw, U8P), _p(ref, F32P), mode,
+                       C.byref(loss))
+    if st:
+        raise RuntimeError(f"or_adj_loss: {st}")
+    return loss.value
