@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operator leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     return ap.parse_args()
 
 
@@ -129,6 +130,39 @@ def cpu_oracle_rate(pl, frames, max_seconds=30.0):
             break
     dt = time.perf_counter() - t0
     return done * pl.pixels / dt / 1e6, done, dt
+
+
+def adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
+    """Adjoint of the calibration chain on C5: 16 x 1006x758 RGGB 12-bit frames, AMAZE, 933
+    parameters; one step = forward recompute + back-propagation + parameter reduction against an
+    FP32 target (the loss and dL/dtheta), CUDA events on the launching stream."""
+    from imop_gb300 import abi, workloads
+    from imop_gb300 import adjoint as A
+    d = workloads.c5_desc()
+    th_true = workloads.c5_theta_true(d)
+    raw = torch.from_numpy(workloads.c5_frames(d)).cuda()
+    theta_true = torch.from_numpy(th_true).cuda()
+    target = A.render_forward(isp, d, theta_true, raw)
+    theta = torch.from_numpy(workloads.c5_theta_init(th_true)).cuda()
+    for _ in range(args.warmup):
+        A.backward(isp, d, theta, raw, target, abi.ADJ_TARGET)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        A.backward(isp, d, theta, raw, target, abi.ADJ_TARGET)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    px = d.n_frames * d.width * d.height
+    alg = px * (2 + 12) + 2 * 933 * 4  # raw u16 + FP32 RGB target per pixel, parameters in and out
+    return {"value": round(world * args.steps * px / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s",
+            "ms_per_step": round(ms / args.steps, 4), "bytes_per_step": alg,
+            "gbs_algorithmic": round(world * args.steps * alg / (ms / 1e3) / 1e9, 1),
+            "config": "C5: 16 x 1006x758 RGGB 12-bit u16, AMAZE, 17x13 grid, 933 parameters, L2 to an FP32 target",
+            "gpu_launches_per_step": 2}
 
 
 def dist_init():
@@ -277,6 +311,10 @@ def main():
             step_plain()
         ms_plain = timed(step_plain, args.steps)
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world)
+
     px_step = B * pl.pixels
     mpix = world * args.steps * px_step / (ms / 1e3) / 1e6
     alg_bytes = in_b + out_b + 4096 * 4 + 17 * 13 * 4 * 4  # per frame: RAW12P in, RGB8 out, LUT, grid
@@ -312,6 +350,8 @@ def main():
     if ms_plain is not None:
         line["plain"] = {"value": round(world * args.steps * px_step / (ms_plain / 1e3) / 1e6, 2), "unit": "Mpix/s",
                          "ms_per_step": round(ms_plain / args.steps, 4)}
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     if rank == 0 and not args.no_cpu:
         rate, done, dt = cpu_oracle_rate(pl, host_frames[: max(1, args.cpu_sample_frames)])
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",
