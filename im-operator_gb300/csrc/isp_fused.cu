@@ -52,34 +52,40 @@ __global__ void recip_table_kernel(float* out, int n) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Persistent fused kernel: CTA c takes items c, c + gridDim.x, ... of the launch's (frame, tile)
-// list.  Warp 0 stages the next item into the other raw buffer before the CTA computes the
-// current one, so the copy of tile k+1 overlaps the arithmetic of tile k.
+// Persistent tile kernel: CTA c takes items c, c + gridDim.x, ... of the launch's tile list (the
+// tiles of each rectangle in raster order).  Warp 0 stages the next item into the other raw
+// buffer before the CTA computes the current one, so the copy of tile k+1 overlaps the
+// arithmetic of tile k.
 
-// frame of item `item` (a handful of frames per launch: a linear scan)
-__device__ __forceinline__ int item_frame(const BatchLaunch& bl, int item) {
-    int f = 0;
-    while (f + 1 < bl.n_frames && item >= bl.item_start[f + 1]) f++;
-    return f;
+// rectangle of item `item`: the last rectangle starting at or before it
+__device__ __forceinline__ int item_rect(const BatchLaunch& bl, int item) {
+    int lo = 0, hi = bl.n_rects - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (bl.rect_start[mid] <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // warp 0: copy the item's frame parameters into slot b and start staging its raw rows
 template <int TW, int TH, int OUTB>
 __device__ void stage_item(TileSmem<TW, TH, OUTB>& sm, const BatchLaunch& bl, int item, int b) {
     const int lane = threadIdx.x & 31;
-    const int f = item_frame(bl, item);
-    const FrameParams& src = bl.frames[f];
+    const int r = item_rect(bl, item);
+    const TileRect& R = bl.rects[r];
+    const FrameParams& src = bl.frames[R.frame];
     static_assert(sizeof(FrameParams) % 4 == 0, "frame parameters copy as words");
     const int* s = reinterpret_cast<const int*>(&src);
     int* d = reinterpret_cast<int*>(&sm.fp[b]);
     for (int k = lane; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
-    int t = item - bl.item_start[f];
-    int ty = t / src.tiles_x, tx = t - ty * src.tiles_x;
+    int t = item - bl.rect_start[r];
+    int ty = t / R.tiles_x, tx = t - ty * R.tiles_x;
     int x0, tw, y0, th;
-    tile_span(src.w, TW, src.tiles_x, tx, x0, tw);
-    tile_span(src.h, TH, src.tiles_y, ty, y0, th);
+    tile_span(R.w, TW, R.tiles_x, tx, x0, tw);
+    tile_span(R.h, TH, R.tiles_y, ty, y0, th);
     __syncwarp();
-    stage_tile(sm, b, x0, y0, tw, th);
+    stage_tile(sm, b, R.x0 + x0, R.y0 + y0, tw, th);
 }
 
 template <int TW, int TH, int OUTB>
@@ -248,8 +254,8 @@ struct FusedKernels {
         int limit = 0;
         cudaError_t e = setup(limit);
         if (e != cudaSuccess) return e;
-        int grid = bl.n_items < limit ? bl.n_items : limit;
-        if (grid > 0) fused_batch_kernel<kTileW, kTileH, OUTB><<<grid, kThreads, smem, st>>>(bl);
+        if (bl.n_items > 0)
+            fused_batch_kernel<kTileW, kTileH, OUTB><<<bl.n_items < limit ? bl.n_items : limit, kThreads, smem, st>>>(bl);
         if (fixup) dpc_fixup_kernel<kTileW, kTileH, OUTB><<<bl.n_frames, kThreads, smem, st>>>(bl);
         return cudaGetLastError();
     }
@@ -257,21 +263,35 @@ struct FusedKernels {
 template <int OUTB> int FusedKernels<OUTB>::ctas_per_sm[kMaxDevices] = {};
 template <int OUTB> int FusedKernels<OUTB>::sms[kMaxDevices] = {};
 
+void add_rect(BatchLaunch& bl, int frame, int x0, int y0, int w, int h, int& items) {
+    TileRect& R = bl.rects[bl.n_rects];
+    R.frame = frame;
+    R.x0 = x0;
+    R.y0 = y0;
+    R.w = w;
+    R.h = h;
+    R.tiles_x = tiles_along(w, kTileW);
+    R.tiles_y = tiles_along(h, kTileH);
+    bl.rect_start[bl.n_rects] = items;
+    items += R.tiles_x * R.tiles_y;
+    bl.n_rects++;
+}
+
 cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st) {
     BatchLaunch bl;
     bl.n_frames = n;
+    bl.n_rects = 0;
     int items = 0;
     bool fixup = false;
     for (int f = 0; f < n; f++) {
         FrameParams& fp = frames[f];
         fp.tiles_x = tiles_along(fp.w, kTileW);
         fp.tiles_y = tiles_along(fp.h, kTileH);
-        bl.item_start[f] = items;
-        items += fp.tiles_x * fp.tiles_y;
         bl.frames[f] = fp;
         fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
+        add_rect(bl, f, 0, 0, fp.w, fp.h, items);
     }
-    bl.item_start[n] = items;
+    bl.rect_start[bl.n_rects] = items;
     bl.n_items = items;
     return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st) : FusedKernels<3>::launch(bl, fixup, st);
 }

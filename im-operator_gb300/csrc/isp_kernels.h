@@ -11,13 +11,22 @@ namespace imop {
 constexpr int kTileW = 120;
 constexpr int kTileH = 24;
 
-// Frames of one fused launch, passed by value as the kernel's parameter block: the persistent
-// kernel walks the (frame, tile) items of all frames, frame after frame, tiles in raster order.
+// Frames of one fused launch, passed by value as the kernel's parameter block.  The kernel walks
+// the tiles of a list of rectangles (one per frame), rectangle after rectangle, tiles in raster
+// order.
 constexpr int kBatchInline = 16;
+constexpr int kMaxRects = kBatchInline;
+struct TileRect {
+    int frame;
+    int x0, y0, w, h;  // x0 even; w, h >= 4
+    int tiles_x, tiles_y;
+};
 struct BatchLaunch {
     int n_frames;
     int n_items;
-    int item_start[kBatchInline + 1];  // first item of each frame; item_start[n_frames] = n_items
+    int n_rects;
+    int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
+    TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];
 };
 
