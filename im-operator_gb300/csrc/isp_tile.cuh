@@ -599,6 +599,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     if (demosaic != DM_HQLI) {
         const int nbk = FULL ? (G::F_GPW + 31) / 32 : (gpw + 31) >> 5;
         const float* rtab = fp.rtab;
+        const bool fast_div = fp.bd <= 12;
         for (int item = warp; item < nbk * gh; item += 8) {
             int blk, r;
             if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
@@ -613,7 +614,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 int cc = bp[0], hm1 = bp[-1], hp1 = bp[1], hm2 = bp[-2], hp2 = bp[2];
                 int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
                 if (demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab);
+                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab, fast_div);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);

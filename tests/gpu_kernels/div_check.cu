@@ -1,0 +1,43 @@
+// Exhaustive check of dev::weight_quotients against IEEE division (__fdiv_rn) over every pair of
+// AMAZE weights a = 1/(1+gH), b = 1/(1+gV), gH, gV in [0, 3 (2^bd - 1)].  Built and run by
+// tests/test_gpu_division.py; prints the mismatch count and exits non-zero on any mismatch.
+#include <cstdio>
+#include <cstdlib>
+
+#include "../../im-operator_gb300/csrc/isp_device.cuh"
+
+__global__ void check_pairs(long long n, unsigned long long* bad, long long* first) {
+    const long long total = n * n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int gh = (int)(i / n), gv = (int)(i - (i / n) * n);
+        const float a = __frcp_rn((float)(1 + gh)), b = __frcp_rn((float)(1 + gv));
+        const float s = __fadd_rn(a, b);
+        float wa, wb;
+        imop::dev::weight_quotients(a, b, s, wa, wb);
+        if (wa != __fdiv_rn(a, s) || wb != __fdiv_rn(b, s)) {
+            atomicAdd(bad, 1ull);
+            atomicMin(reinterpret_cast<unsigned long long*>(first), (unsigned long long)i);
+        }
+    }
+}
+
+int main(int argc, char** argv) {
+    const int bd = argc > 1 ? atoi(argv[1]) : 12;
+    const long long n = 3LL * ((1LL << bd) - 1) + 1;
+    unsigned long long* bad = nullptr;
+    long long* first = nullptr;
+    if (cudaMalloc(&bad, sizeof(*bad)) || cudaMalloc(&first, sizeof(*first))) return 2;
+    const long long init_first = 0x7fffffffffffffffLL;
+    cudaMemset(bad, 0, sizeof(*bad));
+    cudaMemcpy(first, &init_first, sizeof(init_first), cudaMemcpyHostToDevice);
+    check_pairs<<<152 * 8, 256>>>(n, bad, first);
+    unsigned long long nb = 0;
+    long long f = 0;
+    if (cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost) || cudaMemcpy(&f, first, sizeof(f), cudaMemcpyDeviceToHost))
+        return 3;
+    printf("bit depth %d: %lld weight pairs, %llu mismatches", bd, n * n, nb);
+    if (nb) printf(" (first gradH %lld gradV %lld)", f / n, f % n);
+    printf("\n");
+    return nb ? 1 : 0;
+}

@@ -1,0 +1,24 @@
+"""The AMAZE weight normalisation divides with a reciprocal estimate, one Newton-Raphson step and a
+remainder correction per quotient (dev::weight_quotients).  This test compares it with IEEE
+division (__fdiv_rn) on every weight pair bit depths up to 12 can produce: 12287^2 pairs."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_weight_quotients_equal_ieee_division_exhaustively(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "div_check")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "--expt-relaxed-constexpr", os.path.join(HERE, "gpu_kernels", "div_check.cu"), "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe, "12"], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 mismatches" in r.stdout
