@@ -600,4 +600,64 @@ int imop_isp_last_stats(imop_isp_t ctx, int* dpc_seeds, int* dpc_overrides) {
     return IMOP_OK;
 }
 
+static int op_prepare(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, ImopIspParams& q, FrameParams& fp) {
+    if (!ctx) return fail(IMOP_ERR_NULL_INPUT, "ctx is null");
+    if (!p) return fail(IMOP_ERR_NULL_INPUT, "params is null");
+    q = *p;
+    q.stages = stage;
+    q.packed = 0;
+    q.out_format = IMOP_OUT_NATIVE;
+    q.stage_order = IMOP_ORDER_RGB_WB;
+    // the operator tables are separate from the ones set_params built for run_device
+    int rc = build_frame_params(&q, ctx->op_tabs, fp, 0);
+    if (rc) return rc;
+    return IMOP_OK;
+}
+
+int imop_op_bayer_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, void* data) {
+    if (stage != IMOP_STAGE_BLACK_LEVEL && stage != IMOP_STAGE_DEFECT && stage != IMOP_STAGE_LENS_SHADING)
+        return fail(IMOP_ERR_INVALID_ARGUMENT, "not a Bayer stage");
+    if (!data) return fail(IMOP_ERR_NULL_INPUT, "null frame pointer");
+    ImopIspParams q;
+    FrameParams fp;
+    int rc = op_prepare(ctx, p, stage, q, fp);
+    if (rc) return rc;
+    const size_t n = (size_t)fp.w * fp.h;
+    const int bps = fp.bd <= 8 ? 1 : 2;
+    cudaError_t e;
+    if ((e = ctx->d_in.ensure(n * bps)) || (e = ctx->plain_a.ensure(n * 2)) || (e = ctx->plain_b.ensure(n * 2)))
+        return cuda_fail(e, "alloc operator buffers");
+    uint16_t* a = (uint16_t*)ctx->plain_a.ptr;
+    FixupScratch fs;
+    attach_fixup(ctx->fix, fp, fs);
+    if ((e = cudaMemcpy(ctx->d_in.ptr, data, n * bps, cudaMemcpyHostToDevice)) ||
+        (e = launch_widen((const uint8_t*)ctx->d_in.ptr, a, n, bps, 0)) ||
+        (e = launch_op_bayer(fp, stage, fs, &ctx->op_tabs.plan, a, (uint16_t*)ctx->plain_b.ptr, 0)) ||
+        (e = launch_narrow(a, (uint8_t*)ctx->d_in.ptr, n, bps, 0)) ||
+        (e = cudaMemcpy(data, ctx->d_in.ptr, n * bps, cudaMemcpyDeviceToHost)))
+        return cuda_fail(e, "bayer stage");
+    return take_status(ctx->fix);
+}
+
+int imop_op_rgb_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, const void* in, void* out) {
+    if (stage != IMOP_STAGE_WHITE_BALANCE && stage != IMOP_STAGE_CCM)
+        return fail(IMOP_ERR_INVALID_ARGUMENT, "not an RGB stage");
+    if (!in || !out) return fail(IMOP_ERR_NULL_INPUT, "null frame pointer");
+    ImopIspParams q;
+    FrameParams fp;
+    int rc = op_prepare(ctx, p, stage, q, fp);
+    if (rc) return rc;
+    const size_t n = (size_t)fp.w * fp.h * 3;
+    const int bps = fp.bd <= 8 ? 1 : 2;
+    cudaError_t e;
+    if ((e = ctx->d_in.ensure(n * bps)) || (e = ctx->plain_rgb.ensure(n * 2))) return cuda_fail(e, "alloc operator buffers");
+    uint16_t* rgb = (uint16_t*)ctx->plain_rgb.ptr;
+    if ((e = cudaMemcpy(ctx->d_in.ptr, in, n * bps, cudaMemcpyHostToDevice)) ||
+        (e = launch_widen((const uint8_t*)ctx->d_in.ptr, rgb, n, bps, 0)) || (e = launch_op_rgb(fp, stage, rgb, 0)) ||
+        (e = launch_narrow(rgb, (uint8_t*)ctx->d_in.ptr, n, bps, 0)) ||
+        (e = cudaMemcpy(out, ctx->d_in.ptr, n * bps, cudaMemcpyDeviceToHost)))
+        return cuda_fail(e, "rgb stage");
+    return IMOP_OK;
+}
+
 }  // extern "C"

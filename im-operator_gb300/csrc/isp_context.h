@@ -105,6 +105,7 @@ struct imop_isp_ctx {
     imop::FrameParams fp{};
     bool has_params = false;
     imop::FrameTables tabs;
+    imop::FrameTables op_tabs;                     // tables of the per-operator entry points
     imop::FixupState fix;
     imop::DevBuf d_in, d_out;                      // run_host staging frames
     imop::DevBuf plain_a, plain_b, plain_rgb;      // plain per-operator intermediates

@@ -83,4 +83,13 @@ struct PlainDumps {  // device pointers, may be null
 cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, const PlainBuffers& b,
                          const PlainDumps* dumps, cudaStream_t st);
 
+// per-operator stages (the per-module drop-ins): u8 / u16-LE samples <-> u16 planes, one Bayer
+// stage (1 black level, 2 defect correction, 4 lens shading) with its result back in `a`, one RGB
+// stage (8 white balance, 16 CCM) in place
+cudaError_t launch_widen(const uint8_t* in, uint16_t* out, size_t n, int bytes_per_sample, cudaStream_t st);
+cudaError_t launch_narrow(const uint16_t* in, uint8_t* out, size_t n, int bytes_per_sample, cudaStream_t st);
+cudaError_t launch_op_bayer(const FrameParams& fp, unsigned stage, const FixupScratch& fs, const MapPlan* plan,
+                            uint16_t* a, uint16_t* b, cudaStream_t st);
+cudaError_t launch_op_rgb(const FrameParams& fp, unsigned stage, uint16_t* rgb, cudaStream_t st);
+
 }  // namespace imop

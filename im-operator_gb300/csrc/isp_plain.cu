@@ -261,6 +261,21 @@ __global__ void output_kernel(const __grid_constant__ FrameParams fp, const uint
     }
 }
 
+// u8 / u16-LE samples <-> u16 plane
+__global__ void widen_kernel(const uint8_t* in, uint16_t* out, size_t n, int bps) {
+    GRID_STRIDE(i, n) out[i] = bps == 1 ? (uint16_t)in[i] : (uint16_t)(in[2 * i] | (in[2 * i + 1] << 8));
+}
+__global__ void narrow_kernel(const uint16_t* in, uint8_t* out, size_t n, int bps) {
+    GRID_STRIDE(i, n) {
+        if (bps == 1) {
+            out[i] = (uint8_t)in[i];
+        } else {
+            out[2 * i] = (uint8_t)in[i];
+            out[2 * i + 1] = (uint8_t)(in[i] >> 8);
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, const PlainBuffers& b,
@@ -308,6 +323,53 @@ cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const Ma
     if (fp.stages & 16u) ccm_kernel<<<nb, kPlainThreads, 0, st>>>(fp, b.rgb);
     dump(dumps->ccm, b.rgb, 3 * n);
     output_kernel<<<nb3, kPlainThreads, 0, st>>>(fp, b.rgb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_widen(const uint8_t* in, uint16_t* out, size_t n, int bytes_per_sample, cudaStream_t st) {
+    widen_kernel<<<plain_blocks(n), kPlainThreads, 0, st>>>(in, out, n, bytes_per_sample);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_narrow(const uint16_t* in, uint8_t* out, size_t n, int bytes_per_sample, cudaStream_t st) {
+    narrow_kernel<<<plain_blocks(n), kPlainThreads, 0, st>>>(in, out, n, bytes_per_sample);
+    return cudaGetLastError();
+}
+
+// One Bayer stage on plane a (result back in a; b is scratch of the same size).
+cudaError_t launch_op_bayer(const FrameParams& fp, unsigned stage, const FixupScratch& fs, const MapPlan* plan,
+                            uint16_t* a, uint16_t* b, cudaStream_t st) {
+    const size_t n = (size_t)fp.w * fp.h;
+    const int nb = plain_blocks(n);
+    cudaError_t e = cudaSuccess;
+    if (stage == 1u) {
+        black_level_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a);
+    } else if (stage == 2u) {
+        if (fp.dpc_mode == 0) {
+            if ((e = cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st))) return e;
+            dpc_jacobi_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
+            dpc_seed_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
+            dpc_fixup_plain_kernel<<<1, 32, 0, st>>>(fp, fs, a, b);
+        } else {
+            if (plan && (e = launch_map_resolve(fp, *plan, st))) return e;
+            dpc_map_apply_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
+        }
+        if ((e = cudaGetLastError())) return e;
+        return cudaMemcpyAsync(a, b, n * sizeof(uint16_t), cudaMemcpyDeviceToDevice, st);
+    } else if (stage == 4u) {
+        lens_shading_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a);
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// One RGB stage (white balance or CCM) on an RGB u16 x 3 plane, in place.
+cudaError_t launch_op_rgb(const FrameParams& fp, unsigned stage, uint16_t* rgb, cudaStream_t st) {
+    const size_t n = (size_t)fp.w * fp.h;
+    if (stage == 8u) rgb_wb_kernel<<<plain_blocks(3 * n), kPlainThreads, 0, st>>>(fp, rgb);
+    else if (stage == 16u) ccm_kernel<<<plain_blocks(n), kPlainThreads, 0, st>>>(fp, rgb);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 

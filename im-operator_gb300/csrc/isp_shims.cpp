@@ -1,0 +1,236 @@
+// isp_shims.cpp - the reference's GPU glue symbols (include/imop_ref_shims.hpp) on this library.
+//
+// Each shim runs on a per-thread context, as the reference's glue keeps per-thread workspaces
+// (src/gpu_dispatch.cpp:45, src/algorithms/cuda_dispatch.cpp:51), and is synchronous with host
+// buffers in and out.  Statuses 0..6 carry over numerically; anything this path does not serve
+// returns InternalError, which sends the reference's dispatcher to its CPU code.
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "../../include/imop_isp.h"
+#include "../../include/imop_ref_shims.hpp"
+
+namespace {
+
+struct ThreadCtx {
+    imop_isp_t ctx = nullptr;
+    ~ThreadCtx() {
+        if (ctx) imop_isp_destroy(ctx);
+    }
+};
+thread_local ThreadCtx t_ctx;
+
+imop_isp_t thread_ctx() {
+    if (!t_ctx.ctx && imop_isp_create(&t_ctx.ctx) != IMOP_OK) t_ctx.ctx = nullptr;
+    return t_ctx.ctx;
+}
+
+// status of this library -> the reference's enum (equal values 0..6, InternalError beyond)
+template <class E>
+E as_status(int rc) {
+    return (rc >= 0 && rc <= 6) ? static_cast<E>(rc) : E::InternalError;
+}
+
+ImopIspParams base_params(int w, int h, int bd, int pattern) {
+    ImopIspParams p;
+    imop_isp_params_default(&p, w, h, bd, 0);
+    p.pattern = pattern;
+    p.out_format = IMOP_OUT_NATIVE;
+    return p;
+}
+
+int demosaic_code(imop::DemosaicAlgorithm a) {
+    switch (a) {
+        case imop::DemosaicAlgorithm::HQLI: return IMOP_DEMOSAIC_HQLI;
+        case imop::DemosaicAlgorithm::MG: return IMOP_DEMOSAIC_MG;
+        case imop::DemosaicAlgorithm::AMAZE: return IMOP_DEMOSAIC_AMAZE;
+        default: return -1;
+    }
+}
+
+}  // namespace
+
+namespace imop {
+
+bool has_cuda() { return imop_has_cuda() == 1; }
+
+const char* cuda_device_name() {
+    static thread_local char name[256] = {0};
+    cudaDeviceProp prop;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "";
+    std::strncpy(name, prop.name, sizeof(name) - 1);
+    return name;
+}
+
+void cuda_synchronize() { cudaDeviceSynchronize(); }
+
+DemosaicError demosaic_cuda(const uint8_t* bayer_data, uint8_t* rgb_data, int width, int height, BayerPattern pattern,
+                            DemosaicAlgorithm algorithm, int bit_depth, bool is_packed) {
+    if (!bayer_data || !rgb_data) return DemosaicError::NullInput;
+    const int code = demosaic_code(algorithm);
+    imop_isp_t ctx = thread_ctx();
+    if (code < 0 || !ctx) return DemosaicError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, static_cast<int>(pattern));
+    p.packed = is_packed ? 1 : 0;
+    p.demosaic = code;
+    int rc = imop_isp_set_params(ctx, &p);
+    if (rc == IMOP_OK)
+        rc = imop_isp_run_host(ctx, bayer_data, imop_isp_input_bytes(&p), rgb_data, imop_isp_output_bytes(&p));
+    return as_status<DemosaicError>(rc);
+}
+
+DemosaicError demosaic_cuda_batch(const uint8_t* const* bayer_data_array, uint8_t* const* rgb_data_array,
+                                  int num_frames, int width, int height, BayerPattern pattern,
+                                  DemosaicAlgorithm algorithm, int bit_depth) {
+    if (num_frames <= 0) return DemosaicError::Ok;
+    if (!bayer_data_array || !rgb_data_array) return DemosaicError::NullInput;
+    const int code = demosaic_code(algorithm);
+    imop_isp_t ctx = thread_ctx();
+    if (code < 0 || !ctx) return DemosaicError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, static_cast<int>(pattern));
+    p.demosaic = code;
+    std::vector<ImopFrameDesc> frames((size_t)num_frames);
+    for (int i = 0; i < num_frames; i++) {
+        if (!bayer_data_array[i] || !rgb_data_array[i]) return DemosaicError::NullInput;
+        frames[i].params = &p;
+        frames[i].in = bayer_data_array[i];
+        frames[i].out = rgb_data_array[i];
+    }
+    return as_status<DemosaicError>(imop_isp_run_host_batch(ctx, frames.data(), num_frames));
+}
+
+}  // namespace imop
+
+namespace black_level {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+BlackLevelError process_black_level_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                         BlackLevelAlgorithm algorithm, int bit_depth, const BlackLevelParams& params) {
+    if (!data) return BlackLevelError::NullInput;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return BlackLevelError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, static_cast<int>(pattern));
+    // process_global uses r_offset for every pixel (src/black_level/global.cpp:14)
+    p.bl_mode = algorithm == BlackLevelAlgorithm::GLOBAL ? IMOP_BL_GLOBAL : IMOP_BL_PER_CHANNEL;
+    p.bl_offset[0] = params.r_offset;
+    p.bl_offset[1] = params.gr_offset;
+    p.bl_offset[2] = params.gb_offset;
+    p.bl_offset[3] = params.b_offset;
+    return as_status<BlackLevelError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_BLACK_LEVEL, data));
+}
+
+}  // namespace black_level
+
+namespace defect_correct {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+DefectCorrectError process_defect_correct_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                               DefectCorrectAlgorithm algorithm, int bit_depth,
+                                               const DefectCorrectParams& params) {
+    if (!data) return DefectCorrectError::NullInput;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return DefectCorrectError::InternalError;
+    static_assert(sizeof(DefectPoint) == sizeof(ImopDefectPoint), "defect point layout");
+    ImopIspParams p = base_params(width, height, bit_depth, static_cast<int>(pattern));
+    p.dpc_mode = algorithm == DefectCorrectAlgorithm::MAP_BASED ? IMOP_DPC_MAP_BASED : IMOP_DPC_ADAPTIVE;
+    p.dpc_threshold = params.threshold;
+    p.dpc_map = reinterpret_cast<const ImopDefectPoint*>(params.map);
+    p.dpc_map_count = params.map ? params.map_count : 0;
+    return as_status<DefectCorrectError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_DEFECT, data));
+}
+
+}  // namespace defect_correct
+
+namespace lens_shading {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+LensShadingError process_lens_shading_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                           LensShadingAlgorithm algorithm, int bit_depth,
+                                           const LensShadingParams& params) {
+    if (!data) return LensShadingError::NullInput;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return LensShadingError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, static_cast<int>(pattern));
+    if (algorithm == LensShadingAlgorithm::FLAT_FIELD) {
+        p.lsc_mode = IMOP_LSC_FLAT_FIELD;
+        p.lsc_flat_field = params.flat_field;
+        p.lsc_flat_w = params.flat_field_width;
+        p.lsc_flat_h = params.flat_field_height;
+    } else {
+        p.lsc_mode = IMOP_LSC_POLYNOMIAL;
+        const ShadingPolynomial* c[4] = {&params.r_coef, &params.gr_coef, &params.gb_coef, &params.b_coef};
+        for (int k = 0; k < 4; k++) {
+            p.lsc_poly[k][0] = c[k]->a2;
+            p.lsc_poly[k][1] = c[k]->a4;
+            p.lsc_poly[k][2] = c[k]->a6;
+        }
+        p.lsc_center[0] = params.center_x;
+        p.lsc_center[1] = params.center_y;
+    }
+    return as_status<LensShadingError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_LENS_SHADING, data));
+}
+
+}  // namespace lens_shading
+
+namespace white_balance {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+WhiteBalanceError process_white_balance_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                             int bit_depth, float r_gain, float g_gain, float b_gain) {
+    if (!input || !output) return WhiteBalanceError::NullInput;
+    if (channels != 3) return WhiteBalanceError::InternalError;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return WhiteBalanceError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, IMOP_RGGB);
+    p.wb_gain[0] = r_gain;
+    p.wb_gain[1] = g_gain;
+    p.wb_gain[2] = b_gain;
+    return as_status<WhiteBalanceError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_WHITE_BALANCE, input, output));
+}
+
+}  // namespace white_balance
+
+namespace ccm {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+CCMError process_ccm_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
+                          const float* matrix) {
+    if (!input || !output) return CCMError::NullInput;
+    if (channels != 3 || !matrix) return CCMError::InternalError;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return CCMError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, IMOP_RGGB);
+    std::memcpy(p.ccm, matrix, sizeof(p.ccm));
+    return as_status<CCMError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_CCM, input, output));
+}
+
+}  // namespace ccm
+
+namespace tone {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+// The reference's tone curves (gamma by std::pow, S-curve, levels, Bezier curves) are not on this
+// path; the dispatcher runs them on the CPU.
+ToneError process_tone_cuda(const uint8_t*, uint8_t*, int, int, int, ToneAlgorithm, int, const ToneParams&) {
+    return ToneError::InternalError;
+}
+
+}  // namespace tone
+
+namespace lut {
+
+bool has_cuda() { return imop::has_cuda(); }
+
+// 3D LUTs are not on this path; the dispatcher runs them on the CPU.
+LUTError process_lut_cuda(const uint8_t*, uint8_t*, int, int, int, int, const LUT3D&) { return LUTError::InternalError; }
+
+}  // namespace lut

@@ -221,6 +221,21 @@ int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames, int n, un
  * ones are copied synchronously by the CUDA runtime.  Synchronous; returns the device status. */
 int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
 
+/* ---- per-operator drop-ins ------------------------------------------------------------ */
+/* One stage of the pipeline on host buffers, synchronous, with the semantics of the reference's
+ * per-module CPU functions (the *_cuda glue of src/gpu_dispatch.cpp:292-571 replaced):
+ *   imop_op_bayer_stage: stage IMOP_STAGE_BLACK_LEVEL, IMOP_STAGE_DEFECT or IMOP_STAGE_LENS_SHADING,
+ *     in place on one unpacked Bayer frame (u8 for bit depth <= 8, u16 otherwise), as
+ *     black_level::process_black_level_cuda, defect_correct::process_defect_correct_cuda and
+ *     lens_shading::process_lens_shading_cuda do;
+ *   imop_op_rgb_stage: stage IMOP_STAGE_WHITE_BALANCE or IMOP_STAGE_CCM, interleaved RGB
+ *     (u8 x 3 for bit depth <= 8, u16 x 3 otherwise) from `in` to `out` (may alias), as
+ *     white_balance::process_white_balance_cuda and ccm::process_ccm_cuda do.
+ * The stage's parameters come from *p (width, height, bit_depth, pattern and the stage's own
+ * fields; the stage bits and the other stages' fields are ignored). */
+int imop_op_bayer_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, void* data);
+int imop_op_rgb_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, const void* in, void* out);
+
 /* ---- differentiable pipeline (calibration) ------------------------------------------- */
 /* No counterpart in the reference, which has no parameter gradients.  The differentiable
  * forward is the calibration chain

@@ -1,0 +1,137 @@
+/*
+ * imop_ref_shims.hpp - C++ entry points with the names, namespaces and signatures of the
+ * reference's GPU glue, so that its CPU dispatchers link against this library unchanged.
+ *
+ * Linking libimop_isp.so in place of src/algorithms/cuda_dispatch.cpp and src/gpu_dispatch.cpp
+ * of im-operator puts the GB300 path behind the reference's own dispatchers: each dispatcher
+ * calls <module>::has_cuda() and then <module>::process_<module>_cuda(); a non-Ok status makes it
+ * run its CPU path.  Enumerations and structures below repeat the reference's (names, enumerator
+ * order, member order and types), because the mangled symbol names and the argument layouts
+ * depend on them; the reference file each one follows is named beside it.  A translation unit
+ * uses either these declarations or the reference's headers, not both.
+ *
+ * Served on the GPU: demosaic HQLI / MG / AMAZE (packed RAW10 / RAW12 included), black level,
+ * adaptive and map-based defect correction, polynomial and flat-field lens shading, manual white
+ * balance, 3x3 CCM.  tone::process_tone_cuda and lut::process_lut_cuda return InternalError, so
+ * the reference runs its CPU tone curves and 3D LUTs.
+ */
+#ifndef IMOP_REF_SHIMS_HPP
+#define IMOP_REF_SHIMS_HPP
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace imop {
+enum class BayerPattern { RGGB, BGGR, GRBG, GBRG };                                   // include/imop/types.hpp:12-17
+enum class DemosaicAlgorithm { SUPER_FAST, HQLI, MG, L7, DFPD, AHD, AMAZE, RCD, PRISM };  // include/imop/types.hpp:19-29
+enum class DemosaicError {                                                            // include/imop/types.hpp:31-39
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidPattern, ImageTooSmall, InternalError
+};
+// include/imop/algorithms.hpp:69-84, defined by src/algorithms/cuda_dispatch.cpp:28-209
+bool has_cuda();
+const char* cuda_device_name();
+void cuda_synchronize();
+DemosaicError demosaic_cuda(const uint8_t* bayer_data, uint8_t* rgb_data, int width, int height, BayerPattern pattern,
+                            DemosaicAlgorithm algorithm, int bit_depth = 8, bool is_packed = false);
+DemosaicError demosaic_cuda_batch(const uint8_t* const* bayer_data_array, uint8_t* const* rgb_data_array,
+                                  int num_frames, int width, int height, BayerPattern pattern,
+                                  DemosaicAlgorithm algorithm, int bit_depth = 8);
+}  // namespace imop
+
+namespace black_level {
+using imop::BayerPattern;
+enum class BlackLevelAlgorithm { PER_CHANNEL, GLOBAL };                               // include/black_level/types.hpp:8-11
+enum class BlackLevelError {                                                          // include/black_level/types.hpp:13-21
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError
+};
+struct BlackLevelParams {                                                             // include/black_level/types.hpp:41-46
+    float r_offset = 0.0f, gr_offset = 0.0f, gb_offset = 0.0f, b_offset = 0.0f;
+};
+bool has_cuda();                                                                      // include/black_level/algorithms.hpp:40-46
+BlackLevelError process_black_level_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                         BlackLevelAlgorithm algorithm, int bit_depth, const BlackLevelParams& params);
+}  // namespace black_level
+
+namespace defect_correct {
+using imop::BayerPattern;
+enum class DefectCorrectAlgorithm { ADAPTIVE, MAP_BASED };                            // include/defect_correct/types.hpp:8-11
+enum class DefectCorrectError {                                                       // include/defect_correct/types.hpp:13-21
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError
+};
+struct DefectPoint { int x, y; };                                                     // include/defect_correct/types.hpp:41-43
+struct DefectCorrectParams {                                                          // include/defect_correct/types.hpp:45-49
+    float threshold = 0.3f;
+    const DefectPoint* map = nullptr;
+    int map_count = 0;
+};
+bool has_cuda();                                                                      // include/defect_correct/algorithms.hpp:40-46
+DefectCorrectError process_defect_correct_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                               DefectCorrectAlgorithm algorithm, int bit_depth,
+                                               const DefectCorrectParams& params);
+}  // namespace defect_correct
+
+namespace lens_shading {
+using imop::BayerPattern;
+enum class LensShadingAlgorithm { POLYNOMIAL, FLAT_FIELD };                           // include/lens_shading/types.hpp:8-11
+enum class LensShadingError {                                                         // include/lens_shading/types.hpp:13-21
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError
+};
+struct ShadingPolynomial { float a2 = 0.0f, a4 = 0.0f, a6 = 0.0f; };                  // include/lens_shading/types.hpp:37-41
+struct LensShadingParams {                                                            // include/lens_shading/types.hpp:43-60
+    ShadingPolynomial r_coef, gr_coef, gb_coef, b_coef;
+    float center_x = 0.5f, center_y = 0.5f;
+    const uint8_t* flat_field = nullptr;
+    int flat_field_width = 0, flat_field_height = 0;
+};
+bool has_cuda();                                                                      // include/lens_shading/algorithms.hpp:40-46
+LensShadingError process_lens_shading_cuda(uint8_t* data, int width, int height, BayerPattern pattern,
+                                           LensShadingAlgorithm algorithm, int bit_depth,
+                                           const LensShadingParams& params);
+}  // namespace lens_shading
+
+namespace white_balance {
+enum class WhiteBalanceError {                                                        // include/white_balance/types.hpp
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError
+};
+bool has_cuda();                                                                      // include/white_balance/algorithms.hpp:59-62
+WhiteBalanceError process_white_balance_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                             int bit_depth, float r_gain, float g_gain, float b_gain);
+}  // namespace white_balance
+
+namespace ccm {
+enum class CCMError {                                                                 // include/ccm/types.hpp
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError
+};
+bool has_cuda();                                                                      // include/ccm/algorithms.hpp:62-65
+CCMError process_ccm_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
+                          const float* matrix);
+}  // namespace ccm
+
+namespace tone {
+enum class ToneAlgorithm { GAMMA, S_CURVE, LEVELS, CURVES_3POINT, SHADOWS_HIGHLIGHTS };  // include/tone/types.hpp
+enum class ToneError { Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError };
+struct ToneParams {                                                                   // include/tone/types.hpp:50-58
+    float gamma = 1.0f, contrast = 0.0f, shadows = 0.0f, highlights = 0.0f;
+    float black_point = 0.0f, white_point = 1.0f, mid_point = 0.5f;
+};
+bool has_cuda();                                                                      // include/tone/algorithms.hpp:47-51
+ToneError process_tone_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                            ToneAlgorithm algorithm, int bit_depth, const ToneParams& params);
+}  // namespace tone
+
+namespace lut {
+enum class LUTError {                                                                 // include/lut/types.hpp
+    Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, LUTSizeMismatch, FileNotFound,
+    FileParseError, ImageTooSmall, InternalError
+};
+struct LUT3D {                                                                        // include/lut/types.hpp
+    int size = 0;
+    std::vector<float> data;
+};
+bool has_cuda();                                                                      // include/lut/algorithms.hpp:89-92
+LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
+                          const LUT3D& lut_data);
+}  // namespace lut
+
+#endif  /* IMOP_REF_SHIMS_HPP */

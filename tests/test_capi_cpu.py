@@ -103,3 +103,10 @@ def test_c2_workload_shape():
     assert g.shape == (13, 17, 4) and abs(g[6, 8, 0] - 1.0) < 0.01 and abs(g[0, 0, 0] - 2.0) < 1e-5
     m = np.array(pl.ccm).reshape(3, 3)
     assert np.allclose(m.sum(1), 1.0, atol=1e-6) and (np.diag(m) >= 1.4).all()
+
+
+def test_reference_shim_symbols_link(tmp_path):
+    """The reference-compatible C++ symbols resolve against the library (link only; no GPU)."""
+    from shim_build import build_shim_check
+    r = build_shim_check(str(tmp_path / "shim_check"))
+    assert r.returncode == 0, r.stderr
