@@ -630,6 +630,9 @@ int imop_op_bayer_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, 
     uint16_t* a = (uint16_t*)ctx->plain_a.ptr;
     FixupScratch fs;
     attach_fixup(ctx->fix, fp, fs);
+    // the frame's own bytes are the input of the stage: map-mode defect values read them there
+    fp.in = (const uint8_t*)ctx->d_in.ptr;
+    fp.out = nullptr;
     if ((e = cudaMemcpy(ctx->d_in.ptr, data, n * bps, cudaMemcpyHostToDevice)) ||
         (e = launch_widen((const uint8_t*)ctx->d_in.ptr, a, n, bps, 0)) ||
         (e = launch_op_bayer(fp, stage, fs, &ctx->op_tabs.plan, a, (uint16_t*)ctx->plain_b.ptr, 0)) ||

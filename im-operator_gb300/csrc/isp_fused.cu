@@ -213,6 +213,7 @@ cudaError_t launch_recip_table(float* d_out, int n, cudaStream_t st) {
 }
 
 cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st) {
+    if (!fp.in) return cudaErrorInvalidValue;  // the resolved values are read from the input frame
     if (plan.n_comp > 0) dpc_map_resolve_kernel<<<(plan.n_comp + 127) / 128, 128, 0, st>>>(fp, plan);
     return cudaGetLastError();
 }
