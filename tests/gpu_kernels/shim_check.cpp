@@ -2,6 +2,7 @@
 // every shim on seeded frames of several sizes, bit depths and patterns, outputs compared byte for
 // byte.  Built and run by tests/test_gpu_shims.py; prints one line per case and exits non-zero on
 // any mismatch.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -19,14 +20,21 @@ static void report(const char* what, int w, int h, int bd, bool ok) {
     if (!ok) failures++;
 }
 
-// seeded frame in the reference's storage: u8 for bd <= 8, u16 otherwise
+// seeded frame in the reference's storage (u8 for bd <= 8, u16 otherwise): a smooth scene with
+// noise and 0.1 % hot / dead pixels, as a camera delivers (uniform noise would make most pixels
+// defect candidates and overflow the defect-chain list, which the library reports as an error)
 static std::vector<uint8_t> frame(int w, int h, int bd, int seed, int channels = 1) {
     std::mt19937 rng(seed);
-    int mv = (1 << bd) - 1;
+    std::normal_distribution<float> noise(0.0f, 0.01f);
+    const int mv = (1 << bd) - 1;
+    const float fx = 0.02f + 0.01f * (seed % 5), fy = 0.03f + 0.01f * (seed % 3);
     size_t n = (size_t)w * h * channels;
     std::vector<uint8_t> f(n * (bd <= 8 ? 1 : 2));
     for (size_t i = 0; i < n; i++) {
-        int v = (int)(rng() % (mv + 1));
+        const int px = (int)(i / channels), x = px % w, y = px / w, c = (int)(i % channels);
+        float t = 0.45f + 0.3f * std::sin(fx * x + c) * std::cos(fy * y) + noise(rng);
+        int v = (int)(t * mv);
+        v = v < 0 ? 0 : (v > mv ? mv : v);
         if (rng() % 997 == 0) v = (rng() & 1) ? mv : 0;
         if (bd <= 8) f[i] = (uint8_t)v;
         else { f[2 * i] = (uint8_t)v; f[2 * i + 1] = (uint8_t)(v >> 8); }
