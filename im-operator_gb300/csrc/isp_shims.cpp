@@ -234,3 +234,48 @@ bool has_cuda() { return imop::has_cuda(); }
 LUTError process_lut_cuda(const uint8_t*, uint8_t*, int, int, int, int, const LUT3D&) { return LUTError::InternalError; }
 
 }  // namespace lut
+
+// ---- modules off this path: CPU fallback ------------------------------------------------------
+namespace denoise {
+bool has_cuda() { return false; }
+DenoiseError process_denoise_cuda(const uint8_t*, uint8_t*, int, int, int, DenoiseAlgorithm, int, float) {
+    return DenoiseError::InternalError;
+}
+}  // namespace denoise
+
+namespace sharpen {
+bool has_cuda() { return false; }
+SharpenError process_sharpen_cuda(const uint8_t*, uint8_t*, int, int, int, SharpenAlgorithm, int, const SharpenParams&) {
+    return SharpenError::InternalError;
+}
+}  // namespace sharpen
+
+namespace local_contrast {
+bool has_cuda() { return false; }
+LocalContrastError process_local_contrast_cuda(const uint8_t*, uint8_t*, int, int, int, int, const LocalContrastParams&) {
+    return LocalContrastError::InternalError;
+}
+}  // namespace local_contrast
+
+namespace saturation {
+bool has_cuda() { return false; }
+SaturationError process_saturation_cuda(const uint8_t*, uint8_t*, int, int, int, int, float, float) {
+    return SaturationError::InternalError;
+}
+}  // namespace saturation
+
+namespace color_temp {
+bool has_cuda() { return false; }
+ColorTempError process_color_temp_cuda(const uint8_t*, uint8_t*, int, int, int, int, float, float, float) {
+    return ColorTempError::InternalError;
+}
+}  // namespace color_temp
+
+namespace highlight_reconstruct {
+bool has_cuda() { return false; }
+HighlightReconstructError process_highlight_reconstruct_cuda(const uint8_t*, uint8_t*, int, int, int,
+                                                             HighlightReconstructAlgorithm, int,
+                                                             const HighlightReconstructParams&) {
+    return HighlightReconstructError::InternalError;
+}
+}  // namespace highlight_reconstruct

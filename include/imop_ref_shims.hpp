@@ -13,7 +13,9 @@
  * Served on the GPU: demosaic HQLI / MG / AMAZE (packed RAW10 / RAW12 included), black level,
  * adaptive and map-based defect correction, polynomial and flat-field lens shading, manual white
  * balance, 3x3 CCM.  tone::process_tone_cuda and lut::process_lut_cuda return InternalError, so
- * the reference runs its CPU tone curves and 3D LUTs.
+ * the reference runs its CPU tone curves and 3D LUTs; the other modules of the same glue file
+ * (denoise, sharpen, local contrast, saturation, colour temperature, highlight reconstruction)
+ * report no CUDA and stay on the CPU.
  */
 #ifndef IMOP_REF_SHIMS_HPP
 #define IMOP_REF_SHIMS_HPP
@@ -133,5 +135,64 @@ bool has_cuda();                                                                
 LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
                           const LUT3D& lut_data);
 }  // namespace lut
+
+// Modules off this path whose GPU glue lives in the same reference translation unit
+// (src/gpu_dispatch.cpp:50-415, 490-520): has_cuda() is false and the *_cuda entry returns
+// InternalError, so their dispatchers run the reference's CPU code.  Parameter types that only
+// appear by reference are declared opaque; the error enumerations repeat the reference's.
+#define IMOP_SHIM_ERROR_ENUM(Name) \
+    enum class Name { Ok = 0, NullInput, InvalidDimensions, InvalidBitDepth, InvalidChannels, ImageTooSmall, InternalError }
+
+namespace denoise {                                                                   // include/denoise/algorithms.hpp:52-55
+enum class DenoiseAlgorithm : int;
+IMOP_SHIM_ERROR_ENUM(DenoiseError);
+bool has_cuda();
+DenoiseError process_denoise_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                  DenoiseAlgorithm algorithm, int bit_depth, float strength);
+}  // namespace denoise
+
+namespace sharpen {                                                                   // include/sharpen/algorithms.hpp:44-48
+enum class SharpenAlgorithm : int;
+IMOP_SHIM_ERROR_ENUM(SharpenError);
+struct SharpenParams;
+bool has_cuda();
+SharpenError process_sharpen_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                  SharpenAlgorithm algorithm, int bit_depth, const SharpenParams& params);
+}  // namespace sharpen
+
+namespace local_contrast {                                                            // include/local_contrast/algorithms.hpp:32-35
+IMOP_SHIM_ERROR_ENUM(LocalContrastError);
+struct LocalContrastParams;
+bool has_cuda();
+LocalContrastError process_local_contrast_cuda(const uint8_t* input, uint8_t* output, int width, int height,
+                                               int channels, int bit_depth, const LocalContrastParams& params);
+}  // namespace local_contrast
+
+namespace saturation {                                                                // include/saturation/algorithms.hpp:44-47
+IMOP_SHIM_ERROR_ENUM(SaturationError);
+bool has_cuda();
+SaturationError process_saturation_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                        int bit_depth, float sat, float vib);
+}  // namespace saturation
+
+namespace color_temp {                                                                // include/color_temp/algorithms.hpp:75-78
+IMOP_SHIM_ERROR_ENUM(ColorTempError);
+bool has_cuda();
+ColorTempError process_color_temp_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                                       int bit_depth, float r_mult, float g_mult, float b_mult);
+}  // namespace color_temp
+
+namespace highlight_reconstruct {                                                     // include/highlight_reconstruct/algorithms.hpp:35-40
+enum class HighlightReconstructAlgorithm : int;
+IMOP_SHIM_ERROR_ENUM(HighlightReconstructError);
+struct HighlightReconstructParams;
+bool has_cuda();
+HighlightReconstructError process_highlight_reconstruct_cuda(const uint8_t* input, uint8_t* output, int width,
+                                                             int height, int channels,
+                                                             HighlightReconstructAlgorithm algorithm, int bit_depth,
+                                                             const HighlightReconstructParams& params);
+}  // namespace highlight_reconstruct
+
+#undef IMOP_SHIM_ERROR_ENUM
 
 #endif  /* IMOP_REF_SHIMS_HPP */

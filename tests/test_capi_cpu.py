@@ -5,8 +5,10 @@ import ctypes as C
 import hashlib
 import os
 import re
+import subprocess
 
 import numpy as np
+import pytest
 
 import imop_gb300 as I
 import oracle_py as O
@@ -110,3 +112,14 @@ def test_reference_shim_symbols_link(tmp_path):
     from shim_build import build_shim_check
     r = build_shim_check(str(tmp_path / "shim_check"))
     assert r.returncode == 0, r.stderr
+
+
+def test_reference_headers_link_against_library():
+    """The reference's own declarations of its GPU glue (every module's process_*_cuda and
+    has_cuda, imop::demosaic_cuda and friends) resolve against this library: the link recipe
+    oracle/Makefile `shimlink` compiles a probe with the reference's headers."""
+    import oracle_py as O
+    if not O.ref_available():
+        pytest.skip("the reference tree is not on this host")
+    r = subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "shimlink"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
