@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operator leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-c4", action="store_true", help="skip the uneven 96-frame batch leg")
     return ap.parse_args()
 
 
@@ -163,6 +164,48 @@ def adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
             "gbs_algorithmic": round(world * args.steps * alg / (ms / 1e3) / 1e9, 1),
             "config": "C5: 16 x 1006x758 RGGB 12-bit u16, AMAZE, 17x13 grid, 933 parameters, L2 to an FP32 target",
             "gpu_launches_per_step": 2}
+
+
+def c4_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
+    """C4: 96 frames of three sizes (1006x758, 4024x3032, 5320x4600) and five formats (RAW8,
+    RAW10/RAW12 packed and unpacked), each with its own BL / WB / CCM, as one recorded batch
+    (one persistent launch per 16 frames) against 96 plain per-operator pipelines."""
+    from imop_gb300 import abi, workloads
+    frames = workloads.c4_batch()
+    dev = []
+    for pl, raw in frames:
+        d_in = torch.from_numpy(raw).cuda()
+        d_out = torch.empty(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+        dev.append((pl, d_in, d_out))
+    descs = [(pl, d_in.data_ptr(), d_out.data_ptr()) for pl, d_in, d_out in dev]
+    px = sum(pl.pixels for pl, _ in frames)
+    alg = sum(pl.input_bytes() + pl.output_bytes() for pl, _ in frames)
+    sh = stream.cuda_stream
+    steps = max(1, min(args.steps, 3))
+
+    def run(flags):
+        for _ in range(2):
+            isp.batch_submit(descs, flags=flags, stream=sh)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(steps):
+            isp.batch_submit(descs, flags=flags, stream=sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return max_over_ranks(ev0.elapsed_time(ev1)) / steps
+
+    ms = run(abi.BATCH_GRAPH)
+    ms_plain = run(abi.BATCH_PLAIN)
+    isp.sync_status(sh)
+    return {"value": round(world * px / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s", "ms_per_step": round(ms, 3),
+            "plain": {"value": round(world * px / (ms_plain / 1e3) / 1e6, 2), "ms_per_step": round(ms_plain, 3)},
+            "gbs_algorithmic": round(world * alg / (ms / 1e3) / 1e9, 1), "frames": len(frames),
+            "megapixels_per_step": round(px / 1e6, 1), "steps": steps,
+            "config": "C4: 96 frames, sizes 1006x758 / 4024x3032 / 5320x4600, RAW8 and RAW10/RAW12 packed and "
+                      "unpacked, own BL (64 or 256) / WB / CCM each, AMAZE, recorded graph vs 96 plain pipelines"}
 
 
 def dist_init():
@@ -314,6 +357,9 @@ def main():
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world)
+    c4 = None
+    if not args.no_c4:
+        c4 = c4_leg(isp, args, torch, stream, barrier, max_over_ranks, world)
 
     px_step = B * pl.pixels
     mpix = world * args.steps * px_step / (ms / 1e3) / 1e6
@@ -352,6 +398,8 @@ def main():
                          "ms_per_step": round(ms_plain / args.steps, 4)}
     if adjoint is not None:
         line["adjoint"] = adjoint
+    if c4 is not None:
+        line["c4"] = c4
     if rank == 0 and not args.no_cpu:
         rate, done, dt = cpu_oracle_rate(pl, host_frames[: max(1, args.cpu_sample_frames)])
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",

@@ -120,3 +120,34 @@ def c5_frames(desc, first=0):
     out = [scene(desc.width, desc.height, 12, desc.pattern, BASE_SEED + 500 + first + k, lo=C5_SCENE[0],
                  hi=C5_SCENE[1]).view(np.uint8).reshape(-1) for k in range(desc.n_frames)]
     return np.concatenate(out)
+
+
+# ---- C4: uneven batch ------------------------------------------------------------------------------
+C4_SIZES = [(1006, 758), (4024, 3032), (5320, 4600)]
+C4_FORMATS = [(8, False), (10, True), (10, False), (12, True), (12, False)]
+
+
+def c4_batch(n_frames=96, seed=BASE_SEED + 4):
+    """(Pipeline, raw bytes) per frame: sizes and formats cycle through C4_SIZES x C4_FORMATS;
+    black level 64 or 256, WB R ~ U(1.5, 2.4), B ~ U(1.2, 2.0), own CCM; BL, Bayer WB, AMAZE,
+    CCM, linear tone -> RGB8.  Scenes are rendered once per (size, bit depth) and shared."""
+    from . import scene, pack_mipi
+    rng = np.random.default_rng(seed)
+    cache = {}
+    out = []
+    for k in range(n_frames):
+        w, h = C4_SIZES[k % len(C4_SIZES)]
+        bd, packed = C4_FORMATS[(k // len(C4_SIZES)) % len(C4_FORMATS)]
+        bl = float(rng.choice([64.0, 256.0])) * ((1 << bd) / 4096.0 if bd < 12 else 1.0)
+        pl = Pipeline(width=w, height=h, bit_depth=bd, packed=packed, pattern=abi.RGGB, demosaic=abi.AMAZE,
+                      stages=abi.STAGE_BLACK_LEVEL | abi.STAGE_WHITE_BALANCE | abi.STAGE_CCM,
+                      stage_order=abi.ORDER_BAYER_WB, bl_offset=(round(bl),) * 4,
+                      wb_gain=(float(rng.uniform(1.5, 2.4)), 1.0, float(rng.uniform(1.2, 2.0))),
+                      ccm=random_ccm(int(rng.integers(0, 2**31))), tone_mode=abi.TONE_LINEAR)
+        key = (w, h, bd, packed)
+        if key not in cache:
+            mv = (1 << bd) - 1
+            f = scene(w, h, bd, abi.RGGB, BASE_SEED + 400 + k, lo=mv // 16, hi=mv)
+            cache[key] = pack_mipi(f, bd) if packed else f.view(np.uint8).reshape(-1)
+        out.append((pl, cache[key]))
+    return out
