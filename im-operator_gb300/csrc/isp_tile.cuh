@@ -441,8 +441,104 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const bool need_align = fp.need_align != 0;
     const int thr = fp.dpc_thr;
     const float2 h5 = make_float2(0.5f, 0.5f);
-    {
-        const int nbk = FULL ? (G::F_BPW + 31) / 32 : (bpw + 31) >> 5;
+    if constexpr (FULL) {
+        // a warp keeps one block of 32 pair columns and the rows r0, r0 + 4, ... (one row
+        // parity), so its colours, gains and lens-shading columns are loop constants
+        const int pc = (warp & 1) * 32 + lane;
+        const int r0 = warp >> 1;
+        const int p = (yb + r0) & 1;
+        const int c0 = bayer_color(p, 0, po), c1 = bayer_color(p, 1, po);
+        const float WB0 = fp.wb_cfa[c0], WB1 = fp.wb_cfa[c1];
+        const int x = xb + 2 * pc;
+        if (pc < G::F_BPW) {
+            float f0 = 0.f, f1 = 0.f;
+            int gxa = 0, gxb = 0;
+            if (lsc_grid) {
+                f0 = sm.col_fx[2 * pc];
+                f1 = sm.col_fx[2 * pc + 1];
+                gxa = sm.col_gx[2 * pc];
+                gxb = sm.col_gx[2 * pc + 1];
+            }
+            const float of0 = dev::fsub(1.0f, f0), of1 = dev::fsub(1.0f, f1);
+            int cache_gy = -1;
+            float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f;
+            const int* ob = orig + 2 * G::OW + (x - xo);
+            for (int r = r0; r < G::F_BH; r += 4) {
+                const int y = yb + r;
+                const int* o = ob + r * G::OW;
+                const int2 c = *reinterpret_cast<const int2*>(o);
+                int j0 = c.x, j1 = c.y;
+                if (adaptive) {
+                    int2 n0 = *reinterpret_cast<const int2*>(o - 2 * G::OW - 2);
+                    int2 n1 = *reinterpret_cast<const int2*>(o - 2 * G::OW);
+                    int2 n2 = *reinterpret_cast<const int2*>(o - 2 * G::OW + 2);
+                    int2 n3 = *reinterpret_cast<const int2*>(o - 2);
+                    int2 n4 = *reinterpret_cast<const int2*>(o + 2);
+                    int2 n5 = *reinterpret_cast<const int2*>(o + 2 * G::OW - 2);
+                    int2 n6 = *reinterpret_cast<const int2*>(o + 2 * G::OW);
+                    int2 n7 = *reinterpret_cast<const int2*>(o + 2 * G::OW + 2);
+                    int mn0 = min(min(min(n0.x, n1.x), min(n2.x, n3.x)), min(min(n4.x, n5.x), min(n6.x, n7.x)));
+                    int mx0 = max(max(max(n0.x, n1.x), max(n2.x, n3.x)), max(max(n4.x, n5.x), max(n6.x, n7.x)));
+                    int mn1 = min(min(min(n0.y, n1.y), min(n2.y, n3.y)), min(min(n4.y, n5.y), min(n6.y, n7.y)));
+                    int mx1 = max(max(max(n0.y, n1.y), max(n2.y, n3.y)), max(max(n4.y, n5.y), max(n6.y, n7.y)));
+                    // |c - median| <= thr is certain when c - min <= thr and max - c <= thr
+                    if (max(c.x - mn0, mx0 - c.x) > thr) {
+                        int nb[8] = {n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x};
+                        j0 = dev::dpc_apply(c.x, nb, 0xFFu, thr);
+                    }
+                    if (max(c.y - mn1, mx1 - c.y) > thr) {
+                        int nb[8] = {n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y};
+                        j1 = dev::dpc_apply(c.y, nb, 0xFFu, thr);
+                    }
+                } else if (dpc_on && fp.dpc_mode == 1 && __ldg(fp.map_row_ptr + y + 1) > __ldg(fp.map_row_ptr + y)) {
+                    int sv = map_lookup(fp, x, y);
+                    if (sv >= 0) j0 = sv;
+                    sv = map_lookup(fp, x + 1, y);
+                    if (sv >= 0) j1 = sv;
+                }
+                const int m = (j0 != c.x) | ((j1 != c.y) << 1);
+                local_mod |= m;
+                sm.mod[r * G::BPW + pc] = (uint8_t)m;
+                int u0 = j0, u1 = j1;
+                if (lsc_grid) {
+                    const int gy_i = sm.row_gy[r];
+                    if (gy_i != cache_gy) {
+                        // g00*(1-fx), g10*fx, g01*(1-fx), g11*fx of both samples for this cell row
+                        cache_gy = gy_i;
+                        const float* g0 = fp.grid + (gy_i * fp.gw + gxa) * 4 + c0;
+                        const float* g1 = fp.grid + (gy_i * fp.gw + gxb) * 4 + c1;
+                        A0 = dev::fmul(__ldg(g0), of0); A1 = dev::fmul(__ldg(g1), of1);
+                        B0 = dev::fmul(__ldg(g0 + 4), f0); B1 = dev::fmul(__ldg(g1 + 4), f1);
+                        C0 = dev::fmul(__ldg(g0 + 4 * fp.gw), of0); C1 = dev::fmul(__ldg(g1 + 4 * fp.gw), of1);
+                        D0 = dev::fmul(__ldg(g0 + 4 * fp.gw + 4), f0); D1 = dev::fmul(__ldg(g1 + 4 * fp.gw + 4), f1);
+                    }
+                    const float fy = sm.row_fy[r], ofy = dev::fsub(1.0f, fy);
+                    float2 pa = make_float2(dev::fmul(A0, ofy), dev::fmul(A1, ofy));
+                    float2 pb = make_float2(dev::fmul(B0, ofy), dev::fmul(B1, ofy));
+                    float2 pcc = make_float2(dev::fmul(C0, fy), dev::fmul(C1, fy));
+                    float2 pd = make_float2(dev::fmul(D0, fy), dev::fmul(D1, fy));
+                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(pa, pb), pcc), pd);
+                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, gain.x), dev::fmul((float)u1, gain.y)), h5);
+                    u0 = u16q(t.x, mv);
+                    u1 = u16q(t.y, mv);
+                } else if (lsc_poly) {
+                    u0 = dev::lsc_poly(fp, u0, x, y, c0);
+                    u1 = dev::lsc_poly(fp, u1, x + 1, y, c1);
+                }
+                if (wb_bayer) {
+                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, WB0), dev::fmul((float)u1, WB1)), h5);
+                    u0 = u16q(t.x, mv);
+                    u1 = u16q(t.y, mv);
+                }
+                if (need_align) {
+                    if (u0 > mv) u0 >>= (16 - fp.bd);
+                    if (u1 > mv) u1 >>= (16 - fp.bd);
+                }
+                *reinterpret_cast<int2*>(sm.bay + r * G::BW + 2 * pc) = make_int2(u0, u1);
+            }
+        }
+    } else {
+        const int nbk = (bpw + 31) >> 5;
         int cache_key = -1;
         float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f, WB0 = 1.f, WB1 = 1.f;
         for (int item = warp; item < nbk * bh; item += 8) {
@@ -596,8 +692,36 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     }
 
     // ---- 4b. green at the red/blue site of each pair (AMAZE, MG) ---------------------------
-    if (demosaic != DM_HQLI) {
-        const int nbk = FULL ? (G::F_GPW + 31) / 32 : (gpw + 31) >> 5;
+    if (FULL && demosaic != DM_HQLI) {
+        // one column block and one row parity per warp, as in the defect phase
+        const float* rtab = fp.rtab;
+        const bool fast_div = fp.bd <= 12;
+        const int pc = (warp & 1) * 32 + lane;
+        const int r0 = warp >> 1;
+        const int rbh = (((yg0 + r0) & 1) == po.r_row) ? po.r_col : po.b_col;
+        if (pc < G::F_GPW) {
+            const int* bp0 = sm.bay + 2 * G::BW + (xg0 + 2 * pc + rbh - xb);
+            for (int r = r0; r < G::F_GH; r += 4) {
+                const int* bp = bp0 + r * G::BW;
+                const int cc = bp[0], hm1 = bp[-1], hp1 = bp[1], hm2 = bp[-2], hp2 = bp[2];
+                const int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
+                float g;
+                if (demosaic == DM_AMAZE) {
+                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab, fast_div);
+                } else if (fp.bd <= 8) {
+                    // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
+                    g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
+                } else {
+                    // src/algorithms/mg.cpp:187-196, exact in FP32 for integer samples
+                    float t = dev::fsub(dev::fadd(dev::fmul(4.0f, (float)cc), dev::fmul(2.0f, (float)(vm1 + vp1 + hp1 + hm1))),
+                                        (float)(vm2 + vp2 + hp2 + hm2));
+                    g = __fdiv_rn(t, 8.0f);
+                }
+                green[r * G::GPW + pc] = g;
+            }
+        }
+    } else if (demosaic != DM_HQLI) {
+        const int nbk = (gpw + 31) >> 5;
         const float* rtab = fp.rtab;
         const bool fast_div = fp.bd <= 12;
         for (int item = warp; item < nbk * gh; item += 8) {
@@ -701,9 +825,126 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const bool border_tile = !FULL && (x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2);
     const bool ccm_on = (stages & 16u) != 0;
     const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
-    {
+    const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
+    // RGB WB, CCM and tone of pair (x, x+1) in tile row r, staged for the stores
+    auto finish = [&](int r, int y, int pc, int x, int R0, int G0, int B0, int R1, int G1, int B1) {
+        // RGB-domain white balance (reference call order), CCM: scalar products, packed sums
+        if (wb_rgb) {
+            float2 t;
+            t = dev::fadd2(make_float2(dev::fmul((float)R0, wr), dev::fmul((float)R1, wr)), h5);
+            R0 = u16q(t.x, mv); R1 = u16q(t.y, mv);
+            t = dev::fadd2(make_float2(dev::fmul((float)G0, wg), dev::fmul((float)G1, wg)), h5);
+            G0 = u16q(t.x, mv); G1 = u16q(t.y, mv);
+            t = dev::fadd2(make_float2(dev::fmul((float)B0, wbl), dev::fmul((float)B1, wbl)), h5);
+            B0 = u16q(t.x, mv); B1 = u16q(t.y, mv);
+        }
+        if (ccm_on) {
+            const float* m = fp.ccm;
+            const float r0 = (float)R0, r1 = (float)R1, g0 = (float)G0, g1 = (float)G1, b0 = (float)B0, b1 = (float)B1;
+            // ((m0*r + m1*g) + m2*b) + 0.5 for both samples, each product rounded on its own
+            float2 ro = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[0], r0), dev::fmul(m[0], r1)),
+                                                         make_float2(dev::fmul(m[1], g0), dev::fmul(m[1], g1))),
+                                              make_float2(dev::fmul(m[2], b0), dev::fmul(m[2], b1))), h5);
+            float2 go = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[3], r0), dev::fmul(m[3], r1)),
+                                                         make_float2(dev::fmul(m[4], g0), dev::fmul(m[4], g1))),
+                                              make_float2(dev::fmul(m[5], b0), dev::fmul(m[5], b1))), h5);
+            float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[6], r0), dev::fmul(m[6], r1)),
+                                                         make_float2(dev::fmul(m[7], g0), dev::fmul(m[7], g1))),
+                                              make_float2(dev::fmul(m[8], b0), dev::fmul(m[8], b1))), h5);
+            // (int)(v + 0.5) clamped to [0, mv]: truncation saturating at 0, then min
+            R0 = u16q(ro.x, mv); R1 = u16q(ro.y, mv);
+            G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
+            B0 = u16q(bo.x, mv); B1 = u16q(bo.y, mv);
+        }
+        int g0 = (y * W + x0) * 3 * bpc;
+        int shift = (int)((out_base + (uintptr_t)g0) & 15);
+        uint8_t* q = outs + r * G::OUT_PITCH + shift + 2 * pc * 3 * bpc;
+        const bool has1 = FULL || x + 1 < x0 + tw;
+        if (out_format == 0) {
+            const uint8_t* tt = tone_smem ? sm.tone8 : fp.tone8;
+            int t0 = tt[R0], t1 = tt[G0], t2 = tt[B0];
+            if (((shift & 1) == 0) && has1) {
+                int t3 = tt[R1], t4 = tt[G1], t5 = tt[B1];
+                uint16_t* q16 = reinterpret_cast<uint16_t*>(q);
+                q16[0] = (uint16_t)(t0 | (t1 << 8));
+                q16[1] = (uint16_t)(t2 | (t3 << 8));
+                q16[2] = (uint16_t)(t4 | (t5 << 8));
+            } else {
+                q[0] = (uint8_t)t0; q[1] = (uint8_t)t1; q[2] = (uint8_t)t2;
+                if (has1) { q[3] = tt[R1]; q[4] = tt[G1]; q[5] = tt[B1]; }
+            }
+        } else if (bpc == 1) {
+            q[0] = (uint8_t)R0; q[1] = (uint8_t)G0; q[2] = (uint8_t)B0;
+            if (has1) { q[3] = (uint8_t)R1; q[4] = (uint8_t)G1; q[5] = (uint8_t)B1; }
+        } else {
+            int v[6] = {R0, G0, B0, R1, G1, B1};
+            for (int k = 0; k < (has1 ? 6 : 3); k++) { q[2 * k] = (uint8_t)v[k]; q[2 * k + 1] = (uint8_t)(v[k] >> 8); }
+        }
+    };
+    if (FULL && demosaic != DM_MG) {
+        // one column block and one row parity per warp: the red/blue column, the row colours and
+        // every neighbour offset are loop constants
+        const int pc = (warp & 1) * 32 + lane;
+        const int r0 = warp >> 1;
+        const bool rrow = ((y0 + r0) & 1) == po.r_row;
+        const int rbh = rrow ? po.r_col : po.b_col;  // sample of the pair at the red/blue site
+        if (pc < G::F_TPW) {
+            const int x = x0 + 2 * pc;
+            const int* br0 = sm.bay + 3 * G::BW + (x + rbh - xb);
+            const int* bg0 = sm.bay + 3 * G::BW + (x + 1 - rbh - xb);
+            const float* gr0 = green + G::GPW + (pc + 1);
+            // pair offsets of columns xr-1 / xr+1 (diagonals) and xg-1 / xg+1 (horizontal)
+            const int pa = rbh ? 0 : -1, pl = rbh ? -1 : 0;
+            for (int r = r0; r < TH; r += 4) {
+                int R0, G0, B0, R1, G1, B1;
+                const int* br = br0 + r * G::BW;  // red/blue site
+                const int* bg = bg0 + r * G::BW;  // green site
+                int own, gq, oq, gg, hz, vt;  // R/B site: own, green, other; G site: green, horizontal, vertical
+                if (demosaic == DM_HQLI) {
+                    // detail::hqli_core (src/algorithms/interp_core.hpp:39-65)
+                    int n4 = br[-1] + br[1] + br[-G::BW] + br[G::BW];
+                    int d4 = br[-G::BW - 1] + br[-G::BW + 1] + br[G::BW - 1] + br[G::BW + 1];
+                    own = min(br[0], mv);
+                    gq = min((n4 + 2) / 4, mv);
+                    oq = min((d4 + 2) / 4, mv);
+                    gg = min(bg[0], mv);
+                    hz = min((bg[-1] + bg[1] + 1) / 2, mv);
+                    vt = min((bg[-G::BW] + bg[G::BW] + 1) / 2, mv);
+                } else {
+                    // AMAZE colour differences (src/algorithms/common.hpp:142-199, amaze.cpp:62-114).
+                    // Red/blue site xr: the other colour from the four diagonals, the red/blue sites of
+                    // rows y-1, y+1 at columns xr-1, xr+1.  Green site xg: horizontal neighbours are
+                    // this row's red/blue sites, vertical ones those of rows y-1, y+1.
+                    const float* gr = gr0 + r * G::GPW;  // this pair row's R/B green
+                    float g_rb = gr[0];
+                    float c00 = dev::fsub((float)br[-G::BW - 1], gr[-G::GPW + pa]);
+                    float c01 = dev::fsub((float)br[-G::BW + 1], gr[-G::GPW + pa + 1]);
+                    float c10 = dev::fsub((float)br[G::BW - 1], gr[G::GPW + pa]);
+                    float c11 = dev::fsub((float)br[G::BW + 1], gr[G::GPW + pa + 1]);
+                    float sum = dev::fadd(dev::fadd(dev::fadd(c00, c01), c10), c11);
+                    float fown = (float)br[0], fgq = (float)bg[0];
+                    float2 hv = dev::fadd2(make_float2(dev::fsub((float)bg[-1], gr[pl]), dev::fsub((float)bg[-G::BW], gr[-G::GPW])),
+                                           make_float2(dev::fsub((float)bg[1], gr[pl + 1]), dev::fsub((float)bg[G::BW], gr[G::GPW])));
+                    // x*0.5 and x*0.25 are exact, so these multiply-adds round once either way
+                    float other = dev::fadd(g_rb, dev::fmul(sum, 0.25f));
+                    float2 rb2 = dev::fadd2(make_float2(fgq, fgq), make_float2(dev::fmul(hv.x, 0.5f), dev::fmul(hv.y, 0.5f)));
+                    own = dev::round_plane(fown, mv);
+                    oq = dev::round_plane(other, mv);
+                    gq = dev::round_plane(g_rb, mv);
+                    gg = dev::round_plane(fgq, mv);
+                    hz = dev::round_plane(rb2.x, mv);
+                    vt = dev::round_plane(rb2.y, mv);
+                }
+                // red/blue site: R,B = own/other by row; green site: R,B = horizontal/vertical by row
+                int rr_rb = rrow ? own : oq, bb_rb = rrow ? oq : own;
+                int rr_g = rrow ? hz : vt, bb_g = rrow ? vt : hz;
+                if (rbh == 0) { R0 = rr_rb; G0 = gq; B0 = bb_rb; R1 = rr_g; G1 = gg; B1 = bb_g; }
+                else { R1 = rr_rb; G1 = gq; B1 = bb_rb; R0 = rr_g; G0 = gg; B0 = bb_g; }
+                finish(r, y0 + r, pc, x, R0, G0, B0, R1, G1, B1);
+            }
+        }
+    } else {
         const int nbk = FULL ? (G::F_TPW + 31) / 32 : (tpw + 31) >> 5;
-        const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
         for (int item = warp; item < nbk * th; item += 8) {
             int blk, r;
             if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
@@ -767,58 +1008,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 dev::border_source(x + 1, y, W, H, fp.border_mode, sx, sy);
                 demosaic_at(sx, sy, R1, G1, B1);
             }
-            // RGB-domain white balance (reference call order), CCM: scalar products, packed sums
-            if (wb_rgb) {
-                float2 t;
-                t = dev::fadd2(make_float2(dev::fmul((float)R0, wr), dev::fmul((float)R1, wr)), h5);
-                R0 = u16q(t.x, mv); R1 = u16q(t.y, mv);
-                t = dev::fadd2(make_float2(dev::fmul((float)G0, wg), dev::fmul((float)G1, wg)), h5);
-                G0 = u16q(t.x, mv); G1 = u16q(t.y, mv);
-                t = dev::fadd2(make_float2(dev::fmul((float)B0, wbl), dev::fmul((float)B1, wbl)), h5);
-                B0 = u16q(t.x, mv); B1 = u16q(t.y, mv);
-            }
-            if (ccm_on) {
-                const float* m = fp.ccm;
-                const float r0 = (float)R0, r1 = (float)R1, g0 = (float)G0, g1 = (float)G1, b0 = (float)B0, b1 = (float)B1;
-                // ((m0*r + m1*g) + m2*b) + 0.5 for both samples, each product rounded on its own
-                float2 ro = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[0], r0), dev::fmul(m[0], r1)),
-                                                             make_float2(dev::fmul(m[1], g0), dev::fmul(m[1], g1))),
-                                                  make_float2(dev::fmul(m[2], b0), dev::fmul(m[2], b1))), h5);
-                float2 go = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[3], r0), dev::fmul(m[3], r1)),
-                                                             make_float2(dev::fmul(m[4], g0), dev::fmul(m[4], g1))),
-                                                  make_float2(dev::fmul(m[5], b0), dev::fmul(m[5], b1))), h5);
-                float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[6], r0), dev::fmul(m[6], r1)),
-                                                             make_float2(dev::fmul(m[7], g0), dev::fmul(m[7], g1))),
-                                                  make_float2(dev::fmul(m[8], b0), dev::fmul(m[8], b1))), h5);
-                // (int)(v + 0.5) clamped to [0, mv]: truncation saturating at 0, then min
-                R0 = u16q(ro.x, mv); R1 = u16q(ro.y, mv);
-                G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
-                B0 = u16q(bo.x, mv); B1 = u16q(bo.y, mv);
-            }
-            int g0 = (y * W + x0) * 3 * bpc;
-            int shift = (int)((out_base + (uintptr_t)g0) & 15);
-            uint8_t* q = outs + r * G::OUT_PITCH + shift + 2 * pc * 3 * bpc;
-            const bool has1 = FULL || x + 1 < x0 + tw;
-            if (out_format == 0) {
-                const uint8_t* tt = tone_smem ? sm.tone8 : fp.tone8;
-                int t0 = tt[R0], t1 = tt[G0], t2 = tt[B0];
-                if (((shift & 1) == 0) && has1) {
-                    int t3 = tt[R1], t4 = tt[G1], t5 = tt[B1];
-                    uint16_t* q16 = reinterpret_cast<uint16_t*>(q);
-                    q16[0] = (uint16_t)(t0 | (t1 << 8));
-                    q16[1] = (uint16_t)(t2 | (t3 << 8));
-                    q16[2] = (uint16_t)(t4 | (t5 << 8));
-                } else {
-                    q[0] = (uint8_t)t0; q[1] = (uint8_t)t1; q[2] = (uint8_t)t2;
-                    if (has1) { q[3] = tt[R1]; q[4] = tt[G1]; q[5] = tt[B1]; }
-                }
-            } else if (bpc == 1) {
-                q[0] = (uint8_t)R0; q[1] = (uint8_t)G0; q[2] = (uint8_t)B0;
-                if (has1) { q[3] = (uint8_t)R1; q[4] = (uint8_t)G1; q[5] = (uint8_t)B1; }
-            } else {
-                int v[6] = {R0, G0, B0, R1, G1, B1};
-                for (int k = 0; k < (has1 ? 6 : 3); k++) { q[2 * k] = (uint8_t)v[k]; q[2 * k + 1] = (uint8_t)(v[k] >> 8); }
-            }
+            finish(r, y, pc, x, R0, G0, B0, R1, G1, B1);
         }
     }
     __syncthreads();
