@@ -123,6 +123,85 @@ __device__ int resolve_chains(const FrameParams& fp, Orig orig, const FixupScrat
     return n_ov;
 }
 
+// The same resolution by one warp, for the fix-up launch: lane 0 owns the heap and the override
+// list; for every popped pixel, lanes 0..3 evaluate its earlier neighbours (override or Jacobi
+// value), lanes 4..7 read its later neighbours, lane 8 its own sample and lane 9 its Jacobi
+// value, all at once, so the serial chain waits on one round of loads per pixel instead of six.
+template <class Orig>
+__device__ int resolve_chains_warp(const FrameParams& fp, Orig orig, const FixupScratch& fs) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int W = fp.w, H = fp.h;
+    int* heap = fs.heap;
+    int hn = 0, n_ov = 0, last = -1;
+    if (lane == 0) {
+        const int n_seed = min(*fp.seed_count, fp.seed_cap);
+        for (int i = 0; i < n_seed; i++) heap_push(heap, hn, fp.seeds[i]);
+    }
+    hn = __shfl_sync(full, hn, 0);
+    while (hn > 0) {
+        int p = 0;
+        if (lane == 0) p = heap_pop(heap, hn);
+        p = __shfl_sync(full, p, 0);
+        hn = __shfl_sync(full, hn, 0);
+        if (p == last) continue;
+        last = p;
+        const int x = p % W, y = p / W;
+        const unsigned m = dev::dpc_valid_mask(x, y, W, H);
+        __syncwarp();  // lane 0's override writes are visible to the lanes that search them
+        int v = 0;
+        if (lane < 8) {
+            if ((m >> lane) & 1u) {
+                int dx, dy;
+                nb_offsets(lane, dx, dy);
+                const int nx = x + dx, ny = y + dy;
+                if (lane < 4) {
+                    const int s = find_override(fs.ov_idx, fs.ov_val, n_ov, ny * W + nx);
+                    v = s >= 0 ? s : jacobi_at(fp, orig, nx, ny);
+                } else {
+                    v = orig(nx, ny);
+                }
+            }
+        } else if (lane == 8) {
+            v = orig(x, y);
+        } else if (lane == 9) {
+            v = jacobi_at(fp, orig, x, y);
+        }
+        int nb[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) nb[k] = __shfl_sync(full, v, k);
+        const int c = __shfl_sync(full, v, 8), jac = __shfl_sync(full, v, 9);
+        int stop = 0;
+        if (lane == 0) {
+            const int s = dev::dpc_apply(c, nb, m, fp.dpc_thr);
+            if (s != jac) {
+                if (n_ov >= fs.cap) {
+                    atomicExch(fp.status, 104 /* IMOP_ERR_CAPACITY */);
+                    stop = 1;
+                } else {
+                    fs.ov_idx[n_ov] = p;
+                    fs.ov_val[n_ov] = s;
+                    n_ov++;
+                    for (int k = 4; k < 8; k++) {
+                        if (!((m >> k) & 1u)) continue;
+                        int dx, dy;
+                        nb_offsets(k, dx, dy);
+                        if (hn >= fs.cap) {
+                            atomicExch(fp.status, 104);
+                            break;
+                        }
+                        heap_push(heap, hn, (y + dy) * W + (x + dx));
+                    }
+                }
+            }
+        }
+        n_ov = __shfl_sync(full, n_ov, 0);
+        hn = __shfl_sync(full, hn, 0);
+        if (__shfl_sync(full, stop, 0)) break;
+    }
+    return n_ov;
+}
+
 struct GlobalOrig {
     const FrameParams* fp;
     PatternOffsets po;

@@ -120,37 +120,49 @@ __global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_c
     }
 }
 
-// defect-chain fix-up (adaptive mode), one CTA per frame of the launch
+// Defect-chain fix-up (adaptive mode) in two launches: the raster-order resolution, one warp
+// per frame, then the re-rendering of the output windows around every changed pixel, spread
+// over kRenderCtas CTAs per frame.  Windows may overlap; overlapping windows write identical
+// values.
+constexpr int kRenderCtas = 16;
+
+__global__ void __launch_bounds__(32) dpc_resolve_kernel(const __grid_constant__ BatchLaunch bl) {
+    const FrameParams& fp = bl.frames[blockIdx.x];
+    if (!((fp.stages & 2u) && fp.dpc_mode == 0)) return;
+    int n_ov = 0;
+    if (*fp.seed_count > 0) {
+        const FixupScratch fs{fp.fix_heap, fp.fix_ov_idx, fp.fix_ov_val, fp.fix_n_ov, fp.fix_cap};
+        GlobalOrig orig{&fp, pattern_offsets(fp.pattern)};
+        n_ov = resolve_chains_warp(fp, orig, fs);
+    }
+    if (threadIdx.x == 0) *fp.fix_n_ov = n_ov;
+}
+
 template <int TW, int TH, int OUTB>
-__global__ void __launch_bounds__(kThreads) dpc_fixup_kernel(const __grid_constant__ BatchLaunch bl) {
+__global__ void __launch_bounds__(kThreads) dpc_render_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
-    __shared__ int s_nov;
-    const FrameParams& gfp = bl.frames[blockIdx.x];
-    if (!((gfp.stages & 2u) && gfp.dpc_mode == 0) || *gfp.seed_count == 0) return;
+    const int f = blockIdx.x / kRenderCtas, part = blockIdx.x - f * kRenderCtas;
+    const FrameParams& gfp = bl.frames[f];
+    if (!((gfp.stages & 2u) && gfp.dpc_mode == 0)) return;
+    const int n_ov = *gfp.fix_n_ov;
+    if (part >= n_ov) return;
     tile_init(sm);
     if (threadIdx.x < 32) {
         const int* s = reinterpret_cast<const int*>(&gfp);
         int* d = reinterpret_cast<int*>(&sm.fp[0]);
         for (int k = threadIdx.x; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
     }
-    const FixupScratch fs{gfp.fix_heap, gfp.fix_ov_idx, gfp.fix_ov_val, gfp.fix_n_ov, gfp.fix_cap};
-    if (threadIdx.x == 0) {
-        GlobalOrig orig{&gfp, pattern_offsets(gfp.pattern)};
-        s_nov = resolve_chains(gfp, orig, fs);
-        *fs.n_ov = s_nov;
-    }
     __syncthreads();
-    const int n_ov = s_nov;
-    Overrides ov{fs.ov_idx, fs.ov_val, n_ov};
+    const Overrides ov{gfp.fix_ov_idx, gfp.fix_ov_val, n_ov};
     uint32_t parity = 0;
-    // re-render the output window around each changed pixel: radius 3 of demosaic support plus
-    // 2 of border copies, started on an even column
-    for (int k = 0; k < n_ov; k++) {
-        int p = fs.ov_idx[k];
-        int x = p % gfp.w, y = p / gfp.w;
-        int wx0 = max(0, (x - 5) & ~1), wx1 = min(gfp.w, x + 6);
-        int wy0 = max(0, y - 5), wy1 = min(gfp.h, y + 6);
+    // the output window around a changed pixel: radius 3 of demosaic support plus 2 of border
+    // copies, started on an even column
+    for (int k = part; k < n_ov; k += kRenderCtas) {
+        const int p = gfp.fix_ov_idx[k];
+        const int x = p % gfp.w, y = p / gfp.w;
+        const int wx0 = max(0, (x - 5) & ~1), wx1 = min(gfp.w, x + 6);
+        const int wy0 = max(0, y - 5), wy1 = min(gfp.h, y + 6);
         if (!process_tile_sync<TW, TH, OUTB>(sm, wx0, wy0, wx1 - wx0, wy1 - wy0, ov, parity)) return;
     }
 }
@@ -237,7 +249,7 @@ struct FusedKernels {
             e = cudaFuncSetAttribute(fused_batch_kernel<kTileW, kTileH, OUTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem);
             if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(dpc_fixup_kernel<kTileW, kTileH, OUTB>,
+                e = cudaFuncSetAttribute(dpc_render_kernel<kTileW, kTileH, OUTB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int n = 0, m = 0;
             if (e == cudaSuccess)
@@ -257,7 +269,10 @@ struct FusedKernels {
         if (e != cudaSuccess) return e;
         if (bl.n_items > 0)
             fused_batch_kernel<kTileW, kTileH, OUTB><<<bl.n_items < limit ? bl.n_items : limit, kThreads, smem, st>>>(bl);
-        if (fixup) dpc_fixup_kernel<kTileW, kTileH, OUTB><<<bl.n_frames, kThreads, smem, st>>>(bl);
+        if (fixup) {
+            dpc_resolve_kernel<<<bl.n_frames, 32, 0, st>>>(bl);
+            dpc_render_kernel<kTileW, kTileH, OUTB><<<bl.n_frames * kRenderCtas, kThreads, smem, st>>>(bl);
+        }
         return cudaGetLastError();
     }
 };

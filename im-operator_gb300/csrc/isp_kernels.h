@@ -57,7 +57,8 @@ cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots
 cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st);
 // map resolve (map mode) + seed reset + fused tiles + fix-up, in stream order
 cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st);
-// Up to kBatchInline frames in one persistent launch plus one fix-up launch.  Each frame carries
+// Up to kBatchInline frames in one persistent launch plus the two fix-up launches (chain
+// resolution, window re-rendering).  Each frame carries
 // its own seed counter, seed list and fix-up scratch (FrameParams::fix_*); its seed counter must be
 // zero and its map-mode values resolved when the launch runs.  tiles_x / tiles_y are filled in.
 cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st);
