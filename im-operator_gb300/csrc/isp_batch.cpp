@@ -118,18 +118,6 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         fp.gh = p->lsc_mode == IMOP_LSC_FLAT_FIELD ? 24 : p->lsc_grid_h;
         fp.grid = (const float*)slot->ptr;
     }
-    if (p->demosaic == IMOP_DEMOSAIC_AMAZE) {
-        auto& slot = tc.rtab[p->bit_depth];
-        if (!slot) {
-            std::unique_ptr<DevBuf> b(new DevBuf());
-            int n = 3 * fp.mv + 1;
-            if ((e = b->ensure((size_t)n * sizeof(float)))) return cuda_fail(e, "alloc rtab");
-            if ((e = launch_recip_table((float*)b->ptr, n, c->aux)) || (e = cudaStreamSynchronize(c->aux)))
-                return cuda_fail(e, "rtab kernel");
-            slot = std::move(b);
-        }
-        fp.rtab = (const float*)slot->ptr;
-    }
     {
         Hash h;
         h.val(p->out_format);

@@ -350,12 +350,6 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
             fp.grid = (const float*)tabs.grid.ptr;
         }
     }
-    // AMAZE reciprocal table 1/(1+k), k = 0 .. 3*mv (the largest gradient sum)
-    if (p->demosaic == IMOP_DEMOSAIC_AMAZE) {
-        if ((e = tabs.rtab.ensure((size_t)(3 * fp.mv + 1) * sizeof(float)))) return cuda_fail(e, "alloc rtab");
-        if ((e = launch_recip_table((float*)tabs.rtab.ptr, 3 * fp.mv + 1, st))) return cuda_fail(e, "rtab kernel");
-        fp.rtab = (const float*)tabs.rtab.ptr;
-    }
     // tone table (padded: the kernel reads it in 4-byte words)
     if ((e = tabs.tone8.ensure(std::max<size_t>((size_t)fp.mv + 1, 4096) + 16))) return cuda_fail(e, "alloc tone table");
     fp.tone8 = (const uint8_t*)tabs.tone8.ptr;

@@ -100,8 +100,6 @@ struct FrameParams {
     float ccm[9];
     // tone: 2^bd-entry u8 table
     const uint8_t* tone8;
-    // AMAZE: rtab[k] = 1/(1+k) correctly rounded, k in [0, 3*mv]
-    const float* rtab;
     // the demosaic's u16 read shifts MSB-aligned samples (no earlier stage clamped them)
     int need_align;
     // data

@@ -27,7 +27,7 @@ struct DevBuf {
 
 // device copies of one frame's parameter tables
 struct FrameTables {
-    DevBuf grid, lut, knots, tone8, rtab;
+    DevBuf grid, lut, knots, tone8;
     DevBuf map_row_ptr, map_ent, map_val, slot_xy, comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
     MapPlan plan{};
     int n_slots = 0;  // unique map pixels (entries of map_val)
@@ -52,7 +52,6 @@ cudaError_t upload(DevBuf& b, const std::vector<T>& v) {
 struct TableCache {
     std::unordered_map<uint64_t, std::unique_ptr<DevBuf>> grids, tones;
     std::unordered_map<uint64_t, std::unique_ptr<FrameTables>> maps;
-    std::unique_ptr<DevBuf> rtab[17];
     size_t entries() const { return grids.size() + tones.size() + maps.size(); }
 };
 

@@ -45,12 +45,6 @@ __global__ void tone_table_kernel(int mode, const float* lut, const float* knots
     out[v] = (uint8_t)dev::clampi(q, 0, 255);
 }
 
-// rtab[k] = 1 / (1 + k), correctly rounded (the AMAZE weights 1.0f / (1.0f + gradient))
-__global__ void recip_table_kernel(float* out, int n) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) out[k] = __frcp_rn((float)(1 + k));
-}
-
 // ---------------------------------------------------------------------------------------------
 // Persistent tile kernel: CTA c takes items c, c + gridDim.x, ... of the launch's tile list (the
 // tiles of each rectangle in raster order).  Warp 0 stages the next item into the other raw
@@ -216,11 +210,6 @@ cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots
                               cudaStream_t st) {
     int n = max_val_of(bd) + 1;
     tone_table_kernel<<<(n + 255) / 256, 256, 0, st>>>(mode, d_lut, d_knots, bd, d_out);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_recip_table(float* d_out, int n, cudaStream_t st) {
-    recip_table_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_out, n);
     return cudaGetLastError();
 }
 

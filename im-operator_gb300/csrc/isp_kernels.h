@@ -50,7 +50,6 @@ struct MapPlan {
 };
 
 int fused_tile_grid(int w, int h, int& ntx, int& nty);
-cudaError_t launch_recip_table(float* d_out, int n, cudaStream_t st);
 cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots, int bd, uint8_t* d_out,
                               cudaStream_t st);
 // map-mode defect values of one frame (before the kernels that read them)

@@ -6,7 +6,7 @@
 // memory pressure at a moment the caller does not control.  imop_isp_run_device_noalloc() runs
 // the same fused kernel and defect-chain fix-up as imop_isp_run_device(), but everything it needs
 // beyond the caller's input and output frames - the parameter tables (lens-shading grid, tone
-// LUT, the 8-bit tone table, the AMAZE reciprocal table) and the fix-up scratch (seed list, heap,
+// LUT, the 8-bit tone table) and the fix-up scratch (seed list, heap,
 // override list, counters, status word) - lives in the file-scope array g_noalloc_scratch below,
 // which every GPU that loads the library holds until the process exits.
 //
@@ -33,7 +33,6 @@ constexpr int kSeedCap = 16384;          // defect-chain seeds (and heap / overr
 constexpr int kGridMaxNodes = 64 * 64;   // lens-shading grid nodes
 constexpr int kMaxBitDepth = 12;
 constexpr int kToneMax = 1 << kMaxBitDepth;
-constexpr int kRtabMax = 3 * (kToneMax - 1) + 1;
 constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch {
@@ -46,13 +45,12 @@ struct NoAllocScratch {
     int ov_idx[kSeedCap];
     int ov_val[kSeedCap];
     float grid[kGridMaxNodes * 4];
-    float rtab[kRtabMax];
     float lut[kToneMax];
     float knots[36];
     alignas(16) uint8_t tone8[kToneMax + 16];
 };
 
-// about 390 KB per device
+// about 340 KB per device
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 std::mutex g_setup_mu;
@@ -111,10 +109,6 @@ extern "C" int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d
         fp.gw = p->lsc_grid_w;
         fp.gh = p->lsc_grid_h;
         fp.grid = sc->grid;
-    }
-    if (p->demosaic == IMOP_DEMOSAIC_AMAZE) {
-        if ((e = launch_recip_table(sc->rtab, 3 * fp.mv + 1, st))) return cuda_fail(e, "rtab kernel");
-        fp.rtab = sc->rtab;
     }
     fp.tone8 = sc->tone8;
     if (p->out_format == IMOP_OUT_RGB8) {

@@ -694,7 +694,6 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     // ---- 4b. green at the red/blue site of each pair (AMAZE, MG) ---------------------------
     if (FULL && demosaic != DM_HQLI) {
         // one column block and one row parity per warp, as in the defect phase
-        const float* rtab = fp.rtab;
         const bool fast_div = fp.bd <= 12;
         const int pc = (warp & 1) * 32 + lane;
         const int r0 = warp >> 1;
@@ -707,7 +706,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 const int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
                 float g;
                 if (demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab, fast_div);
+                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
@@ -722,7 +721,6 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         }
     } else if (demosaic != DM_HQLI) {
         const int nbk = (gpw + 31) >> 5;
-        const float* rtab = fp.rtab;
         const bool fast_div = fp.bd <= 12;
         for (int item = warp; item < nbk * gh; item += 8) {
             int blk, r;
@@ -738,7 +736,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 int cc = bp[0], hm1 = bp[-1], hp1 = bp[1], hm2 = bp[-2], hp2 = bp[2];
                 int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
                 if (demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_tab(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, rtab, fast_div);
+                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);

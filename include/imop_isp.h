@@ -284,7 +284,7 @@ int imop_isp_backward_device(imop_isp_t ctx, const ImopAdjointDesc* d, const flo
  * its own pool, or a real-time loop that cannot afford cudaMalloc / cudaFree stalling the device.
  * It runs the same fused pipeline as imop_isp_run_device on the caller's device frames and
  * allocates nothing: its parameter tables and defect-chain scratch live in one file-scope device
- * array of about 390 KB that every GPU loading the library keeps until exit.  The first call on
+ * array of about 340 KB that every GPU loading the library keeps until exit.  The first call on
  * each device looks up that array's address (cudaGetSymbolAddress, with the device current); make
  * that first call before any stream capture begins.  Limits: bit depth <= 12, lens shading by an
  * explicit grid of at most 64x64 nodes or by polynomial, adaptive defect correction only (no
