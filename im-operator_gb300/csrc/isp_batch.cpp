@@ -209,6 +209,7 @@ int prepare_batch(imop_isp_ctx* c, const ImopFrameDesc* frames, int n, std::vect
         fp.seeds = (int*)b.seeds.ptr + off;
         fp.seed_cap = b.cap;
         fp.status = (int*)c->fix.status.ptr;
+        fp.tile_counter = (int*)c->fix.tile_counter.ptr;
         fp.fix_heap = (int*)b.heap.ptr + off;
         fp.fix_ov_idx = (int*)b.ov_idx.ptr + off;
         fp.fix_ov_val = (int*)b.ov_val.ptr + off;
@@ -388,6 +389,7 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
         fp.seeds = fix_fp.seeds;
         fp.seed_cap = fix_fp.seed_cap;
         fp.status = fix_fp.status;
+        fp.tile_counter = fix_fp.tile_counter;
         fp.in = (const uint8_t*)P.d_in[s].ptr;
         fp.out = (uint8_t*)P.d_out[s].ptr;
         // copy in once the slot's previous kernels have read it

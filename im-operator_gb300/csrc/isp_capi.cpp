@@ -375,6 +375,7 @@ int ensure_fixup(FixupState& fx, int cap) {
     cudaError_t e;
     if (fx.cap >= cap && fx.seed_count.ptr) return IMOP_OK;
     if ((e = fx.seed_count.ensure(sizeof(int))) || (e = fx.status.ensure(sizeof(int))) ||
+        (e = fx.tile_counter.ensure(sizeof(int))) ||
         (e = fx.seeds.ensure((size_t)cap * sizeof(int))) || (e = fx.heap.ensure((size_t)cap * sizeof(int))) ||
         (e = fx.ov_idx.ensure((size_t)cap * sizeof(int))) || (e = fx.ov_val.ensure((size_t)cap * sizeof(int))) ||
         (e = fx.n_ov.ensure(sizeof(int))))
@@ -391,6 +392,7 @@ void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs) {
     fp.seeds = (int*)fx.seeds.ptr;
     fp.seed_cap = fx.cap;
     fp.status = (int*)fx.status.ptr;
+    fp.tile_counter = (int*)fx.tile_counter.ptr;
     fs.heap = (int*)fx.heap.ptr;
     fs.ov_idx = (int*)fx.ov_idx.ptr;
     fs.ov_val = (int*)fx.ov_val.ptr;

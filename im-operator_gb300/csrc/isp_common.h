@@ -110,6 +110,7 @@ struct FrameParams {
     int* seeds;
     int seed_cap;
     int* status;         // sticky error word (IMOP_ERR_*), 0 when fine
+    int* tile_counter;   // next-tile counter of the fused launch (one per launch, zeroed before it)
     // defect-chain fix-up scratch of this frame (heap, sorted override list)
     int* fix_heap;
     int* fix_ov_idx;

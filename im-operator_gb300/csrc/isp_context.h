@@ -80,7 +80,7 @@ struct BatchGraph {
 
 // defect-chain scratch (seeds, heap, overrides) and the sticky status word
 struct FixupState {
-    DevBuf seed_count, seeds, heap, ov_idx, ov_val, n_ov, status;
+    DevBuf seed_count, seeds, heap, ov_idx, ov_val, n_ov, status, tile_counter;
     int cap = 0;
 };
 

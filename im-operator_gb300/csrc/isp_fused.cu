@@ -46,10 +46,10 @@ __global__ void tone_table_kernel(int mode, const float* lut, const float* knots
 }
 
 // ---------------------------------------------------------------------------------------------
-// Persistent tile kernel: CTA c takes items c, c + gridDim.x, ... of the launch's tile list (the
-// tiles of each rectangle in raster order).  Warp 0 stages the next item into the other raw
-// buffer before the CTA computes the current one, so the copy of tile k+1 overlaps the
-// arithmetic of tile k.
+// Persistent tile kernel: CTA c starts with item c of the launch's tile list (the tiles of each
+// rectangle in raster order) and then claims items from the launch's counter, one item ahead of
+// the one it stages.  Warp 0 stages the next item into the other raw buffer before the CTA
+// computes the current one, so the copy of tile k+1 overlaps the arithmetic of tile k.
 
 // rectangle of item `item`: the last rectangle starting at or before it
 __device__ __forceinline__ int item_rect(const BatchLaunch& bl, int item) {
@@ -86,30 +86,42 @@ template <int TW, int TH, int OUTB>
 __global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
-    int item = blockIdx.x;
-    if (item >= bl.n_items) return;
+    const int n_items = bl.n_items;
+    if ((int)blockIdx.x >= n_items) return;
     tile_init(sm);
     uint32_t par0 = 0, par1 = 0;
     const Overrides none{nullptr, nullptr, 0};
-    if (threadIdx.x < 32) stage_item(sm, bl, item, 0);
+    // lane 0 of warp 0 holds the item claimed after the staged one (its counter read completes
+    // while the CTA computes)
+    int claimed = 0;
+    if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
+    if (threadIdx.x < 32) stage_item(sm, bl, blockIdx.x, 0);
     __syncthreads();
     int b = 0;
     while (true) {
-        const int next = item + gridDim.x;
-        if (next < bl.n_items && threadIdx.x < 32) stage_item(sm, bl, next, b ^ 1);
+        if (threadIdx.x < 32) {
+            const int next = __shfl_sync(0xffffffffu, claimed, 0);
+            if (next < n_items) {
+                if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
+                stage_item(sm, bl, next, b ^ 1);
+            }
+            if (threadIdx.x == 0) sm.next_item[b ^ 1] = next;
+        }
         const FrameParams& fp = sm.fp[b];
         const bool full = tile_is_full<TW, TH>(fp, sm.tile[b][0], sm.tile[b][1], sm.tile[b][2], sm.tile[b][3]);
         uint32_t& par = b ? par1 : par0;
         bool ok = full ? compute_tile<TW, TH, OUTB, true>(sm, b, none, true, par)
                        : compute_tile<TW, TH, OUTB, false>(sm, b, none, true, par);
+        // next_item[b ^ 1] was written before the barriers of compute_tile and is written again two
+        // iterations on, after every thread has passed the barriers of the next compute_tile
+        const bool more = sm.next_item[b ^ 1] < n_items;
         if (!ok) {
             // leave no bulk copy in flight into this CTA's shared memory
-            if (next < bl.n_items && (reinterpret_cast<uintptr_t>(sm.fp[b ^ 1].in) & 15) == 0)
+            if (more && (reinterpret_cast<uintptr_t>(sm.fp[b ^ 1].in) & 15) == 0)
                 wait_bar(&sm.bar[b ^ 1], b ? par0 : par1);
             return;
         }
-        if (next >= bl.n_items) return;
-        item = next;
+        if (!more) return;
         b ^= 1;
     }
 }
@@ -256,8 +268,10 @@ struct FusedKernels {
         int limit = 0;
         cudaError_t e = setup(limit);
         if (e != cudaSuccess) return e;
-        if (bl.n_items > 0)
+        if (bl.n_items > 0) {
+            if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             fused_batch_kernel<kTileW, kTileH, OUTB><<<bl.n_items < limit ? bl.n_items : limit, kThreads, smem, st>>>(bl);
+        }
         if (fixup) {
             dpc_resolve_kernel<<<bl.n_frames, 32, 0, st>>>(bl);
             dpc_render_kernel<kTileW, kTileH, OUTB><<<bl.n_frames * kRenderCtas, kThreads, smem, st>>>(bl);
@@ -286,6 +300,10 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st) {
     BatchLaunch bl;
     bl.n_frames = n;
     bl.n_rects = 0;
+    // the frames of one launch come from one context and share its counter
+    bl.tile_counter = frames[0].tile_counter;
+    for (int f = 0; f < n; f++)
+        if (!frames[f].tile_counter || frames[f].tile_counter != bl.tile_counter) return cudaErrorInvalidValue;
     int items = 0;
     bool fixup = false;
     for (int f = 0; f < n; f++) {

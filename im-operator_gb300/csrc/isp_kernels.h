@@ -13,7 +13,8 @@ constexpr int kTileH = 24;
 
 // Frames of one fused launch, passed by value as the kernel's parameter block.  The kernel walks
 // the tiles of a list of rectangles (one per frame), rectangle after rectangle, tiles in raster
-// order.
+// order; CTAs claim tiles from a device counter, so border tiles (the general path) and
+// partial tiles do not unbalance the CTAs.
 constexpr int kBatchInline = 16;
 constexpr int kMaxRects = kBatchInline;
 struct TileRect {
@@ -25,6 +26,7 @@ struct BatchLaunch {
     int n_frames;
     int n_items;
     int n_rects;
+    int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];

@@ -39,7 +39,7 @@ struct NoAllocScratch {
     int seed_count;
     int n_ov;
     int status;
-    int pad;
+    int tile_counter;
     int seeds[kSeedCap];
     int heap[kSeedCap];
     int ov_idx[kSeedCap];
@@ -133,6 +133,7 @@ extern "C" int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d
     fp.seeds = sc->seeds;
     fp.seed_cap = kSeedCap;
     fp.status = &sc->status;
+    fp.tile_counter = &sc->tile_counter;
     FixupScratch fs{sc->heap, sc->ov_idx, sc->ov_val, &sc->n_ov, kSeedCap};
     if ((e = launch_fused(fp, fs, nullptr, st))) return cuda_fail(e, "fused launch");
     if ((e = cudaStreamSynchronize(st))) return cuda_fail(e, "no-alloc run");

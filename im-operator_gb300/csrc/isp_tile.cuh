@@ -95,6 +95,8 @@ struct TileGeom {
     static constexpr int F_BPW = (TW + 9) / 2, F_BH = TH + 6;
     static constexpr int F_GPW = (TW + 5) / 2, F_GH = TH + 2;
     static constexpr int F_TPW = (TW + 1) / 2;
+    // full tiles give every warp one of two blocks of 32 pair columns
+    static_assert(F_BPW <= 64 && F_GPW <= 64 && F_TPW <= 64, "full-tile loops cover two blocks of 32 pair columns");
 };
 
 template <int TW, int TH, int OUTB>
@@ -114,6 +116,7 @@ struct TileSmem {
     int row_gy[G::BRH];
     float row_fy[G::BRH];
     int tile[2][4];                            // x0, y0, tw, th of each staged tile
+    int next_item[2];                          // item staged into each buffer (>= n_items: none)
     const uint8_t* tone_src;                   // the tone table held in tone8
     alignas(8) uint64_t bar[2];
 };
