@@ -242,6 +242,7 @@ int device_ready() {
 // table pointers are left null for the caller to fill.
 void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
     std::memset(&fp, 0, sizeof(fp));
+    fp.neg_zero = -0.0f;
     fp.w = p->width;
     fp.h = p->height;
     fp.bd = p->bit_depth;

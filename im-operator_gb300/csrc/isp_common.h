@@ -118,6 +118,8 @@ struct FrameParams {
     int* fix_n_ov;
     int fix_cap;         // entries of fix_heap / fix_ov_*
     int tiles_x, tiles_y;  // tile grid of this frame
+    // -0.0f, read at run time: the addend of the packed products (see dev::pmul)
+    float neg_zero;
 };
 
 }  // namespace imop

@@ -306,6 +306,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const int gpw = FULL ? G::F_GPW : (tw + 5) / 2, gh = FULL ? G::F_GH : th + 2;
     const int tpw = FULL ? G::F_TPW : (tw + 1) / 2;  // own pairs
     const bool tone_smem = fp.out_format == 0 && fp.bd <= 12;
+    const float2 z2 = make_float2(fp.neg_zero, fp.neg_zero);  // addend of the packed products
     uint8_t* raw = sm.raw[b];
 
     // tone table (when the frame's table changed) and lens-shading tables, then the staged bytes
@@ -451,7 +452,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         const int r0 = warp >> 1;
         const int p = (yb + r0) & 1;
         const int c0 = bayer_color(p, 0, po), c1 = bayer_color(p, 1, po);
-        const float WB0 = fp.wb_cfa[c0], WB1 = fp.wb_cfa[c1];
+        const float2 WB = make_float2(fp.wb_cfa[c0], fp.wb_cfa[c1]);
         const int x = xb + 2 * pc;
         if (pc < G::F_BPW) {
             float f0 = 0.f, f1 = 0.f;
@@ -462,9 +463,10 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 gxa = sm.col_gx[2 * pc];
                 gxb = sm.col_gx[2 * pc + 1];
             }
-            const float of0 = dev::fsub(1.0f, f0), of1 = dev::fsub(1.0f, f1);
+            const float2 f01 = make_float2(f0, f1);
+            const float2 of01 = make_float2(dev::fsub(1.0f, f0), dev::fsub(1.0f, f1));
             int cache_gy = -1;
-            float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f;
+            float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A;
             const int* ob = orig + 2 * G::OW + (x - xo);
             for (int r = r0; r < G::F_BH; r += 4) {
                 const int y = yb + r;
@@ -510,18 +512,17 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                         cache_gy = gy_i;
                         const float* g0 = fp.grid + (gy_i * fp.gw + gxa) * 4 + c0;
                         const float* g1 = fp.grid + (gy_i * fp.gw + gxb) * 4 + c1;
-                        A0 = dev::fmul(__ldg(g0), of0); A1 = dev::fmul(__ldg(g1), of1);
-                        B0 = dev::fmul(__ldg(g0 + 4), f0); B1 = dev::fmul(__ldg(g1 + 4), f1);
-                        C0 = dev::fmul(__ldg(g0 + 4 * fp.gw), of0); C1 = dev::fmul(__ldg(g1 + 4 * fp.gw), of1);
-                        D0 = dev::fmul(__ldg(g0 + 4 * fp.gw + 4), f0); D1 = dev::fmul(__ldg(g1 + 4 * fp.gw + 4), f1);
+                        A = dev::pmul(make_float2(__ldg(g0), __ldg(g1)), of01, z2);
+                        B = dev::pmul(make_float2(__ldg(g0 + 4), __ldg(g1 + 4)), f01, z2);
+                        C = dev::pmul(make_float2(__ldg(g0 + 4 * fp.gw), __ldg(g1 + 4 * fp.gw)), of01, z2);
+                        D = dev::pmul(make_float2(__ldg(g0 + 4 * fp.gw + 4), __ldg(g1 + 4 * fp.gw + 4)), f01, z2);
                     }
                     const float fy = sm.row_fy[r], ofy = dev::fsub(1.0f, fy);
-                    float2 pa = make_float2(dev::fmul(A0, ofy), dev::fmul(A1, ofy));
-                    float2 pb = make_float2(dev::fmul(B0, ofy), dev::fmul(B1, ofy));
-                    float2 pcc = make_float2(dev::fmul(C0, fy), dev::fmul(C1, fy));
-                    float2 pd = make_float2(dev::fmul(D0, fy), dev::fmul(D1, fy));
-                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(pa, pb), pcc), pd);
-                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, gain.x), dev::fmul((float)u1, gain.y)), h5);
+                    const float2 fy2 = make_float2(fy, fy), ofy2 = make_float2(ofy, ofy);
+                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(A, ofy2, z2), dev::pmul(B, ofy2, z2)),
+                                                        dev::pmul(C, fy2, z2)),
+                                             dev::pmul(D, fy2, z2));
+                    float2 t = dev::fadd2(dev::pmul(make_float2((float)u0, (float)u1), gain, z2), h5);
                     u0 = u16q(t.x, mv);
                     u1 = u16q(t.y, mv);
                 } else if (lsc_poly) {
@@ -529,7 +530,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     u1 = dev::lsc_poly(fp, u1, x + 1, y, c1);
                 }
                 if (wb_bayer) {
-                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, WB0), dev::fmul((float)u1, WB1)), h5);
+                    float2 t = dev::fadd2(dev::pmul(make_float2((float)u0, (float)u1), WB, z2), h5);
                     u0 = u16q(t.x, mv);
                     u1 = u16q(t.y, mv);
                 }
@@ -543,7 +544,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     } else {
         const int nbk = (bpw + 31) >> 5;
         int cache_key = -1;
-        float A0 = 0.f, A1 = 0.f, B0 = 0.f, B1 = 0.f, C0 = 0.f, C1 = 0.f, D0 = 0.f, D1 = 0.f, WB0 = 1.f, WB1 = 1.f;
+        float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A, WB = make_float2(1.f, 1.f);
         for (int item = warp; item < nbk * bh; item += 8) {
             int blk, r;
             if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
@@ -608,23 +609,22 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     if (key != cache_key) {
                         // g00*(1-fx), g10*fx, g01*(1-fx), g11*fx of both samples for this cell row
                         cache_key = key;
-                        float f0 = sm.col_fx[2 * pc], f1 = sm.col_fx[2 * pc + 1];
+                        const float2 f01 = make_float2(sm.col_fx[2 * pc], sm.col_fx[2 * pc + 1]);
+                        const float2 of01 = make_float2(dev::fsub(1.0f, f01.x), dev::fsub(1.0f, f01.y));
                         const float* g0 = fp.grid + (gy_i * fp.gw + sm.col_gx[2 * pc]) * 4 + c0;
                         const float* g1 = fp.grid + (gy_i * fp.gw + sm.col_gx[2 * pc + 1]) * 4 + c1;
-                        float of0 = dev::fsub(1.0f, f0), of1 = dev::fsub(1.0f, f1);
-                        A0 = dev::fmul(__ldg(g0), of0); A1 = dev::fmul(__ldg(g1), of1);
-                        B0 = dev::fmul(__ldg(g0 + 4), f0); B1 = dev::fmul(__ldg(g1 + 4), f1);
-                        C0 = dev::fmul(__ldg(g0 + 4 * fp.gw), of0); C1 = dev::fmul(__ldg(g1 + 4 * fp.gw), of1);
-                        D0 = dev::fmul(__ldg(g0 + 4 * fp.gw + 4), f0); D1 = dev::fmul(__ldg(g1 + 4 * fp.gw + 4), f1);
-                        WB0 = fp.wb_cfa[c0]; WB1 = fp.wb_cfa[c1];
+                        A = dev::pmul(make_float2(__ldg(g0), __ldg(g1)), of01, z2);
+                        B = dev::pmul(make_float2(__ldg(g0 + 4), __ldg(g1 + 4)), f01, z2);
+                        C = dev::pmul(make_float2(__ldg(g0 + 4 * fp.gw), __ldg(g1 + 4 * fp.gw)), of01, z2);
+                        D = dev::pmul(make_float2(__ldg(g0 + 4 * fp.gw + 4), __ldg(g1 + 4 * fp.gw + 4)), f01, z2);
+                        WB = make_float2(fp.wb_cfa[c0], fp.wb_cfa[c1]);
                     }
-                    float fy = sm.row_fy[r], ofy = dev::fsub(1.0f, fy);
-                    float2 pa = make_float2(dev::fmul(A0, ofy), dev::fmul(A1, ofy));
-                    float2 pb = make_float2(dev::fmul(B0, ofy), dev::fmul(B1, ofy));
-                    float2 pcc = make_float2(dev::fmul(C0, fy), dev::fmul(C1, fy));
-                    float2 pd = make_float2(dev::fmul(D0, fy), dev::fmul(D1, fy));
-                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(pa, pb), pcc), pd);
-                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, gain.x), dev::fmul((float)u1, gain.y)), h5);
+                    const float fy = sm.row_fy[r], ofy = dev::fsub(1.0f, fy);
+                    const float2 fy2 = make_float2(fy, fy), ofy2 = make_float2(ofy, ofy);
+                    float2 gain = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(A, ofy2, z2), dev::pmul(B, ofy2, z2)),
+                                                        dev::pmul(C, fy2, z2)),
+                                             dev::pmul(D, fy2, z2));
+                    float2 t = dev::fadd2(dev::pmul(make_float2((float)u0, (float)u1), gain, z2), h5);
                     u0 = u16q(t.x, mv);
                     u1 = u16q(t.y, mv);
                 } else {
@@ -632,11 +632,10 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                         u0 = dev::lsc_poly(fp, u0, x, y, c0);
                         u1 = dev::lsc_poly(fp, u1, x + 1, y, c1);
                     }
-                    WB0 = fp.wb_cfa[c0];
-                    WB1 = fp.wb_cfa[c1];
+                    WB = make_float2(fp.wb_cfa[c0], fp.wb_cfa[c1]);
                 }
                 if (wb_bayer) {
-                    float2 t = dev::fadd2(make_float2(dev::fmul((float)u0, WB0), dev::fmul((float)u1, WB1)), h5);
+                    float2 t = dev::fadd2(dev::pmul(make_float2((float)u0, (float)u1), WB, z2), h5);
                     u0 = u16q(t.x, mv);
                     u1 = u16q(t.y, mv);
                 }
@@ -709,7 +708,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 const int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
                 float g;
                 if (demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div);
+                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div, z2);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
@@ -739,7 +738,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                 int cc = bp[0], hm1 = bp[-1], hp1 = bp[1], hm2 = bp[-2], hp2 = bp[2];
                 int vm1 = bp[-G::BW], vp1 = bp[G::BW], vm2 = bp[-2 * G::BW], vp2 = bp[2 * G::BW];
                 if (demosaic == DM_AMAZE) {
-                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div);
+                    g = dev::amaze_green_fast(cc, hm1, hp1, hm2, hp2, vm1, vp1, vm2, vp2, fast_div, z2);
                 } else if (fp.bd <= 8) {
                     // src/algorithms/mg.cpp:58-69 (integer Malvar-He-Cutler green)
                     g = (float)dev::clampi((4 * cc + 2 * (vm1 + vp1 + hp1 + hm1) - (vm2 + vp2 + hp2 + hm2) + 4) >> 3, 0, mv);
@@ -832,26 +831,25 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         // RGB-domain white balance (reference call order), CCM: scalar products, packed sums
         if (wb_rgb) {
             float2 t;
-            t = dev::fadd2(make_float2(dev::fmul((float)R0, wr), dev::fmul((float)R1, wr)), h5);
+            t = dev::fadd2(dev::pmul(make_float2((float)R0, (float)R1), make_float2(wr, wr), z2), h5);
             R0 = u16q(t.x, mv); R1 = u16q(t.y, mv);
-            t = dev::fadd2(make_float2(dev::fmul((float)G0, wg), dev::fmul((float)G1, wg)), h5);
+            t = dev::fadd2(dev::pmul(make_float2((float)G0, (float)G1), make_float2(wg, wg), z2), h5);
             G0 = u16q(t.x, mv); G1 = u16q(t.y, mv);
-            t = dev::fadd2(make_float2(dev::fmul((float)B0, wbl), dev::fmul((float)B1, wbl)), h5);
+            t = dev::fadd2(dev::pmul(make_float2((float)B0, (float)B1), make_float2(wbl, wbl), z2), h5);
             B0 = u16q(t.x, mv); B1 = u16q(t.y, mv);
         }
         if (ccm_on) {
             const float* m = fp.ccm;
-            const float r0 = (float)R0, r1 = (float)R1, g0 = (float)G0, g1 = (float)G1, b0 = (float)B0, b1 = (float)B1;
+            const float2 rr = make_float2((float)R0, (float)R1), gg = make_float2((float)G0, (float)G1),
+                         bb = make_float2((float)B0, (float)B1);
+            auto M = [&](int k) { return make_float2(m[k], m[k]); };
             // ((m0*r + m1*g) + m2*b) + 0.5 for both samples, each product rounded on its own
-            float2 ro = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[0], r0), dev::fmul(m[0], r1)),
-                                                         make_float2(dev::fmul(m[1], g0), dev::fmul(m[1], g1))),
-                                              make_float2(dev::fmul(m[2], b0), dev::fmul(m[2], b1))), h5);
-            float2 go = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[3], r0), dev::fmul(m[3], r1)),
-                                                         make_float2(dev::fmul(m[4], g0), dev::fmul(m[4], g1))),
-                                              make_float2(dev::fmul(m[5], b0), dev::fmul(m[5], b1))), h5);
-            float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(make_float2(dev::fmul(m[6], r0), dev::fmul(m[6], r1)),
-                                                         make_float2(dev::fmul(m[7], g0), dev::fmul(m[7], g1))),
-                                              make_float2(dev::fmul(m[8], b0), dev::fmul(m[8], b1))), h5);
+            float2 ro = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(M(0), rr, z2), dev::pmul(M(1), gg, z2)),
+                                              dev::pmul(M(2), bb, z2)), h5);
+            float2 go = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(M(3), rr, z2), dev::pmul(M(4), gg, z2)),
+                                              dev::pmul(M(5), bb, z2)), h5);
+            float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(M(6), rr, z2), dev::pmul(M(7), gg, z2)),
+                                              dev::pmul(M(8), bb, z2)), h5);
             // (int)(v + 0.5) clamped to [0, mv]: truncation saturating at 0, then min
             R0 = u16q(ro.x, mv); R1 = u16q(ro.y, mv);
             G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
@@ -923,16 +921,17 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     float c10 = dev::fsub((float)br[G::BW - 1], gr[G::GPW + pa]);
                     float c11 = dev::fsub((float)br[G::BW + 1], gr[G::GPW + pa + 1]);
                     float sum = dev::fadd(dev::fadd(dev::fadd(c00, c01), c10), c11);
-                    float fown = (float)br[0], fgq = (float)bg[0];
+                    float fgq = (float)bg[0];
                     float2 hv = dev::fadd2(make_float2(dev::fsub((float)bg[-1], gr[pl]), dev::fsub((float)bg[-G::BW], gr[-G::GPW])),
                                            make_float2(dev::fsub((float)bg[1], gr[pl + 1]), dev::fsub((float)bg[G::BW], gr[G::GPW])));
-                    // x*0.5 and x*0.25 are exact, so these multiply-adds round once either way
-                    float other = dev::fadd(g_rb, dev::fmul(sum, 0.25f));
-                    float2 rb2 = dev::fadd2(make_float2(fgq, fgq), make_float2(dev::fmul(hv.x, 0.5f), dev::fmul(hv.y, 0.5f)));
-                    own = dev::round_plane(fown, mv);
+                    // x*0.25 and x*0.5 are exact, so one fused multiply-add rounds like the add
+                    float other = __fmaf_rn(sum, 0.25f, g_rb);
+                    float2 rb2 = dev::fma2(hv, make_float2(0.5f, 0.5f), make_float2(fgq, fgq));
+                    // the float plane's rounding of an integer sample is a clamp
+                    own = dev::clampi(br[0], 0, mv);
                     oq = dev::round_plane(other, mv);
                     gq = dev::round_plane(g_rb, mv);
-                    gg = dev::round_plane(fgq, mv);
+                    gg = dev::clampi(bg[0], 0, mv);
                     hz = dev::round_plane(rb2.x, mv);
                     vt = dev::round_plane(rb2.y, mv);
                 }
@@ -984,16 +983,17 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     float c10 = dev::fsub((float)br[G::BW - 1], gr[G::GPW + pa]);
                     float c11 = dev::fsub((float)br[G::BW + 1], gr[G::GPW + pa + 1]);
                     float sum = dev::fadd(dev::fadd(dev::fadd(c00, c01), c10), c11);
-                    float fown = (float)br[0], fgq = (float)bg[0];
+                    float fgq = (float)bg[0];
                     float2 hv = dev::fadd2(make_float2(dev::fsub((float)bg[-1], gr[pl]), dev::fsub((float)bg[-G::BW], gr[-G::GPW])),
                                            make_float2(dev::fsub((float)bg[1], gr[pl + 1]), dev::fsub((float)bg[G::BW], gr[G::GPW])));
-                    // x*0.5 and x*0.25 are exact, so these multiply-adds round once either way
-                    float other = dev::fadd(g_rb, dev::fmul(sum, 0.25f));
-                    float2 rb2 = dev::fadd2(make_float2(fgq, fgq), make_float2(dev::fmul(hv.x, 0.5f), dev::fmul(hv.y, 0.5f)));
-                    own = dev::round_plane(fown, mv);
+                    // x*0.25 and x*0.5 are exact, so one fused multiply-add rounds like the add
+                    float other = __fmaf_rn(sum, 0.25f, g_rb);
+                    float2 rb2 = dev::fma2(hv, make_float2(0.5f, 0.5f), make_float2(fgq, fgq));
+                    // the float plane's rounding of an integer sample is a clamp
+                    own = dev::clampi(br[0], 0, mv);
                     oq = dev::round_plane(other, mv);
                     gq = dev::round_plane(g_rb, mv);
-                    gg = dev::round_plane(fgq, mv);
+                    gg = dev::clampi(bg[0], 0, mv);
                     hz = dev::round_plane(rb2.x, mv);
                     vt = dev::round_plane(rb2.y, mv);
                 }

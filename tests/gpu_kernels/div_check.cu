@@ -14,16 +14,16 @@ __global__ void check_rcp(int nmax, unsigned long long* bad) {
         if (imop::dev::rcp_small_int(n) != __frcp_rn((float)n)) atomicAdd(bad, 1ull);
 }
 
-__global__ void check_pairs(long long n, unsigned long long* bad, long long* first) {
+__global__ void check_pairs(long long n, float neg_zero, unsigned long long* bad, long long* first) {
+    const float2 z2 = make_float2(neg_zero, neg_zero);
     const long long total = n * n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
         const int gh = (int)(i / n), gv = (int)(i - (i / n) * n);
         const float a = imop::dev::rcp_small_int(1 + gh), b = imop::dev::rcp_small_int(1 + gv);
         const float s = __fadd_rn(a, b);
-        float wa, wb;
-        imop::dev::weight_quotients(a, b, s, wa, wb);
-        if (wa != __fdiv_rn(a, s) || wb != __fdiv_rn(b, s)) {
+        const float2 w = imop::dev::weight_quotients(a, b, z2);
+        if (w.x != __fdiv_rn(a, s) || w.y != __fdiv_rn(b, s)) {
             atomicAdd(bad, 1ull);
             atomicMin(reinterpret_cast<unsigned long long*>(first), (unsigned long long)i);
         }
@@ -44,7 +44,7 @@ int main(int argc, char** argv) {
     cudaMemcpy(first, &init_first, sizeof(init_first), cudaMemcpyHostToDevice);
     const int nmax = 3 * 65535 + 1;
     check_rcp<<<152, 256>>>(nmax, bad_rcp);
-    check_pairs<<<152 * 8, 256>>>(n, bad, first);
+    check_pairs<<<152 * 8, 256>>>(n, -0.0f, bad, first);
     unsigned long long nb = 0, nr = 0;
     long long f = 0;
     if (cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost) || cudaMemcpy(&nr, bad_rcp, sizeof(nr), cudaMemcpyDeviceToHost) ||
