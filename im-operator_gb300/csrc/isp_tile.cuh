@@ -228,6 +228,20 @@ struct GreenAt {
 
 __device__ __forceinline__ int u16q(float t, int mv) { return (int)min(__float2uint_rz(t), (unsigned)mv); }
 
+// bytes [a, b) of one 16-byte window (dst and src agree modulo 16): naturally aligned 1/2/4/8-byte
+// pieces, rising to the window's alignment and then falling to its end
+__device__ __forceinline__ void store_piece(uint8_t* dst, const uint8_t* src, int a, int b) {
+    int q = a;
+    if ((q & 1) && q + 1 <= b) { dst[q] = src[q]; q += 1; }
+    if ((q & 2) && q + 2 <= b) { *reinterpret_cast<uint16_t*>(dst + q) = *reinterpret_cast<const uint16_t*>(src + q); q += 2; }
+    if ((q & 4) && q + 4 <= b) { *reinterpret_cast<uint32_t*>(dst + q) = *reinterpret_cast<const uint32_t*>(src + q); q += 4; }
+    if ((q & 8) && q + 8 <= b) { *reinterpret_cast<uint2*>(dst + q) = *reinterpret_cast<const uint2*>(src + q); q += 8; }
+    for (; q + 8 <= b; q += 8) *reinterpret_cast<uint2*>(dst + q) = *reinterpret_cast<const uint2*>(src + q);
+    if (q + 4 <= b) { *reinterpret_cast<uint32_t*>(dst + q) = *reinterpret_cast<const uint32_t*>(src + q); q += 4; }
+    if (q + 2 <= b) { *reinterpret_cast<uint16_t*>(dst + q) = *reinterpret_cast<const uint16_t*>(src + q); q += 2; }
+    if (q < b) dst[q] = src[q];
+}
+
 // ---- staging (warp 0): row windows of buffer b, bulk copies completing on bar[b] ----------------
 // sm.fp[b] holds the tile's frame parameters.  With an input pointer that is not 16-byte aligned
 // nothing is copied here: compute_tile copies the same windows with plain loads.
@@ -415,10 +429,11 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
             }
             if (bl_on) {
                 if (bl_int) {
-                    // (int)((float)v - off) == v - off for an integral offset
+                    // (int)((float)v - off) == v - off for an integral offset; clamp(v - off, 0, mv)
+                    // as one add-min-relu
                     const int p = y & 1;
-                    v0 = min(max(v0 - fp.bl_i[p][0], 0), mv);
-                    v1 = min(max(v1 - fp.bl_i[p][1], 0), mv);
+                    v0 = __viaddmin_s32_relu(v0, -fp.bl_i[p][0], mv);
+                    v1 = __viaddmin_s32_relu(v1, -fp.bl_i[p][1], mv);
                 } else {
                     v0 = dev::black_level(fp, v0, bayer_color(y, x, po));
                     v1 = dev::black_level(fp, v1, bayer_color(y, x + 1, po));
@@ -482,10 +497,10 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     int2 n5 = *reinterpret_cast<const int2*>(o + 2 * G::OW - 2);
                     int2 n6 = *reinterpret_cast<const int2*>(o + 2 * G::OW);
                     int2 n7 = *reinterpret_cast<const int2*>(o + 2 * G::OW + 2);
-                    int mn0 = min(min(min(n0.x, n1.x), min(n2.x, n3.x)), min(min(n4.x, n5.x), min(n6.x, n7.x)));
-                    int mx0 = max(max(max(n0.x, n1.x), max(n2.x, n3.x)), max(max(n4.x, n5.x), max(n6.x, n7.x)));
-                    int mn1 = min(min(min(n0.y, n1.y), min(n2.y, n3.y)), min(min(n4.y, n5.y), min(n6.y, n7.y)));
-                    int mx1 = max(max(max(n0.y, n1.y), max(n2.y, n3.y)), max(max(n4.y, n5.y), max(n6.y, n7.y)));
+                    const int mn0 = dev::min8(n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x);
+                    const int mx0 = dev::max8(n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x);
+                    const int mn1 = dev::min8(n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y);
+                    const int mx1 = dev::max8(n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y);
                     // |c - median| <= thr is certain when c - min <= thr and max - c <= thr
                     if (max(c.x - mn0, mx0 - c.x) > thr) {
                         int nb[8] = {n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x};
@@ -566,10 +581,10 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     int2 n5 = *reinterpret_cast<const int2*>(o + 2 * G::OW - 2);
                     int2 n6 = *reinterpret_cast<const int2*>(o + 2 * G::OW);
                     int2 n7 = *reinterpret_cast<const int2*>(o + 2 * G::OW + 2);
-                    int mn0 = min(min(min(n0.x, n1.x), min(n2.x, n3.x)), min(min(n4.x, n5.x), min(n6.x, n7.x)));
-                    int mx0 = max(max(max(n0.x, n1.x), max(n2.x, n3.x)), max(max(n4.x, n5.x), max(n6.x, n7.x)));
-                    int mn1 = min(min(min(n0.y, n1.y), min(n2.y, n3.y)), min(min(n4.y, n5.y), min(n6.y, n7.y)));
-                    int mx1 = max(max(max(n0.y, n1.y), max(n2.y, n3.y)), max(max(n4.y, n5.y), max(n6.y, n7.y)));
+                    const int mn0 = dev::min8(n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x);
+                    const int mx0 = dev::max8(n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x);
+                    const int mn1 = dev::min8(n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y);
+                    const int mx1 = dev::max8(n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y);
                     // |c - median| <= thr is certain when c - min <= thr and max - c <= thr
                     if (max(c.x - mn0, mx0 - c.x) > thr) {
                         int nb[8] = {n0.x, n1.x, n2.x, n3.x, n4.x, n5.x, n6.x, n7.x};
@@ -1029,7 +1044,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         if (lo >= shift && hi <= shift + len) {
             ptx::st_global_v4(dst + lo, *reinterpret_cast<const uint4*>(src + lo));
         } else {
-            for (int qq = max(lo, shift); qq < min(hi, shift + len); qq++) dst[qq] = src[qq];
+            store_piece(dst, src, max(lo, shift), min(hi, shift + len));
         }
     }
     // this tile's generic reads and writes of its raw buffer come before the bulk copy that
