@@ -117,11 +117,15 @@ class Isp:
         self.pipeline = pl
         self._cparams = cp
 
-    def run_host(self, raw):
+    def run_host(self, raw, out=None):
+        """One host frame, synchronous; `out` (ndarray or host tensor, e.g. page-locked) is filled
+        in place when given, else a new array is returned."""
         pl = self.pipeline
         raw = np.ascontiguousarray(raw).view(np.uint8).reshape(-1)
-        out = np.empty(pl.output_shape(), dtype=pl.output_dtype())
-        check(lib().imop_isp_run_host(self.h, raw.ctypes.data, raw.nbytes, out.ctypes.data, out.nbytes))
+        if out is None:
+            out = np.empty(pl.output_shape(), dtype=pl.output_dtype())
+        nbytes = out.nbytes if isinstance(out, np.ndarray) else out.numel() * out.element_size()
+        check(lib().imop_isp_run_host(self.h, raw.ctypes.data, raw.nbytes, _addr(out), nbytes))
         return out
 
     def run_device(self, d_in, d_out, stream=0):

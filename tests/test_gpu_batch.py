@@ -118,6 +118,33 @@ def test_run_host_batch(isp):
         assert max_abs(o, ref) == 0
 
 
+def test_run_host_batch_mixed_memory(isp):
+    """Page-locked and pageable host frames in one call, more frames than device slots."""
+    frames = _mixed(33, 8)
+    descs, outs = [], []
+    for k, (pl, raw, ref) in enumerate(frames):
+        inp = torch.from_numpy(raw.reshape(-1).view(np.uint8)).pin_memory() if k % 3 == 1 else raw
+        if k % 2 == 0:
+            out = torch.zeros(ref.nbytes, dtype=torch.uint8).pin_memory()
+        else:
+            out = np.zeros(ref.shape, ref.dtype)
+        descs.append((pl, inp, out))
+        outs.append(out)
+    isp.run_host_batch(descs)
+    for (pl, _, ref), o in zip(frames, outs):
+        got = o.numpy().view(ref.dtype).reshape(ref.shape) if isinstance(o, torch.Tensor) else o
+        assert max_abs(got, ref) == 0
+
+
+def test_run_host_pinned_output(isp):
+    """Single-frame host call filling a page-locked output frame in place."""
+    pl, raw, ref = _mixed(34, 1)[0]
+    isp.set_params(pl)
+    out = torch.zeros(ref.nbytes, dtype=torch.uint8).pin_memory()
+    isp.run_host(raw, out)
+    assert max_abs(out.numpy().view(ref.dtype).reshape(ref.shape), ref) == 0
+
+
 def test_run_host_batch_pinned_c2(isp):
     """Page-locked host frames of the 4024x3032 RAW12P workload through the pipelined host batch."""
     pl = workloads.c2_pipeline()
