@@ -31,18 +31,55 @@ constexpr int kBatchSeedCap = 16384;  // defect-chain entries per frame of a bat
 constexpr size_t kCacheMaxEntries = 1024;
 
 // FNV-1a, 64 bit
-struct Hash {
-    uint64_t h = 1469598103934665603ull;
+// Content key: the bytes that determine a table (or a recorded batch) and a hash of them.  The
+// hash runs four independent multiply / xor-shift lanes over 8-byte words, so a 16 KB tone table
+// hashes in a few microseconds; equality of the bytes themselves is what a cache hit requires.
+struct Key {
+    std::vector<uint8_t> b;
     void bytes(const void* p, size_t n) {
-        const unsigned char* b = static_cast<const unsigned char*>(p);
-        for (size_t i = 0; i < n; i++) {
-            h ^= b[i];
-            h *= 1099511628211ull;
-        }
+        const uint8_t* q = static_cast<const uint8_t*>(p);
+        b.insert(b.end(), q, q + n);
     }
     template <class T>
     void val(const T& v) { bytes(&v, sizeof(T)); }
+    uint64_t hash() const {
+        const uint64_t M = 0xff51afd7ed558ccdull;
+        uint64_t h[4] = {0x9e3779b97f4a7c15ull, 0xc2b2ae3d27d4eb4full, 0x165667b19e3779f9ull, 0x27d4eb2f165667c5ull};
+        const size_t n = b.size();
+        size_t i = 0;
+        for (; i + 32 <= n; i += 32)
+            for (int l = 0; l < 4; l++) {
+                uint64_t w;
+                std::memcpy(&w, b.data() + i + 8 * l, 8);
+                h[l] = (h[l] ^ w) * M;
+                h[l] ^= h[l] >> 32;
+            }
+        uint64_t r = n;
+        for (; i < n; i++) r = (r ^ b[i]) * 0x100000001b3ull;
+        for (int l = 0; l < 4; l++) {
+            r ^= h[l] + 0x9e3779b97f4a7c15ull + (r << 6) + (r >> 2);
+            r *= M;
+            r ^= r >> 33;
+        }
+        return r;
+    }
 };
+
+// the cache entry of `k`: an empty entry to build on a miss; an entry with other content under
+// the same hash is emptied once the device has finished with it
+template <class T>
+int cache_entry(imop_isp_ctx* c, std::unordered_map<uint64_t, CacheEntry<T>>& m, Key& k, CacheEntry<T>*& out) {
+    CacheEntry<T>& ent = m[k.hash()];
+    if (ent.obj && ent.key != k.b) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "sync before cache replacement");
+        ent.obj.reset();
+        c->graph.key = 0;
+    }
+    if (!ent.obj) ent.key = k.b;
+    out = &ent;
+    return IMOP_OK;
+}
 
 int ensure_aux(imop_isp_ctx* c) {
     if (c->aux) return IMOP_OK;
@@ -65,16 +102,18 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         c->graph.key = 0;
     }
     if ((p->stages & IMOP_STAGE_DEFECT) && p->dpc_mode == IMOP_DPC_MAP_BASED) {
-        Hash h;
-        h.val(p->width);
-        h.val(p->height);
-        h.bytes(p->dpc_map, sizeof(ImopDefectPoint) * (size_t)std::max(0, p->dpc_map_count));
-        auto& slot = tc.maps[h.h];
+        Key k;
+        k.val(p->width);
+        k.val(p->height);
+        k.bytes(p->dpc_map, sizeof(ImopDefectPoint) * (size_t)std::max(0, p->dpc_map_count));
+        CacheEntry<FrameTables>* ent = nullptr;
+        if ((rc = cache_entry(c, tc.maps, k, ent))) return rc;
+        auto& slot = ent->obj;
         if (!slot) {
             slot.reset(new FrameTables());
             FrameParams tmp;
             if ((rc = upload_map_plan(p, *slot, tmp))) {
-                tc.maps.erase(h.h);
+                tc.maps.erase(k.hash());
                 return rc;
             }
         }
@@ -84,25 +123,27 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         *map_tabs = slot.get();
     }
     if ((p->stages & IMOP_STAGE_LENS_SHADING) && p->lsc_mode != IMOP_LSC_POLYNOMIAL) {
-        Hash h;
-        h.val(p->lsc_mode);
+        Key k;
+        k.val(p->lsc_mode);
         if (p->lsc_mode == IMOP_LSC_FLAT_FIELD) {
-            h.val(p->lsc_flat_w);
-            h.val(p->lsc_flat_h);
-            h.val(p->pattern);
-            h.val(p->bit_depth);
-            h.bytes(p->lsc_flat_field, (size_t)p->lsc_flat_w * p->lsc_flat_h * (p->bit_depth <= 8 ? 1 : 2));
+            k.val(p->lsc_flat_w);
+            k.val(p->lsc_flat_h);
+            k.val(p->pattern);
+            k.val(p->bit_depth);
+            k.bytes(p->lsc_flat_field, (size_t)p->lsc_flat_w * p->lsc_flat_h * (p->bit_depth <= 8 ? 1 : 2));
         } else {
-            h.val(p->lsc_grid_w);
-            h.val(p->lsc_grid_h);
-            h.bytes(p->lsc_grid, sizeof(float) * 4 * (size_t)p->lsc_grid_w * p->lsc_grid_h);
+            k.val(p->lsc_grid_w);
+            k.val(p->lsc_grid_h);
+            k.bytes(p->lsc_grid, sizeof(float) * 4 * (size_t)p->lsc_grid_w * p->lsc_grid_h);
         }
-        auto& slot = tc.grids[h.h];
+        CacheEntry<DevBuf>* ent = nullptr;
+        if ((rc = cache_entry(c, tc.grids, k, ent))) return rc;
+        auto& slot = ent->obj;
         if (!slot) {
             std::vector<float> g;
             if (p->lsc_mode == IMOP_LSC_FLAT_FIELD) {
                 if ((rc = flat_field_grid(p->lsc_flat_field, p->lsc_flat_w, p->lsc_flat_h, p->pattern, p->bit_depth, g))) {
-                    tc.grids.erase(h.h);
+                    tc.grids.erase(k.hash());
                     return rc;
                 }
             } else {
@@ -110,7 +151,7 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
             }
             slot.reset(new DevBuf());
             if ((e = upload(*slot, g))) {
-                tc.grids.erase(h.h);
+                tc.grids.erase(k.hash());
                 return cuda_fail(e, "upload lens-shading grid");
             }
         }
@@ -119,15 +160,17 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         fp.grid = (const float*)slot->ptr;
     }
     {
-        Hash h;
-        h.val(p->out_format);
-        h.val(p->bit_depth);
+        Key k;
+        k.val(p->out_format);
+        k.val(p->bit_depth);
         if (p->out_format == IMOP_OUT_RGB8) {
-            h.val(p->tone_mode);
-            if (p->tone_mode == IMOP_TONE_LUT) h.bytes(p->tone_lut, sizeof(float) * (size_t)p->tone_lut_len);
-            if (p->tone_mode == IMOP_TONE_KNOTS) h.bytes(p->tone_knots, sizeof(float) * 33);
+            k.val(p->tone_mode);
+            if (p->tone_mode == IMOP_TONE_LUT) k.bytes(p->tone_lut, sizeof(float) * (size_t)p->tone_lut_len);
+            if (p->tone_mode == IMOP_TONE_KNOTS) k.bytes(p->tone_knots, sizeof(float) * 33);
         }
-        auto& slot = tc.tones[h.h];
+        CacheEntry<DevBuf>* ent = nullptr;
+        if ((rc = cache_entry(c, tc.tones, k, ent))) return rc;
+        auto& slot = ent->obj;
         if (!slot) {
             std::unique_ptr<DevBuf> t(new DevBuf());
             if ((e = t->ensure(std::max<size_t>((size_t)fp.mv + 1, 4096) + 16))) return cuda_fail(e, "alloc tone table");
@@ -232,13 +275,13 @@ cudaError_t enqueue_batch(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaS
     return launch_fused_batch(fps.data(), n, st);
 }
 
-uint64_t batch_key(const std::vector<PreparedFrame>& pf, cudaStream_t st) {
-    Hash h;
-    h.val(st);
+Key batch_key(const std::vector<PreparedFrame>& pf, cudaStream_t st) {
+    Key k;
+    k.val(st);
     int n = (int)pf.size();
-    h.val(n);
-    for (auto& f : pf) h.bytes(&f.fp, sizeof(FrameParams));
-    return h.h | 1ull;  // 0 means "no graph"
+    k.val(n);
+    for (auto& f : pf) k.bytes(&f.fp, sizeof(FrameParams));
+    return k;
 }
 
 int submit_plain(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaStream_t st) {
@@ -262,11 +305,14 @@ int submit_plain(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaStream_t s
 HostPipeline::~HostPipeline() {
     if (!ready) return;
     cudaStreamDestroy(s_in);
-    cudaStreamDestroy(s_comp);
+    cudaStreamDestroy(s_comp[0]);
+    cudaStreamDestroy(s_comp[1]);
+    cudaStreamDestroy(s_fix);
     cudaStreamDestroy(s_out);
     for (int i = 0; i < kSlots; i++) {
         cudaEventDestroy(in_done[i]);
-        cudaEventDestroy(comp_done[i]);
+        cudaEventDestroy(main_done[i]);
+        cudaEventDestroy(fix_done[i]);
         cudaEventDestroy(out_done[i]);
     }
 }
@@ -307,8 +353,9 @@ extern "C" int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames
         if ((e = enqueue_batch(ctx, pf, st))) return cuda_fail(e, "batch launch");
         return IMOP_OK;
     }
-    uint64_t key = batch_key(pf, nullptr);
-    if (ctx->graph.key != key) {
+    Key bk = batch_key(pf, nullptr);
+    const uint64_t key = bk.hash() | 1ull;  // 0 means "no graph"
+    if (ctx->graph.key != key || ctx->graph.key_bytes != bk.b) {
         // record on the context's own stream (the legacy stream cannot be captured), replay on `st`
         if (fused_grid_limit(1) <= 0 || fused_grid_limit(2) <= 0) return set_error(IMOP_ERR_CUDA, "kernel set-up");
         if (ctx->graph.exec) {
@@ -329,6 +376,7 @@ extern "C" int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
         ctx->graph.key = key;
+        ctx->graph.key_bytes = std::move(bk.b);
     }
     if ((e = cudaGraphLaunch(ctx->graph.exec, st))) return cuda_fail(e, "graph launch");
     return IMOP_OK;
@@ -344,15 +392,22 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
     HostPipeline& P = ctx->pipe;
     cudaError_t e;
     if (!P.ready) {
-        if ((e = cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking)) ||
-            (e = cudaStreamCreateWithFlags(&P.s_comp, cudaStreamNonBlocking)) ||
+        int lo = 0, hi = 0;  // hi: the greatest priority (numerically lowest)
+        if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi)) ||
+            (e = cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking)) ||
+            (e = cudaStreamCreateWithFlags(&P.s_comp[0], cudaStreamNonBlocking)) ||
+            (e = cudaStreamCreateWithFlags(&P.s_comp[1], cudaStreamNonBlocking)) ||
+            (e = cudaStreamCreateWithPriority(&P.s_fix, cudaStreamNonBlocking, hi)) ||
             (e = cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking)))
             return cuda_fail(e, "create streams");
-        for (int i = 0; i < HostPipeline::kSlots; i++)
+        for (int i = 0; i < HostPipeline::kSlots; i++) {
             if ((e = cudaEventCreateWithFlags(&P.in_done[i], cudaEventDisableTiming)) ||
-                (e = cudaEventCreateWithFlags(&P.comp_done[i], cudaEventDisableTiming)) ||
+                (e = cudaEventCreateWithFlags(&P.main_done[i], cudaEventDisableTiming)) ||
+                (e = cudaEventCreateWithFlags(&P.fix_done[i], cudaEventDisableTiming)) ||
                 (e = cudaEventCreateWithFlags(&P.out_done[i], cudaEventDisableTiming)))
                 return cuda_fail(e, "create events");
+            if ((rc = ensure_fixup(P.fix[i], 1 << 16))) return rc;
+        }
         P.ready = true;
     }
     // parameters, tables and sizes of every frame first (uploads are synchronous)
@@ -378,37 +433,51 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
             if ((e = P.d_in[s].ensure(max_in)) || (e = P.d_out[s].ensure(max_out))) return cuda_fail(e, "alloc slots");
         }
     }
-    // frames are computed one after another on s_comp, so one defect-chain scratch serves all
-    FixupScratch fs;
-    FrameParams fix_fp;
-    attach_fixup(ctx->fix, fix_fp, fs);
     for (int i = 0; i < n; i++) {
         const int s = i % HostPipeline::kSlots;
+        // the slot's own defect-chain scratch and tile counter; the context's sticky status word
+        FixupScratch fs;
         FrameParams fp = fps[i];
-        fp.seed_count = fix_fp.seed_count;
-        fp.seeds = fix_fp.seeds;
-        fp.seed_cap = fix_fp.seed_cap;
-        fp.status = fix_fp.status;
-        fp.tile_counter = fix_fp.tile_counter;
+        attach_fixup(P.fix[s], fp, fs);
+        fp.status = (int*)ctx->fix.status.ptr;
         fp.in = (const uint8_t*)P.d_in[s].ptr;
         fp.out = (uint8_t*)P.d_out[s].ptr;
-        // copy in once the slot's previous kernels have read it
-        if ((e = cudaStreamWaitEvent(P.s_in, P.comp_done[s], 0)) ||
+        // copy in once the slot's previous frame is fully computed (its fix-up reads the input)
+        if ((e = cudaStreamWaitEvent(P.s_in, P.fix_done[s], 0)) ||
             (e = cudaMemcpyAsync(P.d_in[s].ptr, frames[i].in, ib[i], cudaMemcpyHostToDevice, P.s_in)) ||
             (e = cudaEventRecord(P.in_done[s], P.s_in)))
             return cuda_fail(e, "copy in");
-        // compute once the input arrived and the slot's previous output was copied out
-        if ((e = cudaStreamWaitEvent(P.s_comp, P.in_done[s], 0)) || (e = cudaStreamWaitEvent(P.s_comp, P.out_done[s], 0)))
+        // tile kernel once the input arrived, the slot's previous output was copied out and its
+        // fix-up scratch is free; the chain resolution follows on s_fix
+        cudaStream_t sc = P.s_comp[i & 1];
+        if ((e = cudaStreamWaitEvent(sc, P.in_done[s], 0)) || (e = cudaStreamWaitEvent(sc, P.out_done[s], 0)) ||
+            (e = cudaStreamWaitEvent(sc, P.fix_done[s], 0)))
             return cuda_fail(e, "order compute");
-        if ((e = launch_fused(fp, fs, maps[i] ? &maps[i]->plan : nullptr, P.s_comp)) ||
-            (e = cudaEventRecord(P.comp_done[s], P.s_comp)))
+        // map-mode frames resolve their map values into tables that frames with the same map share:
+        // they follow the previous frame's tile kernel
+        if (i > 0 && maps[i] && (e = cudaStreamWaitEvent(sc, P.main_done[(i - 1) % HostPipeline::kSlots], 0)))
+            return cuda_fail(e, "order map frame");
+        // A page-locked output frame is copied out right after the tile kernel and the fix-up then
+        // writes its re-rendered windows into it; otherwise the copy waits for the whole fix-up.
+        const bool direct_fix = device_mapped_host(frames[i].out, ob[i]);
+        const SplitFixup split{P.s_fix, P.main_done[s], direct_fix};
+        if ((e = launch_fused(fp, fs, maps[i] ? &maps[i]->plan : nullptr, sc, &split)))
             return cuda_fail(e, "fused launch");
-        if ((e = cudaStreamWaitEvent(P.s_out, P.comp_done[s], 0)) ||
+        if (!direct_fix && (e = cudaEventRecord(P.fix_done[s], P.s_fix))) return cuda_fail(e, "fix-up done");
+        if ((e = cudaStreamWaitEvent(P.s_out, direct_fix ? P.main_done[s] : P.fix_done[s], 0)) ||
             (e = cudaMemcpyAsync(frames[i].out, P.d_out[s].ptr, ob[i], cudaMemcpyDeviceToHost, P.s_out)) ||
             (e = cudaEventRecord(P.out_done[s], P.s_out)))
             return cuda_fail(e, "copy out");
+        if (direct_fix) {
+            if ((e = cudaStreamWaitEvent(P.s_fix, P.out_done[s], 0)) ||
+                (e = launch_fused_render(fp, fs, (uint8_t*)frames[i].out, P.s_fix)) ||
+                (e = cudaEventRecord(P.fix_done[s], P.s_fix)))
+                return cuda_fail(e, "fix-up windows");
+        }
     }
-    if ((e = cudaStreamSynchronize(P.s_out)) || (e = cudaStreamSynchronize(P.s_comp)) || (e = cudaStreamSynchronize(P.s_in)))
+    if ((e = cudaStreamSynchronize(P.s_out)) || (e = cudaStreamSynchronize(P.s_fix)) ||
+        (e = cudaStreamSynchronize(P.s_comp[0])) || (e = cudaStreamSynchronize(P.s_comp[1])) ||
+        (e = cudaStreamSynchronize(P.s_in)))
         return cuda_fail(e, "run_host_batch");
     return take_status(ctx->fix);
 }

@@ -388,6 +388,22 @@ int ensure_fixup(FixupState& fx, int cap) {
     return IMOP_OK;
 }
 
+// [p, p + n) is page-locked host memory that the device addresses at the same pointer, so a kernel
+// may store into it directly
+bool device_mapped_host(const void* p, size_t n) {
+    if (!p || n == 0) return false;
+    const void* ends[2] = {p, static_cast<const char*>(p) + (n - 1)};
+    for (const void* q : ends) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer != q) return false;
+    }
+    return true;
+}
+
 void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs) {
     fp.seed_count = (int*)fx.seed_count.ptr;
     fp.seeds = (int*)fx.seeds.ptr;

@@ -48,10 +48,17 @@ cudaError_t upload(DevBuf& b, const std::vector<T>& v) {
     return cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
-// Parameter tables of many parameter sets, one device copy per distinct content (batches).
+// Parameter tables of many parameter sets, one device copy per distinct content (batches).  The
+// maps are keyed by a hash of the content; each entry keeps the content bytes it was built from,
+// so a hit is confirmed byte for byte.
+template <class T>
+struct CacheEntry {
+    std::unique_ptr<T> obj;
+    std::vector<uint8_t> key;
+};
 struct TableCache {
-    std::unordered_map<uint64_t, std::unique_ptr<DevBuf>> grids, tones;
-    std::unordered_map<uint64_t, std::unique_ptr<FrameTables>> maps;
+    std::unordered_map<uint64_t, CacheEntry<DevBuf>> grids, tones;
+    std::unordered_map<uint64_t, CacheEntry<FrameTables>> maps;
     size_t entries() const { return grids.size() + tones.size() + maps.size(); }
 };
 
@@ -61,19 +68,10 @@ struct BatchScratch {
     int frames = 0, cap = 0, map_cap = 0;
 };
 
-// device slots, streams and events of the pipelined host batch
-struct HostPipeline {
-    static constexpr int kSlots = 3;
-    DevBuf d_in[kSlots], d_out[kSlots];
-    cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
-    cudaEvent_t in_done[kSlots] = {}, comp_done[kSlots] = {}, out_done[kSlots] = {};
-    bool ready = false;
-    ~HostPipeline();
-};
-
-// a recorded batch and its key
+// a recorded batch and its key (the stream, frame count and every frame's expanded parameters)
 struct BatchGraph {
     uint64_t key = 0;
+    std::vector<uint8_t> key_bytes;
     cudaGraphExec_t exec = nullptr;
     ~BatchGraph();
 };
@@ -82,6 +80,21 @@ struct BatchGraph {
 struct FixupState {
     DevBuf seed_count, seeds, heap, ov_idx, ov_val, n_ov, status, tile_counter;
     int cap = 0;
+};
+
+// Device slots, streams and events of the pipelined host batch.  Per frame: copy in (s_in), tile
+// kernel (s_comp[frame & 1]: consecutive frames on two streams, so one frame's kernel fills the
+// SMs that the previous one leaves at its end), defect-chain fix-up (s_fix, the highest stream
+// priority, so its kernels take SMs as a tile kernel drains), copy out (s_out).  Each slot has its
+// own fix-up scratch and tile counter, so frames of different slots never share device state.
+struct HostPipeline {
+    static constexpr int kSlots = 4;
+    DevBuf d_in[kSlots], d_out[kSlots];
+    FixupState fix[kSlots];
+    cudaStream_t s_in = nullptr, s_comp[2] = {nullptr, nullptr}, s_fix = nullptr, s_out = nullptr;
+    cudaEvent_t in_done[kSlots] = {}, main_done[kSlots] = {}, fix_done[kSlots] = {}, out_done[kSlots] = {};
+    bool ready = false;
+    ~HostPipeline();
 };
 
 int set_error(int code, const char* msg);
@@ -94,6 +107,7 @@ int upload_map_plan(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp);
 void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan& P);
 int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm);
 int ensure_fixup(FixupState& fx, int cap);
+bool device_mapped_host(const void* p, size_t n);
 void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs);
 int take_status(FixupState& fx);
 

@@ -264,7 +264,7 @@ struct FusedKernels {
         grid_limit = sms[dev] * ctas_per_sm[dev];
         return cudaSuccess;
     }
-    static cudaError_t launch(const BatchLaunch& bl, bool fixup, cudaStream_t st) {
+    static cudaError_t launch(const BatchLaunch& bl, bool fixup, cudaStream_t st, const SplitFixup* split) {
         int limit = 0;
         cudaError_t e = setup(limit);
         if (e != cudaSuccess) return e;
@@ -272,10 +272,26 @@ struct FusedKernels {
             if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             fused_batch_kernel<kTileW, kTileH, OUTB><<<bl.n_items < limit ? bl.n_items : limit, kThreads, smem, st>>>(bl);
         }
-        if (fixup) {
-            dpc_resolve_kernel<<<bl.n_frames, 32, 0, st>>>(bl);
-            dpc_render_kernel<kTileW, kTileH, OUTB><<<bl.n_frames * kRenderCtas, kThreads, smem, st>>>(bl);
+        cudaStream_t fst = st;
+        if (split) {
+            // the fix-up follows the tile kernel on its own stream
+            if ((e = cudaEventRecord(split->main_done, st)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(split->st, split->main_done, 0)) != cudaSuccess)
+                return e;
+            fst = split->st;
         }
+        if (fixup) {
+            dpc_resolve_kernel<<<bl.n_frames, 32, 0, fst>>>(bl);
+            if (!(split && split->defer_render))
+                dpc_render_kernel<kTileW, kTileH, OUTB><<<bl.n_frames * kRenderCtas, kThreads, smem, fst>>>(bl);
+        }
+        return cudaGetLastError();
+    }
+    static cudaError_t render(const BatchLaunch& bl, cudaStream_t st) {
+        int limit = 0;
+        cudaError_t e = setup(limit);
+        if (e != cudaSuccess) return e;
+        dpc_render_kernel<kTileW, kTileH, OUTB><<<bl.n_frames * kRenderCtas, kThreads, smem, st>>>(bl);
         return cudaGetLastError();
     }
 };
@@ -296,16 +312,17 @@ void add_rect(BatchLaunch& bl, int frame, int x0, int y0, int w, int h, int& ite
     bl.n_rects++;
 }
 
-cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st) {
-    BatchLaunch bl;
+// the launch block of frames[0..n): tile counts, one rectangle per frame; false when the frames do
+// not share one tile counter
+bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     bl.n_frames = n;
     bl.n_rects = 0;
     // the frames of one launch come from one context and share its counter
     bl.tile_counter = frames[0].tile_counter;
     for (int f = 0; f < n; f++)
-        if (!frames[f].tile_counter || frames[f].tile_counter != bl.tile_counter) return cudaErrorInvalidValue;
+        if (!frames[f].tile_counter || frames[f].tile_counter != bl.tile_counter) return false;
     int items = 0;
-    bool fixup = false;
+    fixup = false;
     for (int f = 0; f < n; f++) {
         FrameParams& fp = frames[f];
         fp.tiles_x = tiles_along(fp.w, kTileW);
@@ -316,7 +333,25 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st) {
     }
     bl.rect_start[bl.n_rects] = items;
     bl.n_items = items;
-    return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st) : FusedKernels<3>::launch(bl, fixup, st);
+    return true;
+}
+
+cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, const SplitFixup* split = nullptr) {
+    BatchLaunch bl;
+    bool fixup = false;
+    if (!make_launch(frames, n, bl, fixup)) return cudaErrorInvalidValue;
+    return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st, split)
+                                  : FusedKernels<3>::launch(bl, fixup, st, split);
+}
+
+FrameParams with_fixup(const FrameParams& fp_in, const FixupScratch& fs) {
+    FrameParams fp = fp_in;
+    fp.fix_heap = fs.heap;
+    fp.fix_ov_idx = fs.ov_idx;
+    fp.fix_ov_val = fs.ov_val;
+    fp.fix_n_ov = fs.n_ov;
+    fp.fix_cap = fs.cap;
+    return fp;
 }
 
 }  // namespace
@@ -340,13 +375,9 @@ cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st) {
     return cudaSuccess;
 }
 
-cudaError_t launch_fused(const FrameParams& fp_in, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st) {
-    FrameParams fp = fp_in;
-    fp.fix_heap = fs.heap;
-    fp.fix_ov_idx = fs.ov_idx;
-    fp.fix_ov_val = fs.ov_val;
-    fp.fix_n_ov = fs.n_ov;
-    fp.fix_cap = fs.cap;
+cudaError_t launch_fused(const FrameParams& fp_in, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st,
+                         const SplitFixup* split) {
+    FrameParams fp = with_fixup(fp_in, fs);
     if ((fp.stages & 2u) && fp.dpc_mode == 1 && plan) {
         cudaError_t e = launch_map_resolve(fp, *plan, st);
         if (e != cudaSuccess) return e;
@@ -355,7 +386,17 @@ cudaError_t launch_fused(const FrameParams& fp_in, const FixupScratch& fs, const
         cudaError_t e = cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st);
         if (e != cudaSuccess) return e;
     }
-    return launch_batch_group(&fp, 1, st);
+    return launch_batch_group(&fp, 1, st, split);
+}
+
+cudaError_t launch_fused_render(const FrameParams& fp_in, const FixupScratch& fs, uint8_t* out, cudaStream_t st) {
+    FrameParams fp = with_fixup(fp_in, fs);
+    fp.out = out;
+    BatchLaunch bl;
+    bool fixup = false;
+    if (!make_launch(&fp, 1, bl, fixup)) return cudaErrorInvalidValue;
+    if (!fixup) return cudaSuccess;
+    return fp.out_bpc == 2 ? FusedKernels<6>::render(bl, st) : FusedKernels<3>::render(bl, st);
 }
 
 }  // namespace imop

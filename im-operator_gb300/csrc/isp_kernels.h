@@ -57,7 +57,22 @@ cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots
 // map-mode defect values of one frame (before the kernels that read them)
 cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaStream_t st);
 // map resolve (map mode) + seed reset + fused tiles + fix-up, in stream order
-cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st);
+// Optional second stream for the defect-chain fix-up of a single-frame launch: main_done is
+// recorded after the tile kernel on the launch stream, and the fix-up kernels run on `st` after it,
+// so the next frame's tile kernel can start while this frame's chains are resolved.  With
+// defer_render only the chain resolution is enqueued; launch_fused_render enqueues the window
+// re-rendering later (for example into a host frame, after the tile kernel's output was copied
+// there).
+struct SplitFixup {
+    cudaStream_t st;
+    cudaEvent_t main_done;
+    bool defer_render;
+};
+cudaError_t launch_fused(const FrameParams& fp, const FixupScratch& fs, const MapPlan* plan, cudaStream_t st,
+                         const SplitFixup* split = nullptr);
+// the defect-chain window re-rendering of one frame (after launch_fused with defer_render), its
+// windows written to `out`; nothing when the frame has no adaptive defect correction
+cudaError_t launch_fused_render(const FrameParams& fp, const FixupScratch& fs, uint8_t* out, cudaStream_t st);
 // Up to kBatchInline frames in one persistent launch plus the two fix-up launches (chain
 // resolution, window re-rendering).  Each frame carries
 // its own seed counter, seed list and fix-up scratch (FrameParams::fix_*); its seed counter must be
