@@ -50,6 +50,31 @@ struct AdjSmem {
 };
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Shared accumulators that many lanes of a warp hit at once (tone knots, lens-shading nodes):
+// every distinct key of the warp is summed with shuffles and added by one lane.  All 32 lanes call
+// it; a lane with key < 0 adds nothing.  Adds v[k] to acc[key + off[k]] for k < N.
+template <int N>
+__device__ __forceinline__ void warp_accumulate(float* acc, int key, const float (&v)[N], const int (&off)[N]) {
+    const int lane = threadIdx.x & 31;
+    unsigned rem = __ballot_sync(0xffffffffu, key >= 0);
+    while (rem) {
+        const int leader = __ffs(rem) - 1;
+        const int k = __shfl_sync(0xffffffffu, key, leader);
+        const bool mine = key == k;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const float s = warp_sum(mine ? v[j] : 0.0f);
+            if (lane == leader) atomicAdd(&acc[k + off[j]], s);
+        }
+        rem &= ~__ballot_sync(0xffffffffu, mine);
+    }
+}
 __device__ __forceinline__ float inside(float v, float lo, float hi) { return (v > lo && v < hi) ? 1.0f : 0.0f; }
 __device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : (v < 0.0f ? -1.0f : 0.0f); }
 
@@ -77,9 +102,10 @@ __device__ float amaze_df(const AdjSmem& sm, const TileCtx& t, int x, int y, flo
     float vm1 = u[i - kUW], vp1 = u[i + kUW], vm2 = u[i - 2 * kUW], vp2 = u[i + 2 * kUW];
     float lapH = 2.0f * c - hm2 - hp2, lapV = 2.0f * c - vm2 - vp2;
     float gH = fabsf(hm1 - hp1) + fabsf(lapH), gV = fabsf(vm1 - vp1) + fabsf(lapV);
-    float a = 1.0f / (1.0f + gH), b = 1.0f / (1.0f + gV);
-    float s = a + b;
-    float wh = a / s, wv = b / s;
+    // the chain is FP32 to a tolerance, not bit-exact: approximate reciprocals (2 ulp) suffice
+    float a = __fdividef(1.0f, 1.0f + gH), b = __fdividef(1.0f, 1.0f + gV);
+    float rs = __fdividef(1.0f, a + b);
+    float wh = a * rs, wv = b * rs;
     float gh = (hm1 + hp1) * 0.5f + lapH * 0.25f, gv = (vm1 + vp1) * 0.5f + lapV * 0.25f;
     if (parts) {
         parts[0] = a; parts[1] = b; parts[2] = wh; parts[3] = wv; parts[4] = gh; parts[5] = gv;
@@ -261,8 +287,8 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
     }
 }
 
-__device__ __forceinline__ void tone_df(const float* knots, float o, float mvf, float& t, int& idx, float& frac) {
-    float fi = o / mvf * 32.0f;
+__device__ __forceinline__ void tone_df(const float* knots, float o, float o_to_knot, float& t, int& idx, float& frac) {
+    float fi = o * o_to_knot;
     int k = (int)fi;
     float fr = fi - (float)k;
     if (k > 31) { k = 31; fr = 1.0f; }
@@ -284,7 +310,13 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
     const float* M = sm.th + 7;
     const float* knots = sm.th + 16 + 4 * f.gw * f.gh;
     const size_t frame_px = (size_t)f.w * f.h;
-    for (int s = threadIdx.x; s < t.tw * t.th; s += kAdjThreads) {
+    const float o_to_knot = 32.0f / mvf;
+    const int n_own = t.tw * t.th;
+    // whole warps iterate together (the knot sums are warp-wide); lanes past the end repeat the
+    // last pixel with zero weight
+    for (int s0 = threadIdx.x & ~31; s0 < n_own; s0 += kAdjThreads) {
+        const bool valid = s0 + (int)(threadIdx.x & 31) < n_own;
+        const int s = valid ? s0 + (int)(threadIdx.x & 31) : n_own - 1;
         int r = s / t.tw, c = s - r * t.tw;
         int x = t.x0 + c, y = t.y0 + r;
         int sx, sy;
@@ -300,11 +332,13 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
             o[q] = clampf(pre[q], 0.0f, mvf);
         }
 #pragma unroll
-        for (int k = 0; k < 3; k++) tone_df(knots, o[k], mvf, tt[k], idx[k], fr[k]);
+        for (int k = 0; k < 3; k++) tone_df(knots, o[k], o_to_knot, tt[k], idx[k], fr[k]);
         const size_t pi = ((size_t)fi * frame_px + (size_t)y * f.w + x) * 3;
         if constexpr (!BACKWARD) {
+            if (valid) {
 #pragma unroll
-            for (int k = 0; k < 3; k++) L.rgb_out[pi + k] = tt[k];
+                for (int k = 0; k < 3; k++) L.rgb_out[pi + k] = tt[k];
+            }
         } else {
         float gt[3], go[3], grgb[3] = {0.0f, 0.0f, 0.0f}, gv[3];
 #pragma unroll
@@ -312,15 +346,16 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
             float rv = L.ref[pi + k];
             if (L.mode == 0) {
                 float e = tt[k] - rv;
-                acc.loss += e * e;
-                gt[k] = 2.0f * e;
+                gt[k] = valid ? 2.0f * e : 0.0f;
+                if (valid) acc.loss += e * e;
             } else {
-                gt[k] = rv;
-                acc.loss += tt[k] * rv;
+                gt[k] = valid ? rv : 0.0f;
+                if (valid) acc.loss += tt[k] * rv;
             }
-            atomicAdd(&sm.acc_knots[idx[k]], gt[k] * (1.0f - fr[k]));
-            atomicAdd(&sm.acc_knots[idx[k] + 1], gt[k] * fr[k]);
-            go[k] = gt[k] * (knots[idx[k] + 1] - knots[idx[k]]) * 32.0f / mvf;
+            const float kv[2] = {gt[k] * (1.0f - fr[k]), gt[k] * fr[k]};
+            const int ko[2] = {0, 1};
+            warp_accumulate(sm.acc_knots, valid ? idx[k] : -1, kv, ko);
+            go[k] = gt[k] * (knots[idx[k] + 1] - knots[idx[k]]) * o_to_knot;
         }
 #pragma unroll
         for (int q = 0; q < 3; q++) {
@@ -333,7 +368,7 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) gv[k] = grgb[k] * inside(v[k], 0.0f, mvf);
-        demosaic_df_back(sm, t, sx, sy, gv);
+        if (valid) demosaic_df_back(sm, t, sx, sy, gv);
         }
     }
 }
@@ -359,9 +394,10 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
             float P[10];
             amaze_df(sm, t, x, y, P);
             float a = P[0], b = P[1], wh = P[2], wv = P[3], gh_ = P[4], gv_ = P[5];
-            float s2 = (a + b) * (a + b);
-            float dgH = -a * a * b * (gh_ - gv_) / s2;
-            float dgV = -b * b * a * (gv_ - gh_) / s2;
+            float rs = __fdividef(1.0f, a + b);
+            float rs2 = rs * rs;
+            float dgH = -a * a * b * (gh_ - gv_) * rs2;
+            float dgV = -b * b * a * (gv_ - gh_) * rs2;
             float tH = g * (wh * 0.25f + dgH * P[7]);
             float tV = g * (wv * 0.25f + dgV * P[9]);
             atomicAdd(&sm.gu[i - 1], g * (wh * 0.5f + dgH * P[6]));
@@ -376,41 +412,50 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
         }
         __syncthreads();
     }
-    const int uw = t.tw + 6, uh = t.th + 6;
+    const int uw = t.tw + 6, uh = t.th + 6, nu = uw * uh;
     const float* grid = sm.th + 16;
-    for (int s = tid; s < uw * uh; s += kAdjThreads) {
+    const int gnode[4] = {0, 4, 4 * f.gw, 4 * f.gw + 4};
+    // whole warps iterate together (the lens-shading node sums are warp-wide)
+    for (int s0 = tid & ~31; s0 < nu; s0 += kAdjThreads) {
+        const int s = min(s0 + (tid & 31), nu - 1);
         int r = s / uw, c = s - r * uw;
         int i = r * kUW + c;
-        float g = sm.gu[i];
-        if (g == 0.0f) continue;
+        float g = s0 + (tid & 31) < nu ? sm.gu[i] : 0.0f;
         int x = t.xu + c, y = t.yu + r;
-        if (x < 0 || x >= f.w || y < 0 || y >= f.h) continue;
-        int cc = t.cfa(x, y);
-        float rv = sm.raw[i];
-        float b = clampf(rv - sm.th[cc], 0.0f, mvf);
-        int gx = sm.col_gx[c], gy = sm.row_gy[r];
-        float fx = sm.col_fx[c], fy = sm.row_fy[r];
-        int n0 = (gy * f.gw + gx) * 4 + cc;
-        const float* g0 = grid + n0;
-        float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
-        float gain = g0[0] * w00 + g0[4] * w10 + g0[4 * f.gw] * w01 + g0[4 * f.gw + 4] * w11;
-        float l = clampf(b * gain, 0.0f, mvf);
-        float wb = wb_of(sm.th, cc);
-        if (!(l * wb > 0.0f && l * wb < mvf)) continue;
-        float gwb = g * l;
-        if (cc == 0) acc.wb[0] += gwb; else if (cc == 3) acc.wb[2] += gwb; else acc.wb[1] += gwb;
-        float gl = g * wb;
-        if (!(b * gain > 0.0f && b * gain < mvf)) continue;
-        float ggain = gl * b;
-        atomicAdd(&sm.acc_grid[n0], ggain * w00);
-        atomicAdd(&sm.acc_grid[n0 + 4], ggain * w10);
-        atomicAdd(&sm.acc_grid[n0 + 4 * f.gw], ggain * w01);
-        atomicAdd(&sm.acc_grid[n0 + 4 * f.gw + 4], ggain * w11);
-        float v = rv - sm.th[cc];
-        if (v > 0.0f && v < mvf) {
-            float gb = -gl * gain;
-            if (cc == 0) acc.bl[0] += gb; else if (cc == 1) acc.bl[1] += gb; else if (cc == 2) acc.bl[2] += gb; else acc.bl[3] += gb;
+        int key = -1;
+        float gw4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (g != 0.0f && x >= 0 && x < f.w && y >= 0 && y < f.h) {
+            int cc = t.cfa(x, y);
+            float rv = sm.raw[i];
+            float b = clampf(rv - sm.th[cc], 0.0f, mvf);
+            int gx = sm.col_gx[c], gy = sm.row_gy[r];
+            float fx = sm.col_fx[c], fy = sm.row_fy[r];
+            int n0 = (gy * f.gw + gx) * 4 + cc;
+            const float* g0 = grid + n0;
+            float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
+            float gain = g0[0] * w00 + g0[4] * w10 + g0[4 * f.gw] * w01 + g0[4 * f.gw + 4] * w11;
+            float l = clampf(b * gain, 0.0f, mvf);
+            float wb = wb_of(sm.th, cc);
+            if (l * wb > 0.0f && l * wb < mvf) {
+                float gwb = g * l;
+                if (cc == 0) acc.wb[0] += gwb; else if (cc == 3) acc.wb[2] += gwb; else acc.wb[1] += gwb;
+                float gl = g * wb;
+                if (b * gain > 0.0f && b * gain < mvf) {
+                    float ggain = gl * b;
+                    key = n0;
+                    gw4[0] = ggain * w00;
+                    gw4[1] = ggain * w10;
+                    gw4[2] = ggain * w01;
+                    gw4[3] = ggain * w11;
+                    float v = rv - sm.th[cc];
+                    if (v > 0.0f && v < mvf) {
+                        float gb = -gl * gain;
+                        if (cc == 0) acc.bl[0] += gb; else if (cc == 1) acc.bl[1] += gb; else if (cc == 2) acc.bl[2] += gb; else acc.bl[3] += gb;
+                    }
+                }
+            }
         }
+        warp_accumulate(sm.acc_grid, key, gw4, gnode);
     }
     __syncthreads();
 }
