@@ -33,10 +33,19 @@ constexpr int kUW = kTX + 3 + 6, kUH = kTY + 3 + 6;  // u region: tile (merged) 
 constexpr int kGW = kTX + 3 + 2, kGH = kTY + 3 + 2;  // green region: tile +- 1
 constexpr int kMaxParams = 16 + 4 * kAdjMaxGridNodes + 33;
 
+// tile-local lens-shading nodes: a tile's u region spans at most kLNX x kLNY grid nodes in the
+// local table (wider spans fall back to the CTA table)
+constexpr int kLNX = 4, kLNY = 4, kLocalNodes = 4 * kLNX * kLNY;
+
 struct AdjSmem {
     float th[kMaxParams];
     float acc_grid[4 * kAdjMaxGridNodes];
     float acc_knots[33];
+    // Accumulators with one column per lane index, entry [k][lane]: the lanes of a warp never meet
+    // on an address (and hit 32 different banks); only warps with the same lane index can, so the
+    // shared atomics here rarely retry.
+    float knot_lane[33 * 32];
+    float node_lane[kLocalNodes * 32];
     float raw[kUH * kUW];
     float u[kUH * kUW];
     float gu[kUH * kUW];
@@ -51,30 +60,7 @@ struct AdjSmem {
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
-__device__ __forceinline__ float warp_sum(float v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
-// Shared accumulators that many lanes of a warp hit at once (tone knots, lens-shading nodes):
-// every distinct key of the warp is summed with shuffles and added by one lane.  All 32 lanes call
-// it; a lane with key < 0 adds nothing.  Adds v[k] to acc[key + off[k]] for k < N.
-template <int N>
-__device__ __forceinline__ void warp_accumulate(float* acc, int key, const float (&v)[N], const int (&off)[N]) {
-    const int lane = threadIdx.x & 31;
-    unsigned rem = __ballot_sync(0xffffffffu, key >= 0);
-    while (rem) {
-        const int leader = __ffs(rem) - 1;
-        const int k = __shfl_sync(0xffffffffu, key, leader);
-        const bool mine = key == k;
-#pragma unroll
-        for (int j = 0; j < N; j++) {
-            const float s = warp_sum(mine ? v[j] : 0.0f);
-            if (lane == leader) atomicAdd(&acc[k + off[j]], s);
-        }
-        rem &= ~__ballot_sync(0xffffffffu, mine);
-    }
-}
 __device__ __forceinline__ float inside(float v, float lo, float hi) { return (v > lo && v < hi) ? 1.0f : 0.0f; }
 __device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : (v < 0.0f ? -1.0f : 0.0f); }
 
@@ -312,6 +298,7 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
     const size_t frame_px = (size_t)f.w * f.h;
     const float o_to_knot = 32.0f / mvf;
     const int n_own = t.tw * t.th;
+    float* knot_lane = sm.knot_lane + (threadIdx.x & 31);
     // whole warps iterate together (the knot sums are warp-wide); lanes past the end repeat the
     // last pixel with zero weight
     for (int s0 = threadIdx.x & ~31; s0 < n_own; s0 += kAdjThreads) {
@@ -352,9 +339,10 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
                 gt[k] = valid ? rv : 0.0f;
                 if (valid) acc.loss += tt[k] * rv;
             }
-            const float kv[2] = {gt[k] * (1.0f - fr[k]), gt[k] * fr[k]};
-            const int ko[2] = {0, 1};
-            warp_accumulate(sm.acc_knots, valid ? idx[k] : -1, kv, ko);
+            if (valid) {
+                atomicAdd(&knot_lane[idx[k] * 32], gt[k] * (1.0f - fr[k]));
+                atomicAdd(&knot_lane[(idx[k] + 1) * 32], gt[k] * fr[k]);
+            }
             go[k] = gt[k] * (knots[idx[k] + 1] - knots[idx[k]]) * o_to_knot;
         }
 #pragma unroll
@@ -414,15 +402,17 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     }
     const int uw = t.tw + 6, uh = t.th + 6, nu = uw * uh;
     const float* grid = sm.th + 16;
+    // the tile's lens-shading cells: local node (lx, ly) is grid node (gx_lo + lx, gy_lo + ly)
+    const int gx_lo = sm.col_gx[0], gy_lo = sm.row_gy[0];
+    const bool local = sm.col_gx[uw - 1] + 1 - gx_lo < kLNX && sm.row_gy[uh - 1] + 1 - gy_lo < kLNY;
     const int gnode[4] = {0, 4, 4 * f.gw, 4 * f.gw + 4};
-    // whole warps iterate together (the lens-shading node sums are warp-wide)
-    for (int s0 = tid & ~31; s0 < nu; s0 += kAdjThreads) {
-        const int s = min(s0 + (tid & 31), nu - 1);
+    const int lnode[4] = {0, 4 * 32, 4 * kLNX * 32, (4 * kLNX + 4) * 32};
+    float* node_lane = sm.node_lane + (tid & 31);
+    for (int s = tid; s < nu; s += kAdjThreads) {
         int r = s / uw, c = s - r * uw;
         int i = r * kUW + c;
-        float g = s0 + (tid & 31) < nu ? sm.gu[i] : 0.0f;
+        float g = sm.gu[i];
         int x = t.xu + c, y = t.yu + r;
-        int key = -1;
         float gw4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (g != 0.0f && x >= 0 && x < f.w && y >= 0 && y < f.h) {
             int cc = t.cfa(x, y);
@@ -442,11 +432,18 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
                 float gl = g * wb;
                 if (b * gain > 0.0f && b * gain < mvf) {
                     float ggain = gl * b;
-                    key = n0;
                     gw4[0] = ggain * w00;
                     gw4[1] = ggain * w10;
                     gw4[2] = ggain * w01;
                     gw4[3] = ggain * w11;
+                    if (local) {
+                        float* q = node_lane + (((gy - gy_lo) * kLNX + (gx - gx_lo)) * 4 + cc) * 32;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) atomicAdd(q + lnode[k], gw4[k]);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) atomicAdd(&sm.acc_grid[n0 + gnode[k]], gw4[k]);
+                    }
                     float v = rv - sm.th[cc];
                     if (v > 0.0f && v < mvf) {
                         float gb = -gl * gain;
@@ -455,13 +452,25 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
                 }
             }
         }
-        warp_accumulate(sm.acc_grid, key, gw4, gnode);
     }
     __syncthreads();
+    if (local) {
+        // local nodes into the CTA table, lanes in order; the table is cleared for the next tile
+        for (int e = tid; e < kLocalNodes; e += kAdjThreads) {
+            float v = 0.0f;
+            for (int l = 0; l < 32; l++) {
+                v += sm.node_lane[e * 32 + l];
+                sm.node_lane[e * 32 + l] = 0.0f;
+            }
+            const int lx = (e >> 2) % kLNX, ly = (e >> 2) / kLNX;
+            if (v != 0.0f && gx_lo + lx < f.gw && gy_lo + ly < f.gh) sm.acc_grid[((gy_lo + ly) * f.gw + gx_lo + lx) * 4 + (e & 3)] += v;
+        }
+        __syncthreads();
+    }
 }
 
 template <bool BACKWARD>
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
+__global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
     extern __shared__ __align__(16) uint8_t dsm[];
     AdjSmem& sm = *reinterpret_cast<AdjSmem*>(dsm);
     const int tid = threadIdx.x;
@@ -469,6 +478,8 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const __grid_const
     if (BACKWARD) {
         for (int k = tid; k < 4 * kAdjMaxGridNodes; k += kAdjThreads) sm.acc_grid[k] = 0.0f;
         for (int k = tid; k < 33; k += kAdjThreads) sm.acc_knots[k] = 0.0f;
+        for (int k = tid; k < 33 * 32; k += kAdjThreads) sm.knot_lane[k] = 0.0f;
+        for (int k = tid; k < kLocalNodes * 32; k += kAdjThreads) sm.node_lane[k] = 0.0f;
     }
     __syncthreads();
     RegAcc acc;
@@ -516,7 +527,11 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(const __grid_const
     }
     const int ng = 4 * L.f.gw * L.f.gh;
     for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = sm.acc_grid[k];
-    for (int k = tid; k < 33; k += kAdjThreads) part[16 + ng + k] = sm.acc_knots[k];
+    for (int k = tid; k < 33; k += kAdjThreads) {
+        float v = sm.acc_knots[k];
+        for (int l = 0; l < 32; l++) v += sm.knot_lane[k * 32 + l];
+        part[16 + ng + k] = v;
+    }
 }
 
 // grad[k] = sum over CTAs of partial[cta][k], in CTA order; loss likewise
