@@ -31,11 +31,12 @@ constexpr int kAdjThreads = 256;
 constexpr int kTX = 64, kTY = 16;
 constexpr int kUW = kTX + 3 + 6, kUH = kTY + 3 + 6;  // u region: tile (merged) +- 3
 constexpr int kGW = kTX + 3 + 2, kGH = kTY + 3 + 2;  // green region: tile +- 1
+constexpr int kVW = kTX + 3 + 4, kVH = kTY + 3 + 4;  // demosaic-output gradients: tile +- 2
 constexpr int kMaxParams = 16 + 4 * kAdjMaxGridNodes + 33;
 
 // tile-local lens-shading nodes: a tile's u region spans at most kLNX x kLNY grid nodes in the
 // local table (wider spans fall back to the CTA table)
-constexpr int kLNX = 4, kLNY = 4, kLocalNodes = 4 * kLNX * kLNY;
+constexpr int kLNX = 4, kLNY = 3, kLocalNodes = 4 * kLNX * kLNY;
 
 struct AdjSmem {
     float th[kMaxParams];
@@ -51,6 +52,9 @@ struct AdjSmem {
     float gu[kUH * kUW];
     float G[kGH * kGW];
     float gG[kGH * kGW];
+    // dL/d(demosaic output) per channel, summed at each output's source pixel (border copies add
+    // into their source); zero outside the tile's own pixels
+    float gV[3][kVH * kVW];
     int col_gx[kUW];
     float col_fx[kUW];
     int row_gy[kUH];
@@ -76,6 +80,7 @@ struct TileCtx {
     __device__ bool rb(int x, int y) const { return at_r(x, y) || at_b(x, y); }
     __device__ int ui(int x, int y) const { return (y - yu) * kUW + (x - xu); }
     __device__ int gi(int x, int y) const { return (y - yg) * kGW + (x - xg); }
+    __device__ int vi(int x, int y) const { return (y - yg + 1) * kVW + (x - xg + 1); }
 };
 
 __device__ __forceinline__ float wb_of(const float* th, int c) { return th[4 + (c == 0 ? 0 : (c == 3 ? 2 : 1))]; }
@@ -138,49 +143,74 @@ __device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, f
     }
 }
 
-__device__ void demosaic_df_back(AdjSmem& sm, const TileCtx& t, int x, int y, const float gv[3]) {
+// Adjoint of the demosaic as a gather: every pixel q of the green region (own pixels +- 1) adds up
+// what the demosaic outputs that read u(q) or G(q) send back, from the gV planes (zero outside the
+// own pixels).  These are the transposes of demosaic_df's expressions:
+//   HQLI, source p in [2,w-2)^2: R/B site: own channel <- u(p); green <- 1/4 of the four
+//     horizontal / vertical neighbours; other channel <- 1/4 of the four diagonals.  G site:
+//     green <- u(p); the row's colour <- 1/2 (u(p-1) + u(p+1)), the other <- 1/2 (u(p-W) + u(p+W)).
+//   AMAZE, source p in [1,w-1)^2 (else only green <- G(p)): green <- G(p); R/B site: own <- u(p),
+//     other <- G(p) + 1/4 sum over diagonals d of (u(d) - G(d)); G site: R, B <- G(p) + 1/2 sum of
+//     (u - G) over the horizontal or the vertical pair.
+__device__ void demosaic_gather(AdjSmem& sm, const TileCtx& t) {
     const AdjFrame& f = *t.f;
-    float* gu = sm.gu;
-    const bool ar = t.at_r(x, y), ab = t.at_b(x, y), rrow = (y & 1) == t.po.r_row;
-    const int i = t.ui(x, y);
-    if (f.demosaic == DM_HQLI) {
-        if (x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) return;
-        if (ar || ab) {
-            float gown = ar ? gv[0] : gv[2], goth = (ar ? gv[2] : gv[0]) * 0.25f, gg = gv[1] * 0.25f;
-            atomicAdd(&gu[i], gown);
-            atomicAdd(&gu[i - 1], gg); atomicAdd(&gu[i + 1], gg); atomicAdd(&gu[i - kUW], gg); atomicAdd(&gu[i + kUW], gg);
-            atomicAdd(&gu[i - kUW - 1], goth); atomicAdd(&gu[i - kUW + 1], goth);
-            atomicAdd(&gu[i + kUW - 1], goth); atomicAdd(&gu[i + kUW + 1], goth);
+    const int gw = t.tw + 2, gh = t.th + 2;
+    const float* V0 = sm.gV[0];
+    const float* V1 = sm.gV[1];
+    const float* V2 = sm.gV[2];
+    const bool hqli = f.demosaic == DM_HQLI;
+    const int lo = hqli ? 2 : 1;  // sources with colour interpolation: [lo, w - lo) x [lo, h - lo)
+    for (int s = threadIdx.x; s < gw * gh; s += kAdjThreads) {
+        const int r = s / gw, c = s - r * gw;
+        const int x = t.xg + c, y = t.yg + r;
+        const int v = t.vi(x, y), i = t.ui(x, y), j = r * kGW + c;
+        auto in_lo = [&](int xx, int yy) { return xx >= lo && xx < f.w - lo && yy >= lo && yy < f.h - lo; };
+        float gu = 0.0f, gG = 0.0f;
+        if (t.rb(x, y)) {
+            const bool ar = t.at_r(x, y);
+            // own source: the own channel reads u(q); AMAZE's green and other channel read G(q)
+            if (in_lo(x, y)) {
+                gu += ar ? V0[v] : V2[v];
+                if (!hqli) gG += V1[v] + (ar ? V2[v] : V0[v]);
+            } else if (!hqli) {
+                gG += V1[v];
+            }
+            // diagonals: R/B sites of the other colour, whose other channel is this colour
+            const float* Vd = ar ? V0 : V2;  // at a blue diagonal the other channel is red, and back
+            float nb = 0.0f;
+            if (in_lo(x - 1, y - 1)) nb += 0.25f * Vd[v - kVW - 1];
+            if (in_lo(x + 1, y - 1)) nb += 0.25f * Vd[v - kVW + 1];
+            if (in_lo(x - 1, y + 1)) nb += 0.25f * Vd[v + kVW - 1];
+            if (in_lo(x + 1, y + 1)) nb += 0.25f * Vd[v + kVW + 1];
+            // horizontal / vertical neighbours: G sites; a G site in a red row interpolates red
+            // horizontally and blue vertically
+            const bool rrow = (y & 1) == t.po.r_row;  // the neighbours x +- 1 share this row
+            // (the horizontal pair feeds the row's colour, the vertical pair the other row's other
+            // colour: both are this site's colour)
+            const float* Vn = rrow ? V0 : V2;
+            if (in_lo(x - 1, y)) nb += 0.5f * Vn[v - 1];
+            if (in_lo(x + 1, y)) nb += 0.5f * Vn[v + 1];
+            if (in_lo(x, y - 1)) nb += 0.5f * Vn[v - kVW];
+            if (in_lo(x, y + 1)) nb += 0.5f * Vn[v + kVW];
+            gu += nb;
+            if (!hqli) gG -= nb;
         } else {
-            float ghz = (rrow ? gv[0] : gv[2]) * 0.5f, gvt = (rrow ? gv[2] : gv[0]) * 0.5f;
-            atomicAdd(&gu[i], gv[1]);
-            atomicAdd(&gu[i - 1], ghz); atomicAdd(&gu[i + 1], ghz);
-            atomicAdd(&gu[i - kUW], gvt); atomicAdd(&gu[i + kUW], gvt);
+            // G site: its own green channel
+            if (hqli) {
+                if (in_lo(x, y)) gu += V1[v];
+                // the green of each horizontal / vertical R/B neighbour reads 1/4 of u(q)
+                float nb = 0.0f;
+                if (in_lo(x - 1, y)) nb += V1[v - 1];
+                if (in_lo(x + 1, y)) nb += V1[v + 1];
+                if (in_lo(x, y - 1)) nb += V1[v - kVW];
+                if (in_lo(x, y + 1)) nb += V1[v + kVW];
+                gu += 0.25f * nb;
+            } else {
+                gG += in_lo(x, y) ? V0[v] + V1[v] + V2[v] : V1[v];
+            }
         }
-        return;
-    }
-    float* gG = sm.gG;
-    const int j = t.gi(x, y);
-    if (x < 1 || x >= f.w - 1 || y < 1 || y >= f.h - 1) {
-        atomicAdd(&gG[j], gv[1]);
-        return;
-    }
-    if (ar || ab) {
-        float goth = ar ? gv[2] : gv[0];
-        atomicAdd(&gu[i], ar ? gv[0] : gv[2]);
-        atomicAdd(&gG[j], gv[1] + goth);
-        float q = goth * 0.25f;
-        atomicAdd(&gu[i - kUW - 1], q); atomicAdd(&gG[j - kGW - 1], -q);
-        atomicAdd(&gu[i - kUW + 1], q); atomicAdd(&gG[j - kGW + 1], -q);
-        atomicAdd(&gu[i + kUW - 1], q); atomicAdd(&gG[j + kGW - 1], -q);
-        atomicAdd(&gu[i + kUW + 1], q); atomicAdd(&gG[j + kGW + 1], -q);
-    } else {
-        float ghz = (rrow ? gv[0] : gv[2]) * 0.5f, gvt = (rrow ? gv[2] : gv[0]) * 0.5f;
-        atomicAdd(&gG[j], gv[0] + gv[1] + gv[2]);
-        atomicAdd(&gu[i - 1], ghz); atomicAdd(&gG[j - 1], -ghz);
-        atomicAdd(&gu[i + 1], ghz); atomicAdd(&gG[j + 1], -ghz);
-        atomicAdd(&gu[i - kUW], gvt); atomicAdd(&gG[j - kGW], -gvt);
-        atomicAdd(&gu[i + kUW], gvt); atomicAdd(&gG[j + kGW], -gvt);
+        sm.gu[i] = gu;
+        if (!hqli) sm.gG[j] = gG;
     }
 }
 
@@ -256,6 +286,9 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
         sm.u[i] = uv;
         if (BACKWARD) sm.gu[i] = 0.0f;
     }
+    if (BACKWARD) {
+        for (int s = tid; s < 3 * kVH * kVW; s += kAdjThreads) (&sm.gV[0][0])[s] = 0.0f;
+    }
     __syncthreads();
     if (f.demosaic == DM_AMAZE || BACKWARD) {
         const int gw = t.tw + 2, gh = t.th + 2;
@@ -299,6 +332,7 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
     const float o_to_knot = 32.0f / mvf;
     const int n_own = t.tw * t.th;
     float* knot_lane = sm.knot_lane + (threadIdx.x & 31);
+    const bool border_tile = t.x0 < 2 || t.x0 + t.tw > f.w - 2 || t.y0 < 2 || t.y0 + t.th > f.h - 2;
     // whole warps iterate together (the knot sums are warp-wide); lanes past the end repeat the
     // last pixel with zero weight
     for (int s0 = threadIdx.x & ~31; s0 < n_own; s0 += kAdjThreads) {
@@ -356,7 +390,18 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) gv[k] = grgb[k] * inside(v[k], 0.0f, mvf);
-        if (valid) demosaic_df_back(sm, t, sx, sy, gv);
+        if (valid) {
+            // border copies add into their source, which its own output also writes: atomics in
+            // tiles with border outputs, plain stores elsewhere
+            const int vi = t.vi(sx, sy);
+            if (border_tile) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) atomicAdd(&sm.gV[k][vi], gv[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; k++) sm.gV[k][vi] = gv[k];
+            }
+        }
         }
     }
 }
@@ -497,7 +542,11 @@ __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_co
         const uint8_t* in = L.raw + (size_t)fi * L.f.in_bytes;
         tile_forward<BACKWARD>(sm, t, in);
         tile_pixels<BACKWARD>(sm, t, fi, L, acc);
-        if (BACKWARD) tile_back_planes(sm, t, acc);
+        if (BACKWARD) {
+            __syncthreads();
+            demosaic_gather(sm, t);
+            tile_back_planes(sm, t, acc);
+        }
         else __syncthreads();
     }
     if (!BACKWARD) return;
