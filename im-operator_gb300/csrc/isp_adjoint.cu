@@ -234,6 +234,7 @@ __device__ __forceinline__ void tile_of(const AdjLaunch& L, int item, int& fi, T
 __device__ __forceinline__ int adj_raw(const AdjFrame& f, const uint8_t* in, int x, int y) {
     FrameParams fp;
     fp.w = f.w;
+    fp.bd = f.bd;
     fp.mv = f.mv;
     fp.fmt = f.fmt;
     fp.in = in;

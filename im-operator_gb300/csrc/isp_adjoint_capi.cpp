@@ -19,8 +19,6 @@ int validate_desc(const ImopAdjointDesc* d) {
     if (d->bit_depth < 1 || d->bit_depth > 16) return set_error(IMOP_ERR_INVALID_BIT_DEPTH, "bit depth must be 1-16");
     if (d->pattern < 0 || d->pattern > 3) return set_error(IMOP_ERR_INVALID_PATTERN, "invalid Bayer pattern");
     if (d->width < 6 || d->height < 6) return set_error(IMOP_ERR_IMAGE_TOO_SMALL, "image too small (min 6x6)");
-    if (d->packed && d->bit_depth != 10 && d->bit_depth != 12)
-        return set_error(IMOP_ERR_UNSUPPORTED, "packed input must be MIPI RAW10 or RAW12");
     if (d->demosaic != IMOP_DEMOSAIC_HQLI && d->demosaic != IMOP_DEMOSAIC_AMAZE)
         return set_error(IMOP_ERR_UNSUPPORTED, "differentiable demosaic must be HQLI or AMAZE");
     if (d->grid_w < 2 || d->grid_h < 2 || d->grid_w > 32 || d->grid_h > 32 || d->grid_w * d->grid_h > kAdjMaxGridNodes)
@@ -37,13 +35,13 @@ int make_launch(const ImopAdjointDesc* d, AdjLaunch& L) {
     f.h = d->height;
     f.bd = d->bit_depth;
     f.mv = max_val_of(d->bit_depth);
-    f.fmt = d->packed ? (d->bit_depth == 10 ? FMT_P10 : FMT_P12) : (d->bit_depth <= 8 ? FMT_U8 : FMT_U16);
+    f.fmt = input_format_of(d->packed, d->bit_depth);
     f.pattern = d->pattern;
     f.demosaic = d->demosaic;
     f.border_mode = (d->demosaic == IMOP_DEMOSAIC_AMAZE && d->bit_depth <= 8) ? BORDER_BOTH : BORDER_ROWS_THEN_COLS;
     f.gw = d->grid_w;
     f.gh = d->grid_h;
-    f.in_bytes = input_bytes_of(f.fmt, f.w, f.h);
+    f.in_bytes = input_bytes_of(f.fmt, d->bit_depth, f.w, f.h);
     int per = adj_tile_grid(f.w, f.h, f.tiles_x, f.tiles_y);
     L.n_frames = d->n_frames;
     L.n_items = per * d->n_frames;

@@ -184,8 +184,6 @@ int validate_params(const ImopIspParams* p) {
     if (p->width < 6 || p->height < 6) return fail(IMOP_ERR_IMAGE_TOO_SMALL, "image too small for the pipeline (min 6x6)");
     if ((long long)p->width * p->height * 6 >= (1LL << 31))
         return fail(IMOP_ERR_UNSUPPORTED, "frame larger than 2^31 output bytes");
-    if (p->packed && p->bit_depth != 10 && p->bit_depth != 12)
-        return fail(IMOP_ERR_UNSUPPORTED, "packed input must be MIPI RAW10 or RAW12");
     if (p->demosaic != IMOP_DEMOSAIC_HQLI && p->demosaic != IMOP_DEMOSAIC_AMAZE && p->demosaic != IMOP_DEMOSAIC_MG)
         return fail(IMOP_ERR_UNSUPPORTED, "demosaic must be HQLI, MG or AMAZE");
     if (p->stages & ~IMOP_STAGE_ALL) return fail(IMOP_ERR_INVALID_ARGUMENT, "unknown stage bits");
@@ -247,7 +245,7 @@ void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
     fp.h = p->height;
     fp.bd = p->bit_depth;
     fp.mv = max_val_of(p->bit_depth);
-    fp.fmt = p->packed ? (p->bit_depth == 10 ? FMT_P10 : FMT_P12) : (p->bit_depth <= 8 ? FMT_U8 : FMT_U16);
+    fp.fmt = input_format_of(p->packed, p->bit_depth);
     fp.pattern = p->pattern;
     fp.demosaic = p->demosaic;
     fp.border_mode = (p->demosaic == IMOP_DEMOSAIC_AMAZE && p->bit_depth <= 8) ? BORDER_BOTH : BORDER_ROWS_THEN_COLS;
@@ -255,7 +253,7 @@ void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
     fp.stage_order = p->stage_order;
     fp.out_format = p->out_format;
     fp.out_bpc = (p->out_format == IMOP_OUT_NATIVE && p->bit_depth > 8) ? 2 : 1;
-    fp.in_bytes = input_bytes_of(fp.fmt, fp.w, fp.h);
+    fp.in_bytes = input_bytes_of(fp.fmt, fp.bd, fp.w, fp.h);
     for (int c = 0; c < 4; c++) {
         float v = (p->bl_mode == IMOP_BL_GLOBAL) ? p->bl_offset[0] : p->bl_offset[c];
         fp.bl[c] = std::max(0.0f, v);
@@ -460,8 +458,7 @@ void imop_isp_params_default(ImopIspParams* p, int width, int height, int bit_de
 
 size_t imop_isp_input_bytes(const ImopIspParams* p) {
     if (!p || p->width <= 0 || p->height <= 0) return 0;
-    int fmt = p->packed ? (p->bit_depth == 10 ? FMT_P10 : FMT_P12) : (p->bit_depth <= 8 ? FMT_U8 : FMT_U16);
-    return input_bytes_of(fmt, p->width, p->height);
+    return input_bytes_of(input_format_of(p->packed, p->bit_depth), p->bit_depth, p->width, p->height);
 }
 
 size_t imop_isp_output_bytes(const ImopIspParams* p) {

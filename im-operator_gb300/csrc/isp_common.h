@@ -18,8 +18,16 @@ enum InFormat : int {
     FMT_U8 = 0,    // 1 byte per pixel (bit depth <= 8)
     FMT_U16 = 1,   // little-endian u16 per pixel, LSB-aligned
     FMT_P10 = 2,   // MIPI RAW10: 4 pixels in 5 bytes, global pixel order, no row padding
-    FMT_P12 = 3    // MIPI RAW12: 2 pixels in 3 bytes
+    FMT_P12 = 3,   // MIPI RAW12: 2 pixels in 3 bytes
+    FMT_PBITS = 4  // other packed depths: one LSB-first bit stream, bit_depth bits per pixel
 };
+
+// input format of a parameter set: MIPI RAW10 / RAW12, other packed depths as a bit stream
+// (pixel::get_packed_raw, include/imop/pixel_utils.hpp:58-118 of the reference), else u8 / u16
+IMOP_HD int input_format_of(int packed, int bd) {
+    if (packed) return bd == 10 ? FMT_P10 : (bd == 12 ? FMT_P12 : FMT_PBITS);
+    return bd <= 8 ? FMT_U8 : FMT_U16;
+}
 
 // demosaic kernels (values of imop::DemosaicAlgorithm)
 enum Demosaic : int { DM_HQLI = 1, DM_MG = 2, DM_AMAZE = 6 };
@@ -54,13 +62,14 @@ inline int bayer_color_host(int row, int col, int pattern) {
 }
 IMOP_HD int max_val_of(int bd) { return bd >= 16 ? 65535 : (1 << bd) - 1; }
 
-IMOP_HD size_t input_bytes_of(int fmt, int w, int h) {
+IMOP_HD size_t input_bytes_of(int fmt, int bd, int w, int h) {
     size_t n = (size_t)w * (size_t)h;
     switch (fmt) {
         case FMT_U8: return n;
         case FMT_U16: return 2 * n;
         case FMT_P10: return (n * 10 + 7) / 8;
-        default: return (n * 12 + 7) / 8;
+        case FMT_P12: return (n * 12 + 7) / 8;
+        default: return (n * (size_t)bd + 7) / 8;
     }
 }
 

@@ -123,13 +123,23 @@ struct TileSmem {
 
 // ---- small helpers -----------------------------------------------------------------------------
 // byte range [b0, b1) of pixels [i0, i1) (pixel indices) in the input stream
-__device__ __forceinline__ void pixel_bytes(int fmt, int i0, int i1, int& b0, int& b1) {
+__device__ __forceinline__ void pixel_bytes(int fmt, int bd, int i0, int i1, int& b0, int& b1) {
     switch (fmt) {
         case FMT_U8: b0 = i0; b1 = i1; break;
         case FMT_U16: b0 = 2 * i0; b1 = 2 * i1; break;
         case FMT_P12: b0 = 3 * (i0 >> 1); b1 = 3 * ((i1 - 1) >> 1) + 3; break;
-        default: b0 = 5 * (i0 >> 2); b1 = 5 * ((i1 - 1) >> 2) + 5; break;
+        case FMT_P10: b0 = 5 * (i0 >> 2); b1 = 5 * ((i1 - 1) >> 2) + 5; break;
+        default: b0 = (int)(((long long)i0 * bd) >> 3); b1 = (int)(((long long)i1 * bd + 7) >> 3); break;
     }
+}
+
+// sample at bit `shift` of the staged bytes from `rel` on (8 bytes readable there), bit stream
+// formats
+__device__ __forceinline__ int bits_at(const uint8_t* row, int rel, int shift, int mv) {
+    const int o4 = rel & ~3;
+    const uint32_t w0 = *reinterpret_cast<const uint32_t*>(row + o4);
+    const uint32_t w1 = *reinterpret_cast<const uint32_t*>(row + o4 + 4);
+    return (int)((__funnelshift_r(w0, w1, 8 * (rel & 3)) >> shift) & (uint32_t)mv);
 }
 
 // one raw byte of the staged row (or of global memory past the staged window)
@@ -152,12 +162,21 @@ __device__ __forceinline__ int staged_raw(const FrameParams& fp, int a0, int len
             if ((i & 1) == 0) return ((staged_byte(fp, a0, len, row, off) << 4) | (b1 & 0xF)) & fp.mv;
             return ((staged_byte(fp, a0, len, row, off + 2) << 4) | (b1 >> 4)) & fp.mv;
         }
-        default: {
+        case FMT_P10: {
             int off = (i >> 2) * 5;
             int sub = i & 3;
             if (off + 4 >= (int)fp.in_bytes) return 0;
             int b = staged_byte(fp, a0, len, row, off + sub), b4 = staged_byte(fp, a0, len, row, off + 4);
             return ((b << 2) | ((b4 >> (2 * sub)) & 3)) & fp.mv;
+        }
+        default: {
+            const long long bit = (long long)i * fp.bd;
+            const int off = (int)(bit >> 3), shift = (int)(bit & 7);
+            if (off >= (int)fp.in_bytes) return 0;
+            const int n = min((fp.bd + shift + 7) >> 3, (int)fp.in_bytes - off);
+            uint32_t v = 0;
+            for (int k = 0; k < n; k++) v |= (uint32_t)staged_byte(fp, a0, len, row, off + k) << (8 * k);
+            return (int)((v >> shift) & (uint32_t)fp.mv);
         }
     }
 }
@@ -207,7 +226,7 @@ __device__ void tile_init(TileSmem<TW, TH, OUTB>& sm) {
 // the frame with margin (and whose packed rows start on a pair boundary): no bounds checks.
 template <int TW, int TH>
 __device__ __forceinline__ bool tile_is_full(const FrameParams& fp, int x0, int y0, int tw, int th) {
-    const bool even_rows = fp.fmt == FMT_U8 || fp.fmt == FMT_U16 || (fp.w & 1) == 0;
+    const bool even_rows = fp.fmt == FMT_U8 || fp.fmt == FMT_U16 || fp.fmt == FMT_PBITS || (fp.w & 1) == 0;
     return tw == TW && th == TH && x0 >= 8 && y0 >= 8 && x0 + TW + 8 <= fp.w && y0 + TH + 8 <= fp.h && even_rows;
 }
 
@@ -262,7 +281,7 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
         if (y >= 0 && y < H) {
             int xs = max(0, xo), xe = min(W, xo + 2 * opw);
             int b0, b1;
-            pixel_bytes(fp.fmt, y * W + xs, y * W + xe, b0, b1);
+            pixel_bytes(fp.fmt, fp.bd, y * W + xs, y * W + xe, b0, b1);
             b1 = min(b1, (int)fp.in_bytes);
             a0 = b0 & ~15;
             int a1 = min((b1 + 15) & ~15, in16);
@@ -272,7 +291,8 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
                 case FMT_U8: base = i - a0; break;
                 case FMT_U16: base = 2 * i - a0; break;
                 case FMT_P12: base = ((i & 1) == 0) ? 3 * (i >> 1) - a0 : -1; break;
-                default: base = ((i & 1) == 0) ? 5 * (i >> 2) - a0 : -1; break;
+                case FMT_P10: base = ((i & 1) == 0) ? 5 * (i >> 2) - a0 : -1; break;
+                default: base = -1; break;  // bit streams: per-sample offsets (full tiles only)
             }
         }
         sm.row_a0[b][r] = a0;
@@ -409,6 +429,15 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                         v1 = row[off + 1];
                         done = true;
                     }
+                } else if (fmt == FMT_PBITS) {
+                    // bit stream: each sample from its own bit offset (full tiles stage every
+                    // byte the pair needs, and the row buffer has 8 readable bytes past it)
+                    const long long bit0 = ((long long)y * W + x) * fp.bd;
+                    const int a0r = sm.row_a0[b][r];
+                    v0 = bits_at(row, (int)((bit0 >> 3) - a0r), (int)(bit0 & 7), mv);
+                    const long long bit1 = bit0 + fp.bd;
+                    v1 = bits_at(row, (int)((bit1 >> 3) - a0r), (int)(bit1 & 7), mv);
+                    done = true;
                 } else {
                     // MIPI RAW10: the pair is sample 0-1 or 2-3 of its 5-byte group
                     const int i = y * W + x;

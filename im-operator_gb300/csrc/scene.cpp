@@ -204,10 +204,18 @@ extern "C" size_t imop_packed_bytes(int w, int h, int bd) {
 extern "C" int imop_pack_mipi(const uint16_t* in, int w, int h, int bd, uint8_t* out) {
     if (!in || !out) return IMOP_ERR_NULL_INPUT;
     if (w <= 0 || h <= 0) return IMOP_ERR_INVALID_DIMENSIONS;
-    if (bd != 10 && bd != 12) return IMOP_ERR_UNSUPPORTED;
+    if (bd < 1 || bd > 16) return IMOP_ERR_INVALID_BIT_DEPTH;
     size_t n = (size_t)w * h, size = imop_packed_bytes(w, h, bd);
     std::memset(out, 0, size);
-    if (bd == 12) {
+    if (bd != 10 && bd != 12) {
+        // other depths: one LSB-first bit stream, sample i at bits [i bd, (i + 1) bd)
+        const unsigned mv = bd >= 16 ? 0xFFFFu : (1u << bd) - 1;
+        for (size_t i = 0; i < n; i++) {
+            const size_t bit = i * (size_t)bd;
+            const uint32_t v = (uint32_t)(in[i] & mv) << (bit & 7);
+            for (size_t j = bit >> 3, k = 0; k < 3 && j < size; j++, k++) out[j] |= (uint8_t)(v >> (8 * k));
+        }
+    } else if (bd == 12) {
         for (size_t k = 0; 2 * k < n; k++) {
             unsigned p0 = in[2 * k] & 0xFFF, p1 = (2 * k + 1 < n) ? (in[2 * k + 1] & 0xFFF) : 0;
             uint8_t b[3] = {(uint8_t)(p0 >> 4), (uint8_t)((p0 & 0xF) | ((p1 & 0xF) << 4)), (uint8_t)(p1 >> 4)};

@@ -85,6 +85,11 @@ def c3_pipelines():
     return [c1_pipeline(5320, 4600, 8), c1_pipeline(5320, 4600, 12)]
 
 
+def c3_frame(pl, index=0):
+    """A C3 frame (8-bit or 12-bit u16, seeded scene) for one of c3_pipelines()."""
+    return c1_frame(pl, index)
+
+
 # ---- C5: calibration of the differentiable chain ------------------------------------------------
 # 16 x 1006x758 RGGB 12-bit frames (u16 unpacked), 933 parameters (BL 4, WB 3, CCM 9, 17x13x4
 # lens-shading grid, 33 tone knots); the target is the FP64 forward at the true parameters, the

@@ -107,8 +107,9 @@ typedef struct ImopDefectPoint {
 
 typedef struct ImopIspParams {
     int width, height;
-    int bit_depth;   /* 8, 10 or 12 (packed: 10 or 12; unpacked u16 accepts 9..16) */
-    int packed;      /* 0: u8 (bd<=8) or u16 LSB-aligned; 1: MIPI RAW10 (4 px / 5 B) or RAW12 (2 px / 3 B) */
+    int bit_depth;   /* 1..16 */
+    int packed;      /* 0: u8 (bd<=8) or u16 LSB-aligned; 1: MIPI RAW10 (4 px / 5 B), MIPI RAW12
+                        (2 px / 3 B), other depths one LSB-first bit stream (RAW14, RAW16 ...) */
     int pattern;     /* IMOP_RGGB ... */
     int demosaic;    /* IMOP_DEMOSAIC_* */
     unsigned stages; /* IMOP_STAGE_* bits */
@@ -305,7 +306,8 @@ int imop_scene_defects(int width, int height, uint64_t seed, int count, ImopDefe
 /* Write hot (max) / dead (0) values at the listed positions of an unpacked frame. */
 int imop_scene_apply_defects(void* frame, int width, int height, int bit_depth,
                              const ImopDefectPoint* pts, int count);
-/* MIPI pack an unpacked u16 frame (10 or 12 bit); out must hold imop_packed_bytes(). */
+/* Pack an unpacked u16 frame as the packed input of that bit depth (MIPI RAW10 / RAW12, other
+ * depths an LSB-first bit stream); out must hold imop_packed_bytes(). */
 size_t imop_packed_bytes(int width, int height, int bit_depth);
 int imop_pack_mipi(const uint16_t* in, int width, int height, int bit_depth, uint8_t* out);
 

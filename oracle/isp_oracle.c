@@ -692,7 +692,6 @@ static int validate(const ImopIspParams* p) {
     if (p->bit_depth < 1 || p->bit_depth > 16) return IMOP_ERR_INVALID_BIT_DEPTH;
     if (p->pattern < 0 || p->pattern > 3) return IMOP_ERR_INVALID_PATTERN;
     if (p->width < 6 || p->height < 6) return IMOP_ERR_IMAGE_TOO_SMALL;
-    if (p->packed && p->bit_depth != 10 && p->bit_depth != 12) return IMOP_ERR_UNSUPPORTED;
     if (p->demosaic != IMOP_DEMOSAIC_HQLI && p->demosaic != IMOP_DEMOSAIC_AMAZE &&
         p->demosaic != IMOP_DEMOSAIC_MG)
         return IMOP_ERR_UNSUPPORTED;

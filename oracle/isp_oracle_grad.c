@@ -385,8 +385,7 @@ static int frame_run(const ImopAdjointDesc* d, const double* theta, const uint8_
 static int adj_run(const ImopAdjointDesc* d, const double* theta, const uint8_t* raw, double* rgb_out,
                    const float* ref, int mode, double* loss, double* grad) {
     const size_t n = (size_t)d->width * d->height;
-    const size_t in_bytes = d->packed ? (d->bit_depth == 10 ? (n * 10 + 7) / 8 : (n * 12 + 7) / 8)
-                                      : (d->bit_depth <= 8 ? n : 2 * n);
+    const size_t in_bytes = d->packed ? (n * (size_t)d->bit_depth + 7) / 8 : (d->bit_depth <= 8 ? n : 2 * n);
     const int P = or_adj_param_count(d), nf = d->n_frames;
     double* fl = calloc((size_t)nf, sizeof(double));
     double* fg = grad ? calloc((size_t)nf * P, sizeof(double)) : NULL;

@@ -51,7 +51,8 @@ def test_validation_codes_follow_the_reference():
     assert _validate(I.Pipeline(width=10, height=10, bit_depth=17)) == abi.ERR_INVALID_BIT_DEPTH
     assert _validate(I.Pipeline(width=10, height=10, pattern=7)) == abi.ERR_INVALID_PATTERN
     assert _validate(I.Pipeline(width=5, height=10)) == abi.ERR_IMAGE_TOO_SMALL
-    assert _validate(I.Pipeline(width=10, height=10, bit_depth=14, packed=True)) == abi.ERR_UNSUPPORTED
+    # a packed depth other than 10 / 12 is a bit stream: valid (this host then reports no device)
+    assert _validate(I.Pipeline(width=10, height=10, bit_depth=11, packed=True)) == abi.ERR_NO_DEVICE
     assert _validate(I.Pipeline(width=10, height=10, demosaic=3)) == abi.ERR_UNSUPPORTED
     pl = I.Pipeline(width=10, height=10, bit_depth=12, out_format=abi.OUT_RGB8, tone_mode=abi.TONE_LUT)
     pl.tone_lut = np.zeros(100, np.float32)
@@ -95,6 +96,14 @@ def test_mipi_packers_invert_the_unpacker():
             full = n - (n % (4 if bd == 10 else 2))
             assert np.array_equal(got.reshape(-1)[:full], f.reshape(-1)[:full])
             assert not got.reshape(-1)[full:].any()
+    # other depths: one LSB-first bit stream (the reference's generic case), every sample returns
+    for bd in (8, 9, 11, 13, 14, 16):
+        for (w, h) in ((8, 4), (7, 5), (33, 3)):
+            f = rng.integers(0, 1 << bd, (h, w)).astype(np.uint16)
+            buf = I.pack_mipi(f, bd)
+            assert buf.size == (w * h * bd + 7) // 8
+            got = np.array([[O.get_packed_raw(buf, x, y, w, h, bd) for x in range(w)] for y in range(h)])
+            assert np.array_equal(got, f)
 
 
 def test_c2_workload_shape():

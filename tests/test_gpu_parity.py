@@ -50,6 +50,27 @@ def test_fused_matches_oracle(isp, w, h, bd, packed, dm, pat, seed):
     assert max_abs(got, ref) == 0, f"psnr {psnr(got, ref):.2f}"
 
 
+@pytest.mark.parametrize("w,h", [(7, 9), (67, 35), (268, 80), (301, 77)])
+@pytest.mark.parametrize("bd", [8, 9, 11, 13, 14, 16])
+def test_bitstream_packed_matches_oracle(isp, w, h, bd):
+    """Packed depths other than MIPI RAW10 / RAW12: one LSB-first bit stream per frame
+    (pixel::get_packed_raw's generic case), odd widths included, full and border tiles."""
+    rng = np.random.default_rng(1000 * bd + w)
+    dm = DEMOSAICS[(w + bd) % 3]
+    pl = random_pipeline(rng, w, h, bd, True, dm, int(rng.integers(0, 4)))
+    raw = random_frame(rng, pl)
+    assert raw.size == pl.input_bytes()
+    ref, _ = O.pipeline(pl, raw)
+    isp.set_params(pl)
+    got = isp.run_host(raw)
+    assert max_abs(got, ref) == 0, f"psnr {psnr(got, ref):.2f}"
+    torch = pytest.importorskip("torch")
+    d_out = torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+    isp.run_device_plain(torch.from_numpy(raw).cuda(), d_out)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy(), got.view(np.uint8).reshape(-1))
+
+
 @pytest.mark.parametrize("w,h,bd,packed,dm,pat,seed", _cases(21, 2))
 def test_stage_dumps_match_oracle(isp, w, h, bd, packed, dm, pat, seed):
     rng = np.random.default_rng(seed)
@@ -129,6 +150,16 @@ def test_c2_full_frame(isp):
     isp.set_params(pl)
     got = isp.run_host(raw)
     assert max_abs(got, ref) == 0
+
+
+@pytest.mark.parametrize("k", [0, 1], ids=["c3_8bit", "c3_12bit_u16"])
+def test_c3_full_frame(isp, k):
+    """5320x4600 frames (8-bit and 12-bit unpacked) through the C1 pipeline."""
+    pl = workloads.c3_pipelines()[k]
+    raw = workloads.c3_frame(pl, k)
+    ref, _ = O.pipeline(pl, raw)
+    isp.set_params(pl)
+    assert max_abs(isp.run_host(raw), ref) == 0
 
 
 def test_plain_equals_fused_device(isp):

@@ -81,7 +81,7 @@ def test_stages_match_reference(trial):
     assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("bd", [9, 10, 12, 14])
+@pytest.mark.parametrize("bd", [8, 9, 10, 11, 12, 14, 16])
 def test_packed_unpack_matches_reference(bd):
     R = O.ref()
     rng = np.random.default_rng(bd)
