@@ -57,6 +57,10 @@ def lib():
             "imop_scene_apply_defects": (i, [vp, i, i, i, C.POINTER(abi.DefectPoint), i]),
             "imop_packed_bytes": (sz, [i, i, i]),
             "imop_pack_mipi": (i, [vp, i, i, i, vp]),
+            "imop_analyze_data": (i, [vp, sz, C.POINTER(abi.DataInfo)]),
+            "imop_detect_bit_depth": (i, [vp, sz]),
+            "imop_suggest_dimensions": (i, [sz, C.POINTER(C.c_int * 2), i]),
+            "imop_guess_pattern": (i, [vp, i, i, i, i]),
             "imop_last_error_string": (C.c_char_p, []),
             "imop_abi_version": (i, []),
             "imop_has_cuda": (i, []),
@@ -223,3 +227,38 @@ def pack_mipi(frame, bit_depth):
     out = np.empty(lib().imop_packed_bytes(w, h, bit_depth), np.uint8)
     check(lib().imop_pack_mipi(f.ctypes.data, w, h, bit_depth, out.ctypes.data))
     return out
+
+
+# ---- format sniffing (the reference's analyzer heuristics) ----------------------------------------
+def _bytes(buf):
+    a = np.ascontiguousarray(buf).view(np.uint8).reshape(-1)
+    return a, a.nbytes
+
+
+def analyze_data(buf):
+    """dict of the detected bit depth, packing, pixel count, value range and candidate sizes"""
+    a, n = _bytes(buf)
+    info = abi.DataInfo()
+    check(lib().imop_analyze_data(a.ctypes.data if n else None, n, C.byref(info)))
+    dims = [(info.dims[k][0], info.dims[k][1]) for k in range(info.n_dims)]
+    return {"detected_bit_depth": info.detected_bit_depth, "suggested_width": info.suggested_width,
+            "suggested_height": info.suggested_height, "pixel_count": info.pixel_count,
+            "max_value": info.max_value, "min_value": info.min_value,
+            "is_likely_16bit": bool(info.is_likely_16bit), "is_packed": bool(info.is_packed),
+            "possible_dimensions": dims}
+
+
+def detect_bit_depth(buf):
+    a, n = _bytes(buf)
+    return lib().imop_detect_bit_depth(a.ctypes.data if n else None, n)
+
+
+def suggest_dimensions(pixel_count):
+    out = ((C.c_int * 2) * abi.ANALYZE_MAX_DIMS)()
+    k = lib().imop_suggest_dimensions(pixel_count, out, abi.ANALYZE_MAX_DIMS)
+    return [(out[j][0], out[j][1]) for j in range(min(k, abi.ANALYZE_MAX_DIMS))]
+
+
+def guess_pattern(buf, width, height, bit_depth=8, packed=False):
+    a, _ = _bytes(buf)
+    return lib().imop_guess_pattern(a.ctypes.data, width, height, bit_depth, int(bool(packed)))

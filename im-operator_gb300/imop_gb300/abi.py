@@ -63,6 +63,16 @@ class IspParams(C.Structure):
     ]
 
 
+ANALYZE_MAX_DIMS = 16
+
+
+class DataInfo(C.Structure):
+    _fields_ = [("detected_bit_depth", C.c_int), ("suggested_width", C.c_int), ("suggested_height", C.c_int),
+                ("pixel_count", C.c_int), ("max_value", C.c_int), ("min_value", C.c_int),
+                ("is_likely_16bit", C.c_int), ("is_packed", C.c_int), ("n_dims", C.c_int),
+                ("dims", (C.c_int * 2) * ANALYZE_MAX_DIMS)]
+
+
 class StageDumps(C.Structure):
     _fields_ = [
         ("unpacked", C.c_void_p), ("black_level", C.c_void_p), ("defect", C.c_void_p),

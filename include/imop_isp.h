@@ -311,6 +311,30 @@ int imop_scene_apply_defects(void* frame, int width, int height, int bit_depth,
 size_t imop_packed_bytes(int width, int height, int bit_depth);
 int imop_pack_mipi(const uint16_t* in, int width, int height, int bit_depth, uint8_t* out);
 
+/* ---- format sniffing of raw blobs of unknown layout (host) ---------------------------- */
+/* The reference's analyzer heuristics (imop::analyze_data, detect_bit_depth, suggest_dimensions,
+ * guess_pattern in src/analyzer.cpp), with the same results: storage bit depth from the byte
+ * count against known resolutions and from value statistics, packed detection, candidate
+ * dimensions, Bayer phase from 2x2 votes and channel means. */
+#define IMOP_ANALYZE_MAX_DIMS 16
+typedef struct {
+    int detected_bit_depth;
+    int suggested_width, suggested_height;
+    int pixel_count;
+    int max_value, min_value;
+    int is_likely_16bit;
+    int is_packed;
+    int n_dims;                          /* candidate dimensions held in dims */
+    int dims[IMOP_ANALYZE_MAX_DIMS][2];  /* (width, height), most likely first */
+} ImopDataInfo;
+int imop_analyze_data(const void* data, size_t bytes, ImopDataInfo* info);
+int imop_detect_bit_depth(const void* data, size_t bytes);
+/* Candidate (width, height) pairs of a pixel count: writes up to cap of them to out, returns how
+ * many there are (-1: bad arguments). */
+int imop_suggest_dimensions(size_t pixel_count, int (*out)[2], int cap);
+/* IMOP_RGGB ... of a frame of known size and storage (RGGB when undecided). */
+int imop_guess_pattern(const void* data, int width, int height, int bit_depth, int packed);
+
 /* ---- misc --------------------------------------------------------------------------- */
 const char* imop_last_error_string(void);
 int imop_abi_version(void);

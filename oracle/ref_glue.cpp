@@ -22,6 +22,7 @@
 #include "ccm/algorithms.hpp"
 #include "defect_correct/algorithms.hpp"
 #include "imop/algorithms.hpp"
+#include "imop/analyzer.hpp"
 #include "imop/pixel_utils.hpp"
 #include "lens_shading/algorithms.hpp"
 #include "white_balance/algorithms.hpp"
@@ -213,6 +214,31 @@ int ref_ccm(uint16_t* rgb, int w, int h, int bd, const float m[9]) {
     auto e = ccm::process_ccm(s.data(), out.data(), w, h, 3, ccm::CCMAlgorithm::LINEAR_3X3, bd, &mat);
     from_store(out, rgb, n, bd);
     return static_cast<int>(e);
+}
+
+// analyzer: detected depth and sizes; info = {depth, w, h, pixels, max, min, is16, packed, n_dims}
+int ref_detect_bit_depth(const uint8_t* d, size_t n) { return imop::detect_bit_depth(d, n); }
+int ref_suggest_dimensions(size_t n, int* out, int cap) {
+    const auto v = imop::suggest_dimensions(n);
+    for (size_t k = 0; k < v.size() && (int)k < cap; k++) {
+        out[2 * k] = v[k].first;
+        out[2 * k + 1] = v[k].second;
+    }
+    return (int)v.size();
+}
+int ref_analyze_data(const uint8_t* d, size_t n, int* info, int* dims, int cap) {
+    const imop::DataInfo a = imop::analyze_data(d, n);
+    const int v[9] = {a.detected_bit_depth, a.suggested_width, a.suggested_height, a.pixel_count, a.max_value,
+                      a.min_value, a.is_likely_16bit ? 1 : 0, a.is_packed ? 1 : 0, (int)a.possible_dimensions.size()};
+    for (int k = 0; k < 9; k++) info[k] = v[k];
+    for (size_t k = 0; k < a.possible_dimensions.size() && (int)k < cap; k++) {
+        dims[2 * k] = a.possible_dimensions[k].first;
+        dims[2 * k + 1] = a.possible_dimensions[k].second;
+    }
+    return 0;
+}
+int ref_guess_pattern(const uint8_t* d, int w, int h, int bd, int packed) {
+    return (int)imop::guess_pattern(d, w, h, bd, packed != 0);
 }
 
 }  // extern "C"
