@@ -53,7 +53,9 @@ enum {
     IMOP_ERR_CUDA = 102,             /* a CUDA runtime call failed                          */
     IMOP_ERR_TIMEOUT = 103,          /* a bounded device-side wait expired                  */
     IMOP_ERR_CAPACITY = 104,         /* a device-side list (defect chain, queue) overflowed */
-    IMOP_ERR_NO_DEVICE = 105         /* no CUDA device visible                              */
+    IMOP_ERR_NO_DEVICE = 105,        /* no CUDA device visible                              */
+    IMOP_ERR_INSUFFICIENT_PATCHES = 106, /* fewer than 3 patches for a CCM solve             */
+    IMOP_ERR_SINGULAR = 107          /* singular normal equations in a CCM solve            */
 };
 
 /* imop::BayerPattern (include/imop/types.hpp:12-17) */
@@ -334,6 +336,23 @@ int imop_detect_bit_depth(const void* data, size_t bytes);
 int imop_suggest_dimensions(size_t pixel_count, int (*out)[2], int cap);
 /* IMOP_RGGB ... of a frame of known size and storage (RGGB when undecided). */
 int imop_guess_pattern(const void* data, int width, int height, int bit_depth, int packed);
+
+/* ---- colour-correction matrix from patch measurements (host) ------------------------- */
+/* The reference's least-squares CCM solve (color_calibration::process_solve_ccm): per output
+ * channel the normal equations over the patches plus 1e-9 on the diagonal, in FP64, Gaussian
+ * elimination with partial pivoting; same results.  Layouts of PatchColor / SolvedMatrix. */
+enum { IMOP_CCM_LINEAR_3X3 = 0, IMOP_CCM_LINEAR_4X3 = 1, IMOP_CCM_POLY_3X9 = 2 };
+typedef struct {
+    float r, g, b;
+} ImopPatchColor;
+typedef struct {
+    int type;     /* IMOP_CCM_* */
+    float m[27];  /* row-major rows x cols, zeros past the used entries */
+    int rows;     /* 3 */
+    int cols;     /* 3, 4 or 9 */
+} ImopSolvedMatrix;
+int imop_solve_ccm(const ImopPatchColor* measured, const ImopPatchColor* reference, int n, int type,
+                   ImopSolvedMatrix* out);
 
 /* ---- misc --------------------------------------------------------------------------- */
 const char* imop_last_error_string(void);

@@ -83,6 +83,7 @@ def ref():
         _ref.ref_suggest_dimensions.argtypes = [C.c_size_t, IP, i]
         _ref.ref_analyze_data.argtypes = [U8P, C.c_size_t, IP, IP, i]
         _ref.ref_guess_pattern.argtypes = [U8P, i, i, i, i]
+        _ref.ref_solve_ccm.argtypes = [F32P, F32P, i, i, F32P, IP, IP]
     return _ref
 
 

@@ -23,6 +23,7 @@
 #include "defect_correct/algorithms.hpp"
 #include "imop/algorithms.hpp"
 #include "imop/analyzer.hpp"
+#include "color_calibration/algorithms.hpp"
 #include "imop/pixel_utils.hpp"
 #include "lens_shading/algorithms.hpp"
 #include "white_balance/algorithms.hpp"
@@ -239,6 +240,23 @@ int ref_analyze_data(const uint8_t* d, size_t n, int* info, int* dims, int cap) 
 }
 int ref_guess_pattern(const uint8_t* d, int w, int h, int bd, int packed) {
     return (int)imop::guess_pattern(d, w, h, bd, packed != 0);
+}
+
+// colour calibration: m receives rows x cols floats; returns the error code
+int ref_solve_ccm(const float* measured, const float* reference, int n, int type, float* m, int* rows, int* cols) {
+    color_calibration::SolveCCMParams p;
+    p.measured = reinterpret_cast<const color_calibration::PatchColor*>(measured);
+    p.reference = reinterpret_cast<const color_calibration::PatchColor*>(reference);
+    p.patch_count = n;
+    p.matrix_type = static_cast<color_calibration::MatrixType>(type);
+    color_calibration::SolvedMatrix r;
+    const int e = (int)color_calibration::process_solve_ccm(p, &r);
+    if (e == 0) {
+        std::memcpy(m, r.m, sizeof(r.m));
+        *rows = r.rows;
+        *cols = r.cols;
+    }
+    return e;
 }
 
 }  // extern "C"
