@@ -98,6 +98,7 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         if ((e = cudaDeviceSynchronize())) return cuda_fail(e, "sync before cache reset");
         tc.grids.clear();
         tc.tones.clear();
+        tc.lut3ds.clear();
         tc.maps.clear();
         c->graph.key = 0;
     }
@@ -158,6 +159,23 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         fp.gw = p->lsc_mode == IMOP_LSC_FLAT_FIELD ? 32 : p->lsc_grid_w;
         fp.gh = p->lsc_mode == IMOP_LSC_FLAT_FIELD ? 24 : p->lsc_grid_h;
         fp.grid = (const float*)slot->ptr;
+    }
+    if (p->stages & IMOP_STAGE_LUT3D) {
+        Key k;
+        k.val(p->lut3d_size);
+        k.bytes(p->lut3d, sizeof(float) * 3 * (size_t)p->lut3d_size * p->lut3d_size * p->lut3d_size);
+        CacheEntry<DevBuf>* ent = nullptr;
+        if ((rc = cache_entry(c, tc.lut3ds, k, ent))) return rc;
+        if (!ent->obj) {
+            std::vector<float> l(p->lut3d, p->lut3d + 3 * (size_t)p->lut3d_size * p->lut3d_size * p->lut3d_size);
+            std::unique_ptr<DevBuf> d(new DevBuf());
+            if ((e = upload(*d, l))) {
+                tc.lut3ds.erase(k.hash());
+                return cuda_fail(e, "upload 3D LUT");
+            }
+            ent->obj = std::move(d);
+        }
+        fp.lut3d = (const float*)ent->obj->ptr;
     }
     {
         Key k;

@@ -186,7 +186,11 @@ int validate_params(const ImopIspParams* p) {
         return fail(IMOP_ERR_UNSUPPORTED, "frame larger than 2^31 output bytes");
     if (p->demosaic != IMOP_DEMOSAIC_HQLI && p->demosaic != IMOP_DEMOSAIC_AMAZE && p->demosaic != IMOP_DEMOSAIC_MG)
         return fail(IMOP_ERR_UNSUPPORTED, "demosaic must be HQLI, MG or AMAZE");
-    if (p->stages & ~IMOP_STAGE_ALL) return fail(IMOP_ERR_INVALID_ARGUMENT, "unknown stage bits");
+    if (p->stages & ~(IMOP_STAGE_ALL | IMOP_STAGE_LUT3D)) return fail(IMOP_ERR_INVALID_ARGUMENT, "unknown stage bits");
+    if (p->stages & IMOP_STAGE_LUT3D) {
+        if (!p->lut3d) return fail(IMOP_ERR_NULL_INPUT, "lut3d is null");
+        if (p->lut3d_size < 2 || p->lut3d_size > 65) return fail(IMOP_ERR_INVALID_ARGUMENT, "lut3d_size must be 2..65");
+    }
     if (p->stage_order != IMOP_ORDER_BAYER_WB && p->stage_order != IMOP_ORDER_RGB_WB)
         return fail(IMOP_ERR_INVALID_ARGUMENT, "stage_order");
     if (p->stages & IMOP_STAGE_BLACK_LEVEL) {
@@ -250,6 +254,7 @@ void expand_frame_params(const ImopIspParams* p, FrameParams& fp) {
     fp.demosaic = p->demosaic;
     fp.border_mode = (p->demosaic == IMOP_DEMOSAIC_AMAZE && p->bit_depth <= 8) ? BORDER_BOTH : BORDER_ROWS_THEN_COLS;
     fp.stages = p->stages;
+    if (p->stages & IMOP_STAGE_LUT3D) fp.lut3d_size = p->lut3d_size;  // the table pointer is the caller's to fill
     fp.stage_order = p->stage_order;
     fp.out_format = p->out_format;
     fp.out_bpc = (p->out_format == IMOP_OUT_NATIVE && p->bit_depth > 8) ? 2 : 1;
@@ -348,6 +353,11 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
             if ((e = upload(tabs.grid, g))) return cuda_fail(e, "upload lens-shading grid");
             fp.grid = (const float*)tabs.grid.ptr;
         }
+    }
+    if (p->stages & IMOP_STAGE_LUT3D) {
+        std::vector<float> l(p->lut3d, p->lut3d + (size_t)p->lut3d_size * p->lut3d_size * p->lut3d_size * 3);
+        if ((e = upload(tabs.lut3d, l))) return cuda_fail(e, "upload 3D LUT");
+        fp.lut3d = (const float*)tabs.lut3d.ptr;
     }
     // tone table (padded: the kernel reads it in 4-byte words)
     if ((e = tabs.tone8.ensure(std::max<size_t>((size_t)fp.mv + 1, 4096) + 16))) return cuda_fail(e, "alloc tone table");
@@ -653,7 +663,7 @@ int imop_op_bayer_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, 
 }
 
 int imop_op_rgb_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, const void* in, void* out) {
-    if (stage != IMOP_STAGE_WHITE_BALANCE && stage != IMOP_STAGE_CCM)
+    if (stage != IMOP_STAGE_WHITE_BALANCE && stage != IMOP_STAGE_CCM && stage != IMOP_STAGE_LUT3D)
         return fail(IMOP_ERR_INVALID_ARGUMENT, "not an RGB stage");
     if (!in || !out) return fail(IMOP_ERR_NULL_INPUT, "null frame pointer");
     ImopIspParams q;

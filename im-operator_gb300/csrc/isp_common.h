@@ -129,6 +129,9 @@ struct FrameParams {
     int tiles_x, tiles_y;  // tile grid of this frame
     // -0.0f, read at run time: the addend of the packed products (see dev::pmul)
     float neg_zero;
+    // optional 3D LUT after the CCM (stage bit 5): size^3 x 3 floats, R-major
+    const float* lut3d;
+    int lut3d_size;
 };
 
 }  // namespace imop

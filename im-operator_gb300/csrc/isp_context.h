@@ -27,7 +27,7 @@ struct DevBuf {
 
 // device copies of one frame's parameter tables
 struct FrameTables {
-    DevBuf grid, lut, knots, tone8;
+    DevBuf grid, lut, knots, tone8, lut3d;
     DevBuf map_row_ptr, map_ent, map_val, slot_xy, comp_slot_ptr, comp_slots, comp_ent_ptr, comp_entries;
     MapPlan plan{};
     int n_slots = 0;  // unique map pixels (entries of map_val)
@@ -57,9 +57,9 @@ struct CacheEntry {
     std::vector<uint8_t> key;
 };
 struct TableCache {
-    std::unordered_map<uint64_t, CacheEntry<DevBuf>> grids, tones;
+    std::unordered_map<uint64_t, CacheEntry<DevBuf>> grids, tones, lut3ds;
     std::unordered_map<uint64_t, CacheEntry<FrameTables>> maps;
-    size_t entries() const { return grids.size() + tones.size() + maps.size(); }
+    size_t entries() const { return grids.size() + tones.size() + lut3ds.size() + maps.size(); }
 };
 
 // per-frame defect-chain scratch and map values of a batch

@@ -85,6 +85,8 @@ extern "C" int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d
     if (!d_in || !d_out) return set_error(IMOP_ERR_NULL_INPUT, "null frame pointer");
     if (p->bit_depth > kMaxBitDepth)
         return set_error(IMOP_ERR_UNSUPPORTED, "no-alloc entry point: bit depth above 12");
+    if (p->stages & IMOP_STAGE_LUT3D)
+        return set_error(IMOP_ERR_UNSUPPORTED, "no-alloc entry point: 3D LUTs need a device table");
     if ((p->stages & IMOP_STAGE_DEFECT) && p->dpc_mode != IMOP_DPC_ADAPTIVE)
         return set_error(IMOP_ERR_UNSUPPORTED, "no-alloc entry point: defect maps need device tables");
     const bool grid_lsc = (p->stages & IMOP_STAGE_LENS_SHADING) && p->lsc_mode != IMOP_LSC_POLYNOMIAL;

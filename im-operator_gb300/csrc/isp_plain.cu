@@ -251,6 +251,17 @@ __global__ void ccm_kernel(const __grid_constant__ FrameParams fp, uint16_t* rgb
     }
 }
 
+__global__ void lut3d_kernel(const __grid_constant__ FrameParams fp, uint16_t* rgb) {
+    size_t n = (size_t)fp.w * fp.h;
+    GRID_STRIDE(i, n) {
+        int r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+        dev::lut3d_apply(fp.lut3d, fp.lut3d_size, fp.mv, r, g, b);
+        rgb[3 * i] = (uint16_t)r;
+        rgb[3 * i + 1] = (uint16_t)g;
+        rgb[3 * i + 2] = (uint16_t)b;
+    }
+}
+
 __global__ void output_kernel(const __grid_constant__ FrameParams fp, const uint16_t* rgb) {
     size_t n = (size_t)fp.w * fp.h * 3;
     GRID_STRIDE(i, n) {
@@ -322,6 +333,7 @@ cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const Ma
     }
     if (fp.stages & 16u) ccm_kernel<<<nb, kPlainThreads, 0, st>>>(fp, b.rgb);
     dump(dumps->ccm, b.rgb, 3 * n);
+    if (fp.stages & 32u) lut3d_kernel<<<nb, kPlainThreads, 0, st>>>(fp, b.rgb);
     output_kernel<<<nb3, kPlainThreads, 0, st>>>(fp, b.rgb);
     return cudaGetLastError();
 }
@@ -369,6 +381,7 @@ cudaError_t launch_op_rgb(const FrameParams& fp, unsigned stage, uint16_t* rgb, 
     const size_t n = (size_t)fp.w * fp.h;
     if (stage == 8u) rgb_wb_kernel<<<plain_blocks(3 * n), kPlainThreads, 0, st>>>(fp, rgb);
     else if (stage == 16u) ccm_kernel<<<plain_blocks(n), kPlainThreads, 0, st>>>(fp, rgb);
+    else if (stage == 32u) lut3d_kernel<<<plain_blocks(n), kPlainThreads, 0, st>>>(fp, rgb);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

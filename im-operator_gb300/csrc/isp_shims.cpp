@@ -230,8 +230,20 @@ namespace lut {
 
 bool has_cuda() { return imop::has_cuda(); }
 
-// 3D LUTs are not on this path; the dispatcher runs them on the CPU.
-LUTError process_lut_cuda(const uint8_t*, uint8_t*, int, int, int, int, const LUT3D&) { return LUTError::InternalError; }
+// CUSTOM_3D (src/lut/dispatch.cpp:84-88): the trilinear 3D LUT of lut::apply_lut on the device
+LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
+                          const LUT3D& lut_data) {
+    if (!input || !output) return LUTError::NullInput;
+    const size_t n = (size_t)lut_data.size * lut_data.size * lut_data.size * 3;
+    if (channels != 3 || lut_data.size < 2 || lut_data.size > 65 || lut_data.data.size() != n)
+        return LUTError::InternalError;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return LUTError::InternalError;
+    ImopIspParams p = base_params(width, height, bit_depth, IMOP_RGGB);
+    p.lut3d = lut_data.data.data();
+    p.lut3d_size = lut_data.size;
+    return as_status<LUTError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_LUT3D, input, output));
+}
 
 }  // namespace lut
 

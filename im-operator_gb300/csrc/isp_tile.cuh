@@ -868,6 +868,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const int out_format = fp.out_format;
     const bool border_tile = !FULL && (x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2);
     const bool ccm_on = (stages & 16u) != 0;
+    const bool lut3d_on = (stages & 32u) != 0;
     const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
     const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
     // RGB WB, CCM and tone of pair (x, x+1) in tile row r, staged for the stores
@@ -898,6 +899,10 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
             R0 = u16q(ro.x, mv); R1 = u16q(ro.y, mv);
             G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
             B0 = u16q(bo.x, mv); B1 = u16q(bo.y, mv);
+        }
+        if (lut3d_on) {
+            dev::lut3d_apply(fp.lut3d, fp.lut3d_size, mv, R0, G0, B0);
+            dev::lut3d_apply(fp.lut3d, fp.lut3d_size, mv, R1, G1, B1);
         }
         int g0 = (y * W + x0) * 3 * bpc;
         int shift = (int)((out_base + (uintptr_t)g0) & 15);

@@ -26,6 +26,7 @@ STAGE_LENS_SHADING = 1 << 2
 STAGE_WHITE_BALANCE = 1 << 3
 STAGE_CCM = 1 << 4
 STAGE_ALL = 0x1F
+STAGE_LUT3D = 1 << 5  # optional 3D LUT after the CCM, not in STAGE_ALL
 
 ORDER_BAYER_WB = 0
 ORDER_RGB_WB = 1
@@ -60,6 +61,7 @@ class IspParams(C.Structure):
         ("tone_lut", C.POINTER(C.c_float)), ("tone_lut_len", C.c_int),
         ("tone_knots", C.c_float * 33),
         ("out_format", C.c_int),
+        ("lut3d", C.POINTER(C.c_float)), ("lut3d_size", C.c_int),
     ]
 
 

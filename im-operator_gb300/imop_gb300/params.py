@@ -38,6 +38,7 @@ class Pipeline:
     tone_lut: Optional[np.ndarray] = None         # (2^bd,) float32
     tone_knots: tuple = tuple(i / 32.0 for i in range(33))
     out_format: int = abi.OUT_RGB8
+    lut3d: Optional[np.ndarray] = None            # (n, n, n, 3) float32, R-major (stage STAGE_LUT3D)
     _keep: list = field(default_factory=list, repr=False)
 
     # ---- sizes ----------------------------------------------------------------------------
@@ -108,4 +109,9 @@ class Pipeline:
         for i in range(33):
             p.tone_knots[i] = float(self.tone_knots[i])
         p.out_format = self.out_format
+        if self.lut3d is not None:
+            lt = np.ascontiguousarray(self.lut3d, dtype=np.float32)
+            self._keep.append(lt)
+            p.lut3d = lt.ctypes.data_as(C.POINTER(C.c_float))
+            p.lut3d_size = lt.shape[0]
         return p

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define IMOP_ISP_ABI_VERSION 1
+#define IMOP_ISP_ABI_VERSION 2
 
 /* ---- status codes (0..6 == imop::DemosaicError) ---------------------------------- */
 enum {
@@ -71,7 +71,9 @@ enum {
     IMOP_STAGE_LENS_SHADING = 1u << 2,
     IMOP_STAGE_WHITE_BALANCE = 1u << 3,
     IMOP_STAGE_CCM = 1u << 4,
-    IMOP_STAGE_ALL = 0x1Fu
+    IMOP_STAGE_ALL = 0x1Fu,
+    /* optional 3D LUT after the CCM (lut::apply_lut, trilinear; not part of IMOP_STAGE_ALL) */
+    IMOP_STAGE_LUT3D = 1u << 5
 };
 
 /* where white balance runs */
@@ -141,6 +143,10 @@ typedef struct ImopIspParams {
     float tone_knots[33];
 
     int out_format;       /* IMOP_OUT_* */
+
+    /* IMOP_STAGE_LUT3D: lut3d_size^3 x 3 floats, R-major, RGB interleaved (lut::LUT3D); copied */
+    const float* lut3d;
+    int lut3d_size;       /* samples per axis, 2..65 */
 } ImopIspParams;
 
 /* Fill *p with the identity pipeline for a w x h frame: all stages off, HQLI, linear tone, RGB8. */
@@ -231,7 +237,7 @@ int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
  *     in place on one unpacked Bayer frame (u8 for bit depth <= 8, u16 otherwise), as
  *     black_level::process_black_level_cuda, defect_correct::process_defect_correct_cuda and
  *     lens_shading::process_lens_shading_cuda do;
- *   imop_op_rgb_stage: stage IMOP_STAGE_WHITE_BALANCE or IMOP_STAGE_CCM, interleaved RGB
+ *   imop_op_rgb_stage: stage IMOP_STAGE_WHITE_BALANCE, IMOP_STAGE_CCM or IMOP_STAGE_LUT3D, interleaved RGB
  *     (u8 x 3 for bit depth <= 8, u16 x 3 otherwise) from `in` to `out` (may alias), as
  *     white_balance::process_white_balance_cuda and ccm::process_ccm_cuda do.
  * The stage's parameters come from *p (width, height, bit_depth, pattern and the stage's own

@@ -10,10 +10,10 @@
  * depend on them; the reference file each one follows is named beside it.  A translation unit
  * uses either these declarations or the reference's headers, not both.
  *
- * Served on the GPU: demosaic HQLI / MG / AMAZE (packed RAW10 / RAW12 included), black level,
+ * Served on the GPU: demosaic HQLI / MG / AMAZE (packed input of any depth included), black level,
  * adaptive and map-based defect correction, polynomial and flat-field lens shading, manual white
- * balance, 3x3 CCM.  tone::process_tone_cuda and lut::process_lut_cuda return InternalError, so
- * the reference runs its CPU tone curves and 3D LUTs; the other modules of the same glue file
+ * balance, 3x3 CCM, custom 3D LUTs.  tone::process_tone_cuda returns InternalError, so the
+ * reference runs its CPU tone curves; the other modules of the same glue file
  * (denoise, sharpen, local contrast, saturation, colour temperature, highlight reconstruction)
  * report no CUDA and stay on the CPU.
  */

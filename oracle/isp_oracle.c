@@ -640,6 +640,44 @@ void or_wb_rgb(uint16_t* rgb, int w, int h, int bd, const float gain[3]) {
     }
 }
 
+/* a11: lut::apply_lut (src/lut/core.cpp:11-39) with lut::detail::trilinear_lookup
+ * (src/lut/common.hpp:44-106): v / max into the cube, interpolation along B, then G, then R,
+ * (int)(v * max + 0.5f) clamped to [0, max]. */
+void or_lut3d(uint16_t* rgb, int w, int h, int bd, const float* lut, int size) {
+    const int mv = or_max_val(bd);
+    const float mvf = (float)mv, s1 = (float)(size - 1);
+    const size_t n = (size_t)w * (size_t)h;
+    for (size_t i = 0; i < n; i++) {
+        float sc[3];
+        int lo[3], hi[3];
+        float d[3];
+        for (int c = 0; c < 3; c++) {
+            sc[c] = ((float)rgb[3 * i + c] / mvf) * s1;
+            int k = (int)sc[c];
+            if (k > size - 2) k = size - 2;
+            if (k < 0) k = 0;
+            lo[c] = k;
+            hi[c] = k + 1 < size - 1 ? k + 1 : size - 1;
+            d[c] = sc[c] - (float)k;
+        }
+        float corner[2][2][3]; /* [r][g][channel], interpolated along B */
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++) {
+                const int ri = a ? hi[0] : lo[0], gi = b ? hi[1] : lo[1];
+                const float* p0 = lut + (((size_t)ri * size + (size_t)gi) * size + (size_t)lo[2]) * 3;
+                const float* p1 = lut + (((size_t)ri * size + (size_t)gi) * size + (size_t)hi[2]) * 3;
+                for (int c = 0; c < 3; c++) corner[a][b][c] = p0[c] + d[2] * (p1[c] - p0[c]);
+            }
+        for (int c = 0; c < 3; c++) {
+            const float v0 = corner[0][0][c] + d[1] * (corner[0][1][c] - corner[0][0][c]);
+            const float v1 = corner[1][0][c] + d[1] * (corner[1][1][c] - corner[1][0][c]);
+            const float o = v0 + d[0] * (v1 - v0);
+            int q = (int)(o * mvf + 0.5f);
+            rgb[3 * i + c] = (uint16_t)(q < 0 ? 0 : (q > mv ? mv : q));
+        }
+    }
+}
+
 /* a9: ccm::process_linear_3x3 (src/ccm/linear_3x3.cpp:9-46) */
 void or_ccm(uint16_t* rgb, int w, int h, int bd, const float m[9]) {
     int mv = or_max_val(bd);
@@ -757,6 +795,7 @@ int or_pipeline(const ImopIspParams* p, const void* in, void* out, OracleDumps* 
     }
     if (p->stages & IMOP_STAGE_CCM) or_ccm(rgb, w, h, bd, p->ccm);
     rgb_copy_fill(dumps->ccm, rgb, n * 3);
+    if (p->stages & IMOP_STAGE_LUT3D) or_lut3d(rgb, w, h, bd, p->lut3d, p->lut3d_size);
     if (p->out_format == IMOP_OUT_NATIVE) {
         if (bd <= 8) {
             uint8_t* o = (uint8_t*)out;

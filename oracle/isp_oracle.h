@@ -51,6 +51,7 @@ void or_demosaic_mg(const uint16_t* bay, uint16_t* rgb, int w, int h, int patter
 /* a6 RGB-domain white balance, a9 CCM (in place on RGB u16 x 3) */
 void or_wb_rgb(uint16_t* rgb, int w, int h, int bd, const float gain[3]);
 void or_ccm(uint16_t* rgb, int w, int h, int bd, const float m[9]);
+void or_lut3d(uint16_t* rgb, int w, int h, int bd, const float* lut, int size);
 /* a10: tone value in [0,1] for an integer sample, then the 8-bit quantiser */
 float or_tone_value(int mode, const float* lut, const float* knots, int v, int bd);
 uint8_t or_tone_to_u8(float t);

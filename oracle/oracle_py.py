@@ -84,6 +84,7 @@ def ref():
         _ref.ref_analyze_data.argtypes = [U8P, C.c_size_t, IP, IP, i]
         _ref.ref_guess_pattern.argtypes = [U8P, i, i, i, i]
         _ref.ref_solve_ccm.argtypes = [F32P, F32P, i, i, F32P, IP, IP]
+        _ref.ref_apply_lut.argtypes = [U16P, i, i, i, F32P, i]
     return _ref
 
 
@@ -150,6 +151,7 @@ def stages():
         f.argtypes = [U16P, U16P, i, i, i, i]
     L.or_wb_rgb.argtypes = [U16P, i, i, i, F32P]
     L.or_ccm.argtypes = [U16P, i, i, i, F32P]
+    L.or_lut3d.argtypes = [U16P, i, i, i, F32P, i]
     L.or_unpack.argtypes = [U8P, i, i, i, i, U16P]
     return L
 

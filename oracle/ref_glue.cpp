@@ -24,6 +24,7 @@
 #include "imop/algorithms.hpp"
 #include "imop/analyzer.hpp"
 #include "color_calibration/algorithms.hpp"
+#include "lut/algorithms.hpp"
 #include "imop/pixel_utils.hpp"
 #include "lens_shading/algorithms.hpp"
 #include "white_balance/algorithms.hpp"
@@ -256,6 +257,18 @@ int ref_solve_ccm(const float* measured, const float* reference, int n, int type
         *rows = r.rows;
         *cols = r.cols;
     }
+    return e;
+}
+
+// 3D LUT on interleaved RGB in its storage (u8 for bd <= 8, u16 otherwise), in place
+int ref_apply_lut(uint16_t* rgb, int w, int h, int bd, const float* lut, int size) {
+    lut::LUT3D L;
+    L.size = size;
+    L.data.assign(lut, lut + (size_t)size * size * size * 3);
+    const size_t n = (size_t)w * h * 3;
+    std::vector<uint8_t> in = to_store(rgb, n, bd), out(in.size());
+    const int e = (int)lut::apply_lut(L, in.data(), out.data(), w, h, bd);
+    if (e == 0) from_store(out, rgb, n, bd);
     return e;
 }
 

@@ -135,6 +135,24 @@ int main() {
                 auto st2 = ccm::process_ccm_cuda(g.data(), out.data(), w, h, 3, bd, m);
                 or_ccm(ref2.data(), w, h, bd, m);
                 report("ccm LINEAR_3X3", w, h, bd, st2 == ccm::CCMError::Ok && widen(out, bd) == ref2);
+                // custom 3D LUT (a seeded 9^3 cube around the identity)
+                lut::LUT3D cube;
+                cube.size = 9;
+                uint32_t s = (uint32_t)seed * 2654435761u + 7u;
+                for (int r = 0; r < 9; r++)
+                    for (int gg = 0; gg < 9; gg++)
+                        for (int b = 0; b < 9; b++) {
+                            const float idv[3] = {r / 8.0f, gg / 8.0f, b / 8.0f};
+                            for (int c = 0; c < 3; c++) {
+                                s = s * 1664525u + 1013904223u;
+                                cube.data.push_back(idv[c] + ((float)(s >> 8) / 16777216.0f - 0.5f) * 0.2f);
+                            }
+                        }
+                auto q = frame(w, h, bd, seed++, 3);
+                auto ref3 = widen(q, bd);
+                auto st3 = lut::process_lut_cuda(q.data(), out.data(), w, h, 3, bd, cube);
+                or_lut3d(ref3.data(), w, h, bd, cube.data.data(), cube.size);
+                report("lut CUSTOM_3D", w, h, bd, st3 == lut::LUTError::Ok && widen(out, bd) == ref3);
             }
             // demosaic
             {

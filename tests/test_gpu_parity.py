@@ -71,6 +71,31 @@ def test_bitstream_packed_matches_oracle(isp, w, h, bd):
     assert np.array_equal(d_out.cpu().numpy(), got.view(np.uint8).reshape(-1))
 
 
+@pytest.mark.parametrize("w,h,bd,dm,size", [(67, 35, 10, abi.HQLI, 17), (268, 80, 12, abi.AMAZE, 33),
+                                              (131, 70, 8, abi.MG, 5), (301, 77, 16, abi.AMAZE, 2)])
+def test_lut3d_stage_matches_oracle(isp, w, h, bd, dm, size):
+    """The optional 3D LUT after the CCM (lut::apply_lut): fused, plain and batched paths."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(7 * size + bd)
+    pl = random_pipeline(rng, w, h, bd, False, dm, int(rng.integers(0, 4)))
+    pl.stages |= abi.STAGE_LUT3D
+    pl.lut3d = rng.uniform(-0.1, 1.1, (size, size, size, 3)).astype(np.float32)
+    raw = random_frame(rng, pl)
+    ref, _ = O.pipeline(pl, raw)
+    isp.set_params(pl)
+    got = isp.run_host(raw)
+    assert max_abs(got, ref) == 0, f"psnr {psnr(got, ref):.2f}"
+    d_in = torch.from_numpy(raw).cuda()
+    d_out = torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+    isp.run_device_plain(d_in, d_out)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy(), got.view(np.uint8).reshape(-1))
+    d_out.zero_()
+    isp.batch_submit([(pl, d_in, d_out)])
+    isp.sync_status()
+    assert np.array_equal(d_out.cpu().numpy(), got.view(np.uint8).reshape(-1))
+
+
 @pytest.mark.parametrize("w,h,bd,packed,dm,pat,seed", _cases(21, 2))
 def test_stage_dumps_match_oracle(isp, w, h, bd, packed, dm, pat, seed):
     rng = np.random.default_rng(seed)

@@ -92,3 +92,22 @@ def test_packed_unpack_matches_reference(bd):
         for y in range(h):
             for x in range(w):
                 assert O.get_packed_raw(buf, x, y, w, h, bd) == R.ref_get_packed_raw(buf.ctypes.data_as(U8P), x, y, w, h, bd)
+
+
+@pytest.mark.parametrize("bd", [8, 10, 12, 16])
+@pytest.mark.parametrize("size", [2, 5, 17, 33])
+def test_lut3d_matches_reference(bd, size):
+    """a11: the oracle's 3D LUT stage against lut::apply_lut (trilinear), random cubes."""
+    R = O.ref()
+    L = O.stages()
+    rng = np.random.default_rng(31 * size + bd)
+    w, h = 37, 11
+    mv = (1 << bd) - 1
+    rgb = rng.integers(0, mv + 1, (h, w, 3)).astype(np.uint16)
+    rgb[0, 0] = (0, 0, 0)
+    rgb[0, 1] = (mv, mv, mv)
+    lut = rng.uniform(-0.1, 1.1, (size, size, size, 3)).astype(np.float32)
+    a, b = rgb.copy(), rgb.copy()
+    L.or_lut3d(P(a), w, h, bd, P(lut, F32P), size)
+    assert R.ref_apply_lut(P(b), w, h, bd, P(lut, F32P), size) == 0
+    assert np.array_equal(a, b)
