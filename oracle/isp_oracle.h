@@ -89,6 +89,13 @@ int or_adj_loss_grad(const ImopAdjointDesc* d, const double* theta, const uint8_
 int or_adj_loss(const ImopAdjointDesc* d, const double* theta, const uint8_t* raw, const float* ref, int mode,
                 double* loss);
 
+/* Baseline JPEG encoder (isp_oracle_jpeg.c): the reference's process_encode_baseline byte for byte.
+ * RGB8 interleaved input; returns 0 or the reference's JpegError value; *out_size in = capacity
+ * (0: w*h*9 + 65536), out = bytes written. */
+int or_jpeg_encode(const uint8_t* in, int w, int h, int bd, int quality, int subsample, uint8_t* out,
+                   size_t* out_size);
+void or_jpeg_scale_qtable(int q[64], const int base[64], int quality);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,7 +85,49 @@ def ref():
         _ref.ref_guess_pattern.argtypes = [U8P, i, i, i, i]
         _ref.ref_solve_ccm.argtypes = [F32P, F32P, i, i, F32P, IP, IP]
         _ref.ref_apply_lut.argtypes = [U16P, i, i, i, F32P, i]
+        SP = C.POINTER(C.c_size_t)
+        _ref.ref_jpeg_encode.argtypes = [U8P, i, i, i, i, i, U8P, SP]
+        _ref.ref_jpeg_decode.argtypes = [U8P, C.c_size_t, U8P, IP, IP, IP]
     return _ref
+
+
+def jpeg_max_bytes(w, h):
+    """The reference's default output capacity (get_max_jpeg_size)."""
+    return w * h * 9 + 65536
+
+
+def _jpeg_call(fn, rgb, quality, subsample, cap, bd):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    h, w = rgb.shape[:2]
+    out = np.zeros(max(cap or jpeg_max_bytes(w, h), 1), np.uint8)
+    n = C.c_size_t(cap)
+    st = fn(rgb.ctypes.data_as(U8P), w, h, bd, quality, subsample, out.ctypes.data_as(U8P), C.byref(n))
+    return st, out[: n.value].copy() if st == 0 else None
+
+
+def ref_jpeg_encode(rgb, quality=90, subsample=1, cap=0, bd=8):
+    """(status, bytes) of the reference's process_encode_baseline on an (h, w, 3) u8 frame."""
+    return _jpeg_call(ref().ref_jpeg_encode, rgb, quality, subsample, cap, bd)
+
+
+def ref_jpeg_decode(data):
+    """(status, (h, w, 3) u8) of the reference's process_decode_baseline."""
+    data = np.ascontiguousarray(data, np.uint8)
+    w, h, c = C.c_int(0), C.c_int(0), C.c_int(0)
+    # the decoder needs the frame size up front: read it from SOF0 (FF C0, len, prec, h, w)
+    k = bytes(data).find(b"\xff\xc0")
+    hh, ww = (int(data[k + 5]) << 8 | int(data[k + 6]), int(data[k + 7]) << 8 | int(data[k + 8])) if k >= 0 else (1, 1)
+    out = np.zeros((hh, ww, 3), np.uint8)
+    st = ref().ref_jpeg_decode(data.ctypes.data_as(U8P), data.size, out.ctypes.data_as(U8P), C.byref(w), C.byref(h),
+                               C.byref(c))
+    return st, out
+
+
+def jpeg_encode(rgb, quality=90, subsample=1, cap=0, bd=8):
+    """(status, bytes) of the oracle's restatement of process_encode_baseline."""
+    L = lib()
+    L.or_jpeg_encode.argtypes = [U8P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, U8P, C.POINTER(C.c_size_t)]
+    return _jpeg_call(L.or_jpeg_encode, rgb, quality, subsample, cap, bd)
 
 
 # ---- oracle ---------------------------------------------------------------------------------

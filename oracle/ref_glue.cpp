@@ -25,6 +25,7 @@
 #include "imop/analyzer.hpp"
 #include "color_calibration/algorithms.hpp"
 #include "lut/algorithms.hpp"
+#include "jpeg_codec/algorithms.hpp"
 #include "imop/pixel_utils.hpp"
 #include "lens_shading/algorithms.hpp"
 #include "white_balance/algorithms.hpp"
@@ -270,6 +271,19 @@ int ref_apply_lut(uint16_t* rgb, int w, int h, int bd, const float* lut, int siz
     const int e = (int)lut::apply_lut(L, in.data(), out.data(), w, h, bd);
     if (e == 0) from_store(out, rgb, n, bd);
     return e;
+}
+
+// jpeg_codec::process_encode_baseline / process_decode_baseline (src/jpeg_codec/encode_baseline.cpp,
+// decode_baseline.cpp); *size in = capacity (0: the reference's default), out = bytes written
+int ref_jpeg_encode(const uint8_t* rgb, int w, int h, int bd, int quality, int subsample, uint8_t* out,
+                    size_t* size) {
+    jpeg_codec::JpegParams p;
+    p.quality = quality;
+    p.chroma_subsample = subsample;
+    return (int)jpeg_codec::process_encode_baseline(rgb, out, size, w, h, 3, bd, p);
+}
+int ref_jpeg_decode(const uint8_t* jpg, size_t n, uint8_t* rgb, int* w, int* h, int* c) {
+    return (int)jpeg_codec::process_decode_baseline(jpg, n, rgb, w, h, c);
 }
 
 }  // extern "C"
