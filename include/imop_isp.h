@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define IMOP_ISP_ABI_VERSION 2
+#define IMOP_ISP_ABI_VERSION 3
 
 /* ---- status codes (0..6 == imop::DemosaicError) ---------------------------------- */
 enum {
@@ -359,6 +359,54 @@ typedef struct {
 } ImopSolvedMatrix;
 int imop_solve_ccm(const ImopPatchColor* measured, const ImopPatchColor* reference, int n, int type,
                    ImopSolvedMatrix* out);
+
+/* ---- baseline JPEG encode of RGB8 frames (device) ------------------------------------- */
+/* Byte for byte the output of jpeg_codec::process_encode_baseline (src/jpeg_codec/
+ * encode_baseline.cpp:222-376): JFIF 1.02 header, standard Annex K quantiser scaled by quality and
+ * Huffman tables, 4:4:4 / 4:2:0 / 4:2:2 (subsample 0 / 1 / 2, clamped), the reference's float
+ * colour conversion, DCT and quantisation, and its run-length coding.  Replaces
+ * jpeg_codec::process_encode_cuda (src/jpeg_codec/cuda_dispatch.cpp:121-240) and, on a CUDA host,
+ * process_encode_baseline.  Status codes of these entry points are jpeg_codec::JpegError
+ * (include/jpeg_codec/types.hpp:15-29), checked in the reference's order. */
+enum {
+    IMOP_JPEG_OK = 0,
+    IMOP_JPEG_NULL_INPUT = 1,
+    IMOP_JPEG_NULL_OUTPUT = 2,
+    IMOP_JPEG_INVALID_DIMENSIONS = 3,
+    IMOP_JPEG_INVALID_BIT_DEPTH = 4, /* only 8 */
+    IMOP_JPEG_INVALID_CHANNELS = 5,
+    IMOP_JPEG_INVALID_QUALITY = 6,   /* 1..100 */
+    IMOP_JPEG_IMAGE_TOO_SMALL = 7,   /* below 8x8 */
+    IMOP_JPEG_ENCODE_FAILED = 8,
+    IMOP_JPEG_DECODE_FAILED = 9,
+    IMOP_JPEG_INVALID_DATA = 10,
+    IMOP_JPEG_CUDA_NOT_AVAILABLE = 11,
+    IMOP_JPEG_INTERNAL_ERROR = 12
+};
+typedef struct imop_jpeg_ctx* imop_jpeg_t;
+/* A context owns the device scratch of one encode at a time (grown on demand) and a stream for
+ * the host entry point; it serves the device that was current when it was created.  Calls on
+ * one context are ordered: do not run it on two streams at once. */
+int imop_jpeg_create(imop_jpeg_t* out_ctx);
+int imop_jpeg_destroy(imop_jpeg_t ctx);
+/* jpeg_codec::get_max_jpeg_size (src/jpeg_codec/dispatch.cpp:35-41): w*h*9 + 65536 */
+size_t imop_jpeg_max_bytes(int width, int height);
+/* The header (SOI .. SOS) of an encode; copies up to cap bytes to out (when non-NULL) and
+ * returns its full length. */
+int imop_jpeg_header(int width, int height, int quality, int subsample, uint8_t* out, size_t cap);
+/* Host RGB8 (h x w x 3, interleaved) in, JPEG bytes out.  *out_size: capacity on entry (0: the
+ * default capacity), bytes written on return (min(JPEG size, capacity); the bytes past the
+ * capacity are dropped, as the reference's writer drops them). */
+int imop_jpeg_encode_host(imop_jpeg_t ctx, const uint8_t* rgb, int width, int height, int bit_depth, int quality,
+                          int subsample, uint8_t* out, size_t* out_size);
+/* Device RGB8 in, the whole JPEG written to device memory d_out[0 .. min(size, out_cap)) on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) without a host synchronisation.
+ * d_out_size (device pointer, may be NULL) receives the bytes written when the stream reaches
+ * it; imop_jpeg_last_size reads the sizes on the host (synchronising the stream). */
+int imop_jpeg_encode_device(imop_jpeg_t ctx, const void* d_rgb, int width, int height, int bit_depth, int quality,
+                            int subsample, void* d_out, size_t out_cap, size_t* d_out_size, void* stream);
+int imop_jpeg_last_size(imop_jpeg_t ctx, size_t* jpeg_bytes, size_t* written);
+const char* imop_jpeg_last_error_string(void);
 
 /* ---- misc --------------------------------------------------------------------------- */
 const char* imop_last_error_string(void);

@@ -12,7 +12,11 @@ sources by oracle/Makefile into oracle/_ref/libimop_ref.so (called through oracl
                    white balance, CCM), SHA-256 of every stage output;
   real_strips.npz  the first 24 rows of each 1006x758 capture in the reference's test_data
                    (RG8, RG10, RG12, RG10 packed, RG12 packed) and the SHA-256 of
-                   imop::demosaic_cpu's output on each (HQLI, MG, AMAZE), unpack included.
+                   imop::demosaic_cpu's output on each (HQLI, MG, AMAZE), unpack included;
+  jpeg.npz         RGB8 frames and the exact bytes of jpeg_codec::process_encode_baseline on them:
+                   the images of the reference's tests/unit/test_jpeg_codec.cpp (file:line per
+                   case), seeded frames over every subsampling and a range of qualities and sizes,
+                   capacity truncation, and the status of each invalid argument.
 
 The inputs are stored in the fixtures, so the tests need neither the reference tree nor the
 product library to check the oracle.
@@ -201,12 +205,85 @@ def real_strips(R):
     return out
 
 
+def jpeg_image(kind, w, h, seed=0, colour=(0, 0, 0)):
+    """the reference test's image makers (tests/unit/test_jpeg_codec.cpp:11-38) and seeded ones"""
+    if kind == "flat":
+        return np.broadcast_to(np.array(colour, np.uint8), (h, w, 3)).copy()
+    if kind == "gradient":
+        y, x = np.mgrid[0:h, 0:w]
+        return np.stack([(x * 255) // (w - 1), (y * 255) // (h - 1), np.full_like(x, 128)], -1).astype(np.uint8)
+    if kind == "pattern":
+        return ((np.arange(w * h * 3, dtype=np.int64) * 37 + 127) % 256).astype(np.uint8).reshape(h, w, 3)
+    rng = np.random.default_rng(seed)
+    if kind == "noise":
+        return rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    # smooth scene: sinusoids, edges and mild noise
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    f = rng.uniform(0.02, 0.2, 3)
+    base = np.stack([128 + 100 * np.sin(f[c] * x + (c + 1) * 0.7 * np.cos(f[2 - c] * y)) for c in range(3)], -1)
+    base += np.where((x // 13 + y // 11) % 2 == 0, 30.0, -30.0)[..., None]
+    base += rng.normal(0, 4, base.shape)
+    return np.clip(base, 0, 255).astype(np.uint8)
+
+
+def jpeg_cases(R):
+    """(name, image, quality, subsample, cap, cite) per case"""
+    T = "tests/unit/test_jpeg_codec.cpp"
+    pat32 = jpeg_image("pattern", 32, 32)
+    cases = [
+        ("flat_roundtrip", jpeg_image("flat", 32, 32, colour=(80, 120, 200)), 90, 1, 0, f"{T}:283-316"),
+        ("flat_compresses", jpeg_image("flat", 64, 64, colour=(128, 128, 128)), 90, 1, 0, f"{T}:191-209"),
+        ("quality_q10", pat32, 10, 1, 0, f"{T}:211-260"),
+        ("quality_q50", pat32, 50, 1, 0, f"{T}:211-260"),
+        ("quality_q95", pat32, 95, 1, 0, f"{T}:211-260"),
+        ("non_multiple_37x29", jpeg_image("pattern", 37, 29), 90, 1, 0, f"{T}:262-281"),
+        ("gradient_48", jpeg_image("gradient", 48, 48), 95, 1, 0, f"{T}:318-350"),
+        ("small_16", jpeg_image("pattern", 16, 16), 90, 1, 0, f"{T}:352-376"),
+        ("odd_33x27", jpeg_image("pattern", 33, 27), 90, 1, 0, f"{T}:378-405"),
+    ]
+    k = 0
+    for (w, h) in ((8, 8), (9, 8), (8, 15), (61, 47), (96, 64), (120, 40)):
+        for ss in (0, 1, 2):
+            for kind in (("scene", "noise") if w * h <= 61 * 47 else ("scene", "pattern")):
+                q = (1, 25, 50, 75, 90, 100)[k % 6]
+                cases.append((f"seed{k}_{kind}_{w}x{h}_q{q}_ss{ss}", jpeg_image(kind, w, h, seed=k), q, ss, 0, "seeded"))
+                k += 1
+    sc = jpeg_image("scene", 64, 48, seed=99)
+    for cap in (1, 300, 700, 2000):
+        cases.append((f"truncated_cap{cap}", sc, 80, 1, cap, "capacity"))
+    cases.append(("subsample_clamp_hi", sc, 80, 7, 0, "clamped to 2"))
+    cases.append(("subsample_clamp_lo", sc, 80, -4, 0, "clamped to 0"))
+    out, meta, stored = {}, [], {}
+    for i, (name, img, q, ss, cap, cite) in enumerate(cases):
+        st, data = O.ref_jpeg_encode(img, q, ss, cap)
+        assert st == 0, (name, st)
+        key = id(img)
+        if key not in stored:  # frames shared by several cases are stored once
+            stored[key] = len(stored)
+            out[f"img{stored[key]}"] = img
+        out[f"jpg{i}"] = data
+        meta.append({"name": name, "image": stored[key], "quality": q, "subsample": ss, "cap": cap, "cite": cite})
+    # invalid arguments: (w, h, bit depth, quality, null input, null output) -> status
+    errs = []
+    z = np.zeros((8, 8, 3), np.uint8)
+    for (w, h, bd, q, nin, nout) in ((8, 8, 8, 90, 1, 0), (8, 8, 8, 90, 0, 1), (0, 8, 8, 90, 0, 0), (8, -1, 8, 90, 0, 0),
+                                     (8, 8, 16, 90, 0, 0), (8, 8, 7, 90, 0, 0), (4, 4, 8, 90, 0, 0), (7, 8, 8, 90, 0, 0),
+                                     (8, 8, 8, 0, 0, 0), (8, 8, 8, 101, 0, 0), (4, 4, 16, 0, 1, 1), (8, 8, 8, 0, 0, 1)):
+        buf = np.zeros(1 << 16, np.uint8)
+        n = C.c_size_t(0)
+        st = R.ref_jpeg_encode(None if nin else P(z, U8P), w, h, bd, q, 1, None if nout else P(buf, U8P), C.byref(n))
+        errs.append({"w": w, "h": h, "bd": bd, "quality": q, "null_in": nin, "null_out": nout, "status": int(st)})
+    out["meta"] = np.frombuffer(json.dumps({"cases": meta, "errors": errs}).encode(), np.uint8)
+    return out
+
+
 def main():
     R = O.ref()
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump(kat_cases(R), f)
     np.savez_compressed(os.path.join(HERE, "chains.npz"), **chain_cases(R))
     np.savez_compressed(os.path.join(HERE, "real_strips.npz"), **real_strips(R))
+    np.savez_compressed(os.path.join(HERE, "jpeg.npz"), **jpeg_cases(R))
     print("golden fixtures written to", HERE)
 
 

@@ -1,0 +1,140 @@
+"""GPU parity of the baseline JPEG encoder: byte-identical to the reference's encoder (golden bytes
+of jpeg_codec::process_encode_baseline) and to the oracle on full-size frames, through the host
+and the device entry points, with the reference's status codes and capacity truncation."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import imop_gb300 as I
+from imop_gb300 import jpeg as J
+from imop_gb300 import workloads
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "jpeg.npz")
+
+
+def golden():
+    z = np.load(GOLD)
+    meta = json.loads(bytes(z["meta"]))
+    return [(c, z[f"img{c['image']}"], z[f"jpg{i}"]) for i, c in enumerate(meta["cases"])], meta["errors"]
+
+
+CASES, ERRORS = golden()
+
+
+@pytest.fixture(scope="module")
+def enc():
+    e = J.JpegEncoder()
+    yield e
+    e.close()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0]["name"] for c in CASES])
+def test_host_matches_golden(enc, case):
+    c, img, want = case
+    got = enc.encode(img, c["quality"], c["subsample"], c["cap"])
+    assert got.size == want.size and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("e", ERRORS, ids=[f"{e['w']}x{e['h']}_bd{e['bd']}_q{e['quality']}_{e['null_in']}{e['null_out']}"
+                                           for e in ERRORS])
+def test_status_codes_match_golden(enc, e):
+    img = None if e["null_in"] else np.zeros((8, 8, 3), np.uint8)
+    if e["null_out"]:
+        import ctypes as C
+        n = C.c_size_t(0)
+        st = J._L().imop_jpeg_encode_host(enc.h, None if img is None else img.ctypes.data, e["w"], e["h"], e["bd"],
+                                          e["quality"], 1, None, C.byref(n))
+    else:
+        st, _ = enc.encode_status(img, e["quality"], 1, bit_depth=e["bd"], width=e["w"], height=e["h"])
+    assert st == e["status"]
+
+
+def _frame(w, h, seed):
+    """an ISP-like RGB8 frame: the oracle's output of a seeded raw scene"""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float32)
+    f = rng.uniform(0.005, 0.05, 3).astype(np.float32)
+    img = np.stack([127 + 110 * np.sin(f[c] * x + 0.8 * np.cos(f[2 - c] * y + c)) for c in range(3)], -1)
+    img += rng.normal(0, 6, img.shape).astype(np.float32)
+    return np.clip(img, 0, 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("w,h", [(1006, 758), (4024, 3032), (1921, 1081)])
+@pytest.mark.parametrize("ss", [0, 1, 2])
+def test_full_size_matches_oracle(enc, w, h, ss):
+    img = _frame(w, h, w + ss)
+    q = (90, 75, 98)[ss]
+    st, want = O.jpeg_encode(img, q, ss)
+    assert st == 0
+    got = enc.encode(img, q, ss)
+    assert got.size == want.size and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("q", [1, 5, 30, 50, 51, 99, 100])
+def test_noise_every_quality_matches_oracle(enc, q):
+    """high-entropy input: long codes, 0xFF bytes to stuff, ZRL runs at low quality"""
+    rng = np.random.default_rng(q)
+    img = rng.integers(0, 256, (517, 389, 3), dtype=np.uint8)
+    st, want = O.jpeg_encode(img, q, q % 3)
+    got = enc.encode(img, q, q % 3)
+    assert np.array_equal(got, want)
+
+
+def test_device_entry_point_and_reuse(enc):
+    """device in / device out on a side stream, sizes on the device, truncation, and scratch
+    reuse across frames of changing sizes (the cleared word stream)"""
+    import torch
+    dev = torch.device("cuda:0")
+    s = torch.cuda.Stream()
+    frames = [(_frame(640, 480, 1), 90, 1), (_frame(33, 27, 2), 50, 0), (_frame(1500, 900, 3), 95, 2),
+              (_frame(640, 480, 1), 90, 1)]
+    for img, q, ss in frames:
+        h, w = img.shape[:2]
+        st, want = O.jpeg_encode(img, q, ss)
+        d_in = torch.from_numpy(img).to(dev)
+        cap = J.max_bytes(w, h)
+        d_out = torch.zeros(cap, dtype=torch.uint8, device=dev)
+        d_size = torch.zeros(1, dtype=torch.int64, device=dev)
+        torch.cuda.current_stream().synchronize()
+        with torch.cuda.stream(s):
+            enc.encode_device(d_in, w, h, d_out, cap, q, ss, d_size=d_size, stream=s.cuda_stream)
+        total, written = enc.last_size()
+        s.synchronize()
+        assert total == written == want.size == int(d_size.item())
+        assert np.array_equal(d_out[:written].cpu().numpy(), want)
+    # truncation on the device: the first cap bytes, size = cap
+    img, q, ss = frames[0]
+    st, want = O.jpeg_encode(img, q, ss)
+    for cap in (10, 623, 624, 5000):
+        d_in = torch.from_numpy(img).to(dev)
+        d_out = torch.full((cap + 64,), 0xAB, dtype=torch.uint8, device=dev)
+        enc.encode_device(d_in, img.shape[1], img.shape[0], d_out, cap, q, ss)
+        total, written = enc.last_size()
+        assert total == want.size and written == cap
+        out = d_out.cpu().numpy()
+        assert np.array_equal(out[:cap], want[:cap]) and np.all(out[cap:] == 0xAB)
+
+
+def test_isp_to_jpeg_on_device(enc):
+    """the fused ISP's RGB8 output encoded where it lies: RAW -> JPEG without a host round trip"""
+    import torch
+    pl = workloads.c2_pipeline(1006, 758)
+    raw = workloads.c2_frame(pl, 0)
+    rgb_ref, _ = O.pipeline(pl, raw)
+    st, want = O.jpeg_encode(rgb_ref.reshape(758, 1006, 3), 90, 1)
+    isp = I.Isp(pl)
+    d_raw = torch.from_numpy(np.ascontiguousarray(raw)).cuda()
+    d_rgb = torch.empty((758, 1006, 3), dtype=torch.uint8, device="cuda")
+    cap = J.max_bytes(1006, 758)
+    d_out = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    isp.run_device(d_raw, d_rgb, stream)
+    enc.encode_device(d_rgb, 1006, 758, d_out, cap, 90, 1, stream=stream)
+    total, written = enc.last_size()
+    isp.close()
+    assert written == want.size and np.array_equal(d_out[:written].cpu().numpy(), want)
