@@ -3,9 +3,10 @@
 // Exactness: every float operation of the reference's encoder is one explicitly rounded IEEE
 // operation here, in the reference's order (colour conversion common.hpp:196-201, DCT
 // common.hpp:104-151 with the cosine factors the host evaluates with the same cosf, quantiser
-// division and std::round encode_baseline.cpp:24-26).  The coefficient array is the reference's
-// zz[kZigzag[i]] = round(block[i] / q[i]) (common.hpp:84-93), and the run-length / Huffman rules
-// are those of encode_baseline.cpp:28-101, restated per 8-coefficient lane:
+// division and std::round encode_baseline.cpp:24-26; the division as a correctly rounded
+// reciprocal product with one residual correction, equal to IEEE division).  The coefficient
+// array is the reference's zz[kZigzag[i]] = round(block[i] / q[i]) (common.hpp:84-93), and the
+// run-length / Huffman rules are those of encode_baseline.cpp:28-101, restated per slot:
 //   - a non-zero AC coefficient at p whose previous non-zero AC (or the DC slot) is at p' codes
 //     floor((p - p' - 1) / 16) ZRL symbols, then symbol (((p - p' - 1) mod 16) << 4) | cat with
 //     its cat value bits, or nothing at all when that symbol is absent from the table;
@@ -15,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "isp_device.cuh"
 #include "isp_jpeg.h"
 
 namespace imop {
@@ -120,71 +122,50 @@ __device__ __forceinline__ uint64_t block_mask(const Lane8& l, int r) {
     return m;
 }
 
-// Walks the AC codes of lane r's slots [8r, 8r + 8) in order; emit(bits, len) receives each
-// code with its value bits appended.  Returns the bits of the lane (EOB included when the lane
-// holds the last non-zero coefficient, or is lane 0 of a block without any).
-template <bool kEmit, class Emit>
-__device__ __forceinline__ int lane_ac(const Lane8& l, int r, uint64_t mask, const uint32_t* ac, Emit&& emit) {
-    const uint32_t zrl = ac[0xF0], eob = ac[0x00];
+// OR len (<= 26) bits MSB-first at bit position pos of a shared word buffer
+__device__ __forceinline__ void smem_put(uint32_t* buf, int pos, uint32_t bits, int len) {
+    const int w = pos >> 5, end = (pos & 31) + len;
+    if (end <= 32) {
+        atomicOr(buf + w, bits << (32 - end));
+    } else {
+        atomicOr(buf + w, bits >> (end - 32));
+        atomicOr(buf + w + 1, bits << (64 - end));
+    }
+}
+
+// The AC codes of lane r's slots [8r, 8r + 8): per slot the ZRL count (bits 8..15 of cl) and the
+// symbol code with its value bits appended (cw, length in bits 0..7 of cl; 0 when the symbol is
+// absent from the table).  Returns the lane's bits, EOB included when the lane holds the last
+// non-zero coefficient (lane 0 of a block without any).
+struct LaneCodes {
+    uint32_t cw[8];
+    int cl[8];
+    bool eob;
+};
+
+__device__ __forceinline__ int lane_codes(const Lane8& l, int r, uint64_t mask, const uint32_t* ac, LaneCodes& c) {
+    const int zrl = (int)(ac[0xF0] >> 16), eob = (int)(ac[0x00] >> 16);
     int bits = 0;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
+        c.cw[j] = 0u;
+        c.cl[j] = 0;
         const int p = 8 * r + j;
         if (!((mask >> p) & 1)) continue;
         const uint64_t below = mask & ((1ull << p) - 1);
         const int prev = below ? 63 - __clzll((long long)below) : 0;
-        const int run = p - prev - 1;
-        const int v = l.z[j], cat = category(v);
+        const int run = p - prev - 1, v = l.z[j], cat = category(v);
         const uint32_t e = ac[((run & 15) << 4) | cat];
-        const int size = (int)(e >> 16);
-        bits += (run >> 4) * (int)(zrl >> 16) + (size ? size + cat : 0);
-        if (kEmit) {
-            for (int k = 0; k < (run >> 4); k++) emit(zrl & 0xFFFFu, (int)(zrl >> 16));
-            if (size) emit(((e & 0xFFFFu) << cat) | value_bits(v, cat), size + cat);
-        }
+        const int size = (int)(e >> 16), len = size ? size + cat : 0;
+        c.cw[j] = size ? ((e & 0xFFFFu) << cat) | value_bits(v, cat) : 0u;
+        c.cl[j] = ((run >> 4) << 8) | len;
+        bits += (run >> 4) * zrl + len;
     }
     const int last = mask ? 63 - __clzll((long long)mask) : 0;
-    if ((last >> 3) == r) {
-        bits += (int)(eob >> 16);
-        if (kEmit) emit(eob & 0xFFFFu, (int)(eob >> 16));
-    }
+    c.eob = (last >> 3) == r;
+    if (c.eob) bits += eob;
     return bits;
 }
-
-// MSB-first writer into the zeroed big-endian word stream from an absolute bit position.  Only
-// the first and the last word of a lane's span can hold other lanes' bits: those two are ORed
-// atomically, the words in between belong to the lane alone and are stored.
-struct BitSink {
-    uint32_t* w;
-    unsigned long long idx;
-    uint64_t acc;
-    int n;
-    bool first;
-    __device__ BitSink(uint32_t* words, unsigned long long start)
-        : w(words), idx(start >> 5), acc(0), n((int)(start & 31)), first(true) {}
-    __device__ __forceinline__ void operator()(uint32_t bits, int len) {
-        acc = (acc << len) | bits;
-        n += len;
-        if (n >= 32) {
-            n -= 32;
-            const uint32_t word = (uint32_t)(acc >> n);
-            if (first)
-                atomicOr(w + idx, word);
-            else
-                w[idx] = word;
-            first = false;
-            idx++;
-            acc &= (1ull << n) - 1;
-        }
-    }
-    __device__ __forceinline__ void finish() {
-        if (n > 0) atomicOr(w + idx, (uint32_t)(acc << (32 - n)));
-    }
-};
-
-struct NoEmit {
-    __device__ void operator()(uint32_t, int) const {}
-};
 
 // exclusive scan over the CTA; warp_sums holds NT / 32 entries
 template <int NT, class T>
@@ -210,32 +191,52 @@ __device__ __forceinline__ T cta_excl_scan(T v, T* warp_sums, T& total) {
     return pre + incl - v;
 }
 
-// one CTA of 1024 threads: out[i] = sum(in[0..i)), returns the total
+// one CTA of NT threads: out[i] = sum(in[0..i)), returns the total (in[] read past L1: other
+// CTAs wrote it)
+template <int NT>
 __device__ unsigned long long cta_scan_array(const int* in, unsigned long long* out, long long n) {
-    __shared__ unsigned long long ws[32];
+    __shared__ unsigned long long ws[NT / 32];
     unsigned long long carry = 0;
-    for (long long base = 0; base < n; base += 1024) {
+    for (long long base = 0; base < n; base += NT) {
         const long long i = base + threadIdx.x;
-        const unsigned long long v = i < n ? (unsigned long long)in[i] : 0ull;
+        const unsigned long long v = i < n ? (unsigned long long)__ldcg(in + i) : 0ull;
         unsigned long long tot;
-        const unsigned long long ex = cta_excl_scan<1024>(v, ws, tot);
+        const unsigned long long ex = cta_excl_scan<NT>(v, ws, tot);
         if (i < n) out[i] = carry + ex;
         carry += tot;
     }
     return carry;
 }
 
+// True in the CTA that finishes last (all CTAs' earlier global writes visible to it), which also
+// rewinds the counter for the next launch on the stream.  No CTA waits for another.
+__device__ __forceinline__ bool last_cta(unsigned* counter) {
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned done = atomicAdd(counter, 1u);
+        last = done == gridDim.x - 1;
+        if (last) *counter = 0u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last != 0;
+}
+
 // ---- transform: 8 threads per block; thread r owns sample row r, then coefficient column r ---
 __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) {
     __shared__ __align__(16) float T[kJpegBlocksPerCta][72];  // row-DCT output, [u * 8 + y]
     __shared__ __align__(16) int16_t Z[kJpegBlocksPerCta][64];
-    __shared__ float sq[2][64];
+    __shared__ uint32_t SB[kJpegBlocksPerCta][kJpegAcWords];  // each block's AC code, from bit 0
+    __shared__ float sq[2][64], srq[2][64];
     __shared__ uint8_t szz[64];
     __shared__ uint32_t sac[2][256];
     const int t = threadIdx.x;
-    if (t < 128) sq[t >> 6][t & 63] = L.q[t >> 6][t & 63];
+    if (t < 128) sq[t >> 6][t & 63] = L.q[t >> 6][t & 63], srq[t >> 6][t & 63] = L.rq[t >> 6][t & 63];
     if (t < 64) szz[t] = c_zz[t];
     for (int i = t; i < 512; i += kThreads) sac[i >> 8][i & 255] = L.huff->ac[i >> 8][i & 255];
+    for (int i = t; i < kJpegBlocksPerCta * kJpegAcWords; i += kThreads) (&SB[0][0])[i] = 0u;
 
     const int lb = t >> 3, r = t & 7;
     const long long bl = (long long)blockIdx.x * kJpegBlocksPerCta + lb;
@@ -246,26 +247,37 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
     if (live) P = block_pos(L.g, b);
 
     // sample row r -> row DCT, written transposed
-    float x[8];
+    int xi[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) xi[i] = 0;
     if (live) {
         const int py = min(P.y0 + r * P.sy, L.g.h - 1);
-        const uint8_t* row = L.rgb + (size_t)py * (size_t)L.g.w * 3;
+        const uint8_t* row = L.rgb + ((size_t)py * (size_t)L.g.w + (size_t)P.x0) * 3;
+        if (P.x0 + 7 * P.sx < L.g.w) {  // interior: fixed offsets from one base
+            const int step = 3 * P.sx;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int px = min(P.x0 + i * P.sx, L.g.w - 1);
-            const uint8_t* s = row + (size_t)px * 3;
-            x[i] = (float)(ycc(s[0], s[1], s[2], P.comp) - 128);
+            for (int i = 0; i < 8; i++) xi[i] = ycc(row[i * step], row[i * step + 1], row[i * step + 2], P.comp) - 128;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int dx = min(P.x0 + i * P.sx, L.g.w - 1) - P.x0;
+                const uint8_t* s = row + dx * 3;
+                xi[i] = ycc(s[0], s[1], s[2], P.comp) - 128;
+            }
         }
-    } else {
-#pragma unroll
-        for (int i = 0; i < 8; i++) x[i] = 0.0f;
     }
+    float x[8];
 #pragma unroll
-    for (int u = 0; u < 8; u++) {
-        float s = 0.0f;
+    for (int i = 0; i < 8; i++) x[i] = (float)xi[i];
+    // u = 0: every factor is cosf(0) = 1, so the products are the samples and the running sums are
+    // integers of magnitude <= 1024, exact in float: the integer sum is the float sum
+    T[lb][r] = fmul(kC0, (float)(((xi[0] + xi[1]) + (xi[2] + xi[3])) + ((xi[4] + xi[5]) + (xi[6] + xi[7]))));
 #pragma unroll
-        for (int i = 0; i < 8; i++) s = fadd(s, fmul(x[i], c_cos[u * 8 + i]));
-        T[lb][u * 8 + r] = fmul(u == 0 ? kC0 : 0.5f, s);
+    for (int u = 1; u < 8; u++) {
+        float s = fmul(x[0], c_cos[u * 8]);
+#pragma unroll
+        for (int i = 1; i < 8; i++) s = fadd(s, fmul(x[i], c_cos[u * 8 + i]));
+        T[lb][u * 8 + r] = fmul(0.5f, s);
     }
     __syncthreads();
 
@@ -275,34 +287,58 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
         const float4 c1 = *reinterpret_cast<const float4*>(&T[lb][r * 8 + 4]);
         const float col[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
         const float* qt = sq[P.comp > 0 ? 1 : 0];
+        const float* rqt = srq[P.comp > 0 ? 1 : 0];
 #pragma unroll
         for (int v = 0; v < 8; v++) {
-            float s = 0.0f;
+            // the first product joins the running sum 0 exactly (a zero's sign cannot reach the
+            // rounded integer); for v = 0 the factors are 1 and the products are the inputs
+            float s = v == 0 ? col[0] : fmul(col[0], c_cos[v * 8]);
 #pragma unroll
-            for (int y = 0; y < 8; y++) s = fadd(s, fmul(col[y], c_cos[v * 8 + y]));
+            for (int y = 1; y < 8; y++) s = fadd(s, v == 0 ? col[y] : fmul(col[y], c_cos[v * 8 + y]));
             const float X = fmul(v == 0 ? kC0 : 0.5f, s);
             const int i = v * 8 + r;
-            Z[lb][szz[i]] = (int16_t)__float2int_rz(roundf(__fdiv_rn(X, qt[i])));
+            Z[lb][szz[i]] = (int16_t)__float2int_rz(roundf(dev::quotient_by(X, qt[i], rqt[i])));
         }
     }
     __syncthreads();
 
-    const uint4 raw = *reinterpret_cast<const uint4*>(&Z[lb][r * 8]);
-    const Lane8 l = unpack8(raw);
+    // AC codes: lane r codes slots [8r, 8r + 8) at its offset inside the block's code
+    const Lane8 l = unpack8(*reinterpret_cast<const uint4*>(&Z[lb][r * 8]));
     const uint64_t mask = block_mask(l, r);
-    int bits = lane_ac<false>(l, r, mask, sac[P.comp > 0 ? 1 : 0], NoEmit{});
-    bits += __shfl_xor_sync(kFull, bits, 1);
-    bits += __shfl_xor_sync(kFull, bits, 2);
-    bits += __shfl_xor_sync(kFull, bits, 4);
+    const uint32_t* ac = sac[P.comp > 0 ? 1 : 0];
+    LaneCodes c;
+    const int bits = lane_codes(l, r, mask, ac, c);
+    int incl = bits;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const int nb = __shfl_up_sync(kFull, incl, o, 8);
+        if (r >= o) incl += nb;
+    }
+    const int total = __shfl_sync(kFull, incl, 7, 8);
     if (!live) return;
-    *reinterpret_cast<uint4*>(L.coef + (size_t)b * 64 + r * 8) = raw;
+    uint32_t* sb = SB[lb];
+    int pos = incl - bits;
+    const uint32_t zrl = ac[0xF0], eob = ac[0x00];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        for (int k = 0; k < (c.cl[j] >> 8); k++, pos += (int)(zrl >> 16)) smem_put(sb, pos, zrl & 0xFFFFu, (int)(zrl >> 16));
+        const int len = c.cl[j] & 0xFF;
+        if (len) smem_put(sb, pos, c.cw[j], len), pos += len;
+    }
+    if (c.eob) smem_put(sb, pos, eob & 0xFFFFu, (int)(eob >> 16));
+    __syncwarp(kFull & (0xFFu << (threadIdx.x & 24)));
+    // the used words and one zero word after them
+    const int nw = ((total + 31) >> 5) + 1;
+    uint32_t* dst = L.acw + (size_t)b * kJpegAcWords;
+    for (int k = r; k < nw; k += 8) dst[k] = sb[k];
     if (r == 0) {
-        L.acbits[b] = bits;
+        L.acbits[b] = total;
         L.dc[b] = l.z[0];
     }
 }
 
-// ---- offsets: per-block length with the DC difference; tile-local exclusive offsets ---------
+// ---- offsets: per-block length with the DC difference, tile-local exclusive offsets; the last
+// CTA turns the tile sums into tile offsets ---------------------------------------------------
 __global__ void __launch_bounds__(kThreads) jpeg_offsets_kernel(JpegLaunch L) {
     __shared__ uint32_t sdc[2][16];
     __shared__ int ws[kThreads / 32];
@@ -331,65 +367,57 @@ __global__ void __launch_bounds__(kThreads) jpeg_offsets_kernel(JpegLaunch L) {
         off += len[j];
     }
     if (t == 0) L.tile_sum[blockIdx.x] = total;
-}
-
-// ---- tiles: one CTA scans the tile sums -------------------------------------------------------
-__global__ void __launch_bounds__(1024) jpeg_tiles_kernel(JpegLaunch L) {
-    const unsigned long long total = cta_scan_array(L.tile_sum, L.tile_off, L.g.ntiles);
-    if (threadIdx.x == 0) {
-        L.info->total_bits = total;
-        L.info->data_bytes = (total + 7) >> 3;
+    // the last CTA scans the tile sums into tile offsets and the total
+    if (!last_cta(L.counters)) return;
+    const unsigned long long bits = cta_scan_array<kThreads>(L.tile_sum, L.tile_off, L.g.ntiles);
+    if (t == 0) {
+        L.info->total_bits = bits;
+        L.info->data_bytes = (bits + 7) >> 3;
     }
 }
 
-// ---- emit: 8 threads per block write their codes at the block's offset ----------------------
-__global__ void __launch_bounds__(kThreads) jpeg_emit_kernel(JpegLaunch L) {
-    __shared__ uint32_t sac[2][256];
+// ---- place: each block's DC code and AC code at its stream offset; 8 threads per block, thread
+// r writes words r, r + 8, ... of the block's span.  The first and the last word, which the
+// neighbouring blocks share, are ORed atomically into the zeroed stream. ----------------------
+__global__ void __launch_bounds__(kThreads) jpeg_place_kernel(JpegLaunch L) {
     __shared__ uint32_t sdc[2][16];
     const int t = threadIdx.x;
-    for (int i = t; i < 512; i += kThreads) sac[i >> 8][i & 255] = L.huff->ac[i >> 8][i & 255];
     if (t < 32) sdc[t >> 4][t & 15] = L.huff->dc[t >> 4][t & 15];
     __syncthreads();
-
     const int lb = t >> 3, r = t & 7;
     const long long bl = (long long)blockIdx.x * kJpegBlocksPerCta + lb;
-    const bool live = bl < L.g.nb;
+    if (bl >= L.g.nb) return;
     const int b = (int)bl;
-    uint4 raw = make_uint4(0u, 0u, 0u, 0u);
-    BlockPos P;
-    P.comp = 0;
-    P.prev = -1;
-    if (live) {
-        raw = *reinterpret_cast<const uint4*>(L.coef + (size_t)b * 64 + r * 8);
-        P = block_pos(L.g, b);
+    const BlockPos P = block_pos(L.g, b);
+    const int diff = L.dc[b] - (P.prev >= 0 ? L.dc[P.prev] : 0);
+    const int cat = category(diff);
+    const uint32_t e = sdc[P.comp > 0 ? 1 : 0][min(cat, 15)];
+    const int dlen = (int)(e >> 16) + cat;
+    const uint32_t dcode = ((e & 0xFFFFu) << cat) | value_bits(diff, cat);
+    const unsigned long long start = L.tile_off[b / kJpegTileBlocks] + (unsigned long long)L.blk_off[b];
+    // the span as a virtual stream: (start mod 32) zero bits, the DC code, the AC code
+    const int pre = (int)(start & 31) + dlen;  // 2 .. 53
+    const int end = pre + L.acbits[b];
+    const int nw = (end + 31) >> 5;
+    const uint64_t pl = (uint64_t)dcode << (64 - pre);
+    const uint32_t* A = L.acw + (size_t)b * kJpegAcWords;
+    uint32_t* g = L.words + (start >> 5);
+    for (int k = r; k < nw; k += 8) {
+        const int lo = 32 * k;
+        uint32_t v = lo < pre ? (uint32_t)((pl << lo) >> 32) : 0u;
+        const int off = lo - pre;  // AC bit at the word's first position
+        if (off >= 0) {
+            const int j = off >> 5, s = off & 31;
+            v |= (A[j] << s) | (s ? A[j + 1] >> (32 - s) : 0u);
+        } else if (off > -32) {
+            v |= A[0] >> (-off);
+        }
+        if (end - lo < 32) v &= ~0u << (32 - (end - lo));
+        if (k == 0 || k == nw - 1)
+            atomicOr(g + k, v);
+        else
+            g[k] = v;
     }
-    const Lane8 l = unpack8(raw);
-    const uint64_t mask = block_mask(l, r);
-    const int tab = P.comp > 0 ? 1 : 0;
-    int bits = lane_ac<false>(l, r, mask, sac[tab], NoEmit{});
-    uint32_t dcode = 0;
-    int dlen = 0;
-    if (live && r == 0) {
-        const int diff = l.z[0] - (P.prev >= 0 ? L.dc[P.prev] : 0);
-        const int cat = category(diff);
-        const uint32_t e = sdc[tab][min(cat, 15)];
-        dlen = (int)(e >> 16) + cat;
-        dcode = ((e & 0xFFFFu) << cat) | value_bits(diff, cat);
-    }
-    bits += dlen;
-    int incl = bits;
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
-        const int nb = __shfl_up_sync(kFull, incl, o, 8);
-        if (r >= o) incl += nb;
-    }
-    if (!live || bits == 0) return;
-    const unsigned long long start =
-        L.tile_off[b / kJpegTileBlocks] + (unsigned long long)L.blk_off[b] + (unsigned long long)(incl - bits);
-    BitSink sink(L.words, start);
-    if (dlen) sink(dcode, dlen);
-    lane_ac<true>(l, r, mask, sac[tab], sink);
-    sink.finish();
 }
 
 // the 16 bytes of 4 big-endian words, most significant byte first
@@ -404,10 +432,12 @@ __device__ __forceinline__ int ff_count(const uint32_t w[4]) {
     return c;
 }
 
-// ---- ffcount: 0xFF bytes per 4 KB chunk (bytes past the stream are zero words) ---------------
+// ---- ffcount: 0xFF bytes per 4 KB chunk (bytes past the stream are zero words); the last CTA
+// scans the counts into chunk offsets, sets the sizes and writes the EOI marker ---------------
 __global__ void __launch_bounds__(kThreads) jpeg_ffcount_kernel(JpegLaunch L) {
     __shared__ int ws[kThreads / 32];
-    const long long nch = (long long)((L.info->data_bytes + kJpegChunkBytes - 1) / kJpegChunkBytes);
+    const unsigned long long nbytes = L.info->data_bytes;
+    const long long nch = (long long)((nbytes + kJpegChunkBytes - 1) / kJpegChunkBytes);
     for (long long c = blockIdx.x; c < nch; c += gridDim.x) {
         const uint4 v = *reinterpret_cast<const uint4*>(L.words + (size_t)c * (kJpegChunkBytes / 4) + threadIdx.x * 4);
         const uint32_t w[4] = {v.x, v.y, v.z, v.w};
@@ -415,13 +445,8 @@ __global__ void __launch_bounds__(kThreads) jpeg_ffcount_kernel(JpegLaunch L) {
         cta_excl_scan<kThreads>(ff_count(w), ws, total);
         if (threadIdx.x == 0) L.chunk_ff[c] = total;
     }
-}
-
-// ---- ffscan: chunk offsets, sizes and the EOI marker ---------------------------------------
-__global__ void __launch_bounds__(1024) jpeg_ffscan_kernel(JpegLaunch L) {
-    const unsigned long long nbytes = L.info->data_bytes;
-    const long long nch = (long long)((nbytes + kJpegChunkBytes - 1) / kJpegChunkBytes);
-    const unsigned long long nff = cta_scan_array(L.chunk_ff, L.chunk_off, nch);
+    if (!last_cta(L.counters + 1)) return;
+    const unsigned long long nff = cta_scan_array<kThreads>(L.chunk_ff, L.chunk_off, nch);
     if (threadIdx.x == 0) {
         const unsigned long long stuffed = nbytes + nff, eoi = L.base + stuffed;
         if (eoi < L.out_cap) L.out[eoi] = 0xFF;
@@ -434,31 +459,36 @@ __global__ void __launch_bounds__(1024) jpeg_ffscan_kernel(JpegLaunch L) {
     }
 }
 
-// ---- stuff: bytes out with a 0x00 after each 0xFF; the consumed words are cleared -----------
+// ---- stuff: bytes out with a 0x00 after each 0xFF, staged per chunk in shared memory so the
+// global writes are consecutive bytes per warp; the consumed words are cleared -----------------
 __global__ void __launch_bounds__(kThreads) jpeg_stuff_kernel(JpegLaunch L) {
     __shared__ int ws[kThreads / 32];
+    __shared__ uint8_t sb[2 * kJpegChunkBytes];
     const unsigned long long nbytes = L.info->data_bytes;
     const long long nch = (long long)((nbytes + kJpegChunkBytes - 1) / kJpegChunkBytes);
     for (long long c = blockIdx.x; c < nch; c += gridDim.x) {
         uint4* src = reinterpret_cast<uint4*>(L.words + (size_t)c * (kJpegChunkBytes / 4) + threadIdx.x * 4);
         const uint4 v = *src;
+        *src = make_uint4(0u, 0u, 0u, 0u);
         const uint32_t w[4] = {v.x, v.y, v.z, v.w};
         int total;
         const int before = cta_excl_scan<kThreads>(ff_count(w), ws, total);
-        const unsigned long long byte0 = (unsigned long long)c * kJpegChunkBytes + threadIdx.x * 16ull;
-        unsigned long long pos = L.base + byte0 + L.chunk_off[c] + (unsigned long long)before;
+        const unsigned long long chunk0 = (unsigned long long)c * kJpegChunkBytes;
+        const int in_chunk = (int)min((unsigned long long)kJpegChunkBytes, nbytes - chunk0);
+        int pos = threadIdx.x * 16 + before;
 #pragma unroll
         for (int k = 0; k < 16; k++) {
-            if (byte0 + k >= nbytes) break;
+            if (threadIdx.x * 16 + k >= in_chunk) break;
             const uint8_t bv = byte_of(w, k);
-            if (pos < L.out_cap) L.out[pos] = bv;
-            pos++;
-            if (bv == 0xFF) {
-                if (pos < L.out_cap) L.out[pos] = 0x00;
-                pos++;
-            }
+            sb[pos++] = bv;
+            if (bv == 0xFF) sb[pos++] = 0x00;
         }
-        *src = make_uint4(0u, 0u, 0u, 0u);
+        __syncthreads();
+        const int n = in_chunk + total;
+        const unsigned long long dst = L.base + chunk0 + L.chunk_off[c];
+        for (int k = threadIdx.x; k < n; k += kThreads)
+            if (dst + k < L.out_cap) L.out[dst + k] = sb[k];
+        __syncthreads();
     }
 }
 
@@ -494,10 +524,8 @@ cudaError_t launch_jpeg_encode(const JpegLaunch& L, cudaStream_t st) {
     const unsigned grid_chunks = (unsigned)(L.g.chunks < 152 * 8 ? L.g.chunks : 152 * 8);
     jpeg_transform_kernel<<<grid_blocks, kThreads, 0, st>>>(L);
     jpeg_offsets_kernel<<<(unsigned)L.g.ntiles, kThreads, 0, st>>>(L);
-    jpeg_tiles_kernel<<<1, 1024, 0, st>>>(L);
-    jpeg_emit_kernel<<<grid_blocks, kThreads, 0, st>>>(L);
+    jpeg_place_kernel<<<grid_blocks, kThreads, 0, st>>>(L);
     jpeg_ffcount_kernel<<<grid_chunks, kThreads, 0, st>>>(L);
-    jpeg_ffscan_kernel<<<1, 1024, 0, st>>>(L);
     jpeg_stuff_kernel<<<grid_chunks, kThreads, 0, st>>>(L);
     return cudaGetLastError();
 }

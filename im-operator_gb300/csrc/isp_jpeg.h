@@ -4,17 +4,17 @@
 // (src/jpeg_codec/encode_baseline.cpp:222-376 of the reference): the same headers, the same
 // float colour conversion and separable DCT, the same quantisation with the reference's
 // coefficient permutation, and the same Huffman / run-length coding with its quirks.  The
-// sequential bit writer is replaced by per-block bit lengths, a device prefix sum, parallel
-// emission into a zeroed 32-bit word stream, and a parallel 0xFF byte-stuffing pass.
+// sequential bit writer is replaced by per-block code strings and lengths, a device prefix sum,
+// parallel placement into a zeroed 32-bit word stream, and a parallel 0xFF byte-stuffing pass.
 //
 // Kernels (one stream, no host synchronisation between them):
-//   transform  RGB8 -> Y/Cb/Cr sample blocks -> DCT -> quantise -> int16 coefficients per block
-//              in coding order, the block's DC, and the bit length of its AC part
-//   offsets    per-block bit length with the DC difference, tile-local exclusive offsets, tile sums
-//   tiles      exclusive scan of the tile sums (one CTA) -> tile offsets, total bit count
-//   emit       each block's codes at its offset (8 threads per block, one per 8 coefficients)
-//   ffcount    0xFF bytes per 4 KB chunk of the bit stream
-//   ffscan     exclusive scan of the chunk counts (one CTA), sizes, EOI marker
+//   transform  RGB8 -> Y/Cb/Cr sample blocks -> DCT -> quantise -> the block's DC and its AC
+//              codes (ZRL / symbol / EOB) as a word-aligned bit string with its length
+//   offsets    per-block bit length with the DC difference, tile-local exclusive offsets, tile
+//              sums; the CTA that finishes last scans the tile sums -> tile offsets, total bits
+//   place      each block's DC code and AC string at its offset in the word stream
+//   ffcount    0xFF bytes per 4 KB chunk of the bit stream; the last CTA scans the counts ->
+//              chunk offsets, sizes, EOI marker
 //   stuff      bytes to the output with a 0x00 after every 0xFF; clears the words it consumed
 #pragma once
 
@@ -23,11 +23,12 @@
 
 namespace imop {
 
-constexpr int kJpegBlocksPerCta = 32;    // transform / emit: 8 threads per block, 256 threads
+constexpr int kJpegBlocksPerCta = 32;    // transform: 8 threads per block, 256 threads
 constexpr int kJpegTileBlocks = 2048;    // offsets: 256 threads x 8 blocks
 constexpr int kJpegChunkBytes = 4096;    // stuffing: 256 threads x 16 bytes
-constexpr int kJpegMaxBlockBits = 1680;  // bound of one block's code (8-bit samples): DC <= 20,
-                                         // 63 AC x (16 + 10), EOB <= 16
+constexpr int kJpegMaxBlockBits = 1680;  // bound of one block's code (8-bit samples): DC <= 22,
+                                         // 63 AC x (16 + 10), EOB <= 4
+constexpr int kJpegAcWords = 53;         // per-block AC code slot: <= 1642 bits + one zero word
 
 // Huffman lookup: (size << 16) | code per symbol; size 0 = symbol absent from the table
 struct JpegHuff {
@@ -35,7 +36,7 @@ struct JpegHuff {
     uint32_t ac[2][256];  // [luma, chroma][(run << 4) | category]
 };
 
-// sizes the device reports (written by the ffscan kernel)
+// sizes the device reports (written by the last CTA of the ffcount kernel)
 struct JpegInfo {
     unsigned long long total_bits;  // entropy-coded bits before stuffing
     unsigned long long data_bytes;  // ceil(total_bits / 8)
@@ -58,12 +59,13 @@ struct JpegGeom {
 
 struct JpegLaunch {
     JpegGeom g;
-    float q[2][64];  // quantiser (natural order) as float, [luma, chroma]
+    float q[2][64];   // quantiser (natural order) as float, [luma, chroma]
+    float rq[2][64];  // 1 / q rounded to nearest (host IEEE division)
     const uint8_t* rgb;
     const JpegHuff* huff;
-    int16_t* coef;                   // nb x 64, coding order, zigzag-permuted
-    int* dc;                         // nb
-    int* acbits;                     // nb
+    uint32_t* acw;                   // nb x kJpegAcWords: each block's AC code from bit 0, big-endian
+    int* dc;                         // nb: quantised DC
+    int* acbits;                     // nb: bits of the AC code
     int* blk_off;                    // nb: offset of the block inside its tile (bits)
     int* tile_sum;                   // ntiles
     unsigned long long* tile_off;    // ntiles
@@ -71,6 +73,7 @@ struct JpegLaunch {
     int* chunk_ff;                   // chunks
     unsigned long long* chunk_off;   // chunks
     JpegInfo* info;
+    unsigned* counters;              // 2 CTA-completion counters, zero between launches
     uint8_t* out;                    // stuffed bytes go to out[base ...], then FF D9
     unsigned long long base;         // bytes before the entropy-coded segment (header), 0 or its size
     unsigned long long out_cap;      // bytes of out that may be written

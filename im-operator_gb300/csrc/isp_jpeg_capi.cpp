@@ -154,9 +154,9 @@ int validate(const void* in, const void* out, int w, int h, int bd, int quality)
 struct imop_jpeg_ctx {
     int device = 0;
     cudaStream_t st = nullptr;  // the host entry point's stream
-    DevBuf rgb, coef, dc, acbits, blk_off, tile_sum, tile_off, words, chunk_ff, chunk_off, info, out, huff, hdr;
+    DevBuf rgb, acw, dc, acbits, blk_off, tile_sum, tile_off, words, chunk_ff, chunk_off, info, counters, out, huff, hdr;
     JpegInfo* h_info = nullptr;  // pinned
-    bool words_dirty = true;     // the word stream must be zero before the emit kernel
+    bool words_dirty = true;     // the word stream and the counters must be zero before a launch
     std::vector<uint8_t> header;
     int hdr_key[4] = {-1, -1, -1, -1};
     bool hdr_on_device = false;
@@ -173,7 +173,7 @@ int prepare(imop_jpeg_ctx* c, const JpegGeom& g, cudaStream_t st) {
     const size_t nb = (size_t)g.nb;
     const size_t wbytes = (size_t)g.words * 4;
     const bool grow_words = c->words.size < wbytes;
-    if ((e = c->coef.ensure(nb * 64 * sizeof(int16_t))) != cudaSuccess ||
+    if ((e = c->acw.ensure(nb * kJpegAcWords * sizeof(uint32_t))) != cudaSuccess ||
         (e = c->dc.ensure(nb * sizeof(int))) != cudaSuccess || (e = c->acbits.ensure(nb * sizeof(int))) != cudaSuccess ||
         (e = c->blk_off.ensure(nb * sizeof(int))) != cudaSuccess ||
         (e = c->tile_sum.ensure((size_t)g.ntiles * sizeof(int))) != cudaSuccess ||
@@ -182,8 +182,14 @@ int prepare(imop_jpeg_ctx* c, const JpegGeom& g, cudaStream_t st) {
         (e = c->chunk_off.ensure((size_t)g.chunks * 8)) != cudaSuccess ||
         (e = c->info.ensure(sizeof(JpegInfo))) != cudaSuccess)
         return jcuda(e, "jpeg scratch allocation");
+    if (!c->counters.ptr) {
+        if ((e = c->counters.ensure(2 * sizeof(unsigned))) != cudaSuccess) return jcuda(e, "jpeg scratch allocation");
+        c->words_dirty = true;
+    }
     if (grow_words || c->words_dirty) {
-        if ((e = cudaMemsetAsync(c->words.ptr, 0, c->words.size, st)) != cudaSuccess) return jcuda(e, "jpeg clear");
+        if ((e = cudaMemsetAsync(c->words.ptr, 0, c->words.size, st)) != cudaSuccess ||
+            (e = cudaMemsetAsync(c->counters.ptr, 0, c->counters.size, st)) != cudaSuccess)
+            return jcuda(e, "jpeg clear");
         c->words_dirty = false;
     }
     return IMOP_JPEG_OK;
@@ -195,9 +201,12 @@ void fill_launch(imop_jpeg_ctx* c, const JpegGeom& g, int quality, JpegLaunch& L
     scale_qtable(qc, kQChroma, quality);
     std::memset(&L, 0, sizeof(L));
     L.g = g;
-    for (int i = 0; i < 64; i++) L.q[0][i] = (float)ql[i], L.q[1][i] = (float)qc[i];
+    for (int i = 0; i < 64; i++) {
+        L.q[0][i] = (float)ql[i], L.q[1][i] = (float)qc[i];
+        L.rq[0][i] = 1.0f / L.q[0][i], L.rq[1][i] = 1.0f / L.q[1][i];
+    }
     L.huff = (const JpegHuff*)c->huff.ptr;
-    L.coef = (int16_t*)c->coef.ptr;
+    L.acw = (uint32_t*)c->acw.ptr;
     L.dc = (int*)c->dc.ptr;
     L.acbits = (int*)c->acbits.ptr;
     L.blk_off = (int*)c->blk_off.ptr;
@@ -207,6 +216,7 @@ void fill_launch(imop_jpeg_ctx* c, const JpegGeom& g, int quality, JpegLaunch& L
     L.chunk_ff = (int*)c->chunk_ff.ptr;
     L.chunk_off = (unsigned long long*)c->chunk_off.ptr;
     L.info = (JpegInfo*)c->info.ptr;
+    L.counters = (unsigned*)c->counters.ptr;
 }
 
 // the block count must index with 32-bit ints on the device

@@ -24,3 +24,17 @@ def test_weight_quotients_equal_ieee_division_exhaustively(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.count(" 0 mismatches") == 2
+
+
+def test_jpeg_quotients_equal_ieee_division_exhaustively(tmp_path):
+    """The JPEG quantiser division (reciprocal product plus one residual correction) against
+    __fdiv_rn for every float in [0.5, 2048) and every quantiser 1..255."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "jpeg_quant_check")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "--expt-relaxed-constexpr", os.path.join(HERE, "gpu_kernels", "jpeg_quant_check.cu"), "-o", exe],
+                   check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert " 0 mismatches" in r.stdout
