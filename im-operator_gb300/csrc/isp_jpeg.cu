@@ -145,24 +145,26 @@ struct LaneCodes {
 
 __device__ __forceinline__ int lane_codes(const Lane8& l, int r, uint64_t mask, const uint32_t* ac, LaneCodes& c) {
     const int zrl = (int)(ac[0xF0] >> 16), eob = (int)(ac[0x00] >> 16);
+    // the previous non-zero AC slot before this lane's first one (0: the DC slot)
+    const uint64_t below = mask & ((1ull << (8 * r)) - 1);
+    int prev = below ? 63 - __clzll((long long)below) : 0;
+    const uint32_t mine = (uint32_t)(mask >> (8 * r)) & 0xFFu;
     int bits = 0;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
         c.cw[j] = 0u;
         c.cl[j] = 0;
+        if (!((mine >> j) & 1)) continue;
         const int p = 8 * r + j;
-        if (!((mask >> p) & 1)) continue;
-        const uint64_t below = mask & ((1ull << p) - 1);
-        const int prev = below ? 63 - __clzll((long long)below) : 0;
         const int run = p - prev - 1, v = l.z[j], cat = category(v);
+        prev = p;
         const uint32_t e = ac[((run & 15) << 4) | cat];
         const int size = (int)(e >> 16), len = size ? size + cat : 0;
         c.cw[j] = size ? ((e & 0xFFFFu) << cat) | value_bits(v, cat) : 0u;
         c.cl[j] = ((run >> 4) << 8) | len;
         bits += (run >> 4) * zrl + len;
     }
-    const int last = mask ? 63 - __clzll((long long)mask) : 0;
-    c.eob = (last >> 3) == r;
+    c.eob = mine ? (r == 7 || (mask >> (8 * r + 8)) == 0) : (r == 0 && mask == 0);
     if (c.eob) bits += eob;
     return bits;
 }
@@ -245,6 +247,7 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
     BlockPos P;
     P.comp = 0;
     if (live) P = block_pos(L.g, b);
+    const int comp = P.comp;
 
     // sample row r -> row DCT, written transposed
     int xi[8];
@@ -256,13 +259,13 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
         if (P.x0 + 7 * P.sx < L.g.w) {  // interior: fixed offsets from one base
             const int step = 3 * P.sx;
 #pragma unroll
-            for (int i = 0; i < 8; i++) xi[i] = ycc(row[i * step], row[i * step + 1], row[i * step + 2], P.comp) - 128;
+            for (int i = 0; i < 8; i++) xi[i] = ycc(row[i * step], row[i * step + 1], row[i * step + 2], comp) - 128;
         } else {
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 const int dx = min(P.x0 + i * P.sx, L.g.w - 1) - P.x0;
                 const uint8_t* s = row + dx * 3;
-                xi[i] = ycc(s[0], s[1], s[2], P.comp) - 128;
+                xi[i] = ycc(s[0], s[1], s[2], comp) - 128;
             }
         }
     }
@@ -286,8 +289,8 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
         const float4 c0 = *reinterpret_cast<const float4*>(&T[lb][r * 8]);
         const float4 c1 = *reinterpret_cast<const float4*>(&T[lb][r * 8 + 4]);
         const float col[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-        const float* qt = sq[P.comp > 0 ? 1 : 0];
-        const float* rqt = srq[P.comp > 0 ? 1 : 0];
+        const float* qt = sq[comp > 0 ? 1 : 0];
+        const float* rqt = srq[comp > 0 ? 1 : 0];
 #pragma unroll
         for (int v = 0; v < 8; v++) {
             // the first product joins the running sum 0 exactly (a zero's sign cannot reach the
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(kThreads) jpeg_transform_kernel(JpegLaunch L) 
     // AC codes: lane r codes slots [8r, 8r + 8) at its offset inside the block's code
     const Lane8 l = unpack8(*reinterpret_cast<const uint4*>(&Z[lb][r * 8]));
     const uint64_t mask = block_mask(l, r);
-    const uint32_t* ac = sac[P.comp > 0 ? 1 : 0];
+    const uint32_t* ac = sac[comp > 0 ? 1 : 0];
     LaneCodes c;
     const int bits = lane_codes(l, r, mask, ac, c);
     int incl = bits;

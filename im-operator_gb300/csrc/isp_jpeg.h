@@ -23,7 +23,7 @@
 
 namespace imop {
 
-constexpr int kJpegBlocksPerCta = 32;    // transform: 8 threads per block, 256 threads
+constexpr int kJpegBlocksPerCta = 32;    // transform / place: 8 threads per block, 256 threads
 constexpr int kJpegTileBlocks = 2048;    // offsets: 256 threads x 8 blocks
 constexpr int kJpegChunkBytes = 4096;    // stuffing: 256 threads x 16 bytes
 constexpr int kJpegMaxBlockBits = 1680;  // bound of one block's code (8-bit samples): DC <= 22,
