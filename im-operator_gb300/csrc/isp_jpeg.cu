@@ -389,18 +389,30 @@ __global__ void __launch_bounds__(kThreads) jpeg_place_kernel(JpegLaunch L) {
     __syncthreads();
     const int lb = t >> 3, r = t & 7;
     const long long bl = (long long)blockIdx.x * kJpegBlocksPerCta + lb;
-    if (bl >= L.g.nb) return;
+    if (bl >= L.g.nb) return;  // whole 8-thread groups
     const int b = (int)bl;
-    const BlockPos P = block_pos(L.g, b);
-    const int diff = L.dc[b] - (P.prev >= 0 ? L.dc[P.prev] : 0);
-    const int cat = category(diff);
-    const uint32_t e = sdc[P.comp > 0 ? 1 : 0][min(cat, 15)];
-    const int dlen = (int)(e >> 16) + cat;
-    const uint32_t dcode = ((e & 0xFFFFu) << cat) | value_bits(diff, cat);
-    const unsigned long long start = L.tile_off[b / kJpegTileBlocks] + (unsigned long long)L.blk_off[b];
-    // the span as a virtual stream: (start mod 32) zero bits, the DC code, the AC code
-    const int pre = (int)(start & 31) + dlen;  // 2 .. 53
-    const int end = pre + L.acbits[b];
+    const unsigned grp = 0xFFu << (t & 24);
+    // thread 0 of the group works out the block's DC code and span; the others receive them
+    uint32_t dcode = 0;
+    int dlen = 0, pre = 0, end = 0;
+    unsigned long long start = 0;
+    if (r == 0) {
+        const BlockPos P = block_pos(L.g, b);
+        const int diff = L.dc[b] - (P.prev >= 0 ? L.dc[P.prev] : 0);
+        const int cat = category(diff);
+        const uint32_t e = sdc[P.comp > 0 ? 1 : 0][min(cat, 15)];
+        dlen = (int)(e >> 16) + cat;
+        dcode = ((e & 0xFFFFu) << cat) | value_bits(diff, cat);
+        start = L.tile_off[b / kJpegTileBlocks] + (unsigned long long)L.blk_off[b];
+        // the span as a virtual stream: (start mod 32) zero bits, the DC code, the AC code
+        pre = (int)(start & 31) + dlen;  // 2 .. 53
+        end = pre + L.acbits[b];
+    }
+    const int src = t & 24;
+    dcode = __shfl_sync(grp, dcode, src);
+    pre = __shfl_sync(grp, pre, src);
+    end = __shfl_sync(grp, end, src);
+    start = __shfl_sync(grp, start, src);
     const int nw = (end + 31) >> 5;
     const uint64_t pl = (uint64_t)dcode << (64 - pre);
     const uint32_t* A = L.acw + (size_t)b * kJpegAcWords;
