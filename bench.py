@@ -15,6 +15,10 @@ is needed between steps.
   plain       the same batch through the plain per-operator kernels (one kernel per stage)
   cpu_baseline  the CPU oracle (plain-C restatement of the reference's CPU path) on a bounded
               sample of the same frames on this host's cores
+  jpeg        the step's RGB8 frames encoded to baseline JPEG (quality 90, 4:2:0, the reference's
+              JpegParams defaults), byte-identical to the reference's encoder: device-resident
+              frames, the host entry point with pinned buffers (e2e), RAW -> JPEG on the device
+              (ISP step + encodes), and the CPU restatement of the reference's encoder
 
 `--impl reference` times the reference's CPU algorithm for this path (the oracle port; the
 reference's own sources do not exist on GPU hosts) with all host threads, same metric / config.
@@ -48,6 +52,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-operator leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-c4", action="store_true", help="skip the uneven 96-frame batch leg")
+    ap.add_argument("--no-jpeg", action="store_true", help="skip the JPEG encode leg")
     return ap.parse_args()
 
 
@@ -131,6 +136,109 @@ def cpu_oracle_rate(pl, frames, max_seconds=30.0):
             break
     dt = time.perf_counter() - t0
     return done * pl.pixels / dt / 1e6, done, dt
+
+
+def cpu_jpeg_rate(rgb, quality, subsample, max_seconds=20.0):
+    """Mpix/s of the CPU restatement of the reference's baseline JPEG encoder (one thread, as the
+    reference's encoder) on whole frames."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py as O
+    h, w = rgb.shape[:2]
+    t0 = time.perf_counter()
+    done = 0
+    while done < 3 and (done == 0 or time.perf_counter() - t0 < max_seconds):
+        O.jpeg_encode(rgb, quality, subsample)
+        done += 1
+    dt = time.perf_counter() - t0
+    return done * w * h / dt / 1e6, done, dt
+
+
+def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device, d_rgb, h_rgb, peak, peak_kind):
+    """Baseline JPEG encode of the step's B RGB8 frames (4024x3032, quality 90, 4:2:0)."""
+    from imop_gb300 import jpeg as J
+    B = d_rgb.shape[0]
+    w, h, q, ss = W_C2, H_C2, 90, 1
+    enc = J.JpegEncoder()
+    cap = J.max_bytes(w, h)
+    d_jpg = torch.empty((B, cap), dtype=torch.uint8, device="cuda")
+    sh = stream.cuda_stream
+    sizes = []
+
+    def encode_all():
+        for i in range(B):
+            enc.encode_device(d_rgb[i], w, h, d_jpg[i], cap, q, ss, stream=sh)
+
+    for i in range(B):  # sizes of this step's frames, and the host entry point agrees byte for byte
+        enc.encode_device(d_rgb[i], w, h, d_jpg[i], cap, q, ss, stream=sh)
+        sizes.append(enc.last_size()[1])
+    host0 = enc.encode(h_rgb[0].numpy().reshape(h, w, 3), q, ss)
+    same = bool(host0.size == sizes[0] and (d_jpg[0, :sizes[0]].cpu().numpy() == host0).all())
+    for _ in range(max(3, args.warmup)):
+        encode_all()
+    torch.cuda.synchronize()
+    steps = args.steps
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        encode_all()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(ev0.elapsed_time(ev1)) / steps
+    # RAW -> JPEG on the device: the ISP step, then the encodes of its frames
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        step_device()
+        encode_all()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_chain = max_over_ranks(ev0.elapsed_time(ev1)) / steps
+    # e2e: the host entry point from pinned RGB8 frames into pinned JPEG buffers
+    h_jpg = torch.empty((B, cap), dtype=torch.uint8).pin_memory()
+    import ctypes as C
+    L = J._L()
+
+    def host_all():
+        for i in range(B):
+            n = C.c_size_t(cap)
+            st = L.imop_jpeg_encode_host(enc.h, h_rgb[i].data_ptr(), w, h, 8, q, ss, h_jpg[i].data_ptr(), C.byref(n))
+            if st:
+                raise RuntimeError(f"jpeg encode status {st}")
+
+    host_all()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        host_all()
+    ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3) / steps
+    barrier()
+    px = B * w * h
+    jpeg_bytes = sum(sizes)
+    alg = B * w * h * 3 + jpeg_bytes  # RGB8 in, JPEG out
+    out = {"value": round(world * px / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s", "ms_per_step": round(ms, 4),
+           "frames_per_step": B, "jpeg_bytes_per_step": jpeg_bytes, "device_equals_host_entry": same,
+           "gpu_launches_per_step": 5 * B,
+           "roofline": {"bound": "hbm", "achieved": round(alg / (ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4), "peak_kind": peak_kind,
+                        "note": "algorithmic bytes = RGB8 in + JPEG out; the transform kernel is bound by "
+                                "instruction issue (exact float DCT order), not by HBM"},
+           "e2e": {"value": round(world * px / (ms_e2e / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                   "h2d_bytes_per_step": B * w * h * 3, "d2h_bytes_per_step": jpeg_bytes,
+                   "api": "imop_jpeg_encode_host (pinned RGB8 in, pinned JPEG out)"},
+           "raw_to_jpeg": {"value": round(world * px / (ms_chain / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                           "ms_per_step": round(ms_chain, 4)},
+           "config": "4024x3032 RGB8 from the fused ISP step, quality 90, 4:2:0, bytes equal to "
+                     "jpeg_codec::process_encode_baseline"}
+    if rank == 0 and not args.no_cpu:
+        rate, done, dt = cpu_jpeg_rate(h_rgb[0].numpy().reshape(h, w, 3), q, ss)
+        out["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": 1, "kind": "port",
+                               "sample": f"{done} frames in {dt:.1f} s (plain-C restatement of the reference's "
+                                         f"single-threaded baseline encoder)"}
+    enc.close()
+    return out
 
 
 def adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
@@ -343,6 +451,14 @@ def main():
             step_plain()
         ms_plain = timed(step_plain, args.steps)
 
+    jpeg = None
+    if not args.no_jpeg:
+        pk, pk_kind = peaks()
+        if args.no_e2e:  # the host frames of the JPEG e2e leg are the ISP's outputs
+            isp.run_host_batch(host_batch)
+        jpeg = jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device,
+                        d_out.view(B, H_C2, W_C2, 3), h_out, pk, pk_kind)
+
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world)
@@ -392,6 +508,8 @@ def main():
         line["adjoint"] = adjoint
     if c4 is not None:
         line["c4"] = c4
+    if jpeg is not None:
+        line["jpeg"] = jpeg
     if rank == 0 and not args.no_cpu:
         rate, done, dt = cpu_oracle_rate(pl, host_frames[: max(1, args.cpu_sample_frames)])
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",

@@ -247,6 +247,53 @@ LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int 
 
 }  // namespace lut
 
+// ---- jpeg_codec: the glue of src/jpeg_codec/cuda_dispatch.cpp ----------------------------------
+namespace jpeg_codec {
+
+// the reference's CPU decoder, when the caller links it (weak: absent -> null)
+JpegError process_decode_baseline(const uint8_t*, size_t, uint8_t*, int*, int*, int*) __attribute__((weak));
+
+namespace {
+struct JpegThreadCtx {
+    imop_jpeg_t ctx = nullptr;
+    ~JpegThreadCtx() {
+        if (ctx) imop_jpeg_destroy(ctx);
+    }
+};
+thread_local JpegThreadCtx t_jpeg;
+}  // namespace
+
+bool has_cuda() { return imop::has_cuda(); }
+const char* cuda_device_name() { return imop::cuda_device_name(); }
+void cuda_synchronize() { cudaDeviceSynchronize(); }
+
+// src/jpeg_codec/cuda_dispatch.cpp:121-240: CudaNotAvailable without a device, then the
+// reference's validation (channels taken as 3), then the encode; the status values are equal
+JpegError process_encode_cuda(const uint8_t* input, uint8_t* output, size_t* output_size, int width, int height,
+                              int channels, int bit_depth, const JpegParams& params) {
+    (void)channels;
+    if (!has_cuda()) return JpegError::CudaNotAvailable;
+    if (!t_jpeg.ctx && imop_jpeg_create(&t_jpeg.ctx) != IMOP_JPEG_OK) {
+        t_jpeg.ctx = nullptr;
+        return JpegError::InternalError;
+    }
+    const int rc = imop_jpeg_encode_host(t_jpeg.ctx, input, width, height, bit_depth, params.quality,
+                                         params.chroma_subsample, output, output_size);
+    return (rc >= 0 && rc <= 12) ? static_cast<JpegError>(rc) : JpegError::InternalError;
+}
+
+// src/jpeg_codec/cuda_dispatch.cpp:246-255
+JpegError process_decode_cuda(const uint8_t* input, size_t input_size, uint8_t* output, int* width, int* height,
+                              int* channels) {
+    if (!has_cuda()) return JpegError::CudaNotAvailable;
+    if (!input || !output || !width || !height || !channels) return JpegError::NullInput;
+    if (input_size < 2 || input[0] != 0xFF || input[1] != 0xD8) return JpegError::InvalidJpegData;
+    if (!&process_decode_baseline) return JpegError::InternalError;
+    return process_decode_baseline(input, input_size, output, width, height, channels);
+}
+
+}  // namespace jpeg_codec
+
 // ---- modules off this path: CPU fallback ------------------------------------------------------
 namespace denoise {
 bool has_cuda() { return false; }

@@ -12,7 +12,7 @@
  *
  * Served on the GPU: demosaic HQLI / MG / AMAZE (packed input of any depth included), black level,
  * adaptive and map-based defect correction, polynomial and flat-field lens shading, manual white
- * balance, 3x3 CCM, custom 3D LUTs.  tone::process_tone_cuda returns InternalError, so the
+ * balance, 3x3 CCM, custom 3D LUTs, baseline JPEG encode.  tone::process_tone_cuda returns InternalError, so the
  * reference runs its CPU tone curves; the other modules of the same glue file
  * (denoise, sharpen, local contrast, saturation, colour temperature, highlight reconstruction)
  * report no CUDA and stay on the CPU.
@@ -135,6 +135,33 @@ bool has_cuda();                                                                
 LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels, int bit_depth,
                           const LUT3D& lut_data);
 }  // namespace lut
+
+namespace jpeg_codec {
+// the GPU glue of src/jpeg_codec/cuda_dispatch.cpp (a translation unit of its own)
+enum class JpegError {                                                                // include/jpeg_codec/types.hpp:15-29
+    Ok = 0, NullInput, NullOutput, InvalidDimensions, InvalidBitDepth, InvalidChannels, InvalidQuality,
+    ImageTooSmall, EncodeFailed, DecodeFailed, InvalidJpegData, CudaNotAvailable, InternalError
+};
+struct JpegParams {                                                                   // include/jpeg_codec/types.hpp:66-71
+    int quality = 90;
+    bool progressive = false;
+    bool optimize = true;
+    int chroma_subsample = 1;
+};
+bool has_cuda();                                                                      // include/jpeg_codec/algorithms.hpp
+const char* cuda_device_name();
+void cuda_synchronize();
+// The baseline encoder on the device: the bytes of process_encode_baseline for every
+// subsampling (0 = 4:4:4, 1 = 4:2:0, 2 = 4:2:2).
+JpegError process_encode_cuda(const uint8_t* input, uint8_t* output, size_t* output_size, int width, int height,
+                              int channels, int bit_depth, const JpegParams& params);
+// Checks as the reference's, then the reference's own CPU decoder when it is linked in
+// (src/jpeg_codec/decode_baseline.cpp); InternalError when it is not.
+JpegError process_decode_cuda(const uint8_t* input, size_t input_size, uint8_t* output, int* width, int* height,
+                              int* channels);
+JpegError process_decode_baseline(const uint8_t* input, size_t input_size, uint8_t* output, int* width,
+                                  int* height, int* channels);
+}  // namespace jpeg_codec
 
 // Modules off this path whose GPU glue lives in the same reference translation unit
 // (src/gpu_dispatch.cpp:50-415, 490-520): has_cuda() is false and the *_cuda entry returns

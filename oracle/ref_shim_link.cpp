@@ -1,5 +1,6 @@
 // Link probe: takes the address of every GPU-glue entry point as the reference's own headers
-// declare it (include/<module>/algorithms.hpp, include/imop/algorithms.hpp), so linking this
+// declare it (include/<module>/algorithms.hpp, include/imop/algorithms.hpp,
+// include/jpeg_codec/algorithms.hpp), so linking this
 // against libimop_isp.so proves that the library defines each symbol with the reference's
 // mangled name.  Built by `make -C oracle shimlink` where the reference tree exists.
 #include "denoise/algorithms.hpp"
@@ -16,6 +17,7 @@
 #include "tone/algorithms.hpp"
 #include "lut/algorithms.hpp"
 #include "imop/algorithms.hpp"
+#include "jpeg_codec/algorithms.hpp"
 void* refs[] = {
  (void*)&denoise::process_denoise_cuda, (void*)&denoise::has_cuda,
  (void*)&sharpen::process_sharpen_cuda, (void*)&sharpen::has_cuda,
@@ -28,5 +30,7 @@ void* refs[] = {
  (void*)&imop::cuda_device_name, (void*)&imop::cuda_synchronize,
  (void*)&local_contrast::has_cuda, (void*)&saturation::has_cuda, (void*)&color_temp::has_cuda,
  (void*)&highlight_reconstruct::has_cuda, (void*)&black_level::has_cuda, (void*)&tone::has_cuda, (void*)&lut::has_cuda,
- (void*)&ccm::has_cuda, (void*)&white_balance::has_cuda, (void*)&lens_shading::has_cuda, (void*)&defect_correct::has_cuda};
+ (void*)&ccm::has_cuda, (void*)&white_balance::has_cuda, (void*)&lens_shading::has_cuda, (void*)&defect_correct::has_cuda,
+ (void*)&jpeg_codec::process_encode_cuda, (void*)&jpeg_codec::process_decode_cuda, (void*)&jpeg_codec::has_cuda,
+ (void*)&jpeg_codec::cuda_device_name, (void*)&jpeg_codec::cuda_synchronize};
 int main() { return refs[0] == nullptr; }

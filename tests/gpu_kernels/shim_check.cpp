@@ -199,6 +199,49 @@ int main() {
     uint8_t px[3] = {1, 2, 3}, po[3];
     report("tone fallback", 1, 1, 8, tone::process_tone_cuda(px, po, 1, 1, 3, tone::ToneAlgorithm::GAMMA, 8, tp) ==
                                             tone::ToneError::InternalError);
+    // jpeg_codec::process_encode_cuda: the oracle's bytes (the reference's baseline encoder) for
+    // every subsampling, a range of qualities and sizes; the reference's status codes
+    {
+        std::mt19937 rng(77);
+        const int sizes[4][2] = {{8, 8}, {37, 29}, {640, 480}, {1001, 333}};
+        for (int si = 0; si < 4; si++)
+            for (int ss = 0; ss < 3; ss++) {
+                const int w = sizes[si][0], h = sizes[si][1], q = 10 + 30 * ss + 7 * si;
+                std::vector<uint8_t> rgb((size_t)w * h * 3);
+                for (size_t i = 0; i < rgb.size(); i++) rgb[i] = (uint8_t)((i * 37 + 127 + (rng() & 15)) % 256);
+                const size_t cap = (size_t)w * h * 9 + 65536;
+                std::vector<uint8_t> a(cap), b(cap);
+                size_t na = 0, nb = 0;
+                jpeg_codec::JpegParams jp;
+                jp.quality = q;
+                jp.chroma_subsample = ss;
+                const auto st = jpeg_codec::process_encode_cuda(rgb.data(), a.data(), &na, w, h, 3, 8, jp);
+                const int so = or_jpeg_encode(rgb.data(), w, h, 8, q, ss, b.data(), &nb);
+                report("jpeg process_encode_cuda", w, h, 8,
+                       st == jpeg_codec::JpegError::Ok && so == 0 && na == nb && std::memcmp(a.data(), b.data(), na) == 0);
+            }
+        std::vector<uint8_t> z(8 * 8 * 3), o(1 << 16);
+        size_t n = 0;
+        jpeg_codec::JpegParams jp;
+        report("jpeg null input", 8, 8, 8,
+               jpeg_codec::process_encode_cuda(nullptr, o.data(), &n, 8, 8, 3, 8, jp) == jpeg_codec::JpegError::NullInput);
+        report("jpeg bit depth", 8, 8, 16,
+               jpeg_codec::process_encode_cuda(z.data(), o.data(), &n, 8, 8, 3, 16, jp) ==
+                   jpeg_codec::JpegError::InvalidBitDepth);
+        report("jpeg too small", 4, 4, 8,
+               jpeg_codec::process_encode_cuda(z.data(), o.data(), &n, 4, 4, 3, 8, jp) == jpeg_codec::JpegError::ImageTooSmall);
+        jp.quality = 0;
+        report("jpeg quality", 8, 8, 8,
+               jpeg_codec::process_encode_cuda(z.data(), o.data(), &n, 8, 8, 3, 8, jp) == jpeg_codec::JpegError::InvalidQuality);
+        int dw = 0, dh = 0, dc = 0;
+        const uint8_t junk[4] = {0x12, 0x34, 0x56, 0x78};
+        report("jpeg decode invalid data", 1, 1, 8,
+               jpeg_codec::process_decode_cuda(junk, 4, o.data(), &dw, &dh, &dc) == jpeg_codec::JpegError::InvalidJpegData);
+        // without the reference's CPU decoder linked in, decoding is not served here
+        const uint8_t soi[4] = {0xFF, 0xD8, 0xFF, 0xD9};
+        report("jpeg decode without the CPU decoder", 1, 1, 8,
+               jpeg_codec::process_decode_cuda(soi, 4, o.data(), &dw, &dh, &dc) == jpeg_codec::JpegError::InternalError);
+    }
     std::printf("%s\n", failures ? "FAILED" : "ALL OK");
     return failures ? 1 : 0;
 }
