@@ -13,7 +13,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <array>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -151,51 +154,62 @@ int validate(const void* in, const void* out, int w, int h, int bd, int quality)
 
 }  // namespace
 
+// device scratch of one encode in flight; a context has two, so that a batch runs consecutive
+// frames on two streams and the latency-bound tail kernels of one frame overlap the next
+// frame's transform
+struct JpegLane {
+    DevBuf acw, dc, acbits, blk_off, tile_sum, tile_off, words, chunk_ff, chunk_off, info, counters, rgb, out;
+    bool dirty = true;             // the word stream and the counters must be zero before a launch
+    cudaStream_t st = nullptr;     // batch stream of the lane
+    cudaEvent_t ev = nullptr;      // join / info-ready marker
+    JpegInfo* h_info = nullptr;    // pinned
+};
+
 struct imop_jpeg_ctx {
     int device = 0;
-    cudaStream_t st = nullptr;  // the host entry point's stream
-    DevBuf rgb, acw, dc, acbits, blk_off, tile_sum, tile_off, words, chunk_ff, chunk_off, info, counters, out, huff, hdr;
-    JpegInfo* h_info = nullptr;  // pinned
-    bool words_dirty = true;     // the word stream and the counters must be zero before a launch
-    std::vector<uint8_t> header;
-    int hdr_key[4] = {-1, -1, -1, -1};
-    bool hdr_on_device = false;
+    cudaEvent_t fork = nullptr;  // a device batch starts when the caller's stream reaches it
+    JpegLane lane[2];
+    DevBuf huff;
+    // headers by (width, height, quality, subsample): host bytes and a device copy
+    std::map<std::array<int, 4>, std::pair<std::vector<uint8_t>, std::unique_ptr<DevBuf>>> headers;
     JpegInfo last{};
+    JpegLane* last_lane = nullptr;
     cudaStream_t last_stream = nullptr;
     bool last_pending = false;
+    size_t last_base = 0;
 };
 
 namespace {
 
-// grows the scratch of ctx to the geometry; clears the word stream when it was (re)allocated
-int prepare(imop_jpeg_ctx* c, const JpegGeom& g, cudaStream_t st) {
+// grows a lane's scratch to the geometry; clears its word stream and counters when (re)allocated
+int prepare(JpegLane& l, const JpegGeom& g, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     const size_t nb = (size_t)g.nb;
     const size_t wbytes = (size_t)g.words * 4;
-    const bool grow_words = c->words.size < wbytes;
-    if ((e = c->acw.ensure(nb * kJpegAcWords * sizeof(uint32_t))) != cudaSuccess ||
-        (e = c->dc.ensure(nb * sizeof(int))) != cudaSuccess || (e = c->acbits.ensure(nb * sizeof(int))) != cudaSuccess ||
-        (e = c->blk_off.ensure(nb * sizeof(int))) != cudaSuccess ||
-        (e = c->tile_sum.ensure((size_t)g.ntiles * sizeof(int))) != cudaSuccess ||
-        (e = c->tile_off.ensure((size_t)g.ntiles * 8)) != cudaSuccess || (e = c->words.ensure(wbytes)) != cudaSuccess ||
-        (e = c->chunk_ff.ensure((size_t)g.chunks * sizeof(int))) != cudaSuccess ||
-        (e = c->chunk_off.ensure((size_t)g.chunks * 8)) != cudaSuccess ||
-        (e = c->info.ensure(sizeof(JpegInfo))) != cudaSuccess)
+    const bool grow_words = l.words.size < wbytes;
+    if ((e = l.acw.ensure(nb * kJpegAcWords * sizeof(uint32_t))) != cudaSuccess ||
+        (e = l.dc.ensure(nb * sizeof(int))) != cudaSuccess || (e = l.acbits.ensure(nb * sizeof(int))) != cudaSuccess ||
+        (e = l.blk_off.ensure(nb * sizeof(int))) != cudaSuccess ||
+        (e = l.tile_sum.ensure((size_t)g.ntiles * sizeof(int))) != cudaSuccess ||
+        (e = l.tile_off.ensure((size_t)g.ntiles * 8)) != cudaSuccess || (e = l.words.ensure(wbytes)) != cudaSuccess ||
+        (e = l.chunk_ff.ensure((size_t)g.chunks * sizeof(int))) != cudaSuccess ||
+        (e = l.chunk_off.ensure((size_t)g.chunks * 8)) != cudaSuccess ||
+        (e = l.info.ensure(sizeof(JpegInfo))) != cudaSuccess)
         return jcuda(e, "jpeg scratch allocation");
-    if (!c->counters.ptr) {
-        if ((e = c->counters.ensure(2 * sizeof(unsigned))) != cudaSuccess) return jcuda(e, "jpeg scratch allocation");
-        c->words_dirty = true;
+    if (!l.counters.ptr) {
+        if ((e = l.counters.ensure(2 * sizeof(unsigned))) != cudaSuccess) return jcuda(e, "jpeg scratch allocation");
+        l.dirty = true;
     }
-    if (grow_words || c->words_dirty) {
-        if ((e = cudaMemsetAsync(c->words.ptr, 0, c->words.size, st)) != cudaSuccess ||
-            (e = cudaMemsetAsync(c->counters.ptr, 0, c->counters.size, st)) != cudaSuccess)
+    if (grow_words || l.dirty) {
+        if ((e = cudaMemsetAsync(l.words.ptr, 0, l.words.size, st)) != cudaSuccess ||
+            (e = cudaMemsetAsync(l.counters.ptr, 0, l.counters.size, st)) != cudaSuccess)
             return jcuda(e, "jpeg clear");
-        c->words_dirty = false;
+        l.dirty = false;
     }
     return IMOP_JPEG_OK;
 }
 
-void fill_launch(imop_jpeg_ctx* c, const JpegGeom& g, int quality, JpegLaunch& L) {
+void fill_launch(imop_jpeg_ctx* c, JpegLane& l, const JpegGeom& g, int quality, JpegLaunch& L) {
     int ql[64], qc[64];
     scale_qtable(ql, kQLuma, quality);
     scale_qtable(qc, kQChroma, quality);
@@ -206,29 +220,76 @@ void fill_launch(imop_jpeg_ctx* c, const JpegGeom& g, int quality, JpegLaunch& L
         L.rq[0][i] = 1.0f / L.q[0][i], L.rq[1][i] = 1.0f / L.q[1][i];
     }
     L.huff = (const JpegHuff*)c->huff.ptr;
-    L.acw = (uint32_t*)c->acw.ptr;
-    L.dc = (int*)c->dc.ptr;
-    L.acbits = (int*)c->acbits.ptr;
-    L.blk_off = (int*)c->blk_off.ptr;
-    L.tile_sum = (int*)c->tile_sum.ptr;
-    L.tile_off = (unsigned long long*)c->tile_off.ptr;
-    L.words = (uint32_t*)c->words.ptr;
-    L.chunk_ff = (int*)c->chunk_ff.ptr;
-    L.chunk_off = (unsigned long long*)c->chunk_off.ptr;
-    L.info = (JpegInfo*)c->info.ptr;
-    L.counters = (unsigned*)c->counters.ptr;
+    L.acw = (uint32_t*)l.acw.ptr;
+    L.dc = (int*)l.dc.ptr;
+    L.acbits = (int*)l.acbits.ptr;
+    L.blk_off = (int*)l.blk_off.ptr;
+    L.tile_sum = (int*)l.tile_sum.ptr;
+    L.tile_off = (unsigned long long*)l.tile_off.ptr;
+    L.words = (uint32_t*)l.words.ptr;
+    L.chunk_ff = (int*)l.chunk_ff.ptr;
+    L.chunk_off = (unsigned long long*)l.chunk_off.ptr;
+    L.info = (JpegInfo*)l.info.ptr;
+    L.counters = (unsigned*)l.counters.ptr;
 }
 
 // the block count must index with 32-bit ints on the device
 bool geometry_fits(const JpegGeom& g) { return g.nb < (1LL << 30); }
 
-int launch(imop_jpeg_ctx* c, const JpegLaunch& L, cudaStream_t st) {
+int launch(JpegLane& l, const JpegLaunch& L, cudaStream_t st) {
     const cudaError_t e = launch_jpeg_encode(L, st);
     if (e != cudaSuccess) {
-        c->words_dirty = true;
+        l.dirty = true;
         return jcuda(e, "jpeg kernels");
     }
     return IMOP_JPEG_OK;
+}
+
+// the header of (w, h, quality, subsample); its device copy is uploaded on first use
+int header_for(imop_jpeg_ctx* c, int w, int h, int quality, int ss, cudaStream_t st,
+               const std::pair<std::vector<uint8_t>, std::unique_ptr<DevBuf>>** out) {
+    const std::array<int, 4> key = {w, h, quality, ss};
+    auto it = c->headers.find(key);
+    if (it == c->headers.end()) {
+        if (c->headers.size() >= 64) c->headers.clear();  // cudaFree waits for copies still reading them
+        auto& ent = c->headers[key];
+        ent.first = jpeg_header(w, h, quality, ss);
+        ent.second.reset(new DevBuf());
+        cudaError_t e;
+        if ((e = ent.second->ensure(ent.first.size())) != cudaSuccess ||
+            (e = cudaMemcpyAsync(ent.second->ptr, ent.first.data(), ent.first.size(), cudaMemcpyHostToDevice, st)) !=
+                cudaSuccess) {
+            c->headers.erase(key);
+            return jcuda(e, "jpeg header upload");
+        }
+        it = c->headers.find(key);
+    }
+    *out = &it->second;
+    return IMOP_JPEG_OK;
+}
+
+// one frame, device in and out, on stream st with lane l (no host synchronisation)
+int encode_device_on(imop_jpeg_ctx* c, JpegLane& l, const void* d_rgb, int w, int h, int quality, int ss, void* d_out,
+                     size_t out_cap, size_t* d_out_size, cudaStream_t st) {
+    const JpegGeom g = jpeg_geometry(w, h, ss);
+    if (!geometry_fits(g)) return jfail(IMOP_JPEG_ENCODE_FAILED, "frame too large for one encode");
+    const size_t cap = out_cap > 0 ? out_cap : imop_jpeg_max_bytes(w, h);
+    int s;
+    if ((s = prepare(l, g, st))) return s;
+    const std::pair<std::vector<uint8_t>, std::unique_ptr<DevBuf>>* hd = nullptr;
+    if ((s = header_for(c, w, h, quality, ss, st, &hd))) return s;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_out, hd->second->ptr, std::min(cap, hd->first.size()), cudaMemcpyDeviceToDevice, st)) !=
+        cudaSuccess)
+        return jcuda(e, "jpeg header copy");
+    JpegLaunch L;
+    fill_launch(c, l, g, quality, L);
+    L.rgb = (const uint8_t*)d_rgb;
+    L.out = (uint8_t*)d_out;
+    L.base = hd->first.size();
+    L.out_cap = cap;
+    L.size_out = (unsigned long long*)d_out_size;
+    return launch(l, L, st);
 }
 
 }  // namespace
@@ -254,10 +315,15 @@ int imop_jpeg_create(imop_jpeg_t* out_ctx) {
     huff_lookup(kAcLumaBits, kAcLumaVals, hf.ac[0], 256);
     huff_lookup(kAcChromaBits, kAcChromaVals, hf.ac[1], 256);
     if (e == cudaSuccess) e = jpeg_init_constants(cs);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        JpegLane& l = c->lane[k];
+        e = cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaHostAlloc((void**)&l.h_info, sizeof(JpegInfo), cudaHostAllocDefault);
+    }
     if (e == cudaSuccess) e = c->huff.ensure(sizeof(JpegHuff));
     if (e == cudaSuccess) e = cudaMemcpy(c->huff.ptr, &hf, sizeof(JpegHuff), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_info, sizeof(JpegInfo), cudaHostAllocDefault);
     if (e != cudaSuccess) {
         imop_jpeg_destroy(c);
         return jcuda(e, "jpeg context");
@@ -268,10 +334,13 @@ int imop_jpeg_create(imop_jpeg_t* out_ctx) {
 
 int imop_jpeg_destroy(imop_jpeg_t c) {
     if (!c) return IMOP_JPEG_OK;
-    if (c->st) cudaStreamSynchronize(c->st);
-    if (c->last_pending && c->last_stream) cudaStreamSynchronize(c->last_stream);
-    if (c->h_info) cudaFreeHost(c->h_info);
-    if (c->st) cudaStreamDestroy(c->st);
+    cudaDeviceSynchronize();
+    for (auto& l : c->lane) {
+        if (l.h_info) cudaFreeHost(l.h_info);
+        if (l.ev) cudaEventDestroy(l.ev);
+        if (l.st) cudaStreamDestroy(l.st);
+    }
+    if (c->fork) cudaEventDestroy(c->fork);
     delete c;
     return IMOP_JPEG_OK;
 }
@@ -287,48 +356,56 @@ int imop_jpeg_header(int width, int height, int quality, int subsample, uint8_t*
     return (int)h.size();
 }
 
-int imop_jpeg_encode_host(imop_jpeg_t c, const uint8_t* rgb, int width, int height, int bit_depth, int quality,
-                          int subsample, uint8_t* out, size_t* out_size) {
-    if (!c) return jfail(IMOP_JPEG_INTERNAL_ERROR, "null context");
-    int s = validate(rgb, out, width, height, bit_depth, quality);
-    if (s) return s;
-    if (!out_size) return jfail(IMOP_JPEG_NULL_OUTPUT, "null output size");
-    const int ss = std::max(0, std::min(2, subsample));
-    const JpegGeom g = jpeg_geometry(width, height, ss);
+namespace {
+
+// host frame -> lane: validation, input copy, kernels, size read-back queued on the lane's
+// stream (lane.ev marks the size record); the bytes are fetched by host_finish
+int host_enqueue(imop_jpeg_ctx* c, JpegLane& l, const uint8_t* rgb, int w, int h, int quality, int ss, size_t cap,
+                 size_t hdr_bytes) {
+    const JpegGeom g = jpeg_geometry(w, h, ss);
     if (!geometry_fits(g)) return jfail(IMOP_JPEG_ENCODE_FAILED, "frame too large for one encode");
-    const size_t cap = *out_size > 0 ? *out_size : imop_jpeg_max_bytes(width, height);
-    const std::vector<uint8_t> hdr = jpeg_header(width, height, quality, ss);
-    const size_t seg_cap = cap > hdr.size() ? cap - hdr.size() : 0;
-    cudaStream_t st = c->st;
-    if ((s = prepare(c, g, st))) return s;
-    const size_t in_bytes = (size_t)width * height * 3;
+    cudaStream_t st = l.st;
+    int s;
+    if ((s = prepare(l, g, st))) return s;
+    const size_t seg_cap = cap > hdr_bytes ? cap - hdr_bytes : 0;
     const size_t stage = std::min(seg_cap, (size_t)g.words * 8 + 2);
+    const size_t in_bytes = (size_t)w * h * 3;
     cudaError_t e;
-    if ((e = c->rgb.ensure(in_bytes)) != cudaSuccess || (e = c->out.ensure(stage + 1)) != cudaSuccess)
+    if ((e = l.rgb.ensure(in_bytes)) != cudaSuccess || (e = l.out.ensure(stage + 1)) != cudaSuccess)
         return jcuda(e, "jpeg staging allocation");
-    if ((e = cudaMemcpyAsync(c->rgb.ptr, rgb, in_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(l.rgb.ptr, rgb, in_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return jcuda(e, "jpeg input copy");
     JpegLaunch L;
-    fill_launch(c, g, quality, L);
-    L.rgb = (const uint8_t*)c->rgb.ptr;
-    L.out = (uint8_t*)c->out.ptr;
+    fill_launch(c, l, g, quality, L);
+    L.rgb = (const uint8_t*)l.rgb.ptr;
+    L.out = (uint8_t*)l.out.ptr;
     L.base = 0;
     L.out_cap = stage;
     L.size_out = nullptr;
-    if ((s = launch(c, L, st))) return s;
-    if ((e = cudaMemcpyAsync(c->h_info, c->info.ptr, sizeof(JpegInfo), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-        c->words_dirty = true;
+    if ((s = launch(l, L, st))) return s;
+    if ((e = cudaMemcpyAsync(l.h_info, l.info.ptr, sizeof(JpegInfo), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaEventRecord(l.ev, st)) != cudaSuccess) {
+        l.dirty = true;
         return jcuda(e, "jpeg encode");
     }
-    const JpegInfo info = *c->h_info;
-    std::memcpy(out, hdr.data(), std::min(cap, hdr.size()));
-    if (seg_cap > 0 && info.written > 0) {
-        if ((e = cudaMemcpyAsync(out + hdr.size(), c->out.ptr, (size_t)info.written, cudaMemcpyDeviceToHost, st)) !=
-                cudaSuccess ||
-            (e = cudaStreamSynchronize(st)) != cudaSuccess)
-            return jcuda(e, "jpeg output copy");
+    return IMOP_JPEG_OK;
+}
+
+// waits for the lane's size record, writes the header and queues the bytes' copy on the lane's
+// stream; *out_size = min(JPEG size, cap)
+int host_finish(imop_jpeg_ctx* c, JpegLane& l, const std::vector<uint8_t>& hdr, uint8_t* out, size_t cap,
+                size_t* out_size) {
+    cudaError_t e;
+    if ((e = cudaEventSynchronize(l.ev)) != cudaSuccess) {
+        l.dirty = true;
+        return jcuda(e, "jpeg encode");
     }
+    const JpegInfo info = *l.h_info;
+    std::memcpy(out, hdr.data(), std::min(cap, hdr.size()));
+    if (cap > hdr.size() && info.written > 0 &&
+        (e = cudaMemcpyAsync(out + hdr.size(), l.out.ptr, (size_t)info.written, cudaMemcpyDeviceToHost, l.st)) !=
+            cudaSuccess)
+        return jcuda(e, "jpeg output copy");
     c->last = info;
     c->last.jpeg_bytes = hdr.size() + info.stuffed + 2;
     c->last.written = std::min((size_t)c->last.jpeg_bytes, cap);
@@ -337,39 +414,114 @@ int imop_jpeg_encode_host(imop_jpeg_t c, const uint8_t* rgb, int width, int heig
     return IMOP_JPEG_OK;
 }
 
+int ctx_check(imop_jpeg_ctx* c) {
+    if (!c) return jfail(IMOP_JPEG_INTERNAL_ERROR, "null context");
+    int dev = -1;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev != c->device) cudaSetDevice(c->device);
+    return IMOP_JPEG_OK;
+}
+
+}  // namespace
+
+int imop_jpeg_encode_host(imop_jpeg_t c, const uint8_t* rgb, int width, int height, int bit_depth, int quality,
+                          int subsample, uint8_t* out, size_t* out_size) {
+    int s;
+    if ((s = ctx_check(c))) return s;
+    if ((s = validate(rgb, out, width, height, bit_depth, quality))) return s;
+    if (!out_size) return jfail(IMOP_JPEG_NULL_OUTPUT, "null output size");
+    const int ss = std::max(0, std::min(2, subsample));
+    const size_t cap = *out_size > 0 ? *out_size : imop_jpeg_max_bytes(width, height);
+    const std::vector<uint8_t> hdr = jpeg_header(width, height, quality, ss);
+    JpegLane& l = c->lane[0];
+    if ((s = host_enqueue(c, l, rgb, width, height, quality, ss, cap, hdr.size()))) return s;
+    if ((s = host_finish(c, l, hdr, out, cap, out_size))) return s;
+    const cudaError_t e = cudaStreamSynchronize(l.st);
+    return e == cudaSuccess ? IMOP_JPEG_OK : jcuda(e, "jpeg output copy");
+}
+
+int imop_jpeg_encode_host_batch(imop_jpeg_t c, ImopJpegHostFrame* frames, int n) {
+    int s;
+    if ((s = ctx_check(c))) return s;
+    if (n < 0 || (n > 0 && !frames)) return jfail(IMOP_JPEG_NULL_INPUT, "null frame list");
+    int first = IMOP_JPEG_OK;
+    int prev = -1;  // frame whose bytes are still to be fetched
+    std::vector<uint8_t> hdr_prev;
+    int slot = 0;
+    for (int k = 0; k <= n; k++) {
+        int cur = -1;
+        std::vector<uint8_t> hdr;
+        if (k < n) {
+            ImopJpegHostFrame& f = frames[k];
+            f.out_size = 0;
+            f.status = validate(f.rgb, f.out, f.width, f.height, 8, f.quality);
+            if (f.status == IMOP_JPEG_OK) {
+                const int ss = std::max(0, std::min(2, f.subsample));
+                const size_t cap = f.out_cap > 0 ? f.out_cap : imop_jpeg_max_bytes(f.width, f.height);
+                hdr = jpeg_header(f.width, f.height, f.quality, ss);
+                f.status = host_enqueue(c, c->lane[slot], f.rgb, f.width, f.height, f.quality, ss, cap, hdr.size());
+                if (f.status == IMOP_JPEG_OK) cur = k;
+            }
+            if (f.status != IMOP_JPEG_OK && first == IMOP_JPEG_OK) first = f.status;
+        }
+        if (prev >= 0) {  // the previous frame's bytes, while this frame's copy and kernels run
+            ImopJpegHostFrame& f = frames[prev];
+            const size_t cap = f.out_cap > 0 ? f.out_cap : imop_jpeg_max_bytes(f.width, f.height);
+            f.status = host_finish(c, c->lane[slot ^ 1], hdr_prev, f.out, cap, &f.out_size);
+            if (f.status != IMOP_JPEG_OK && first == IMOP_JPEG_OK) first = f.status;
+        }
+        prev = cur;
+        if (cur >= 0) {
+            hdr_prev.swap(hdr);
+            slot ^= 1;
+        }
+    }
+    for (auto& l : c->lane) {
+        const cudaError_t e = cudaStreamSynchronize(l.st);
+        if (e != cudaSuccess && first == IMOP_JPEG_OK) first = jcuda(e, "jpeg output copy");
+    }
+    return first;
+}
+
 int imop_jpeg_encode_device(imop_jpeg_t c, const void* d_rgb, int width, int height, int bit_depth, int quality,
                             int subsample, void* d_out, size_t out_cap, size_t* d_out_size, void* stream) {
-    if (!c) return jfail(IMOP_JPEG_INTERNAL_ERROR, "null context");
-    int s = validate(d_rgb, d_out, width, height, bit_depth, quality);
-    if (s) return s;
+    int s;
+    if ((s = ctx_check(c))) return s;
+    if ((s = validate(d_rgb, d_out, width, height, bit_depth, quality))) return s;
     const int ss = std::max(0, std::min(2, subsample));
-    const JpegGeom g = jpeg_geometry(width, height, ss);
-    if (!geometry_fits(g)) return jfail(IMOP_JPEG_ENCODE_FAILED, "frame too large for one encode");
-    const size_t cap = out_cap > 0 ? out_cap : imop_jpeg_max_bytes(width, height);
     cudaStream_t st = (cudaStream_t)stream;
-    if ((s = prepare(c, g, st))) return s;
+    if ((s = encode_device_on(c, c->lane[0], d_rgb, width, height, quality, ss, d_out, out_cap, d_out_size, st)))
+        return s;
+    c->last_lane = &c->lane[0];
+    c->last_stream = st;
+    c->last_pending = true;
+    return IMOP_JPEG_OK;
+}
+
+int imop_jpeg_encode_device_batch(imop_jpeg_t c, const ImopJpegFrame* frames, int n, void* stream) {
+    int s;
+    if ((s = ctx_check(c))) return s;
+    if (n < 0 || (n > 0 && !frames)) return jfail(IMOP_JPEG_NULL_INPUT, "null frame list");
+    for (int k = 0; k < n; k++)
+        if ((s = validate(frames[k].d_rgb, frames[k].d_out, frames[k].width, frames[k].height, 8, frames[k].quality)))
+            return s;
+    if (n == 0) return IMOP_JPEG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
-    const int key[4] = {width, height, quality, ss};
-    if (!c->hdr_on_device || std::memcmp(key, c->hdr_key, sizeof(key)) != 0) {
-        c->header = jpeg_header(width, height, quality, ss);
-        if ((e = c->hdr.ensure(c->header.size())) != cudaSuccess ||
-            (e = cudaMemcpyAsync(c->hdr.ptr, c->header.data(), c->header.size(), cudaMemcpyHostToDevice, st)) !=
-                cudaSuccess)
-            return jcuda(e, "jpeg header upload");
-        std::memcpy(c->hdr_key, key, sizeof(key));
-        c->hdr_on_device = true;
+    if ((e = cudaEventRecord(c->fork, st)) != cudaSuccess) return jcuda(e, "jpeg batch fork");
+    for (auto& l : c->lane)
+        if ((e = cudaStreamWaitEvent(l.st, c->fork, 0)) != cudaSuccess) return jcuda(e, "jpeg batch fork");
+    int rc = IMOP_JPEG_OK;
+    for (int k = 0; k < n && rc == IMOP_JPEG_OK; k++) {
+        const ImopJpegFrame& f = frames[k];
+        JpegLane& l = c->lane[k & 1];
+        rc = encode_device_on(c, l, f.d_rgb, f.width, f.height, f.quality, std::max(0, std::min(2, f.subsample)),
+                              f.d_out, f.out_cap, f.d_out_size, l.st);
     }
-    const size_t hbytes = std::min(cap, c->header.size());
-    if ((e = cudaMemcpyAsync(d_out, c->hdr.ptr, hbytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
-        return jcuda(e, "jpeg header copy");
-    JpegLaunch L;
-    fill_launch(c, g, quality, L);
-    L.rgb = (const uint8_t*)d_rgb;
-    L.out = (uint8_t*)d_out;
-    L.base = c->header.size();
-    L.out_cap = cap;
-    L.size_out = (unsigned long long*)d_out_size;
-    if ((s = launch(c, L, st))) return s;
+    for (auto& l : c->lane)  // the caller's stream continues after both lanes
+        if ((e = cudaEventRecord(l.ev, l.st)) != cudaSuccess || (e = cudaStreamWaitEvent(st, l.ev, 0)) != cudaSuccess)
+            return jcuda(e, "jpeg batch join");
+    if (rc != IMOP_JPEG_OK) return rc;
+    c->last_lane = &c->lane[(n - 1) & 1];
     c->last_stream = st;
     c->last_pending = true;
     return IMOP_JPEG_OK;
@@ -377,13 +529,13 @@ int imop_jpeg_encode_device(imop_jpeg_t c, const void* d_rgb, int width, int hei
 
 int imop_jpeg_last_size(imop_jpeg_t c, size_t* jpeg_bytes, size_t* written) {
     if (!c) return jfail(IMOP_JPEG_INTERNAL_ERROR, "null context");
-    if (c->last_pending) {
+    if (c->last_pending && c->last_lane) {
         cudaError_t e;
-        if ((e = cudaMemcpyAsync(c->h_info, c->info.ptr, sizeof(JpegInfo), cudaMemcpyDeviceToHost, c->last_stream)) !=
-                cudaSuccess ||
+        if ((e = cudaMemcpyAsync(c->last_lane->h_info, c->last_lane->info.ptr, sizeof(JpegInfo), cudaMemcpyDeviceToHost,
+                                 c->last_stream)) != cudaSuccess ||
             (e = cudaStreamSynchronize(c->last_stream)) != cudaSuccess)
             return jcuda(e, "jpeg size read-back");
-        c->last = *c->h_info;
+        c->last = *c->last_lane->h_info;
         c->last_pending = false;
     }
     if (jpeg_bytes) *jpeg_bytes = (size_t)c->last.jpeg_bytes;

@@ -20,6 +20,17 @@ INVALID_QUALITY, IMAGE_TOO_SMALL, ENCODE_FAILED, DECODE_FAILED, INVALID_DATA = 6
 CUDA_NOT_AVAILABLE, INTERNAL_ERROR = 11, 12
 
 
+class JpegFrame(C.Structure):
+    _fields_ = [("d_rgb", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("quality", C.c_int),
+                ("subsample", C.c_int), ("d_out", C.c_void_p), ("out_cap", C.c_size_t), ("d_out_size", C.c_void_p)]
+
+
+class JpegHostFrame(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("quality", C.c_int),
+                ("subsample", C.c_int), ("out", C.c_void_p), ("out_cap", C.c_size_t), ("out_size", C.c_size_t),
+                ("status", C.c_int)]
+
+
 class JpegError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"jpeg status {code}: {msg}")
@@ -43,6 +54,8 @@ def _L():
             ("imop_jpeg_encode_host", i, [vp, vp, i, i, i, i, i, vp, SP]),
             ("imop_jpeg_encode_device", i, [vp, vp, i, i, i, i, i, vp, sz, vp, vp]),
             ("imop_jpeg_last_size", i, [vp, SP, SP]),
+            ("imop_jpeg_encode_device_batch", i, [vp, C.POINTER(JpegFrame), i, vp]),
+            ("imop_jpeg_encode_host_batch", i, [vp, C.POINTER(JpegHostFrame), i]),
             ("imop_jpeg_last_error_string", C.c_char_p, []),
         ):
             f = getattr(L, name)
@@ -114,6 +127,26 @@ class JpegEncoder:
         without synchronising.  d_size: optional device size_t receiving the bytes written."""
         _check(_L().imop_jpeg_encode_device(self.h, _addr(d_rgb), width, height, 8, quality, subsample,
                                             _addr(d_out), out_cap, _addr(d_size), stream or None))
+
+    def encode_device_batch(self, frames, stream=0):
+        """frames: (d_rgb, width, height, d_out, out_cap, quality, subsample, d_size or None) per
+        frame (addresses or tensors); encoded on two internal streams after `stream` reaches the
+        call, `stream` continues after the last; no host synchronisation."""
+        arr = (JpegFrame * len(frames))()
+        for k, (d_rgb, w, h, d_out, cap, q, ss, d_size) in enumerate(frames):
+            arr[k] = JpegFrame(_addr(d_rgb), w, h, q, ss, _addr(d_out), cap, _addr(d_size))
+        _check(_L().imop_jpeg_encode_device_batch(self.h, arr, len(frames), stream or None))
+
+    def encode_host_batch(self, frames):
+        """frames: (rgb, quality, subsample, out) per frame, rgb an (h, w, 3) u8 array or host
+        tensor, out a u8 array / host tensor with room for the JPEG; returns [(status, size)]."""
+        arr = (JpegHostFrame * len(frames))()
+        for k, (rgb, q, ss, out) in enumerate(frames):
+            h, w = rgb.shape[:2]
+            cap = out.nbytes if isinstance(out, np.ndarray) else out.numel()
+            arr[k] = JpegHostFrame(_addr(rgb), w, h, q, ss, _addr(out), cap, 0, 0)
+        _L().imop_jpeg_encode_host_batch(self.h, arr, len(frames))
+        return [(arr[k].status, arr[k].out_size) for k in range(len(frames))]
 
     def last_size(self):
         """(JPEG bytes, bytes written) of the last encode (synchronises a pending device call)"""

@@ -384,9 +384,9 @@ enum {
     IMOP_JPEG_INTERNAL_ERROR = 12
 };
 typedef struct imop_jpeg_ctx* imop_jpeg_t;
-/* A context owns the device scratch of one encode at a time (grown on demand) and a stream for
- * the host entry point; it serves the device that was current when it was created.  Calls on
- * one context are ordered: do not run it on two streams at once. */
+/* A context owns the device scratch of two encodes in flight (grown on demand) and two internal
+ * streams; it serves the device that was current when it was created.  Calls on one context are
+ * ordered: do not run it on two caller streams at once. */
 int imop_jpeg_create(imop_jpeg_t* out_ctx);
 int imop_jpeg_destroy(imop_jpeg_t ctx);
 /* jpeg_codec::get_max_jpeg_size (src/jpeg_codec/dispatch.cpp:35-41): w*h*9 + 65536 */
@@ -405,6 +405,29 @@ int imop_jpeg_encode_host(imop_jpeg_t ctx, const uint8_t* rgb, int width, int he
  * it; imop_jpeg_last_size reads the sizes on the host (synchronising the stream). */
 int imop_jpeg_encode_device(imop_jpeg_t ctx, const void* d_rgb, int width, int height, int bit_depth, int quality,
                             int subsample, void* d_out, size_t out_cap, size_t* d_out_size, void* stream);
+/* Frames encoded back to back on two internal streams (the tail kernels of one frame overlap the
+ * next frame's transform); they start when `stream` reaches the call and `stream` continues after
+ * the last.  Every frame is validated first; nothing runs when one is invalid. */
+typedef struct {
+    const void* d_rgb;            /* h x w x 3 RGB8 in device memory */
+    int width, height, quality, subsample;
+    void* d_out;                  /* device output, out_cap bytes (0: the default capacity) */
+    size_t out_cap;
+    size_t* d_out_size;           /* device size_t receiving the bytes written, or NULL */
+} ImopJpegFrame;
+int imop_jpeg_encode_device_batch(imop_jpeg_t ctx, const ImopJpegFrame* frames, int n, void* stream);
+/* Host frames with the copies overlapped: frame k's input copy and kernels run while frame k-1's
+ * bytes come back.  Synchronous; each frame gets its own status and size; returns the first
+ * non-zero status. */
+typedef struct {
+    const uint8_t* rgb;           /* h x w x 3 RGB8 (page-locked memory lets the copies overlap) */
+    int width, height, quality, subsample;
+    uint8_t* out;
+    size_t out_cap;               /* 0: the default capacity */
+    size_t out_size;              /* out: bytes written */
+    int status;                   /* out: JpegError value */
+} ImopJpegHostFrame;
+int imop_jpeg_encode_host_batch(imop_jpeg_t ctx, ImopJpegHostFrame* frames, int n);
 int imop_jpeg_last_size(imop_jpeg_t ctx, size_t* jpeg_bytes, size_t* written);
 const char* imop_jpeg_last_error_string(void);
 

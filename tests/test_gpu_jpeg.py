@@ -138,3 +138,49 @@ def test_isp_to_jpeg_on_device(enc):
     total, written = enc.last_size()
     isp.close()
     assert written == want.size and np.array_equal(d_out[:written].cpu().numpy(), want)
+
+
+def test_device_batch_matches_oracle(enc):
+    """frames of different sizes, qualities and subsamplings on the two internal streams, with
+    device size records; the caller's stream continues after the batch"""
+    import torch
+    specs = [(640, 480, 90, 1), (33, 27, 50, 0), (1500, 900, 95, 2), (1006, 758, 10, 1), (8, 8, 100, 0),
+             (2000, 1000, 75, 2), (640, 480, 90, 1)]
+    imgs = [_frame(w, h, 40 + k) for k, (w, h, q, ss) in enumerate(specs)]
+    s = torch.cuda.Stream()
+    d_in = [torch.from_numpy(im).cuda() for im in imgs]
+    caps = [J.max_bytes(w, h) for (w, h, q, ss) in specs]
+    d_out = [torch.full((c,), 0xAB, dtype=torch.uint8, device="cuda") for c in caps]
+    d_size = torch.zeros(len(specs), dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    frames = [(d_in[k], w, h, d_out[k], caps[k], q, ss, d_size[k:k + 1]) for k, (w, h, q, ss) in enumerate(specs)]
+    with torch.cuda.stream(s):
+        enc.encode_device_batch(frames, stream=s.cuda_stream)
+        sizes = d_size.clone()  # ordered after the batch on the caller's stream
+    s.synchronize()
+    for k, (w, h, q, ss) in enumerate(specs):
+        st, want = O.jpeg_encode(imgs[k], q, ss)
+        n = int(sizes[k].item())
+        assert n == want.size, k
+        assert np.array_equal(d_out[k][:n].cpu().numpy(), want), k
+    assert enc.last_size()[0] == int(sizes[-1].item())
+
+
+def test_host_batch_matches_oracle(enc):
+    """pinned and pageable host frames, an invalid frame in the middle (its own status, the others
+    encoded), a truncating capacity"""
+    import torch
+    specs = [(640, 480, 90, 1), (1500, 900, 60, 0), (4, 4, 90, 1), (1006, 758, 85, 2), (333, 217, 30, 1)]
+    frames, wants = [], []
+    for k, (w, h, q, ss) in enumerate(specs):
+        img = _frame(w, h, 70 + k)
+        rgb = torch.from_numpy(img).pin_memory() if k % 2 == 0 else img
+        cap = J.max_bytes(w, h) if k != 4 else 700
+        out = np.zeros(cap, np.uint8)
+        frames.append((rgb, q, ss, out))
+        wants.append(O.jpeg_encode(img, q, ss, cap) if (w >= 8 and h >= 8) else (J.IMAGE_TOO_SMALL, None))
+    res = enc.encode_host_batch(frames)
+    for k, ((st, n), (wst, want)) in enumerate(zip(res, wants)):
+        assert st == wst, k
+        if st == 0:
+            assert n == want.size and np.array_equal(frames[k][3][:n], want), k
