@@ -319,7 +319,9 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
 // ---- compute one staged tile (all threads) ------------------------------------------------------
 // `parity` is buffer b's barrier phase, flipped when its bytes are consumed.  Returns false, the
 // same on every thread, when the staged bytes never arrived (the status word is set).
-template <int TW, int TH, int OUTB, bool FULL>
+// EXTRA = false leaves out the bit-stream unpack and the 3D LUT (a launch without such frames
+// runs a copy of the kernel without their code; they cost ~2 % each in instruction footprint)
+template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true>
 __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bool detect_seeds, uint32_t& parity) {
     using G = TileGeom<TW, TH, OUTB>;
     const FrameParams& fp = sm.fp[b];
@@ -429,7 +431,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                         v1 = row[off + 1];
                         done = true;
                     }
-                } else if (fmt == FMT_PBITS) {
+                } else if (EXTRA && fmt == FMT_PBITS) {
                     // bit stream: each sample from its own bit offset (full tiles stage every
                     // byte the pair needs, and the row buffer has 8 readable bytes past it)
                     const long long bit0 = ((long long)y * W + x) * fp.bd;
@@ -900,7 +902,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
             G0 = u16q(go.x, mv); G1 = u16q(go.y, mv);
             B0 = u16q(bo.x, mv); B1 = u16q(bo.y, mv);
         }
-        if (lut3d_on) {
+        if (EXTRA && lut3d_on) {
             dev::lut3d_apply(fp.lut3d, fp.lut3d_size, mv, R0, G0, B0);
             dev::lut3d_apply(fp.lut3d, fp.lut3d_size, mv, R1, G1, B1);
         }
