@@ -82,7 +82,7 @@ __device__ void stage_item(TileSmem<TW, TH, OUTB>& sm, const BatchLaunch& bl, in
     stage_tile(sm, b, R.x0 + x0, R.y0 + y0, tw, th);
 }
 
-template <int TW, int TH, int OUTB, bool EXTRA>
+template <int TW, int TH, int OUTB, bool EXTRA, int DM>
 __global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_c
         const FrameParams& fp = sm.fp[b];
         const bool full = tile_is_full<TW, TH>(fp, sm.tile[b][0], sm.tile[b][1], sm.tile[b][2], sm.tile[b][3]);
         uint32_t& par = b ? par1 : par0;
-        bool ok = full ? compute_tile<TW, TH, OUTB, true, EXTRA>(sm, b, none, true, par)
-                       : compute_tile<TW, TH, OUTB, false, EXTRA>(sm, b, none, true, par);
+        bool ok = full ? compute_tile<TW, TH, OUTB, true, EXTRA, DM>(sm, b, none, true, par)
+                       : compute_tile<TW, TH, OUTB, false, EXTRA, DM>(sm, b, none, true, par);
         // next_item[b ^ 1] was written before the barriers of compute_tile and is written again two
         // iterations on, after every thread has passed the barriers of the next compute_tile
         const bool more = sm.next_item[b ^ 1] < n_items;
@@ -238,6 +238,19 @@ constexpr int kMaxDevices = 64;
 template <int OUTB>
 struct FusedKernels {
     static constexpr size_t smem = sizeof(TileSmem<kTileW, kTileH, OUTB>);
+    // 0: every format, stage and algorithm; 1..3: no bit stream / 3D LUT, one demosaic algorithm
+    static void (*kernel(int k))(BatchLaunch) {
+        switch (k) {
+            case 1: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_HQLI>;
+            case 2: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_MG>;
+            case 3: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_AMAZE>;
+            default: return fused_batch_kernel<kTileW, kTileH, OUTB, true, 0>;
+        }
+    }
+    static int variant(const BatchLaunch& bl) {
+        if (bl.extra) return 0;
+        return bl.demosaic == DM_HQLI ? 1 : bl.demosaic == DM_MG ? 2 : bl.demosaic == DM_AMAZE ? 3 : 0;
+    }
     // dynamic shared memory opt-in and resident CTAs per SM, once per device
     static int ctas_per_sm[kMaxDevices];
     static int sms[kMaxDevices];
@@ -247,18 +260,14 @@ struct FusedKernels {
         if (e != cudaSuccess) return e;
         if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
         if (!ctas_per_sm[dev]) {
-            e = cudaFuncSetAttribute(fused_batch_kernel<kTileW, kTileH, OUTB, false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(fused_batch_kernel<kTileW, kTileH, OUTB, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            for (int k = 0; k < 4 && e == cudaSuccess; k++)
+                e = cudaFuncSetAttribute(kernel(k), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(dpc_render_kernel<kTileW, kTileH, OUTB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int n = 0, m = 0;
             if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_batch_kernel<kTileW, kTileH, OUTB, true>,
-                                                                  kThreads, smem);
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel(0), kThreads, smem);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return e;
             sms[dev] = m;
@@ -274,10 +283,7 @@ struct FusedKernels {
         if (bl.n_items > 0) {
             if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             const int grid = bl.n_items < limit ? bl.n_items : limit;
-            if (bl.extra)
-                fused_batch_kernel<kTileW, kTileH, OUTB, true><<<grid, kThreads, smem, st>>>(bl);
-            else
-                fused_batch_kernel<kTileW, kTileH, OUTB, false><<<grid, kThreads, smem, st>>>(bl);
+            kernel(variant(bl))<<<grid, kThreads, smem, st>>>(bl);
         }
         cudaStream_t fst = st;
         if (split) {
@@ -325,6 +331,7 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     bl.n_frames = n;
     bl.n_rects = 0;
     bl.extra = 0;
+    bl.demosaic = 0;
     // the frames of one launch come from one context and share its counter
     bl.tile_counter = frames[0].tile_counter;
     for (int f = 0; f < n; f++)
@@ -337,6 +344,8 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
         fp.tiles_y = tiles_along(fp.h, kTileH);
         bl.frames[f] = fp;
         if (fp.fmt == FMT_PBITS || (fp.stages & 32u)) bl.extra = 1;
+        if (f == 0) bl.demosaic = fp.demosaic;
+        else if (fp.demosaic != bl.demosaic) bl.demosaic = 0;
         fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
         add_rect(bl, f, 0, 0, fp.w, fp.h, items);
     }

@@ -27,6 +27,7 @@ struct BatchLaunch {
     int n_items;
     int n_rects;
     int extra;                      // some frame reads a bit stream or applies a 3D LUT
+    int demosaic;                   // the frames' common demosaic algorithm, 0 when they differ
     int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];

@@ -319,9 +319,10 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
 // ---- compute one staged tile (all threads) ------------------------------------------------------
 // `parity` is buffer b's barrier phase, flipped when its bytes are consumed.  Returns false, the
 // same on every thread, when the staged bytes never arrived (the status word is set).
-// EXTRA = false leaves out the bit-stream unpack and the 3D LUT (a launch without such frames
-// runs a copy of the kernel without their code; they cost ~2 % each in instruction footprint)
-template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true>
+// EXTRA = false leaves out the bit-stream unpack and the 3D LUT, DM != 0 fixes the demosaic
+// algorithm: a launch whose frames allow it runs a copy of the kernel without the other paths'
+// code (unused paths cost the kernel through its instruction footprint, ~2 % for the 3D LUT alone)
+template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true, int DM = 0>
 __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bool detect_seeds, uint32_t& parity) {
     using G = TileGeom<TW, TH, OUTB>;
     const FrameParams& fp = sm.fp[b];
@@ -333,7 +334,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const unsigned stages = fp.stages;
     const bool dpc_on = (stages & 2u) != 0;
     const bool adaptive = dpc_on && fp.dpc_mode == 0;
-    const int demosaic = fp.demosaic;
+    const int demosaic = DM ? DM : fp.demosaic;
     const int xo = x0 - 6, yo = y0 - 5;  // orig region origin (xo even)
     const int opw = FULL ? G::F_OPW : (tw + 13) / 2, oh = FULL ? G::F_OH : th + 10;
     const int xb = x0 - 4, yb = y0 - 3;  // bay region origin
