@@ -16,6 +16,7 @@
 
 #include "isp_kernels.h"
 #include "isp_dpc.cuh"
+#include "isp_fused_kernel.cuh"
 #include "isp_tile.cuh"
 
 namespace imop {
@@ -43,87 +44,6 @@ __global__ void tone_table_kernel(int mode, const float* lut, const float* knots
     }
     int q = dev::ftoi(dev::fadd(dev::fmul(t, 255.0f), 0.5f));
     out[v] = (uint8_t)dev::clampi(q, 0, 255);
-}
-
-// ---------------------------------------------------------------------------------------------
-// Persistent tile kernel: CTA c starts with item c of the launch's tile list (the tiles of each
-// rectangle in raster order) and then claims items from the launch's counter, one item ahead of
-// the one it stages.  Warp 0 stages the next item into the other raw buffer before the CTA
-// computes the current one, so the copy of tile k+1 overlaps the arithmetic of tile k.
-
-// rectangle of item `item`: the last rectangle starting at or before it
-__device__ __forceinline__ int item_rect(const BatchLaunch& bl, int item) {
-    int lo = 0, hi = bl.n_rects - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bl.rect_start[mid] <= item) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// warp 0: copy the item's frame parameters into slot b and start staging its raw rows
-template <int TW, int TH, int OUTB>
-__device__ void stage_item(TileSmem<TW, TH, OUTB>& sm, const BatchLaunch& bl, int item, int b) {
-    const int lane = threadIdx.x & 31;
-    const int r = item_rect(bl, item);
-    const TileRect& R = bl.rects[r];
-    const FrameParams& src = bl.frames[R.frame];
-    static_assert(sizeof(FrameParams) % 4 == 0, "frame parameters copy as words");
-    const int* s = reinterpret_cast<const int*>(&src);
-    int* d = reinterpret_cast<int*>(&sm.fp[b]);
-    for (int k = lane; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
-    int t = item - bl.rect_start[r];
-    int ty = t / R.tiles_x, tx = t - ty * R.tiles_x;
-    int x0, tw, y0, th;
-    tile_span(R.w, TW, R.tiles_x, tx, x0, tw);
-    tile_span(R.h, TH, R.tiles_y, ty, y0, th);
-    __syncwarp();
-    stage_tile(sm, b, R.x0 + x0, R.y0 + y0, tw, th);
-}
-
-template <int TW, int TH, int OUTB, bool EXTRA, int DM>
-__global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_constant__ BatchLaunch bl) {
-    extern __shared__ __align__(16) uint8_t dsm[];
-    auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
-    const int n_items = bl.n_items;
-    if ((int)blockIdx.x >= n_items) return;
-    tile_init(sm);
-    uint32_t par0 = 0, par1 = 0;
-    const Overrides none{nullptr, nullptr, 0};
-    // lane 0 of warp 0 holds the item claimed after the staged one (its counter read completes
-    // while the CTA computes)
-    int claimed = 0;
-    if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
-    if (threadIdx.x < 32) stage_item(sm, bl, blockIdx.x, 0);
-    __syncthreads();
-    int b = 0;
-    while (true) {
-        if (threadIdx.x < 32) {
-            const int next = __shfl_sync(0xffffffffu, claimed, 0);
-            if (next < n_items) {
-                if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
-                stage_item(sm, bl, next, b ^ 1);
-            }
-            if (threadIdx.x == 0) sm.next_item[b ^ 1] = next;
-        }
-        const FrameParams& fp = sm.fp[b];
-        const bool full = tile_is_full<TW, TH>(fp, sm.tile[b][0], sm.tile[b][1], sm.tile[b][2], sm.tile[b][3]);
-        uint32_t& par = b ? par1 : par0;
-        bool ok = full ? compute_tile<TW, TH, OUTB, true, EXTRA, DM>(sm, b, none, true, par)
-                       : compute_tile<TW, TH, OUTB, false, EXTRA, DM>(sm, b, none, true, par);
-        // next_item[b ^ 1] was written before the barriers of compute_tile and is written again two
-        // iterations on, after every thread has passed the barriers of the next compute_tile
-        const bool more = sm.next_item[b ^ 1] < n_items;
-        if (!ok) {
-            // leave no bulk copy in flight into this CTA's shared memory
-            if (more && (reinterpret_cast<uintptr_t>(sm.fp[b ^ 1].in) & 15) == 0)
-                wait_bar(&sm.bar[b ^ 1], b ? par0 : par1);
-            return;
-        }
-        if (!more) return;
-        b ^= 1;
-    }
 }
 
 // Defect-chain fix-up (adaptive mode) in two launches: the raster-order resolution, one warp
@@ -231,6 +151,21 @@ cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaS
     return cudaGetLastError();
 }
 
+cudaError_t launch_fused_spec_u8(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_u16(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_p10(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_p12(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+
+cudaError_t launch_fused_spec(int fmt, int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
+    switch (fmt) {
+        case FMT_U8: return launch_fused_spec_u8(dm, bl, grid, smem, st);
+        case FMT_U16: return launch_fused_spec_u16(dm, bl, grid, smem, st);
+        case FMT_P10: return launch_fused_spec_p10(dm, bl, grid, smem, st);
+        case FMT_P12: return launch_fused_spec_p12(dm, bl, grid, smem, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 namespace {
 
 constexpr int kMaxDevices = 64;
@@ -241,10 +176,10 @@ struct FusedKernels {
     // 0: every format, stage and algorithm; 1..3: no bit stream / 3D LUT, one demosaic algorithm
     static void (*kernel(int k))(BatchLaunch) {
         switch (k) {
-            case 1: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_HQLI>;
-            case 2: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_MG>;
-            case 3: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_AMAZE>;
-            default: return fused_batch_kernel<kTileW, kTileH, OUTB, true, 0>;
+            case 1: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_HQLI, 0>;
+            case 2: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_MG, 0>;
+            case 3: return fused_batch_kernel<kTileW, kTileH, OUTB, false, DM_AMAZE, 0>;
+            default: return fused_batch_kernel<kTileW, kTileH, OUTB, true, 0, 0>;
         }
     }
     static int variant(const BatchLaunch& bl) {
@@ -283,7 +218,11 @@ struct FusedKernels {
         if (bl.n_items > 0) {
             if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             const int grid = bl.n_items < limit ? bl.n_items : limit;
-            kernel(variant(bl))<<<grid, kThreads, smem, st>>>(bl);
+            if (OUTB == 3 && bl.simple && !bl.extra && bl.demosaic && bl.fmt >= FMT_U8 && bl.fmt <= FMT_P12) {
+                if ((e = launch_fused_spec(bl.fmt, bl.demosaic, bl, grid, smem, st)) != cudaSuccess) return e;
+            } else {
+                kernel(variant(bl))<<<grid, kThreads, smem, st>>>(bl);
+            }
         }
         cudaStream_t fst = st;
         if (split) {
@@ -332,6 +271,8 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     bl.n_rects = 0;
     bl.extra = 0;
     bl.demosaic = 0;
+    bl.fmt = -1;
+    bl.simple = 1;
     // the frames of one launch come from one context and share its counter
     bl.tile_counter = frames[0].tile_counter;
     for (int f = 0; f < n; f++)
@@ -344,8 +285,13 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
         fp.tiles_y = tiles_along(fp.h, kTileH);
         bl.frames[f] = fp;
         if (fp.fmt == FMT_PBITS || (fp.stages & 32u)) bl.extra = 1;
-        if (f == 0) bl.demosaic = fp.demosaic;
-        else if (fp.demosaic != bl.demosaic) bl.demosaic = 0;
+        if (f == 0) bl.demosaic = fp.demosaic, bl.fmt = fp.fmt;
+        if (fp.demosaic != bl.demosaic) bl.demosaic = 0;
+        if (fp.fmt != bl.fmt) bl.fmt = -1;
+        // the stage configuration the per-format kernels fix at compile time
+        const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
+                            (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
+        if (!simple) bl.simple = 0;
         fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
         add_rect(bl, f, 0, 0, fp.w, fp.h, items);
     }

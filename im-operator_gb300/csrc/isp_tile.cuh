@@ -320,9 +320,12 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
 // `parity` is buffer b's barrier phase, flipped when its bytes are consumed.  Returns false, the
 // same on every thread, when the staged bytes never arrived (the status word is set).
 // EXTRA = false leaves out the bit-stream unpack and the 3D LUT, DM != 0 fixes the demosaic
-// algorithm: a launch whose frames allow it runs a copy of the kernel without the other paths'
-// code (unused paths cost the kernel through its instruction footprint, ~2 % for the 3D LUT alone)
-template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true, int DM = 0>
+// algorithm, SPEC != 0 fixes the input format (SPEC & 7 = format + 1) and, with SPEC & 8, the
+// common stage configuration (adaptive or no defect correction, no polynomial shading, white
+// balance on the mosaic, RGB8 output): a launch whose frames allow it runs a copy of the kernel
+// without the other paths' code (unused paths cost the kernel through its instruction footprint:
+// ~2 % for the 3D LUT alone, ~5 % for all of them on a C2 batch)
+template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true, int DM = 0, int SPEC = 0>
 __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bool detect_seeds, uint32_t& parity) {
     using G = TileGeom<TW, TH, OUTB>;
     const FrameParams& fp = sm.fp[b];
@@ -333,7 +336,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned stages = fp.stages;
     const bool dpc_on = (stages & 2u) != 0;
-    const bool adaptive = dpc_on && fp.dpc_mode == 0;
+    const bool adaptive = dpc_on && ((SPEC & 8) || fp.dpc_mode == 0);
     const int demosaic = DM ? DM : fp.demosaic;
     const int xo = x0 - 6, yo = y0 - 5;  // orig region origin (xo even)
     const int opw = FULL ? G::F_OPW : (tw + 13) / 2, oh = FULL ? G::F_OH : th + 10;
@@ -390,7 +393,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     int* orig = reinterpret_cast<int*>(sm.regB);
     const bool bl_on = (stages & 1u) != 0;
     const bool bl_int = fp.bl_int != 0;
-    const int fmt = fp.fmt;
+    const int fmt = (SPEC & 7) ? (SPEC & 7) - 1 : fp.fmt;
     constexpr int OPW_LOOP = FULL ? G::F_OPW : G::OPW;
     constexpr int OH_LOOP = FULL ? G::F_OH : G::ORH;
     for (int s = tid; s < OH_LOOP * OPW_LOOP; s += kThreads) {
@@ -487,8 +490,8 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     // keeps one row parity and one column pair, so its colour constants stay in registers
     int local_mod = 0;
     const bool lsc_grid = (stages & 4u) && fp.lsc_mode == 0;
-    const bool lsc_poly = (stages & 4u) && fp.lsc_mode == 1;
-    const bool wb_bayer = (stages & 8u) && fp.stage_order == 0;
+    const bool lsc_poly = !(SPEC & 8) && (stages & 4u) && fp.lsc_mode == 1;
+    const bool wb_bayer = (stages & 8u) && ((SPEC & 8) || fp.stage_order == 0);
     const bool need_align = fp.need_align != 0;
     const int thr = fp.dpc_thr;
     const float2 h5 = make_float2(0.5f, 0.5f);
@@ -542,7 +545,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                         int nb[8] = {n0.y, n1.y, n2.y, n3.y, n4.y, n5.y, n6.y, n7.y};
                         j1 = dev::dpc_apply(c.y, nb, 0xFFu, thr);
                     }
-                } else if (dpc_on && fp.dpc_mode == 1 && __ldg(fp.map_row_ptr + y + 1) > __ldg(fp.map_row_ptr + y)) {
+                } else if (!(SPEC & 8) && dpc_on && fp.dpc_mode == 1 && __ldg(fp.map_row_ptr + y + 1) > __ldg(fp.map_row_ptr + y)) {
                     int sv = map_lookup(fp, x, y);
                     if (sv >= 0) j0 = sv;
                     sv = map_lookup(fp, x + 1, y);
@@ -634,7 +637,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
                     if (x >= 2 && x < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x); if (sv >= 0) j0 = sv; }
                     if (x + 1 >= 2 && x + 1 < W - 2) { int sv = find_override(ov.idx, ov.val, ov.n, y * W + x + 1); if (sv >= 0) j1 = sv; }
                 }
-            } else if (yin && dpc_on && fp.dpc_mode == 1 && y >= 2 && y < H - 2 &&
+            } else if (!(SPEC & 8) && yin && dpc_on && fp.dpc_mode == 1 && y >= 2 && y < H - 2 &&
                        __ldg(fp.map_row_ptr + y + 1) > __ldg(fp.map_row_ptr + y)) {
                 if (x >= 2 && x < W - 2) { int sv = map_lookup(fp, x, y); if (sv >= 0) j0 = sv; }
                 if (x + 1 >= 2 && x + 1 < W - 2) { int sv = map_lookup(fp, x + 1, y); if (sv >= 0) j1 = sv; }
@@ -868,11 +871,11 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     uint8_t* outs = sm.regB;
     const int bpc = fp.out_bpc;
     const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
-    const int out_format = fp.out_format;
+    const int out_format = (SPEC & 8) ? 0 : fp.out_format;
     const bool border_tile = !FULL && (x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2);
     const bool ccm_on = (stages & 16u) != 0;
     const bool lut3d_on = (stages & 32u) != 0;
-    const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
+    const bool wb_rgb = !(SPEC & 8) && (stages & 8u) && fp.stage_order == 1;
     const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
     // RGB WB, CCM and tone of pair (x, x+1) in tile row r, staged for the stores
     auto finish = [&](int r, int y, int pc, int x, int R0, int G0, int B0, int R1, int G1, int B1) {

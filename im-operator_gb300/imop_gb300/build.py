@@ -45,7 +45,7 @@ def _deps_newer(obj, src):
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh", ".inl"))]
     hdrs.append(os.path.join(REPO, "include", "imop_isp.h"))
     return any(os.path.getmtime(p) > t for p in [src] + hdrs)
 
