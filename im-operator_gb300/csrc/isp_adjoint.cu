@@ -105,13 +105,14 @@ __device__ float amaze_df(const AdjSmem& sm, const TileCtx& t, int x, int y, flo
     return wh * gh + wv * gv;
 }
 
+template <int DM>
 __device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, float v[3]) {
     const AdjFrame& f = *t.f;
     const float* u = sm.u;
     v[0] = v[1] = v[2] = 0.0f;
     const bool ar = t.at_r(x, y), ab = t.at_b(x, y), rrow = (y & 1) == t.po.r_row;
     const int i = t.ui(x, y);
-    if (f.demosaic == DM_HQLI) {
+    if (DM == DM_HQLI) {
         if (x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) return;
         float n4 = u[i - 1] + u[i + 1] + u[i - kUW] + u[i + kUW];
         float d4 = u[i - kUW - 1] + u[i - kUW + 1] + u[i + kUW - 1] + u[i + kUW + 1];
@@ -152,13 +153,14 @@ __device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, f
 //   AMAZE, source p in [1,w-1)^2 (else only green <- G(p)): green <- G(p); R/B site: own <- u(p),
 //     other <- G(p) + 1/4 sum over diagonals d of (u(d) - G(d)); G site: R, B <- G(p) + 1/2 sum of
 //     (u - G) over the horizontal or the vertical pair.
+template <int DM>
 __device__ void demosaic_gather(AdjSmem& sm, const TileCtx& t) {
     const AdjFrame& f = *t.f;
     const int gw = t.tw + 2, gh = t.th + 2;
     const float* V0 = sm.gV[0];
     const float* V1 = sm.gV[1];
     const float* V2 = sm.gV[2];
-    const bool hqli = f.demosaic == DM_HQLI;
+    const bool hqli = DM == DM_HQLI;
     const int lo = hqli ? 2 : 1;  // sources with colour interpolation: [lo, w - lo) x [lo, h - lo)
     for (int s = threadIdx.x; s < gw * gh; s += kAdjThreads) {
         const int r = s / gw, c = s - r * gw;
@@ -243,7 +245,7 @@ __device__ __forceinline__ int adj_raw(const AdjFrame& f, const uint8_t* in, int
 }
 
 // forward planes of one tile: raw, u (apron 3), green (apron 1); gradient planes cleared
-template <bool BACKWARD>
+template <bool BACKWARD, int DM>
 __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
     const AdjFrame& f = *t.f;
     const int tid = threadIdx.x;
@@ -291,14 +293,14 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
         for (int s = tid; s < 3 * kVH * kVW; s += kAdjThreads) (&sm.gV[0][0])[s] = 0.0f;
     }
     __syncthreads();
-    if (f.demosaic == DM_AMAZE || BACKWARD) {
+    if (DM == DM_AMAZE || BACKWARD) {
         const int gw = t.tw + 2, gh = t.th + 2;
         for (int s = tid; s < gw * gh; s += kAdjThreads) {
             int r = s / gw, c = s - r * gw;
             int x = t.xg + c, y = t.yg + r;
             int j = r * kGW + c;
             float g = -1.0f;
-            if (f.demosaic == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
+            if (DM == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
                 g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
             sm.G[j] = g;
             if (BACKWARD) sm.gG[j] = 0.0f;
@@ -323,7 +325,7 @@ struct RegAcc {
 };
 
 // forward (+ adjoint) of the tile's own pixels
-template <bool BACKWARD>
+template <bool BACKWARD, int DM>
 __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaunch& L, RegAcc& acc) {
     const AdjFrame& f = *t.f;
     const float mvf = (float)f.mv;
@@ -345,7 +347,7 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
         dev::border_source(x, y, f.w, f.h, f.border_mode, sx, sy);
         float v[3], rgb[3], pre[3], o[3], tt[3], fr[3];
         int idx[3];
-        demosaic_df(sm, t, sx, sy, v);
+        demosaic_df<DM>(sm, t, sx, sy, v);
 #pragma unroll
         for (int k = 0; k < 3; k++) rgb[k] = clampf(v[k], 0.0f, mvf);
 #pragma unroll
@@ -408,12 +410,13 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
 }
 
 // adjoint of the green plane into u, then of u into the per-pixel parameters
+template <int DM>
 __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     const AdjFrame& f = *t.f;
     const int tid = threadIdx.x;
     const float mvf = (float)f.mv;
     __syncthreads();
-    if (f.demosaic == DM_AMAZE) {
+    if (DM == DM_AMAZE) {
         const int gw = t.tw + 2, gh = t.th + 2;
         for (int s = tid; s < gw * gh; s += kAdjThreads) {
             int r = s / gw, c = s - r * gw;
@@ -515,7 +518,8 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     }
 }
 
-template <bool BACKWARD>
+// DM: the launch's demosaic algorithm (every frame of a launch shares the descriptor)
+template <bool BACKWARD, int DM>
 __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
     extern __shared__ __align__(16) uint8_t dsm[];
     AdjSmem& sm = *reinterpret_cast<AdjSmem*>(dsm);
@@ -541,12 +545,12 @@ __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_co
         TileCtx t;
         tile_of(L, item, fi, t);
         const uint8_t* in = L.raw + (size_t)fi * L.f.in_bytes;
-        tile_forward<BACKWARD>(sm, t, in);
-        tile_pixels<BACKWARD>(sm, t, fi, L, acc);
+        tile_forward<BACKWARD, DM>(sm, t, in);
+        tile_pixels<BACKWARD, DM>(sm, t, fi, L, acc);
         if (BACKWARD) {
             __syncthreads();
-            demosaic_gather(sm, t);
-            tile_back_planes(sm, t, acc);
+            demosaic_gather<DM>(sm, t);
+            tile_back_planes<DM>(sm, t, acc);
         }
         else __syncthreads();
     }
@@ -612,11 +616,13 @@ cudaError_t adj_grid_limit(int& limit) {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (!cached[dev]) {
         const int smem = (int)sizeof(AdjSmem);
-        if ((e = cudaFuncSetAttribute(adjoint_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
-            (e = cudaFuncSetAttribute(adjoint_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+        if ((e = cudaFuncSetAttribute(adjoint_kernel<true, DM_AMAZE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+            (e = cudaFuncSetAttribute(adjoint_kernel<false, DM_AMAZE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+            (e = cudaFuncSetAttribute(adjoint_kernel<true, DM_HQLI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||
+            (e = cudaFuncSetAttribute(adjoint_kernel<false, DM_HQLI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
             return e;
         int n = 0, sms = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel<true>, kAdjThreads, smem)) ||
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel<true, DM_AMAZE>, kAdjThreads, smem)) ||
             (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
             return e;
         cached[dev] = sms * (n > 0 ? n : 1);
@@ -627,12 +633,18 @@ cudaError_t adj_grid_limit(int& limit) {
 
 cudaError_t launch_adjoint(const AdjLaunch& L, bool backward, int grid, float* d_grad, float* d_loss, cudaStream_t st) {
     const size_t smem = sizeof(AdjSmem);
+    const bool hqli = L.f.demosaic == DM_HQLI;
     if (backward) {
-        adjoint_kernel<true><<<grid, kAdjThreads, smem, st>>>(L);
+        if (hqli)
+            adjoint_kernel<true, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
+        else
+            adjoint_kernel<true, DM_AMAZE><<<grid, kAdjThreads, smem, st>>>(L);
         reduce_partials_kernel<<<(L.n_params + 1 + 255) / 256, 256, 0, st>>>(L.partials, grid, L.n_params, d_grad,
                                                                             d_loss);
+    } else if (hqli) {
+        adjoint_kernel<false, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
     } else {
-        adjoint_kernel<false><<<grid, kAdjThreads, smem, st>>>(L);
+        adjoint_kernel<false, DM_AMAZE><<<grid, kAdjThreads, smem, st>>>(L);
     }
     return cudaGetLastError();
 }
