@@ -14,6 +14,9 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "isp_kernels.h"
 #include "isp_dpc.cuh"
 #include "isp_fused_kernel.cuh"
@@ -326,13 +329,32 @@ int fused_grid_limit(int out_bpc) {
     return e == cudaSuccess ? limit : 0;
 }
 
+// which kernel instantiation a frame can use: frames with equal keys share the most specialised
+// one (output channel width, bit-stream / 3D-LUT paths, demosaic algorithm, stage set, format)
+static long long instantiation_key(const FrameParams& fp) {
+    const bool extra = fp.fmt == FMT_PBITS || (fp.stages & 32u);
+    const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
+                        (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
+    if (extra) return (long long)fp.out_bpc << 32;
+    return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
+           (simple ? fp.fmt + 1 : 0);
+}
+
 cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st) {
-    // one launch per run of at most kBatchInline frames sharing an output channel width
+    // frames grouped by instantiation (stable: frames keep their order inside a group), then one
+    // launch per run of at most kBatchInline frames of a group
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::vector<long long> key(n);
+    for (int i = 0; i < n; i++) key[i] = instantiation_key(frames[i]);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    std::vector<FrameParams> grouped(n);
+    for (int i = 0; i < n; i++) grouped[i] = frames[order[i]];
     int i = 0;
     while (i < n) {
         int j = i + 1;
-        while (j < n && j - i < kBatchInline && frames[j].out_bpc == frames[i].out_bpc) j++;
-        cudaError_t e = launch_batch_group(frames + i, j - i, st);
+        while (j < n && j - i < kBatchInline && key[order[j]] == key[order[i]]) j++;
+        cudaError_t e = launch_batch_group(grouped.data() + i, j - i, st);
         if (e != cudaSuccess) return e;
         i = j;
     }
