@@ -154,17 +154,18 @@ cudaError_t launch_map_resolve(const FrameParams& fp, const MapPlan& plan, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused_spec_u8(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
-cudaError_t launch_fused_spec_u16(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
-cudaError_t launch_fused_spec_p10(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
-cudaError_t launch_fused_spec_p12(int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_u8(int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_u16(int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_p10(int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_fused_spec_p12(int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
 
-cudaError_t launch_fused_spec(int fmt, int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
+cudaError_t launch_fused_spec(int fmt, int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem,
+                              cudaStream_t st) {
     switch (fmt) {
-        case FMT_U8: return launch_fused_spec_u8(dm, bl, grid, smem, st);
-        case FMT_U16: return launch_fused_spec_u16(dm, bl, grid, smem, st);
-        case FMT_P10: return launch_fused_spec_p10(dm, bl, grid, smem, st);
-        case FMT_P12: return launch_fused_spec_p12(dm, bl, grid, smem, st);
+        case FMT_U8: return launch_fused_spec_u8(dm, lite, bl, grid, smem, st);
+        case FMT_U16: return launch_fused_spec_u16(dm, lite, bl, grid, smem, st);
+        case FMT_P10: return launch_fused_spec_p10(dm, lite, bl, grid, smem, st);
+        case FMT_P12: return launch_fused_spec_p12(dm, lite, bl, grid, smem, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -222,7 +223,8 @@ struct FusedKernels {
             if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             const int grid = bl.n_items < limit ? bl.n_items : limit;
             if (OUTB == 3 && bl.simple && !bl.extra && bl.demosaic && bl.fmt >= FMT_U8 && bl.fmt <= FMT_P12) {
-                if ((e = launch_fused_spec(bl.fmt, bl.demosaic, bl, grid, smem, st)) != cudaSuccess) return e;
+                if ((e = launch_fused_spec(bl.fmt, bl.demosaic, bl.no_dpc_lsc != 0, bl, grid, smem, st)) != cudaSuccess)
+                    return e;
             } else {
                 kernel(variant(bl))<<<grid, kThreads, smem, st>>>(bl);
             }
@@ -276,6 +278,7 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     bl.demosaic = 0;
     bl.fmt = -1;
     bl.simple = 1;
+    bl.no_dpc_lsc = 1;
     // the frames of one launch come from one context and share its counter
     bl.tile_counter = frames[0].tile_counter;
     for (int f = 0; f < n; f++)
@@ -295,6 +298,7 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
         const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
                             (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
         if (!simple) bl.simple = 0;
+        if (fp.stages & 6u) bl.no_dpc_lsc = 0;
         fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
         add_rect(bl, f, 0, 0, fp.w, fp.h, items);
     }
@@ -336,8 +340,9 @@ static long long instantiation_key(const FrameParams& fp) {
     const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
                         (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
     if (extra) return (long long)fp.out_bpc << 32;
+    const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
-           (simple ? fp.fmt + 1 : 0);
+           (lite ? (1 << 12) : 0) | (simple ? fp.fmt + 1 : 0);
 }
 
 cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st) {

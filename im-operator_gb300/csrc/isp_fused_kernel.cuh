@@ -115,7 +115,9 @@ cudaError_t launch_fused_variant(const BatchLaunch& bl, int grid, size_t smem, c
 // mosaic, RGB8 output)
 constexpr int spec_of_format(int fmt) { return (fmt + 1) | 8; }
 
-// launch of the per-format instantiation for the frames' format and algorithm (isp_fused_spec_*.cu)
-cudaError_t launch_fused_spec(int fmt, int dm, const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st);
+// launch of the per-format instantiation for the frames' format and algorithm (isp_fused_spec_*.cu);
+// lite: none of the frames corrects defects or lens shading
+cudaError_t launch_fused_spec(int fmt, int dm, bool lite, const BatchLaunch& bl, int grid, size_t smem,
+                              cudaStream_t st);
 
 }  // namespace imop

@@ -30,6 +30,7 @@ struct BatchLaunch {
     int demosaic;                   // the frames' common demosaic algorithm, 0 when they differ
     int fmt;                        // the frames' common input format, -1 when they differ
     int simple;                     // every frame has the common stage configuration (per-format kernels)
+    int no_dpc_lsc;                 // no frame corrects defects or lens shading
     int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];

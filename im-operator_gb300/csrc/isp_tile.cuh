@@ -322,7 +322,8 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
 // EXTRA = false leaves out the bit-stream unpack and the 3D LUT, DM != 0 fixes the demosaic
 // algorithm, SPEC != 0 fixes the input format (SPEC & 7 = format + 1) and, with SPEC & 8, the
 // common stage configuration (adaptive or no defect correction, no polynomial shading, white
-// balance on the mosaic, RGB8 output): a launch whose frames allow it runs a copy of the kernel
+// balance on the mosaic, RGB8 output); SPEC & 16 also leaves out defect correction and lens
+// shading (frames that use neither): a launch whose frames allow it runs a copy of the kernel
 // without the other paths' code (unused paths cost the kernel through its instruction footprint:
 // ~2 % for the 3D LUT alone, ~5 % for all of them on a C2 batch)
 template <int TW, int TH, int OUTB, bool FULL, bool EXTRA = true, int DM = 0, int SPEC = 0>
@@ -335,7 +336,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const PatternOffsets po = pattern_offsets(fp.pattern);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned stages = fp.stages;
-    const bool dpc_on = (stages & 2u) != 0;
+    const bool dpc_on = !(SPEC & 16) && (stages & 2u) != 0;
     const bool adaptive = dpc_on && ((SPEC & 8) || fp.dpc_mode == 0);
     const int demosaic = DM ? DM : fp.demosaic;
     const int xo = x0 - 6, yo = y0 - 5;  // orig region origin (xo even)
@@ -355,7 +356,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         for (int k = tid * 4; k < n; k += kThreads * 4)
             *reinterpret_cast<uint32_t*>(sm.tone8 + k) = __ldg(reinterpret_cast<const uint32_t*>(fp.tone8 + k));
     }
-    if ((stages & 4u) && fp.lsc_mode == 0) {
+    if (!(SPEC & 16) && (stages & 4u) && fp.lsc_mode == 0) {
         for (int c = tid; c < 2 * bpw; c += kThreads) {
             int x = min(max(xb + c, 0), W - 1);
             float gx_f = __fdiv_rn(dev::fmul((float)x, (float)(fp.gw - 1)), (float)(W - 1));
@@ -489,7 +490,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     // warp-rows: a warp takes 32 pair columns of one row; with two column blocks every warp
     // keeps one row parity and one column pair, so its colour constants stay in registers
     int local_mod = 0;
-    const bool lsc_grid = (stages & 4u) && fp.lsc_mode == 0;
+    const bool lsc_grid = !(SPEC & 16) && (stages & 4u) && fp.lsc_mode == 0;
     const bool lsc_poly = !(SPEC & 8) && (stages & 4u) && fp.lsc_mode == 1;
     const bool wb_bayer = (stages & 8u) && ((SPEC & 8) || fp.stage_order == 0);
     const bool need_align = fp.need_align != 0;
