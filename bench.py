@@ -15,6 +15,7 @@ is needed between steps.
   plain       the same batch through the plain per-operator kernels (one kernel per stage)
   cpu_baseline  the CPU oracle (plain-C restatement of the reference's CPU path) on a bounded
               sample of the same frames on this host's cores
+  c3          one 5320x4600 frame per step (8-bit and 12-bit), per-frame time and HBM GB/s
   jpeg        the step's RGB8 frames encoded to baseline JPEG (quality 90, 4:2:0, the reference's
               JpegParams defaults), byte-identical to the reference's encoder: device-resident
               frames, the host entry point with pinned buffers (e2e), RAW -> JPEG on the device
@@ -53,6 +54,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-c4", action="store_true", help="skip the uneven 96-frame batch leg")
     ap.add_argument("--no-jpeg", action="store_true", help="skip the JPEG encode leg")
+    ap.add_argument("--no-c3", action="store_true", help="skip the per-frame 5320x4600 leg")
     return ap.parse_args()
 
 
@@ -237,6 +239,48 @@ def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_dev
                                "sample": f"{done} frames in {dt:.1f} s (plain-C restatement of the reference's "
                                          f"single-threaded baseline encoder)"}
     enc.close()
+    return out
+
+
+def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind):
+    """C3: one 5320x4600 frame per step, 8-bit and 12-bit u16 (BL, RGB WB, HQLI, linear tone ->
+    RGB8), device-resident, one recorded single-frame batch per step; per-frame time and HBM
+    GB/s against the measured peak.  Inputs and outputs of one frame (98 / 122 MB) are larger than
+    half the L2; a 256 MB buffer is rewritten between steps so each step starts cold."""
+    import imop_gb300 as I
+    from imop_gb300 import abi, workloads
+    out = {}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    sh = stream.cuda_stream
+    for pl in workloads.c3_pipelines():
+        isp = I.Isp(pl)
+        d_in = torch.from_numpy(workloads.c3_frame(pl, 0)).cuda()
+        d_out = torch.empty(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+        desc = [(None, d_in.data_ptr(), d_out.data_ptr())]
+        for _ in range(max(3, args.warmup)):
+            isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+        total = 0.0
+        steps = max(1, min(args.steps, 5))
+        for _ in range(steps):
+            flush.fill_(1)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            total += max_over_ranks(ev0.elapsed_time(ev1))
+        isp.sync_status(sh)
+        isp.close()
+        ms = total / steps
+        alg = pl.input_bytes() + pl.output_bytes()
+        gbs = alg / (ms / 1e3) / 1e9
+        out[f"{pl.bit_depth}bit"] = {"ms_per_frame": round(ms, 4), "Mpix/s": round(world * pl.pixels / (ms / 1e3) / 1e6, 1),
+                                     "gbs_algorithmic": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+                                     "bytes_per_frame": alg}
+    out["config"] = ("C3: 5320x4600 RGGB, an 8-bit frame and a 12-bit u16 frame, BL, RGB-order WB, HQLI, "
+                     "linear tone -> RGB8; L2 flushed between steps; peak " + peak_kind)
     return out
 
 
@@ -458,6 +502,11 @@ def main():
         jpeg = jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device,
                         d_out.view(B, H_C2, W_C2, 3), h_out, pk, pk_kind)
 
+    c3 = None
+    if not args.no_c3:
+        pk, pk_kind = peaks()
+        c3 = c3_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
+
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world)
@@ -509,6 +558,8 @@ def main():
         line["c4"] = c4
     if jpeg is not None:
         line["jpeg"] = jpeg
+    if c3 is not None:
+        line["c3"] = c3
     if rank == 0 and not args.no_cpu:
         rate, done, dt = cpu_oracle_rate(pl, host_frames[: max(1, args.cpu_sample_frames)])
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",

@@ -296,7 +296,7 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
         if (fp.fmt != bl.fmt) bl.fmt = -1;
         // the stage configuration the per-format kernels fix at compile time
         const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
-                            (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
+                            fp.out_format == 0 && fp.out_bpc == 1;
         if (!simple) bl.simple = 0;
         if (fp.stages & 6u) bl.no_dpc_lsc = 0;
         fixup |= (fp.stages & 2u) && fp.dpc_mode == 0;
@@ -338,7 +338,7 @@ int fused_grid_limit(int out_bpc) {
 static long long instantiation_key(const FrameParams& fp) {
     const bool extra = fp.fmt == FMT_PBITS || (fp.stages & 32u);
     const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
-                        (!(fp.stages & 8u) || fp.stage_order == 0) && fp.out_format == 0 && fp.out_bpc == 1;
+                        fp.out_format == 0 && fp.out_bpc == 1;
     if (extra) return (long long)fp.out_bpc << 32;
     const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |

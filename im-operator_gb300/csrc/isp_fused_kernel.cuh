@@ -111,8 +111,7 @@ cudaError_t launch_fused_variant(const BatchLaunch& bl, int grid, size_t smem, c
 }
 
 // SPEC of the per-format units: the input format plus one, and the flag of the common stage
-// configuration (adaptive or no defect correction, no polynomial shading, white balance on the
-// mosaic, RGB8 output)
+// configuration (adaptive or no defect correction, no polynomial shading, RGB8 output)
 constexpr int spec_of_format(int fmt) { return (fmt + 1) | 8; }
 
 // launch of the per-format instantiation for the frames' format and algorithm (isp_fused_spec_*.cu);

@@ -321,8 +321,8 @@ __device__ void stage_tile(TileSmem<TW, TH, OUTB>& sm, int b, int x0, int y0, in
 // same on every thread, when the staged bytes never arrived (the status word is set).
 // EXTRA = false leaves out the bit-stream unpack and the 3D LUT, DM != 0 fixes the demosaic
 // algorithm, SPEC != 0 fixes the input format (SPEC & 7 = format + 1) and, with SPEC & 8, the
-// common stage configuration (adaptive or no defect correction, no polynomial shading, white
-// balance on the mosaic, RGB8 output); SPEC & 16 also leaves out defect correction and lens
+// common stage configuration (adaptive or no defect correction, no polynomial shading, RGB8
+// output; white balance in either order); SPEC & 16 also leaves out defect correction and lens
 // shading (frames that use neither): a launch whose frames allow it runs a copy of the kernel
 // without the other paths' code (unused paths cost the kernel through its instruction footprint:
 // ~2 % for the 3D LUT alone, ~5 % for all of them on a C2 batch)
@@ -492,7 +492,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     int local_mod = 0;
     const bool lsc_grid = !(SPEC & 16) && (stages & 4u) && fp.lsc_mode == 0;
     const bool lsc_poly = !(SPEC & 8) && (stages & 4u) && fp.lsc_mode == 1;
-    const bool wb_bayer = (stages & 8u) && ((SPEC & 8) || fp.stage_order == 0);
+    const bool wb_bayer = (stages & 8u) && fp.stage_order == 0;
     const bool need_align = fp.need_align != 0;
     const int thr = fp.dpc_thr;
     const float2 h5 = make_float2(0.5f, 0.5f);
@@ -876,7 +876,7 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
     const bool border_tile = !FULL && (x0 < 2 || x0 + tw > W - 2 || y0 < 2 || y0 + th > H - 2);
     const bool ccm_on = (stages & 16u) != 0;
     const bool lut3d_on = (stages & 32u) != 0;
-    const bool wb_rgb = !(SPEC & 8) && (stages & 8u) && fp.stage_order == 1;
+    const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
     const float wr = fp.wb_rgb[0], wg = fp.wb_rgb[1], wbl = fp.wb_rgb[2];
     // RGB WB, CCM and tone of pair (x, x+1) in tile row r, staged for the stores
     auto finish = [&](int r, int y, int pc, int x, int R0, int G0, int B0, int R1, int G1, int B1) {
