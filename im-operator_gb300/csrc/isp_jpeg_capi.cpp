@@ -162,6 +162,8 @@ struct JpegLane {
     bool dirty = true;             // the word stream and the counters must be zero before a launch
     cudaStream_t st = nullptr;     // batch stream of the lane
     cudaEvent_t ev = nullptr;      // join / info-ready marker
+    cudaEvent_t ev_last = nullptr; // end of the lane's last use, on whichever stream it ran
+    bool used = false;
     JpegInfo* h_info = nullptr;    // pinned
 };
 
@@ -180,6 +182,16 @@ struct imop_jpeg_ctx {
 };
 
 namespace {
+
+// a use of the lane's scratch on stream st starts after its previous use, whatever stream that
+// ran on (the host calls use the lane's own stream, the device calls the caller's)
+cudaError_t lane_acquire(JpegLane& l, cudaStream_t st) {
+    return l.used ? cudaStreamWaitEvent(st, l.ev_last, 0) : cudaSuccess;
+}
+cudaError_t lane_release(JpegLane& l, cudaStream_t st) {
+    l.used = true;
+    return cudaEventRecord(l.ev_last, st);
+}
 
 // grows a lane's scratch to the geometry; clears its word stream and counters when (re)allocated
 int prepare(JpegLane& l, const JpegGeom& g, cudaStream_t st) {
@@ -275,10 +287,11 @@ int encode_device_on(imop_jpeg_ctx* c, JpegLane& l, const void* d_rgb, int w, in
     if (!geometry_fits(g)) return jfail(IMOP_JPEG_ENCODE_FAILED, "frame too large for one encode");
     const size_t cap = out_cap > 0 ? out_cap : imop_jpeg_max_bytes(w, h);
     int s;
+    cudaError_t e;
+    if ((e = lane_acquire(l, st)) != cudaSuccess) return jcuda(e, "jpeg lane");
     if ((s = prepare(l, g, st))) return s;
     const std::pair<std::vector<uint8_t>, std::unique_ptr<DevBuf>>* hd = nullptr;
     if ((s = header_for(c, w, h, quality, ss, st, &hd))) return s;
-    cudaError_t e;
     if ((e = cudaMemcpyAsync(d_out, hd->second->ptr, std::min(cap, hd->first.size()), cudaMemcpyDeviceToDevice, st)) !=
         cudaSuccess)
         return jcuda(e, "jpeg header copy");
@@ -289,7 +302,8 @@ int encode_device_on(imop_jpeg_ctx* c, JpegLane& l, const void* d_rgb, int w, in
     L.base = hd->first.size();
     L.out_cap = cap;
     L.size_out = (unsigned long long*)d_out_size;
-    return launch(l, L, st);
+    if ((s = launch(l, L, st))) return s;
+    return (e = lane_release(l, st)) == cudaSuccess ? IMOP_JPEG_OK : jcuda(e, "jpeg lane");
 }
 
 }  // namespace
@@ -320,6 +334,7 @@ int imop_jpeg_create(imop_jpeg_t* out_ctx) {
         JpegLane& l = c->lane[k];
         e = cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.ev_last, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaHostAlloc((void**)&l.h_info, sizeof(JpegInfo), cudaHostAllocDefault);
     }
     if (e == cudaSuccess) e = c->huff.ensure(sizeof(JpegHuff));
@@ -338,6 +353,7 @@ int imop_jpeg_destroy(imop_jpeg_t c) {
     for (auto& l : c->lane) {
         if (l.h_info) cudaFreeHost(l.h_info);
         if (l.ev) cudaEventDestroy(l.ev);
+        if (l.ev_last) cudaEventDestroy(l.ev_last);
         if (l.st) cudaStreamDestroy(l.st);
     }
     if (c->fork) cudaEventDestroy(c->fork);
@@ -366,11 +382,12 @@ int host_enqueue(imop_jpeg_ctx* c, JpegLane& l, const uint8_t* rgb, int w, int h
     if (!geometry_fits(g)) return jfail(IMOP_JPEG_ENCODE_FAILED, "frame too large for one encode");
     cudaStream_t st = l.st;
     int s;
+    cudaError_t e;
+    if ((e = lane_acquire(l, st)) != cudaSuccess) return jcuda(e, "jpeg lane");
     if ((s = prepare(l, g, st))) return s;
     const size_t seg_cap = cap > hdr_bytes ? cap - hdr_bytes : 0;
     const size_t stage = std::min(seg_cap, (size_t)g.words * 8 + 2);
     const size_t in_bytes = (size_t)w * h * 3;
-    cudaError_t e;
     if ((e = l.rgb.ensure(in_bytes)) != cudaSuccess || (e = l.out.ensure(stage + 1)) != cudaSuccess)
         return jcuda(e, "jpeg staging allocation");
     if ((e = cudaMemcpyAsync(l.rgb.ptr, rgb, in_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
@@ -406,6 +423,7 @@ int host_finish(imop_jpeg_ctx* c, JpegLane& l, const std::vector<uint8_t>& hdr, 
         (e = cudaMemcpyAsync(out + hdr.size(), l.out.ptr, (size_t)info.written, cudaMemcpyDeviceToHost, l.st)) !=
             cudaSuccess)
         return jcuda(e, "jpeg output copy");
+    if ((e = lane_release(l, l.st)) != cudaSuccess) return jcuda(e, "jpeg lane");
     c->last = info;
     c->last.jpeg_bytes = hdr.size() + info.stuffed + 2;
     c->last.written = std::min((size_t)c->last.jpeg_bytes, cap);

@@ -184,3 +184,24 @@ def test_host_batch_matches_oracle(enc):
         assert st == wst, k
         if st == 0:
             assert n == want.size and np.array_equal(frames[k][3][:n], want), k
+
+
+def test_device_then_host_calls_without_sync(enc):
+    """a device encode on the caller's stream followed at once by host encodes on the same
+    context: the context orders the uses of its scratch across streams"""
+    import torch
+    big = _frame(3000, 2000, 5)
+    small = _frame(640, 480, 6)
+    st_big, want_big = O.jpeg_encode(big, 90, 1)
+    st_small, want_small = O.jpeg_encode(small, 80, 0)
+    s = torch.cuda.Stream()
+    d_in = torch.from_numpy(big).cuda()
+    cap = J.max_bytes(3000, 2000)
+    d_out = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        enc.encode_device(d_in, 3000, 2000, d_out, cap, 90, 1, stream=s.cuda_stream)
+        got = enc.encode(small, 80, 0)  # no synchronisation with s in between
+        assert np.array_equal(got, want_small)
+    s.synchronize()
+    assert np.array_equal(d_out[:want_big.size].cpu().numpy(), want_big)
