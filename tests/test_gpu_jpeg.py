@@ -205,3 +205,30 @@ def test_device_then_host_calls_without_sync(enc):
         assert np.array_equal(got, want_small)
     s.synchronize()
     assert np.array_equal(d_out[:want_big.size].cpu().numpy(), want_big)
+
+
+@pytest.mark.parametrize("kind", ["noise_8k_q100_444", "q1", "flat0", "flat255", "spike", "stripes_odd"])
+def test_extremes_match_oracle(enc, kind):
+    """the bit-stream capacity bound at full load (8K noise at quality 100, 4:4:4: about 250 MB of
+    output), all-zero AC blocks (quality 1), flat frames, a lone bright pixel, and odd sizes with
+    one-pixel stripes (runs of 16 zeros and long codes)"""
+    rng = np.random.default_rng(len(kind))
+    if kind == "noise_8k_q100_444":
+        img, q, ss = rng.integers(0, 256, (4320, 7680, 3), dtype=np.uint8), 100, 0
+    elif kind == "q1":
+        img, q, ss = _frame(1001, 777, 3), 1, 1
+    elif kind in ("flat0", "flat255"):
+        img, q, ss = np.full((64, 80, 3), 0 if kind == "flat0" else 255, np.uint8), 90, 2
+    elif kind == "spike":
+        img = np.zeros((48, 48, 3), np.uint8)
+        img[21, 30] = (255, 255, 255)
+        q, ss = 100, 1
+    else:
+        img = np.zeros((259, 333, 3), np.uint8)
+        img[:, ::2] = 255
+        img[::3, :, 1] = 17
+        q, ss = 97, 0
+    st, want = O.jpeg_encode(img, q, ss)
+    assert st == 0
+    got = enc.encode(img, q, ss)
+    assert got.size == want.size and np.array_equal(got, want)
