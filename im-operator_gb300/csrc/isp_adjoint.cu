@@ -554,37 +554,38 @@ __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_co
         }
         else __syncthreads();
     }
-    if (!BACKWARD) return;
-    // block reduction of the register accumulators, warps in order
-    float vals[17];
+    if constexpr (BACKWARD) {
+        // block reduction of the register accumulators, warps in order
+        float vals[17];
 #pragma unroll
-    for (int k = 0; k < 4; k++) vals[k] = acc.bl[k];
+        for (int k = 0; k < 4; k++) vals[k] = acc.bl[k];
 #pragma unroll
-    for (int k = 0; k < 3; k++) vals[4 + k] = acc.wb[k];
+        for (int k = 0; k < 3; k++) vals[4 + k] = acc.wb[k];
 #pragma unroll
-    for (int k = 0; k < 9; k++) vals[7 + k] = acc.ccm[k];
-    vals[16] = acc.loss;
-    const int lane = tid & 31, warp = tid >> 5;
+        for (int k = 0; k < 9; k++) vals[7 + k] = acc.ccm[k];
+        vals[16] = acc.loss;
+        const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-    for (int k = 0; k < 17; k++) {
-        float v = vals[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sm.red[warp][k] = v;
-    }
-    __syncthreads();
-    float* part = L.partials + (size_t)blockIdx.x * (L.n_params + 1);
-    if (tid < 17) {
-        float v = 0.0f;
-        for (int w = 0; w < kAdjThreads / 32; w++) v += sm.red[w][tid];
-        if (tid < 16) part[tid] = v;
-        else part[L.n_params] = v;
-    }
-    const int ng = 4 * L.f.gw * L.f.gh;
-    for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = sm.acc_grid[k];
-    for (int k = tid; k < 33; k += kAdjThreads) {
-        float v = sm.acc_knots[k];
-        for (int l = 0; l < 32; l++) v += sm.knot_lane[k * 32 + l];
-        part[16 + ng + k] = v;
+        for (int k = 0; k < 17; k++) {
+            float v = vals[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) sm.red[warp][k] = v;
+        }
+        __syncthreads();
+        float* part = L.partials + (size_t)blockIdx.x * (L.n_params + 1);
+        if (tid < 17) {
+            float v = 0.0f;
+            for (int w = 0; w < kAdjThreads / 32; w++) v += sm.red[w][tid];
+            if (tid < 16) part[tid] = v;
+            else part[L.n_params] = v;
+        }
+        const int ng = 4 * L.f.gw * L.f.gh;
+        for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = sm.acc_grid[k];
+        for (int k = tid; k < 33; k += kAdjThreads) {
+            float v = sm.acc_knots[k];
+            for (int l = 0; l < 32; l++) v += sm.knot_lane[k * 32 + l];
+            part[16 + ng + k] = v;
+        }
     }
 }
 

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <cstring>
 
 #include "../../include/imop_isp.h"
@@ -61,7 +62,7 @@ const char* cuda_device_name() {
     cudaDeviceProp prop;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "";
-    std::strncpy(name, prop.name, sizeof(name) - 1);
+    std::snprintf(name, sizeof(name), "%s", prop.name);
     return name;
 }
 
