@@ -537,11 +537,11 @@ def main():
         "hbm_frac": round(world * args.steps * B * alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
         "fused_equals_plain": parity_ok,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": 383124736, "peak_kind": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": 382078976, "peak_kind": peak_kind,
                      "kernel": "fused_batch_kernel: one persistent launch over the step's frames "
                                "(timed with its seed reset and the two defect fix-up launches)",
                      "bytes_per_launch": B * alg_bytes, "launch_ms": round(per_launch_ms, 4),
-                     "traffic_note": "ncu: 383.1 MB DRAM read+write per launch of 8 frames (profiles/)"},
+                     "traffic_note": "ncu: 382.1 MB DRAM read+write per launch of 8 frames (profiles/)"},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
     }
