@@ -155,7 +155,8 @@ def cpu_jpeg_rate(rgb, quality, subsample, max_seconds=20.0):
     return done * w * h / dt / 1e6, done, dt
 
 
-def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device, d_rgb, h_rgb, peak, peak_kind):
+def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device, d_rgb, h_rgb, isp, h_raw, peak,
+             peak_kind):
     """Baseline JPEG encode of the step's B RGB8 frames (4024x3032, quality 90, 4:2:0)."""
     from imop_gb300 import jpeg as J
     B = d_rgb.shape[0]
@@ -216,6 +217,17 @@ def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_dev
         host_all()
     ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3) / steps
     barrier()
+    # RAW -> JPEG end to end: pinned RAW12P frames in, pinned JPEG bytes out, the RGB8 frames
+    # staying in HBM (chunks of two frames: raw copies, fused batch, encoder batch, JPEG copies)
+    raw_frames = [(None, h_raw[i], q, ss, h_jpg[i]) for i in range(B)]
+    rj_sizes = J.raw_to_jpeg_host_batch(isp, enc, raw_frames)
+    rj_same = bool(rj_sizes == sizes and (h_jpg[0, :sizes[0]].numpy() == d_jpg[0, :sizes[0]].cpu().numpy()).all())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        J.raw_to_jpeg_host_batch(isp, enc, raw_frames)
+    ms_rj = max_over_ranks((time.perf_counter() - t0) * 1e3) / steps
+    barrier()
     px = B * w * h
     jpeg_bytes = sum(sizes)
     alg = B * w * h * 3 + jpeg_bytes  # RGB8 in, JPEG out
@@ -231,6 +243,10 @@ def jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_dev
                    "api": "imop_jpeg_encode_host_batch (pinned RGB8 in, pinned JPEG out)"},
            "raw_to_jpeg": {"value": round(world * px / (ms_chain / 1e3) / 1e6, 2), "unit": "Mpix/s",
                            "ms_per_step": round(ms_chain, 4)},
+           "raw_to_jpeg_e2e": {"value": round(world * px / (ms_rj / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                               "ms_per_step": round(ms_rj, 4), "h2d_bytes_per_step": int(h_raw.numel()),
+                               "d2h_bytes_per_step": jpeg_bytes, "bytes_equal_device_chain": rj_same,
+                               "api": "imop_isp_run_host_jpeg_batch (pinned RAW12P in, pinned JPEG out)"},
            "config": "4024x3032 RGB8 from the fused ISP step, quality 90, 4:2:0, bytes equal to "
                      "jpeg_codec::process_encode_baseline"}
     if rank == 0 and not args.no_cpu:
@@ -477,7 +493,7 @@ def main():
     ms_e2e = None
     if not args.no_e2e:
         # end to end through the host-buffer batch call: pinned frames, copies in, kernels and
-        # copies out pipelined over three device slots; synchronous, so wall-clock timed
+        # copies out pipelined over four device slots; synchronous, so wall-clock timed
         for _ in range(max(1, args.warmup // 2)):
             isp.run_host_batch(host_batch)
         barrier()
@@ -500,7 +516,7 @@ def main():
         if args.no_e2e:  # the host frames of the JPEG e2e leg are the ISP's outputs
             isp.run_host_batch(host_batch)
         jpeg = jpeg_leg(args, torch, stream, barrier, max_over_ranks, world, rank, step_device,
-                        d_out.view(B, H_C2, W_C2, 3), h_out, pk, pk_kind)
+                        d_out.view(B, H_C2, W_C2, 3), h_out, isp, h_in, pk, pk_kind)
 
     c3 = None
     if not args.no_c3:

@@ -97,6 +97,23 @@ struct HostPipeline {
     ~HostPipeline();
 };
 
+// Device slots, streams and events of the RAW -> JPEG host batch.  Chunks of frames alternate
+// between two slots; per chunk: raw copies in (s_in), one fused batch launch (s_isp), the
+// encoder's device batch and the size read-back (s_jpg; the encoder runs on its own two lanes
+// behind it), JPEG bytes out once their sizes are on the host (s_out).  A slot holds a chunk's
+// frames back to back, each at a 256-byte aligned offset.
+struct RawJpegPipe {
+    static constexpr int kSlots = 2;
+    static constexpr int kChunkFrames = 4;
+    static constexpr long long kChunkPixels = 25000000;  // two 4024 x 3032 frames
+    DevBuf raw[kSlots], rgb[kSlots], jpg[kSlots], size[kSlots];
+    size_t* h_size[kSlots] = {nullptr, nullptr};  // page-locked copies of a chunk's JPEG sizes
+    cudaStream_t s_in = nullptr, s_isp = nullptr, s_jpg = nullptr, s_out = nullptr;
+    cudaEvent_t in_done[kSlots] = {}, isp_done[kSlots] = {}, jpg_done[kSlots] = {}, out_done[kSlots] = {};
+    bool ready = false;
+    ~RawJpegPipe();
+};
+
 int set_error(int code, const char* msg);
 int cuda_fail(cudaError_t e, const char* what);
 int validate_params(const ImopIspParams* p);
@@ -125,6 +142,7 @@ struct imop_isp_ctx {
     imop::TableCache cache;                        // batch parameter tables
     imop::BatchScratch batch;                      // batch defect-chain scratch
     imop::HostPipeline pipe;                       // run_host_batch slots and streams
+    imop::RawJpegPipe rawjpeg;                     // run_host_jpeg_batch slots and streams
     imop::BatchGraph graph;                        // last recorded batch
     cudaStream_t aux = nullptr;                    // table builds and graph capture
     imop::DevBuf adj_partials;                     // adjoint per-CTA partial sums

@@ -4,6 +4,7 @@
     data = enc.encode(rgb, quality=90, subsample=1)             # host (h, w, 3) u8 -> bytes array
     n = enc.encode_device(d_rgb, w, h, d_out, cap, stream=s)    # device in, device out, no sync
     enc.last_size()                                             # (jpeg bytes, written)
+    raw_to_jpeg_host_batch(isp, enc, [(None, raw, 90, 1, out)])  # host RAW -> host JPEG via HBM
 
 The bytes are those of jpeg_codec::process_encode_baseline for the same frame, quality and
 subsampling (0 = 4:4:4, 1 = 4:2:0, 2 = 4:2:2).  Status codes are jpeg_codec::JpegError values;
@@ -29,6 +30,11 @@ class JpegHostFrame(C.Structure):
     _fields_ = [("rgb", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("quality", C.c_int),
                 ("subsample", C.c_int), ("out", C.c_void_p), ("out_cap", C.c_size_t), ("out_size", C.c_size_t),
                 ("status", C.c_int)]
+
+
+class RawJpegFrame(C.Structure):
+    _fields_ = [("params", C.c_void_p), ("raw", C.c_void_p), ("quality", C.c_int), ("subsample", C.c_int),
+                ("out", C.c_void_p), ("out_cap", C.c_size_t), ("out_size", C.c_size_t)]
 
 
 class JpegError(RuntimeError):
@@ -57,6 +63,7 @@ def _L():
             ("imop_jpeg_encode_device_batch", i, [vp, C.POINTER(JpegFrame), i, vp]),
             ("imop_jpeg_encode_host_batch", i, [vp, C.POINTER(JpegHostFrame), i]),
             ("imop_jpeg_last_error_string", C.c_char_p, []),
+            ("imop_isp_run_host_jpeg_batch", i, [vp, vp, C.POINTER(RawJpegFrame), i]),
         ):
             f = getattr(L, name)
             f.restype, f.argtypes = res, args
@@ -153,3 +160,22 @@ class JpegEncoder:
         a, b = C.c_size_t(0), C.c_size_t(0)
         _check(_L().imop_jpeg_last_size(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+def raw_to_jpeg_host_batch(isp, enc, frames):
+    """RAW host frames -> JPEG host bytes through an ISP context (imop_gb300.Isp) and an encoder
+    (imop_isp_run_host_jpeg_batch); the RGB8 frames stay on the device.  frames: (Pipeline or
+    None, raw, quality, subsample, out) per frame, out a u8 array or host tensor with room for
+    the JPEG (its size is the capacity).  Synchronous; returns the bytes written per frame and
+    raises imop_gb300.ImopError on a non-zero status."""
+    from . import check
+    arr = (RawJpegFrame * max(1, len(frames)))()
+    keep = []
+    for k, (pl, raw, q, ss, out) in enumerate(frames):
+        cp = pl.to_c() if pl is not None else None
+        keep.append(cp)
+        cap = out.nbytes if isinstance(out, np.ndarray) else out.numel()
+        arr[k] = RawJpegFrame(C.addressof(cp) if cp is not None else None, _addr(raw), q, ss, _addr(out), cap, 0)
+    check(_L().imop_isp_run_host_jpeg_batch(isp.h, enc.h, arr, len(frames)))
+    del keep
+    return [arr[k].out_size for k in range(len(frames))]

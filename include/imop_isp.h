@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define IMOP_ISP_ABI_VERSION 3
+#define IMOP_ISP_ABI_VERSION 4
 
 /* ---- status codes (0..6 == imop::DemosaicError) ---------------------------------- */
 enum {
@@ -225,8 +225,9 @@ enum {
 int imop_isp_batch_submit(imop_isp_t ctx, const ImopFrameDesc* frames, int n, unsigned flags, void* stream);
 
 /* Host frames (the drop-in call shape of demosaic_cuda_batch): copies in, fused kernel and
- * copies out are pipelined over three device slots and three streams, so the transfers of one
- * frame overlap the kernels of its neighbours.  Page-locked host buffers overlap fully; pageable
+ * copies out are pipelined over four device slots and separate streams for the copies in, the
+ * tile kernels, the defect fix-up and the copies out, so the transfers of one frame overlap the
+ * kernels of its neighbours.  Page-locked host buffers overlap fully; pageable
  * ones are copied synchronously by the CUDA runtime.  Synchronous; returns the device status. */
 int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
 
@@ -430,6 +431,24 @@ typedef struct {
 int imop_jpeg_encode_host_batch(imop_jpeg_t ctx, ImopJpegHostFrame* frames, int n);
 int imop_jpeg_last_size(imop_jpeg_t ctx, size_t* jpeg_bytes, size_t* written);
 const char* imop_jpeg_last_error_string(void);
+
+/* ---- RAW host frames to JPEG host bytes ----------------------------------------------- */
+/* The two drop-ins chained without the RGB8 frame leaving the device: the bytes of
+ * imop_isp_run_host followed by imop_jpeg_encode_host on its output, for every frame.  Frames
+ * go in chunks (up to 4 frames, about 25 Mpix) through one fused batch launch and one encoder
+ * device batch each; the raw copies of the next chunk and the JPEG copies of the previous one
+ * overlap them.  The parameters must select IMOP_OUT_RGB8.  Every frame is validated first
+ * (nothing runs when one is invalid); synchronous; returns an IMOP_ERR_* status, the device
+ * status of the ISP (as imop_isp_sync_status) included. */
+typedef struct {
+    const ImopIspParams* params;  /* this frame's parameters; NULL = the ISP context's */
+    const void* raw;              /* host input frame (page-locked memory lets the copies overlap) */
+    int quality, subsample;       /* as imop_jpeg_encode_host */
+    uint8_t* out;                 /* host JPEG bytes */
+    size_t out_cap;               /* 0: the default capacity (imop_jpeg_max_bytes) */
+    size_t out_size;              /* out: bytes written, min(JPEG size, capacity) */
+} ImopRawJpegFrame;
+int imop_isp_run_host_jpeg_batch(imop_isp_t isp, imop_jpeg_t jpeg, ImopRawJpegFrame* frames, int n);
 
 /* ---- misc --------------------------------------------------------------------------- */
 const char* imop_last_error_string(void);

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_function():
     assert len(names) >= 20
     for n in names:
         assert hasattr(L, n), f"{n} declared in include/imop_isp.h but not exported"
-    assert L.imop_abi_version() == 3
+    assert L.imop_abi_version() == 4
 
 
 def _validate(pl_or_none):
