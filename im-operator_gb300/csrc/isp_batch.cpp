@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <initializer_list>
 #include <vector>
 
 #include "../../include/imop_isp.h"
@@ -320,19 +321,12 @@ int submit_plain(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaStream_t s
 
 }  // namespace
 
-HostPipeline::~HostPipeline() {
-    if (!ready) return;
-    cudaStreamDestroy(s_in);
-    cudaStreamDestroy(s_comp[0]);
-    cudaStreamDestroy(s_comp[1]);
-    cudaStreamDestroy(s_fix);
-    cudaStreamDestroy(s_out);
-    for (int i = 0; i < kSlots; i++) {
-        cudaEventDestroy(in_done[i]);
-        cudaEventDestroy(main_done[i]);
-        cudaEventDestroy(fix_done[i]);
-        cudaEventDestroy(out_done[i]);
-    }
+HostPipeline::~HostPipeline() {  // also after a set-up that failed half way
+    for (cudaStream_t st : {s_in, s_comp[0], s_comp[1], s_fix, s_out})
+        if (st) cudaStreamDestroy(st);
+    for (int i = 0; i < kSlots; i++)
+        for (cudaEvent_t ev : {in_done[i], main_done[i], fix_done[i], out_done[i]})
+            if (ev) cudaEventDestroy(ev);
 }
 
 BatchGraph::~BatchGraph() {
@@ -410,20 +404,16 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
     HostPipeline& P = ctx->pipe;
     cudaError_t e;
     if (!P.ready) {
+        // handles made by an earlier attempt that failed half way are kept, not made again
         int lo = 0, hi = 0;  // hi: the greatest priority (numerically lowest)
-        if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi)) ||
-            (e = cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking)) ||
-            (e = cudaStreamCreateWithFlags(&P.s_comp[0], cudaStreamNonBlocking)) ||
-            (e = cudaStreamCreateWithFlags(&P.s_comp[1], cudaStreamNonBlocking)) ||
-            (e = cudaStreamCreateWithPriority(&P.s_fix, cudaStreamNonBlocking, hi)) ||
-            (e = cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking)))
+        if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi))) return cuda_fail(e, "create streams");
+        for (cudaStream_t* st : {&P.s_in, &P.s_comp[0], &P.s_comp[1], &P.s_out})
+            if (!*st && (e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking))) return cuda_fail(e, "create streams");
+        if (!P.s_fix && (e = cudaStreamCreateWithPriority(&P.s_fix, cudaStreamNonBlocking, hi)))
             return cuda_fail(e, "create streams");
         for (int i = 0; i < HostPipeline::kSlots; i++) {
-            if ((e = cudaEventCreateWithFlags(&P.in_done[i], cudaEventDisableTiming)) ||
-                (e = cudaEventCreateWithFlags(&P.main_done[i], cudaEventDisableTiming)) ||
-                (e = cudaEventCreateWithFlags(&P.fix_done[i], cudaEventDisableTiming)) ||
-                (e = cudaEventCreateWithFlags(&P.out_done[i], cudaEventDisableTiming)))
-                return cuda_fail(e, "create events");
+            for (cudaEvent_t* ev : {&P.in_done[i], &P.main_done[i], &P.fix_done[i], &P.out_done[i]})
+                if (!*ev && (e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming))) return cuda_fail(e, "create events");
             if ((rc = ensure_fixup(P.fix[i], 1 << 16))) return rc;
         }
         P.ready = true;
