@@ -59,6 +59,17 @@ def test_validation_codes_follow_the_reference():
     assert _validate(pl) == abi.ERR_INVALID_ARGUMENT
 
 
+def test_raw_to_jpeg_argument_checks_without_device():
+    """the host checks of imop_isp_run_host_jpeg_batch come before any device work"""
+    from imop_gb300 import jpeg as J
+    f = J._L().imop_isp_run_host_jpeg_batch
+    assert f(None, None, None, 0) == abi.ERR_NULL_INPUT
+    fake = C.c_void_p(1)  # never dereferenced: the frame checks fail first
+    assert f(fake, fake, None, -1) == abi.ERR_INVALID_ARGUMENT
+    assert f(fake, fake, None, 0) == abi.OK
+    assert f(fake, fake, None, 2) == abi.ERR_NULL_INPUT
+
+
 def test_params_default_and_sizes():
     L = I.lib()
     p = abi.IspParams()
