@@ -112,7 +112,9 @@ extern "C" int imop_isp_run_host_jpeg_batch(imop_isp_t isp, imop_jpeg_t jpeg, Im
             if (rc) return rc;
             const long long fpx = (long long)fr[i].p->width * fr[i].p->height;
             const int in_chunk = chunk_begin.empty() ? 0 : i - chunk_begin.back();
-            if (chunk_begin.empty() || in_chunk == RawJpegPipe::kChunkFrames || px + fpx > RawJpegPipe::kChunkPixels) {
+            // the first chunk is half as large: less to copy before the first launch can start
+            const long long limit = RawJpegPipe::kChunkPixels / (chunk_begin.size() == 1 ? 2 : 1);
+            if (chunk_begin.empty() || in_chunk == RawJpegPipe::kChunkFrames || px + fpx > limit) {
                 chunk_begin.push_back(i);
                 raw = rgb = jpg = 0;
                 px = 0;

@@ -435,9 +435,9 @@ const char* imop_jpeg_last_error_string(void);
 /* ---- RAW host frames to JPEG host bytes ----------------------------------------------- */
 /* The two drop-ins chained without the RGB8 frame leaving the device: the bytes of
  * imop_isp_run_host followed by imop_jpeg_encode_host on its output, for every frame.  Frames
- * go in chunks (up to 4 frames, about 25 Mpix) through one fused batch launch and one encoder
- * device batch each; the raw copies of the next chunk and the JPEG copies of the previous one
- * overlap them.  The parameters must select IMOP_OUT_RGB8.  Every frame is validated first
+ * go in chunks (up to 4 frames, about 25 Mpix; the first half as large) through one fused
+ * batch launch and one encoder device batch each; the raw copies of the next chunk and the JPEG
+ * copies of the previous one overlap them.  The parameters must select IMOP_OUT_RGB8.  Every frame is validated first
  * (nothing runs when one is invalid); synchronous; returns an IMOP_ERR_* status, the device
  * status of the ISP (as imop_isp_sync_status) included. */
 typedef struct {

@@ -154,5 +154,5 @@ def test_adam_calibration_c5(isp, c5):
         loss = A.l2_loss(isp, d, (phi * scale).contiguous(), raw_t, tgt)
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < 1e-2 * losses[0], f"loss {losses[0]:.4g} -> {losses[-1]:.4g}"
