@@ -1,6 +1,7 @@
 """RAW host frames to JPEG host bytes (imop_isp_run_host_jpeg_batch): every frame's bytes equal the
 oracle's encoder run on the oracle's pipeline output, across chunks (more than four frames, two
-full-size 4024x3032 frames that fill a chunk alone), mixed formats and parameters, the context's
+full-size 4024x3032 frames that fill a chunk alone), mixed formats and parameters (defect maps,
+polynomial lens shading, both white-balance orders), the context's
 parameters, pinned and pageable buffers, a truncating capacity; and the argument checks."""
 import numpy as np
 import pytest
@@ -39,10 +40,16 @@ def test_mixed_frames_across_chunks(ctxs):
     specs = [(640, 480, 12, True, abi.AMAZE), (333, 217, 10, False, abi.HQLI), (1006, 758, 8, False, abi.MG),
              (96, 64, 10, True, abi.AMAZE), (517, 389, 12, False, abi.HQLI), (128, 8, 14, True, abi.MG),
              (800, 600, 12, True, abi.AMAZE)]
+    specs += [(720, 404, 12, False, abi.AMAZE), (301, 255, 10, True, abi.MG)]
     for k, (w, h, bd, packed, dm) in enumerate(specs):
-        pl = random_pipeline(rng, w, h, bd, packed, dm, k % 4)
+        extra = {}
+        if k == 7:  # a defect list (map-based correction)
+            extra = dict(dpc_mode=abi.DPC_MAP_BASED, lsc_mode=abi.LSC_POLYNOMIAL)
+        elif k == 8:
+            extra = dict(lsc_mode=abi.LSC_POLYNOMIAL, order=abi.ORDER_RGB_WB)
+        pl = random_pipeline(rng, w, h, bd, packed, dm, k % 4, **extra)
         raw = random_frame(rng, pl)
-        q, ss = (90, 75, 50, 100, 20, 95, 85)[k], k % 3
+        q, ss = (90, 75, 50, 100, 20, 95, 85, 70, 99)[k], k % 3
         cap = J.max_bytes(w, h) if k != 4 else 900  # frame 4 truncated
         raw_h = torch.from_numpy(np.ascontiguousarray(raw)).pin_memory() if k % 2 else raw
         out = torch.zeros(cap, dtype=torch.uint8).pin_memory() if k % 3 == 0 else np.zeros(cap, np.uint8)
