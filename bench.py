@@ -124,31 +124,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_oracle_rate(pl, frames, max_seconds=30.0):
-    """Mpix/s of the CPU oracle (the reference's algorithm, plain C) on whole frames."""
+def cpu_oracle_rate(pl, frames, min_seconds=10.0):
+    """Mpix/s of the CPU oracle (the reference's algorithm, plain C) on whole frames, cycling
+    through `frames` until at least `min_seconds` of CPU work are timed."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_py as O
     O.pipeline(pl, frames[0])  # warm-up (page-in, OpenMP pool)
     t0 = time.perf_counter()
     done = 0
-    for f in frames:
-        O.pipeline(pl, f)
+    while done == 0 or time.perf_counter() - t0 < min_seconds:
+        O.pipeline(pl, frames[done % len(frames)])
         done += 1
-        if time.perf_counter() - t0 > max_seconds:
-            break
     dt = time.perf_counter() - t0
     return done * pl.pixels / dt / 1e6, done, dt
 
 
-def cpu_jpeg_rate(rgb, quality, subsample, max_seconds=20.0):
+def cpu_jpeg_rate(rgb, quality, subsample, min_seconds=10.0):
     """Mpix/s of the CPU restatement of the reference's baseline JPEG encoder (one thread, as the
-    reference's encoder) on whole frames."""
+    reference's encoder) on whole frames, repeated until at least `min_seconds` are timed."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_py as O
     h, w = rgb.shape[:2]
     t0 = time.perf_counter()
     done = 0
-    while done < 3 and (done == 0 or time.perf_counter() - t0 < max_seconds):
+    while done == 0 or time.perf_counter() - t0 < min_seconds:
         O.jpeg_encode(rgb, quality, subsample)
         done += 1
     dt = time.perf_counter() - t0
