@@ -38,6 +38,8 @@ sys.path.insert(0, os.path.join(REPO, "im-operator_gb300"))
 
 METRIC = "ISP Mpix/s & % HBM peak, fused-batched vs plain (1 GB300, <=1 LSB); adjoint Mpix/s"
 W_C2, H_C2 = 4024, 3032
+# ncu smsp__inst_executed.sum of one fused_batch_kernel launch over 8 C2 frames
+WARP_INST_PER_LAUNCH_8 = 1.002e9
 
 
 def parse():
@@ -560,6 +562,17 @@ def main():
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
     }
+    # the ceiling that binds this kernel: warp-instruction issue (4 per SM per clock)
+    sm_mhz = line["clocks"]["sm_mhz"] or line["clocks"]["sm_max_mhz"] or 2070.0
+    n_sm = torch.cuda.get_device_properties(0).multi_processor_count
+    issue_peak = n_sm * 4 * sm_mhz * 1e6
+    issue_achieved = WARP_INST_PER_LAUNCH_8 * B / 8 / (per_launch_ms / 1e3)
+    line["roofline"]["issue"] = {
+        "achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
+        "unit": "T warp instructions/s", "frac": round(issue_achieved / issue_peak, 4),
+        "warp_instructions_per_launch": int(WARP_INST_PER_LAUNCH_8 * B / 8),
+        "note": f"ncu smsp__inst_executed.sum of one launch over 8 frames (profiles/); peak = {n_sm} SMs x 4 "
+                f"schedulers x the median SM clock sampled in the timed region"}
     if ms_e2e is not None:
         line["e2e"] = {"value": round(world * args.steps * px_step / (ms_e2e / 1e3) / 1e6, 2), "unit": "Mpix/s",
                        "h2d_bytes_per_step": B * in_b, "d2h_bytes_per_step": B * out_b,
