@@ -383,6 +383,31 @@ def dist_init():
     return world, rank, local
 
 
+def frame_indices(rank, frames_per_rank):
+    """scene indices of a replica's frames: every rank renders frames of its own"""
+    return [rank * frames_per_rank + i for i in range(frames_per_rank)]
+
+
+def rank_sync(world, device):
+    """(barrier, max_over_ranks) of a replica run: no-ops for one rank; otherwise a process-group
+    barrier and an all-reduce MAX of a time in ms (the tensor on `device`: "cuda" under NCCL,
+    "cpu" under gloo)"""
+    import torch
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(ms):
+        if world > 1:
+            t = torch.tensor([ms], dtype=torch.float64, device=device)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    return barrier, max_over_ranks
+
+
 def run_reference(args):
     world, rank, _ = dist_init()
     if rank != 0:
@@ -433,7 +458,7 @@ def main():
     pl = workloads.c2_pipeline()
     B = args.frames
     in_b, out_b = pl.input_bytes(), pl.output_bytes()
-    host_frames = [workloads.c2_frame(pl, rank * B + i) for i in range(B)]
+    host_frames = [workloads.c2_frame(pl, k) for k in frame_indices(rank, B)]
     h_in = torch.empty((B, in_b), dtype=torch.uint8).pin_memory()
     for i, f in enumerate(host_frames):
         h_in[i].copy_(torch.from_numpy(f))
@@ -454,16 +479,7 @@ def main():
     def step_plain():
         isp.batch_submit(dev_frames, flags=abi.BATCH_PLAIN, stream=sh)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    def max_over_ranks(ms):
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+    barrier, max_over_ranks = rank_sync(world, "cuda")
 
     def timed(fn, steps):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
