@@ -143,3 +143,24 @@ def test_reference_headers_link_against_library():
         pytest.skip("the reference tree is not on this host")
     r = subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "shimlink"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_c_abi_header_is_plain_c(tmp_path):
+    """include/imop_isp.h compiles as strict C99 (the ABI carries no C++ types), and a C caller of
+    the RAW-to-JPEG batch call links against the library."""
+    src = tmp_path / "caller.c"
+    src.write_text('#include "imop_isp.h"\n'
+                   "int run(imop_isp_t isp, imop_jpeg_t j, const void* raw, uint8_t* out, size_t cap) {\n"
+                   "    ImopRawJpegFrame f = {0};\n"
+                   "    f.raw = raw; f.quality = 90; f.subsample = 1; f.out = out; f.out_cap = cap;\n"
+                   "    int st = imop_isp_run_host_jpeg_batch(isp, j, &f, 1);\n"
+                   "    return st ? st : (int)f.out_size;\n"
+                   "}\n"
+                   "int main(void) { return imop_abi_version() == IMOP_ISP_ABI_VERSION ? 0 : 1; }\n")
+    lib_dir = os.path.dirname(I.lib()._name)
+    exe = tmp_path / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(REPO, "include"),
+                        str(src), "-o", str(exe), "-L", lib_dir, "-limop_isp", f"-Wl,-rpath,{lib_dir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0
