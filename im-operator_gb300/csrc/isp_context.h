@@ -136,6 +136,7 @@ struct imop_isp_ctx {
     bool has_params = false;
     imop::FrameTables tabs;
     imop::FrameTables op_tabs;                     // tables of the per-operator entry points
+    imop::DevBuf op_tone;                          // tone table of imop_op_rgb_table
     imop::FixupState fix;
     imop::DevBuf d_in, d_out;                      // run_host staging frames
     imop::DevBuf plain_a, plain_b, plain_rgb;      // plain per-operator intermediates

@@ -113,5 +113,8 @@ cudaError_t launch_narrow(const uint16_t* in, uint8_t* out, size_t n, int bytes_
 cudaError_t launch_op_bayer(const FrameParams& fp, unsigned stage, const FixupScratch& fs, const MapPlan* plan,
                             uint16_t* a, uint16_t* b, cudaStream_t st);
 cudaError_t launch_op_rgb(const FrameParams& fp, unsigned stage, uint16_t* rgb, cudaStream_t st);
+// every one of n samples (u8 when bytes_per_sample is 1, u16 otherwise) through table, in -> out (may alias)
+cudaError_t launch_table_map(const uint8_t* in, uint8_t* out, size_t n, int bytes_per_sample, const uint16_t* table,
+                             cudaStream_t st);
 
 }  // namespace imop

@@ -377,6 +377,33 @@ cudaError_t launch_op_bayer(const FrameParams& fp, unsigned stage, const FixupSc
 }
 
 // One RGB stage (white balance or CCM) on an RGB u16 x 3 plane, in place.
+// per-sample table map (tone curves): each thread maps 8 consecutive samples, the tail one by one
+template <typename T>
+__global__ void table_map_kernel(const T* in, T* out, size_t n, const uint16_t* __restrict__ table) {
+    const size_t groups = n / 8;
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < groups; g += (size_t)gridDim.x * blockDim.x) {
+        T v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = in[8 * g + k];
+#pragma unroll
+        for (int k = 0; k < 8; k++) out[8 * g + k] = (T)__ldg(table + v[k]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < n - 8 * groups) {
+        const size_t i = 8 * groups + threadIdx.x;
+        out[i] = (T)__ldg(table + in[i]);
+    }
+}
+
+cudaError_t launch_table_map(const uint8_t* in, uint8_t* out, size_t n, int bytes_per_sample, const uint16_t* table,
+                             cudaStream_t st) {
+    const int nb = plain_blocks((n + 7) / 8);
+    if (bytes_per_sample == 1) table_map_kernel<uint8_t><<<nb, kPlainThreads, 0, st>>>(in, out, n, table);
+    else
+        table_map_kernel<uint16_t><<<nb, kPlainThreads, 0, st>>>(reinterpret_cast<const uint16_t*>(in),
+                                                                 reinterpret_cast<uint16_t*>(out), n, table);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_op_rgb(const FrameParams& fp, unsigned stage, uint16_t* rgb, cudaStream_t st) {
     const size_t n = (size_t)fp.w * fp.h;
     if (stage == 8u) rgb_wb_kernel<<<plain_blocks(3 * n), kPlainThreads, 0, st>>>(fp, rgb);

@@ -7,8 +7,10 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "../../include/imop_isp.h"
 #include "../../include/imop_ref_shims.hpp"
@@ -32,6 +34,16 @@ imop_isp_t thread_ctx() {
 template <class E>
 E as_status(int rc) {
     return (rc >= 0 && rc <= 6) ? static_cast<E>(rc) : E::InternalError;
+}
+
+// calls that ran on the device and returned Ok (imop_shim_calls_served)
+std::atomic<long long> g_served{0};
+
+// as_status, counting a call that the device served
+template <class E>
+E served(int rc) {
+    if (rc == 0) g_served.fetch_add(1, std::memory_order_relaxed);
+    return as_status<E>(rc);
 }
 
 ImopIspParams base_params(int w, int h, int bd, int pattern) {
@@ -80,7 +92,7 @@ DemosaicError demosaic_cuda(const uint8_t* bayer_data, uint8_t* rgb_data, int wi
     int rc = imop_isp_set_params(ctx, &p);
     if (rc == IMOP_OK)
         rc = imop_isp_run_host(ctx, bayer_data, imop_isp_input_bytes(&p), rgb_data, imop_isp_output_bytes(&p));
-    return as_status<DemosaicError>(rc);
+    return served<DemosaicError>(rc);
 }
 
 DemosaicError demosaic_cuda_batch(const uint8_t* const* bayer_data_array, uint8_t* const* rgb_data_array,
@@ -100,7 +112,7 @@ DemosaicError demosaic_cuda_batch(const uint8_t* const* bayer_data_array, uint8_
         frames[i].in = bayer_data_array[i];
         frames[i].out = rgb_data_array[i];
     }
-    return as_status<DemosaicError>(imop_isp_run_host_batch(ctx, frames.data(), num_frames));
+    return served<DemosaicError>(imop_isp_run_host_batch(ctx, frames.data(), num_frames));
 }
 
 }  // namespace imop
@@ -121,7 +133,7 @@ BlackLevelError process_black_level_cuda(uint8_t* data, int width, int height, B
     p.bl_offset[1] = params.gr_offset;
     p.bl_offset[2] = params.gb_offset;
     p.bl_offset[3] = params.b_offset;
-    return as_status<BlackLevelError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_BLACK_LEVEL, data));
+    return served<BlackLevelError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_BLACK_LEVEL, data));
 }
 
 }  // namespace black_level
@@ -142,7 +154,7 @@ DefectCorrectError process_defect_correct_cuda(uint8_t* data, int width, int hei
     p.dpc_threshold = params.threshold;
     p.dpc_map = reinterpret_cast<const ImopDefectPoint*>(params.map);
     p.dpc_map_count = params.map ? params.map_count : 0;
-    return as_status<DefectCorrectError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_DEFECT, data));
+    return served<DefectCorrectError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_DEFECT, data));
 }
 
 }  // namespace defect_correct
@@ -174,7 +186,7 @@ LensShadingError process_lens_shading_cuda(uint8_t* data, int width, int height,
         p.lsc_center[0] = params.center_x;
         p.lsc_center[1] = params.center_y;
     }
-    return as_status<LensShadingError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_LENS_SHADING, data));
+    return served<LensShadingError>(imop_op_bayer_stage(ctx, &p, IMOP_STAGE_LENS_SHADING, data));
 }
 
 }  // namespace lens_shading
@@ -193,7 +205,7 @@ WhiteBalanceError process_white_balance_cuda(const uint8_t* input, uint8_t* outp
     p.wb_gain[0] = r_gain;
     p.wb_gain[1] = g_gain;
     p.wb_gain[2] = b_gain;
-    return as_status<WhiteBalanceError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_WHITE_BALANCE, input, output));
+    return served<WhiteBalanceError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_WHITE_BALANCE, input, output));
 }
 
 }  // namespace white_balance
@@ -210,7 +222,7 @@ CCMError process_ccm_cuda(const uint8_t* input, uint8_t* output, int width, int 
     if (!ctx) return CCMError::InternalError;
     ImopIspParams p = base_params(width, height, bit_depth, IMOP_RGGB);
     std::memcpy(p.ccm, matrix, sizeof(p.ccm));
-    return as_status<CCMError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_CCM, input, output));
+    return served<CCMError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_CCM, input, output));
 }
 
 }  // namespace ccm
@@ -219,10 +231,23 @@ namespace tone {
 
 bool has_cuda() { return imop::has_cuda(); }
 
-// The reference's tone curves (gamma by std::pow, S-curve, levels, Bezier curves) are not on this
-// path; the dispatcher runs them on the CPU.
-ToneError process_tone_cuda(const uint8_t*, uint8_t*, int, int, int, ToneAlgorithm, int, const ToneParams&) {
-    return ToneError::InternalError;
+// GAMMA, S_CURVE, LEVELS and CURVES_3POINT: a per-sample table of the reference's expression
+// (imop_tone_table), applied to the frame on the device.  SHADOWS_HIGHLIGHTS couples the channels
+// and returns InternalError, so the dispatcher runs the reference's CPU code for it.
+ToneError process_tone_cuda(const uint8_t* input, uint8_t* output, int width, int height, int channels,
+                            ToneAlgorithm algorithm, int bit_depth, const ToneParams& params) {
+    if (!input || !output) return ToneError::NullInput;
+    if (channels != 3 || algorithm == ToneAlgorithm::SHADOWS_HIGHLIGHTS) return ToneError::InternalError;
+    imop_isp_t ctx = thread_ctx();
+    if (!ctx) return ToneError::InternalError;
+    static_assert(sizeof(ToneParams) == sizeof(ImopToneParams), "tone parameter layout");
+    ImopToneParams tp;
+    std::memcpy(&tp, &params, sizeof(tp));
+    thread_local std::vector<uint16_t> table;
+    table.resize(imop_tone_table_entries(bit_depth));
+    int rc = imop_tone_table(static_cast<int>(algorithm), bit_depth, &tp, table.data(), table.size());
+    if (rc == IMOP_OK) rc = imop_op_rgb_table(ctx, width, height, bit_depth, table.data(), input, output);
+    return served<ToneError>(rc);
 }
 
 }  // namespace tone
@@ -243,7 +268,7 @@ LUTError process_lut_cuda(const uint8_t* input, uint8_t* output, int width, int 
     ImopIspParams p = base_params(width, height, bit_depth, IMOP_RGGB);
     p.lut3d = lut_data.data.data();
     p.lut3d_size = lut_data.size;
-    return as_status<LUTError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_LUT3D, input, output));
+    return served<LUTError>(imop_op_rgb_stage(ctx, &p, IMOP_STAGE_LUT3D, input, output));
 }
 
 }  // namespace lut
@@ -280,6 +305,7 @@ JpegError process_encode_cuda(const uint8_t* input, uint8_t* output, size_t* out
     }
     const int rc = imop_jpeg_encode_host(t_jpeg.ctx, input, width, height, bit_depth, params.quality,
                                          params.chroma_subsample, output, output_size);
+    if (rc == IMOP_JPEG_OK) g_served.fetch_add(1, std::memory_order_relaxed);
     return (rc >= 0 && rc <= 12) ? static_cast<JpegError>(rc) : JpegError::InternalError;
 }
 
@@ -294,6 +320,8 @@ JpegError process_decode_cuda(const uint8_t* input, size_t input_size, uint8_t* 
 }
 
 }  // namespace jpeg_codec
+
+extern "C" long long imop_shim_calls_served(void) { return g_served.load(std::memory_order_relaxed); }
 
 // ---- modules off this path: CPU fallback ------------------------------------------------------
 namespace denoise {

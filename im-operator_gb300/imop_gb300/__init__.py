@@ -64,6 +64,10 @@ def lib():
             "imop_last_error_string": (C.c_char_p, []),
             "imop_abi_version": (i, []),
             "imop_has_cuda": (i, []),
+            "imop_shim_calls_served": (C.c_longlong, []),
+            "imop_tone_table_entries": (sz, [i]),
+            "imop_tone_table": (i, [i, i, C.POINTER(abi.ToneParams), vp, sz]),
+            "imop_op_rgb_table": (i, [vp, i, i, i, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -262,3 +266,18 @@ def suggest_dimensions(pixel_count):
 def guess_pattern(buf, width, height, bit_depth=8, packed=False):
     a, _ = _bytes(buf)
     return lib().imop_guess_pattern(a.ctypes.data, width, height, bit_depth, int(bool(packed)))
+
+
+def tone_params(gamma=1.0, contrast=0.0, shadows=0.0, highlights=0.0, black_point=0.0, white_point=1.0,
+                mid_point=0.5):
+    """tone::ToneParams with the reference's defaults (include/tone/types.hpp:50-58)."""
+    return abi.ToneParams(gamma, contrast, shadows, highlights, black_point, white_point, mid_point)
+
+
+def tone_table(algorithm, bit_depth, params):
+    """Output sample of one of the reference's tone curves for every storable input sample value
+    (uint16, 256 entries for bit depth <= 8, 65536 otherwise)."""
+    n = lib().imop_tone_table_entries(bit_depth)
+    t = np.zeros(n, np.uint16)
+    check(lib().imop_tone_table(algorithm, bit_depth, C.byref(params), t.ctypes.data, n))
+    return t

@@ -99,3 +99,11 @@ class AdjointDesc(C.Structure):
 
 ADJ_TARGET = 0
 ADJ_UPSTREAM = 1
+
+# the reference's tone curves (tone::ToneAlgorithm) and their parameters (tone::ToneParams)
+TONE_CURVE_GAMMA, TONE_CURVE_S_CURVE, TONE_CURVE_LEVELS, TONE_CURVE_3POINT, TONE_CURVE_SHADOWS_HIGHLIGHTS = range(5)
+
+
+class ToneParams(C.Structure):
+    _fields_ = [("gamma", C.c_float), ("contrast", C.c_float), ("shadows", C.c_float), ("highlights", C.c_float),
+                ("black_point", C.c_float), ("white_point", C.c_float), ("mid_point", C.c_float)]

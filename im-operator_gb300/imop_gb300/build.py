@@ -81,15 +81,23 @@ def build_library(verbose=False):
 
 
 def build_oracle(verbose=False):
-    """The CPU oracle (test infrastructure), and the reference's own CPU library where its
-    source tree exists on this machine."""
+    """The CPU oracle (test infrastructure), and the reference's own CPU library (and its
+    dispatchers over this library) where the reference's sources exist: the reference tree
+    (IMOP_REFERENCE_ROOT, default the checkout beside this one) is first copied into the
+    git-ignored oracle/_ref/src, so a host without the tree builds the same files from the copy."""
     oracle = os.path.join(REPO, "oracle")
     r = subprocess.run(["make", "-C", oracle, "-j8"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     ref_root = os.environ.get("IMOP_REFERENCE_ROOT", "/root/reference")
     if os.path.isdir(os.path.join(ref_root, "src", "algorithms")):
-        r = subprocess.run(["make", "-C", oracle, "ref", "-j8", f"REF_ROOT={ref_root}"],
+        r = subprocess.run(["make", "-C", oracle, "stage", f"REF_ROOT={ref_root}"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"staging the reference sources failed:\n{r.stdout}\n{r.stderr}")
+    staged = os.path.join(oracle, "_ref", "src")
+    if os.path.isdir(os.path.join(staged, "src", "algorithms")):
+        jobs = str(min(16, os.cpu_count() or 4))
+        r = subprocess.run(["make", "-C", oracle, "ref", "dropin", "-j" + jobs, f"REF_ROOT={staged}"],
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")

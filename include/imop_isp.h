@@ -246,6 +246,35 @@ int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* frames, int n);
 int imop_op_bayer_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, void* data);
 int imop_op_rgb_stage(imop_isp_t ctx, const ImopIspParams* p, unsigned stage, const void* in, void* out);
 
+/* ---- the reference's RGB tone curves (tone::process_tone) ------------------------------ */
+/* tone::ToneAlgorithm values (include/tone/types.hpp:8-14 of im-operator) */
+enum {
+    IMOP_TONE_CURVE_GAMMA = 0,
+    IMOP_TONE_CURVE_S_CURVE = 1,
+    IMOP_TONE_CURVE_LEVELS = 2,
+    IMOP_TONE_CURVE_3POINT = 3,
+    IMOP_TONE_CURVE_SHADOWS_HIGHLIGHTS = 4
+};
+/* tone::ToneParams (include/tone/types.hpp:50-58): same members in the same order */
+typedef struct {
+    float gamma, contrast, shadows, highlights, black_point, white_point, mid_point;
+} ImopToneParams;
+/* Entries of a per-sample table: every value the frame's storage holds (256 for u8, bit depth
+ * <= 8; 65536 for u16). */
+size_t imop_tone_table_entries(int bit_depth);
+/* The output sample of tone curve `algorithm` for every input sample value (host).  GAMMA,
+ * S_CURVE, LEVELS and CURVES_3POINT map each sample on its own with one function for R, G and B
+ * (src/tone/gamma.cpp:22-32, s_curve.cpp:21-39, levels.cpp:40-57, curves_3point.cpp:64-101), so
+ * the table, evaluated with the reference's float expressions, gives its output exactly.
+ * SHADOWS_HIGHLIGHTS couples the channels through a luminance and returns IMOP_ERR_UNSUPPORTED.
+ * `entries` must be at least imop_tone_table_entries(bit_depth). */
+int imop_tone_table(int algorithm, int bit_depth, const ImopToneParams* params, uint16_t* table, size_t entries);
+/* Every sample of an interleaved RGB frame (u8 x 3 for bit depth <= 8, u16 x 3 otherwise) through
+ * `table` (imop_tone_table_entries(bit_depth) host entries) on the device: host buffers in and out
+ * (may alias), synchronous; the GPU form of tone::process_tone_cuda (src/gpu_dispatch.cpp:292-312). */
+int imop_op_rgb_table(imop_isp_t ctx, int width, int height, int bit_depth, const uint16_t* table, const void* in,
+                      void* out);
+
 /* ---- differentiable pipeline (calibration) ------------------------------------------- */
 /* No counterpart in the reference, which has no parameter gradients.  The differentiable
  * forward is the calibration chain
@@ -455,6 +484,10 @@ const char* imop_last_error_string(void);
 int imop_abi_version(void);
 /* 1 when a CUDA device is visible (cached, like has_cuda_shared in src/gpu_dispatch.cpp:37-43). */
 int imop_has_cuda(void);
+/* Calls of the reference-named GPU glue (include/imop_ref_shims.hpp) that this process ran on the
+ * device and that returned Ok: a reference dispatcher linked against this library falls back to
+ * its CPU code silently on any other status, so this count tells an integrator which one ran. */
+long long imop_shim_calls_served(void);
 
 #ifdef __cplusplus
 }

@@ -12,8 +12,10 @@
  *
  * Served on the GPU: demosaic HQLI / MG / AMAZE (packed input of any depth included), black level,
  * adaptive and map-based defect correction, polynomial and flat-field lens shading, manual white
- * balance, 3x3 CCM, custom 3D LUTs, baseline JPEG encode.  tone::process_tone_cuda returns InternalError, so the
- * reference runs its CPU tone curves; the other modules of the same glue file
+ * balance, 3x3 CCM, custom 3D LUTs, the GAMMA / S_CURVE / LEVELS / CURVES_3POINT tone curves (a
+ * per-sample table of the reference's expression, mapped on the device), baseline JPEG encode.
+ * tone::process_tone_cuda returns InternalError for SHADOWS_HIGHLIGHTS, whose luminance couples
+ * the channels, so the reference runs that curve on its CPU; the other modules of the same glue file
  * (denoise, sharpen, local contrast, saturation, colour temperature, highlight reconstruction)
  * report no CUDA and stay on the CPU.
  */

@@ -78,6 +78,7 @@ def ref():
         _ref.ref_demosaic_raw.argtypes = [U8P, U16P, i, i, i, i, i, i]
         _ref.ref_wb_rgb.argtypes = [U16P, i, i, i, F32P]
         _ref.ref_ccm.argtypes = [U16P, i, i, i, F32P]
+        _ref.ref_tone.argtypes = [U16P, U16P, i, i, i, i, F32P]
         IP = C.POINTER(C.c_int)
         _ref.ref_detect_bit_depth.argtypes = [U8P, C.c_size_t]
         _ref.ref_suggest_dimensions.argtypes = [C.c_size_t, IP, i]

@@ -25,6 +25,7 @@
 #include "imop/analyzer.hpp"
 #include "color_calibration/algorithms.hpp"
 #include "lut/algorithms.hpp"
+#include "tone/algorithms.hpp"
 #include "jpeg_codec/algorithms.hpp"
 #include "imop/pixel_utils.hpp"
 #include "lens_shading/algorithms.hpp"
@@ -59,6 +60,12 @@ WhiteBalanceError process_white_balance_cuda(const uint8_t*, uint8_t*, int, int,
     return WhiteBalanceError::InternalError;
 }
 }  // namespace white_balance
+namespace tone {
+bool has_cuda() { return false; }
+ToneError process_tone_cuda(const uint8_t*, uint8_t*, int, int, int, ToneAlgorithm, int, const ToneParams&) {
+    return ToneError::InternalError;
+}
+}  // namespace tone
 namespace ccm {
 bool has_cuda() { return false; }
 CCMError process_ccm_cuda(const uint8_t*, uint8_t*, int, int, int, int, const float*) {
@@ -258,6 +265,19 @@ int ref_solve_ccm(const float* measured, const float* reference, int n, int type
         *rows = r.rows;
         *cols = r.cols;
     }
+    return e;
+}
+
+// tone::process_tone on interleaved RGB in its storage (u8 for bd <= 8, u16 otherwise), in -> out;
+// p = gamma, contrast, shadows, highlights, black_point, white_point, mid_point
+int ref_tone(const uint16_t* rgb, uint16_t* out, int w, int h, int bd, int algo, const float p[7]) {
+    tone::ToneParams tp;
+    tp.gamma = p[0]; tp.contrast = p[1]; tp.shadows = p[2]; tp.highlights = p[3];
+    tp.black_point = p[4]; tp.white_point = p[5]; tp.mid_point = p[6];
+    const size_t n = (size_t)w * h * 3;
+    std::vector<uint8_t> in = to_store(rgb, n, bd), o(in.size());
+    const int e = (int)tone::process_tone(in.data(), o.data(), w, h, 3, static_cast<tone::ToneAlgorithm>(algo), bd, tp);
+    if (e == 0) from_store(o, out, n, bd);
     return e;
 }
 

@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures of the oracle pin (run where the reference tree exists).
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [kat chains real_strips jpeg tone]
 
 Every expected value here is produced by the reference's own CPU functions, compiled from its
 sources by oracle/Makefile into oracle/_ref/libimop_ref.so (called through oracle/ref_glue.cpp):
@@ -13,6 +13,8 @@ sources by oracle/Makefile into oracle/_ref/libimop_ref.so (called through oracl
   real_strips.npz  the first 24 rows of each 1006x758 capture in the reference's test_data
                    (RG8, RG10, RG12, RG10 packed, RG12 packed) and the SHA-256 of
                    imop::demosaic_cpu's output on each (HQLI, MG, AMAZE), unpack included;
+  tone.npz         tone::process_tone's output (GAMMA, S_CURVE, LEVELS, CURVES_3POINT) for every
+                   storable sample value at several bit depths and parameter sets;
   jpeg.npz         RGB8 frames and the exact bytes of jpeg_codec::process_encode_baseline on them:
                    the images of the reference's tests/unit/test_jpeg_codec.cpp (file:line per
                    case), seeded frames over every subsampling and a range of qualities and sizes,
@@ -277,13 +279,40 @@ def jpeg_cases(R):
     return out
 
 
+def tone_cases(R):
+    """tone::process_tone on a ramp of every storable sample value (a n x 1 RGB frame with R = G = B)"""
+    sets = [(2.2, 0.0, 0.0, 0.0, 0.0, 1.0, 0.5), (0.45, 0.8, -0.4, 0.6, 0.1, 0.9, 0.3),
+            (10.5, -1.3, 1.1, -1.1, 0.5, 0.4, 0.95), (1.0, 2.4, 0.2, 0.2, -0.05, 1.05, 0.02)]
+    out, bds, algos, params = {}, [], [], []
+    k = 0
+    for bd in (1, 8, 12, 16):
+        for algo in range(4):
+            for p in (sets[(bd + algo) % 4],):
+                n = 256 if bd <= 8 else 65536
+                ramp = np.repeat(np.arange(n, dtype=np.uint16), 3)
+                res = np.zeros_like(ramp)
+                pa = np.asarray(p, np.float32)
+                st = R.ref_tone(P(ramp), P(res), n, 1, bd, algo, P(pa, F32P))
+                assert st == 0
+                out[f"table{k}"] = res.reshape(n, 3)[:, 0].copy()
+                bds.append(bd)
+                algos.append(algo)
+                params.append(p)
+                k += 1
+    out.update(n=np.int32(k), bd=np.array(bds, np.int32), algo=np.array(algos, np.int32),
+               params=np.array(params, np.float32))
+    return out
+
+
 def main():
     R = O.ref()
-    with open(os.path.join(HERE, "kat.json"), "w") as f:
-        json.dump(kat_cases(R), f)
-    np.savez_compressed(os.path.join(HERE, "chains.npz"), **chain_cases(R))
-    np.savez_compressed(os.path.join(HERE, "real_strips.npz"), **real_strips(R))
-    np.savez_compressed(os.path.join(HERE, "jpeg.npz"), **jpeg_cases(R))
+    only = set(sys.argv[1:])
+    if not only or "kat" in only:
+        with open(os.path.join(HERE, "kat.json"), "w") as f:
+            json.dump(kat_cases(R), f)
+    for name, fn in (("chains", chain_cases), ("real_strips", real_strips), ("jpeg", jpeg_cases), ("tone", tone_cases)):
+        if not only or name in only:
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fn(R))
     print("golden fixtures written to", HERE)
 
 

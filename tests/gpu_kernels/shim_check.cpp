@@ -8,6 +8,7 @@
 #include <random>
 #include <vector>
 
+#include "../../include/imop_isp.h"
 #include "../../include/imop_ref_shims.hpp"
 extern "C" {
 #include "../../oracle/isp_oracle.h"
@@ -194,11 +195,44 @@ int main() {
                 report("demosaic_cuda_batch", w, h, bd, ok);
             }
         }
-    // tone and 3D LUT are served by the CPU
-    tone::ToneParams tp;
-    uint8_t px[3] = {1, 2, 3}, po[3];
-    report("tone fallback", 1, 1, 8, tone::process_tone_cuda(px, po, 1, 1, 3, tone::ToneAlgorithm::GAMMA, 8, tp) ==
-                                            tone::ToneError::InternalError);
+    // tone curves: GAMMA, S_CURVE, LEVELS and CURVES_3POINT on the device, every sample equal to the
+    // per-sample table of the reference's expression (imop_tone_table, pinned against the reference
+    // on the CPU); SHADOWS_HIGHLIGHTS couples the channels and falls back to the CPU
+    {
+        const long long served0 = imop_shim_calls_served();
+        int tone_calls = 0;
+        const int tsz[2][2] = {{64, 48}, {1006, 758}};
+        for (int bd : {8, 10, 12, 16})
+            for (int ti = 0; ti < 2; ti++)
+                for (int a = 0; a < 4; a++) {
+                    const int w = tsz[ti][0], h = tsz[ti][1];
+                    auto f = frame(w, h, bd == 16 ? 15 : bd, 900 + bd * 10 + a, 3);
+                    std::vector<uint8_t> out(f.size());
+                    tone::ToneParams tp;
+                    tp.gamma = 2.2f + 0.3f * a; tp.contrast = 0.35f * a - 0.2f; tp.shadows = 0.4f - 0.3f * a;
+                    tp.highlights = 0.1f * a; tp.black_point = 0.04f * a; tp.white_point = 0.97f - 0.05f * a;
+                    tp.mid_point = 0.4f + 0.05f * a;
+                    const auto algo = static_cast<tone::ToneAlgorithm>(a);
+                    const auto st = tone::process_tone_cuda(f.data(), out.data(), w, h, 3, algo, bd, tp);
+                    std::vector<uint16_t> table(imop_tone_table_entries(bd));
+                    ImopToneParams ip;
+                    std::memcpy(&ip, &tp, sizeof(ip));
+                    bool ok = st == tone::ToneError::Ok &&
+                              imop_tone_table(a, bd, &ip, table.data(), table.size()) == IMOP_OK;
+                    const auto in16 = widen(f, bd), out16 = widen(out, bd);
+                    for (size_t i = 0; ok && i < in16.size(); i++) ok = out16[i] == table[in16[i]];
+                    tone_calls++;
+                    static const char* names[4] = {"tone GAMMA", "tone S_CURVE", "tone LEVELS", "tone CURVES_3POINT"};
+                    report(names[a], w, h, bd, ok);
+                }
+        report("tone calls served on the device", tone_calls, 1, 0,
+               imop_shim_calls_served() - served0 == tone_calls);
+        tone::ToneParams tp;
+        uint8_t px[3] = {1, 2, 3}, po[3];
+        report("tone SHADOWS_HIGHLIGHTS fallback", 1, 1, 8,
+               tone::process_tone_cuda(px, po, 1, 1, 3, tone::ToneAlgorithm::SHADOWS_HIGHLIGHTS, 8, tp) ==
+                   tone::ToneError::InternalError);
+    }
     // jpeg_codec::process_encode_cuda: the oracle's bytes (the reference's baseline encoder) for
     // every subsampling, a range of qualities and sizes; the reference's status codes
     {
