@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "isp_adjoint.h"
+#include "isp_kernels.h"
 #include "isp_device.cuh"
 #include "isp_tile.cuh"
 
@@ -615,6 +616,7 @@ cudaError_t adj_grid_limit(int& limit) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(device_setup_mutex());
     if (!cached[dev]) {
         const int smem = (int)sizeof(AdjSmem);
         if ((e = cudaFuncSetAttribute(adjoint_kernel<true, DM_AMAZE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) ||

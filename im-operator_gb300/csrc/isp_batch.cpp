@@ -9,9 +9,10 @@
 //
 // imop_isp_run_host_batch: the drop-in shape of imop::demosaic_cuda_batch
 // (src/algorithms/cuda_dispatch.cpp:150-209), which double-buffers pinned staging copies around a
-// graph per frame.  Here the caller's host frames are copied straight into one of three device
-// slots on a copy-in stream, computed on a compute stream and copied back on a copy-out stream,
-// with events between them, so frame k+1 is copied in and frame k-1 copied out while frame k runs.
+// graph per frame.  Here the caller's host frames are copied straight into one of four device
+// slots on a copy-in stream, computed on two compute streams (consecutive frames alternate), their
+// defect chains resolved on a fix-up stream, and copied back on a copy-out stream, with events
+// between them, so frame k+1 is copied in and frame k-1 copied out while frame k runs.
 
 #include <cuda_runtime.h>
 
@@ -31,7 +32,6 @@ namespace {
 constexpr int kBatchSeedCap = 16384;  // defect-chain entries per frame of a batch
 constexpr size_t kCacheMaxEntries = 1024;
 
-// FNV-1a, 64 bit
 // Content key: the bytes that determine a table (or a recorded batch) and a hash of them.  The
 // hash runs four independent multiply / xor-shift lanes over 8-byte words, so a 16 KB tone table
 // hashes in a few microseconds; equality of the bytes themselves is what a cache hit requires.
@@ -441,6 +441,13 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
             if ((e = P.d_in[s].ensure(max_in)) || (e = P.d_out[s].ensure(max_out))) return cuda_fail(e, "alloc slots");
         }
     }
+    // Once a copy is queued, an error return first waits for every stream of the pipeline: copies
+    // from or to the caller's host frames may still be running, and the caller may free them as
+    // soon as the call returns.
+    auto fail = [&](cudaError_t err, const char* what) {
+        for (cudaStream_t q : {P.s_in, P.s_comp[0], P.s_comp[1], P.s_fix, P.s_out}) cudaStreamSynchronize(q);
+        return cuda_fail(err, what);
+    };
     for (int i = 0; i < n; i++) {
         const int s = i % HostPipeline::kSlots;
         // the slot's own defect-chain scratch and tile counter; the context's sticky status word
@@ -454,38 +461,38 @@ extern "C" int imop_isp_run_host_batch(imop_isp_t ctx, const ImopFrameDesc* fram
         if ((e = cudaStreamWaitEvent(P.s_in, P.fix_done[s], 0)) ||
             (e = cudaMemcpyAsync(P.d_in[s].ptr, frames[i].in, ib[i], cudaMemcpyHostToDevice, P.s_in)) ||
             (e = cudaEventRecord(P.in_done[s], P.s_in)))
-            return cuda_fail(e, "copy in");
+            return fail(e, "copy in");
         // tile kernel once the input arrived, the slot's previous output was copied out and its
         // fix-up scratch is free; the chain resolution follows on s_fix
         cudaStream_t sc = P.s_comp[i & 1];
         if ((e = cudaStreamWaitEvent(sc, P.in_done[s], 0)) || (e = cudaStreamWaitEvent(sc, P.out_done[s], 0)) ||
             (e = cudaStreamWaitEvent(sc, P.fix_done[s], 0)))
-            return cuda_fail(e, "order compute");
+            return fail(e, "order compute");
         // map-mode frames resolve their map values into tables that frames with the same map share:
         // they follow the previous frame's tile kernel
         if (i > 0 && maps[i] && (e = cudaStreamWaitEvent(sc, P.main_done[(i - 1) % HostPipeline::kSlots], 0)))
-            return cuda_fail(e, "order map frame");
+            return fail(e, "order map frame");
         // A page-locked output frame is copied out right after the tile kernel and the fix-up then
         // writes its re-rendered windows into it; otherwise the copy waits for the whole fix-up.
         const bool direct_fix = device_mapped_host(frames[i].out, ob[i]);
         const SplitFixup split{P.s_fix, P.main_done[s], direct_fix};
         if ((e = launch_fused(fp, fs, maps[i] ? &maps[i]->plan : nullptr, sc, &split)))
-            return cuda_fail(e, "fused launch");
-        if (!direct_fix && (e = cudaEventRecord(P.fix_done[s], P.s_fix))) return cuda_fail(e, "fix-up done");
+            return fail(e, "fused launch");
+        if (!direct_fix && (e = cudaEventRecord(P.fix_done[s], P.s_fix))) return fail(e, "fix-up done");
         if ((e = cudaStreamWaitEvent(P.s_out, direct_fix ? P.main_done[s] : P.fix_done[s], 0)) ||
             (e = cudaMemcpyAsync(frames[i].out, P.d_out[s].ptr, ob[i], cudaMemcpyDeviceToHost, P.s_out)) ||
             (e = cudaEventRecord(P.out_done[s], P.s_out)))
-            return cuda_fail(e, "copy out");
+            return fail(e, "copy out");
         if (direct_fix) {
             if ((e = cudaStreamWaitEvent(P.s_fix, P.out_done[s], 0)) ||
                 (e = launch_fused_render(fp, fs, (uint8_t*)frames[i].out, P.s_fix)) ||
                 (e = cudaEventRecord(P.fix_done[s], P.s_fix)))
-                return cuda_fail(e, "fix-up windows");
+                return fail(e, "fix-up windows");
         }
     }
     if ((e = cudaStreamSynchronize(P.s_out)) || (e = cudaStreamSynchronize(P.s_fix)) ||
         (e = cudaStreamSynchronize(P.s_comp[0])) || (e = cudaStreamSynchronize(P.s_comp[1])) ||
         (e = cudaStreamSynchronize(P.s_in)))
-        return cuda_fail(e, "run_host_batch");
+        return fail(e, "run_host_batch");
     return take_status(ctx->fix);
 }

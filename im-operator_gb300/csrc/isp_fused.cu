@@ -198,6 +198,7 @@ struct FusedKernels {
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
         if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(device_setup_mutex());
         if (!ctas_per_sm[dev]) {
             for (int k = 0; k < 4 && e == cudaSuccess; k++)
                 e = cudaFuncSetAttribute(kernel(k), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -326,6 +327,11 @@ FrameParams with_fixup(const FrameParams& fp_in, const FixupScratch& fs) {
 }
 
 }  // namespace
+
+std::mutex& device_setup_mutex() {
+    static std::mutex m;
+    return m;
+}
 
 int fused_grid_limit(int out_bpc) {
     int limit = 0;

@@ -100,11 +100,14 @@ cudaError_t launch_fused_variant(const BatchLaunch& bl, int grid, size_t smem, c
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!attr_done[dev]) {
-        e = cudaFuncSetAttribute(fused_batch_kernel<TW, TH, OUTB, EXTRA, DM, SPEC>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_done[dev] = true;
+    {
+        std::lock_guard<std::mutex> lock(device_setup_mutex());
+        if (!attr_done[dev]) {
+            e = cudaFuncSetAttribute(fused_batch_kernel<TW, TH, OUTB, EXTRA, DM, SPEC>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            attr_done[dev] = true;
+        }
     }
     fused_batch_kernel<TW, TH, OUTB, EXTRA, DM, SPEC><<<grid, kThreads, smem, st>>>(bl);
     return cudaGetLastError();

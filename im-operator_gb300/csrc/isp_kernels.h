@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "isp_common.h"
 
 namespace imop {
@@ -55,6 +57,11 @@ struct MapPlan {
     const int* comp_entries;   // slot of each map entry, in map order
     const int2* slot_xy;       // pixel of each slot
 };
+
+// guards the once-per-device kernel set-up (shared-memory opt-in, occupancy queries): the
+// reference-named glue gives each host thread its own context, so first calls can come from
+// several threads at once
+std::mutex& device_setup_mutex();
 
 int fused_tile_grid(int w, int h, int& ntx, int& nty);
 cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots, int bd, uint8_t* d_out,

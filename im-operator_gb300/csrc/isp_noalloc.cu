@@ -16,6 +16,9 @@
 // as IMOP_ERR_CAPACITY after the call).  The array is shared by every call on a device and keeps
 // the last call's contents: each call re-uploads its tables and clears the counters that must
 // start at zero, so calls that overlap on the GPU (two streams, two host threads) race on it.
+// The array's device address, looked up on a device's first call, is kept for the life of the
+// process: after a cudaDeviceReset of that device the module is loaded anew, so this entry point
+// must not be used across a reset.
 
 #include <cuda_runtime.h>
 
@@ -138,9 +141,12 @@ extern "C" int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d
     fp.tile_counter = &sc->tile_counter;
     FixupScratch fs{sc->heap, sc->ov_idx, sc->ov_val, &sc->n_ov, kSeedCap};
     if ((e = launch_fused(fp, fs, nullptr, st))) return cuda_fail(e, "fused launch");
-    if ((e = cudaStreamSynchronize(st))) return cuda_fail(e, "no-alloc run");
+    // the status word is read on the caller's stream, so the call waits for its own work only
+    // (a copy on the legacy default stream would also wait for unrelated blocking streams)
     int status = 0;
-    if ((e = cudaMemcpy(&status, &sc->status, sizeof(int), cudaMemcpyDeviceToHost))) return cuda_fail(e, "read status");
+    if ((e = cudaMemcpyAsync(&status, &sc->status, sizeof(int), cudaMemcpyDeviceToHost, st)))
+        return cuda_fail(e, "read status");
+    if ((e = cudaStreamSynchronize(st))) return cuda_fail(e, "no-alloc run");
     if (status) return set_error(status, "device status after the no-alloc run (defect-chain capacity or wait limit)");
     return IMOP_OK;
 }

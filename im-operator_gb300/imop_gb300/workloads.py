@@ -60,8 +60,10 @@ def c1_frame(pl, index=0):
     return f.view(np.uint8).reshape(-1)
 
 
-def c2_pipeline(width=4024, height=3032, seed=BASE_SEED, defect_frac=1e-4):
-    from . import defects
+def c2_pipeline(width=4024, height=3032, seed=BASE_SEED, defect_frac=1e-4, defects=None):
+    """defects: the defect-position generator (default the library's imop_scene_defects)"""
+    if defects is None:
+        from . import defects
     n_def = int(round(defect_frac * width * height))
     return Pipeline(width=width, height=height, bit_depth=12, packed=True, pattern=abi.RGGB,
                     demosaic=abi.AMAZE, stages=abi.STAGE_ALL, stage_order=abi.ORDER_BAYER_WB,
@@ -72,9 +74,13 @@ def c2_pipeline(width=4024, height=3032, seed=BASE_SEED, defect_frac=1e-4):
                     tone_lut=gamma_lut(12).astype(np.float32))
 
 
-def c2_frame(pl, index=0):
-    """RAW12P bytes of one C2 frame: scene in [256, 4095], defects burnt in, MIPI packed."""
-    from . import scene, apply_defects, pack_mipi
+def c2_frame(pl, index=0, gen=None):
+    """RAW12P bytes of one C2 frame: scene in [256, 4095], defects burnt in, MIPI packed.  gen: a
+    module with scene / apply_defects / pack_mipi (default this package's, i.e. the library's)."""
+    if gen is None:
+        from . import scene, apply_defects, pack_mipi
+    else:
+        scene, apply_defects, pack_mipi = gen.scene, gen.apply_defects, gen.pack_mipi
     f = scene(pl.width, pl.height, 12, pl.pattern, BASE_SEED + index, lo=256, hi=4095)
     if pl.dpc_map is not None:
         apply_defects(f, pl.dpc_map, 12)

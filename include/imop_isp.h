@@ -331,7 +331,8 @@ int imop_isp_backward_device(imop_isp_t ctx, const ImopAdjointDesc* d, const flo
  * parameters return IMOP_ERR_UNSUPPORTED before any work.  All calls share the array and each
  * call resets what must start at zero, so calls that overlap on the GPU (two streams or host
  * threads at once) race.  The call enqueues on `stream`, waits for it, and returns the device
- * status. */
+ * status.  The array's address is kept from a device's first call on: do not use this entry point
+ * across a cudaDeviceReset of that device. */
 int imop_isp_run_device_noalloc(const ImopIspParams* p, const void* d_in, void* d_out, void* stream);
 
 /* ---- synthetic scene (seeded, bit-identical on every host) --------------------------- */

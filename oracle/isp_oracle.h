@@ -71,6 +71,14 @@ typedef struct OracleDumps {
 } OracleDumps;
 int or_pipeline(const ImopIspParams* p, const void* in, void* out, OracleDumps* dumps);
 
+/* seeded synthetic frames (isp_oracle_scene.c): the workloads' scene, defect positions and MIPI
+ * packing, equal to the product's generator byte for byte */
+int or_scene_render(int w, int h, int bd, int pattern, uint64_t seed, float lo, float hi, float gain,
+                    float read_sigma, void* out);
+int or_scene_defects(int w, int h, uint64_t seed, int count, int* xy);
+void or_scene_apply_defects(uint16_t* frame, int w, int bd, const int* xy, int count);
+void or_pack_mipi(const uint16_t* in, size_t n, int bd, uint8_t* out);
+
 /* Differentiable FP64 forward of the calibration pipeline (no integer rounding):
  * raw u16 -> BL -> LSC grid -> WB -> HQLI-style bilinear (same stencil) -> CCM -> knots curve.
  * theta layout = imop_isp_param_count().  rgb out: h*w*3 doubles. */

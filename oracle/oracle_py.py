@@ -261,3 +261,98 @@ def adj_loss(desc, theta, raw, ref, mode=0):
     if st:
         raise RuntimeError(f"or_adj_loss: {st}")
     return loss.value
+
+
+# ---- seeded synthetic frames, without the product library (timed CPU baseline) ------------------
+def _scene_lib():
+    L = lib()
+    L.or_scene_render.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_float, C.c_float, C.c_float,
+                                  C.c_float, C.c_void_p]
+    L.or_scene_defects.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_void_p]
+    L.or_scene_apply_defects.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    L.or_pack_mipi.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p]
+    return L
+
+
+def scene(width, height, bit_depth, pattern=0, seed=20261203, lo=None, hi=None, gain=0.5, read_sigma=2.0):
+    """The workloads' seeded Bayer frame (uint8 for bd <= 8, uint16 otherwise), equal to the
+    product's imop_scene_render byte for byte."""
+    mv = (1 << bit_depth) - 1
+    lo = float(lo if lo is not None else 0.0625 * (mv + 1))
+    hi = float(hi if hi is not None else mv)
+    out = np.empty((height, width), np.uint8 if bit_depth <= 8 else np.uint16)
+    if _scene_lib().or_scene_render(width, height, bit_depth, pattern, seed, lo, hi, gain, read_sigma,
+                                    out.ctypes.data) != 0:
+        raise ValueError("bad scene arguments")
+    return out
+
+
+def defects(width, height, count, seed=20261203):
+    xy = np.zeros((max(1, count), 2), np.int32)
+    if _scene_lib().or_scene_defects(width, height, seed, count, xy.ctypes.data) != 0:
+        raise ValueError("bad defect arguments")
+    return xy[:count]
+
+
+def apply_defects(frame, pts, bit_depth):
+    pts = np.ascontiguousarray(pts, np.int32).reshape(-1, 2)
+    assert frame.dtype == np.uint16 and frame.flags.c_contiguous
+    _scene_lib().or_scene_apply_defects(frame.ctypes.data, frame.shape[1], bit_depth, pts.ctypes.data, pts.shape[0])
+    return frame
+
+
+def pack_mipi(frame, bit_depth):
+    """MIPI RAW10 / RAW12 bytes of an unpacked frame"""
+    assert bit_depth in (10, 12)
+    f = np.ascontiguousarray(frame, np.uint16)
+    out = np.empty((f.size * bit_depth + 7) // 8, np.uint8)
+    _scene_lib().or_pack_mipi(f.ctypes.data, f.size, bit_depth, out.ctypes.data)
+    return out
+
+
+# ---- the reference's own CPU chain for the C2 configuration (timed reference arm) ---------------
+def _ref_chain_lib():
+    R = ref()
+    i, vp = C.c_int, C.c_void_p
+    R.ref_unpack_packed.argtypes = [vp, C.c_size_t, vp, i, i, i]
+    R.ref_black_level_store.argtypes = [vp, i, i, i, i, F32P]
+    R.ref_dpc_adaptive_store.argtypes = [vp, i, i, i, i, C.c_float]
+    R.ref_demosaic_store.argtypes = [vp, vp, i, i, i, i, i]
+    R.ref_ccm_store.argtypes = [vp, vp, i, i, i, F32P]
+    return R
+
+
+def ref_chain(pl, raw):
+    """RGB8 of one frame through the reference's per-module calls in the order they compose
+    (packed unpack by pixel::get_packed_raw, black_level::process_black_level, the adaptive
+    defect_correct::process_defect_correct, imop::demosaic_cpu, ccm::process_ccm), with the
+    oracle's restatements for the three stages the reference has no function for (explicit-grid
+    lens shading, Bayer-domain white balance, the 1-D LUT to RGB8).  Serves the C2 configuration:
+    a packed 12-bit (or 10-bit) frame, per-channel black level, adaptive defect correction, grid
+    lens shading, Bayer WB, any of the three demosaics, CCM, LUT tone."""
+    assert pl.packed and pl.bit_depth in (10, 12) and pl.stage_order == abi.ORDER_BAYER_WB
+    assert pl.bl_mode == abi.BL_PER_CHANNEL and pl.dpc_mode == abi.DPC_ADAPTIVE and pl.lsc_mode == abi.LSC_GRID
+    assert pl.stages == abi.STAGE_ALL and pl.tone_mode == abi.TONE_LUT and pl.out_format == abi.OUT_RGB8
+    R, L = _ref_chain_lib(), stages()
+    L.or_tone_rgb8.argtypes = [U16P, U8P, C.c_int, C.c_int, C.c_int, C.c_int, F32P, F32P]
+    w, h, bd, pat = pl.width, pl.height, pl.bit_depth, pl.pattern
+    raw = np.ascontiguousarray(raw, np.uint8)
+    bay = np.empty((h, w), np.uint16)
+    R.ref_unpack_packed(raw.ctypes.data, raw.size, bay.ctypes.data, w, h, bd)
+    off = np.asarray(pl.bl_offset, np.float32)
+    R.ref_black_level_store(bay.ctypes.data, w, h, pat, bd, off.ctypes.data_as(F32P))
+    R.ref_dpc_adaptive_store(bay.ctypes.data, w, h, pat, bd, float(pl.dpc_threshold))
+    grid = np.ascontiguousarray(pl.lsc_grid, np.float32)
+    L.or_lsc_grid(bay.ctypes.data_as(U16P), w, h, pat, bd, grid.ctypes.data_as(F32P), grid.shape[1], grid.shape[0])
+    wb = np.asarray(pl.wb_gain, np.float32)
+    L.or_wb_bayer(bay.ctypes.data_as(U16P), w, h, pat, bd, wb.ctypes.data_as(F32P))
+    rgb = np.empty((h, w, 3), np.uint16)
+    R.ref_demosaic_store(bay.ctypes.data, rgb.ctypes.data, w, h, pat, pl.demosaic, bd)
+    m = np.asarray(pl.ccm, np.float32)
+    rgb2 = np.empty_like(rgb)
+    R.ref_ccm_store(rgb.ctypes.data, rgb2.ctypes.data, w, h, bd, m.ctypes.data_as(F32P))
+    out = np.empty((h, w, 3), np.uint8)
+    lut = np.ascontiguousarray(pl.tone_lut, np.float32)
+    L.or_tone_rgb8(rgb2.ctypes.data_as(U16P), out.ctypes.data_as(U8P), w, h, bd, pl.tone_mode,
+                   lut.ctypes.data_as(F32P), None)
+    return out

@@ -268,6 +268,38 @@ int ref_solve_ccm(const float* measured, const float* reference, int n, int type
     return e;
 }
 
+// ---- the reference's per-module calls on frames in the reference's own storage (no conversion
+// copies), the form the timed CPU baseline composes: u8 samples for bd <= 8, u16 otherwise
+// pixel::get_packed_raw (include/imop/pixel_utils.hpp:58-118) of every pixel of a packed frame
+void ref_unpack_packed(const uint8_t* raw, size_t nbytes, uint16_t* out, int w, int h, int bd) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            out[(size_t)y * w + x] = (uint16_t)imop::pixel::get_packed_raw(raw, x, y, w, bd, nbytes, h);
+}
+int ref_black_level_store(uint8_t* data, int w, int h, int pattern, int bd, const float off[4]) {
+    black_level::BlackLevelParams p;
+    p.r_offset = off[0]; p.gr_offset = off[1]; p.gb_offset = off[2]; p.b_offset = off[3];
+    return (int)black_level::process_black_level(data, w, h, static_cast<imop::BayerPattern>(pattern),
+                                                 black_level::BlackLevelAlgorithm::PER_CHANNEL, bd, p);
+}
+int ref_dpc_adaptive_store(uint8_t* data, int w, int h, int pattern, int bd, float threshold) {
+    defect_correct::DefectCorrectParams p;
+    p.threshold = threshold;
+    return (int)defect_correct::process_defect_correct(data, w, h, static_cast<imop::BayerPattern>(pattern),
+                                                       defect_correct::DefectCorrectAlgorithm::ADAPTIVE, bd, p);
+}
+int ref_demosaic_store(const uint8_t* bay, uint8_t* rgb, int w, int h, int pattern, int algo, int bd) {
+    reserve_pool();
+    return (int)imop::demosaic_cpu(bay, rgb, w, h, static_cast<imop::BayerPattern>(pattern),
+                                   static_cast<imop::DemosaicAlgorithm>(algo), bd, false);
+}
+int ref_ccm_store(const uint8_t* in, uint8_t* out, int w, int h, int bd, const float m[9]) {
+    ccm::CCMatrix3x3 mat;
+    for (int i = 0; i < 9; i++) mat.m[i] = m[i];
+    return (int)ccm::process_ccm(in, out, w, h, 3, ccm::CCMAlgorithm::LINEAR_3X3, bd, &mat);
+}
+
 // tone::process_tone on interleaved RGB in its storage (u8 for bd <= 8, u16 otherwise), in -> out;
 // p = gamma, contrast, shadows, highlights, black_point, white_point, mid_point
 int ref_tone(const uint16_t* rgb, uint16_t* out, int w, int h, int bd, int algo, const float p[7]) {

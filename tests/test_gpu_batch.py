@@ -160,3 +160,36 @@ def test_run_host_batch_pinned_c2(isp):
     isp.run_device(d_in, d_out)
     torch.cuda.synchronize()
     assert torch.equal(d_out.cpu(), outs[0])
+
+
+def test_c4_batch_at_its_own_configuration(isp):
+    """The 96-frame uneven batch the bench times (1006x758 / 4024x3032 / 5320x4600, RAW8 and
+    RAW10 / RAW12 packed and unpacked, each frame its own BL / WB / CCM), as one recorded batch:
+    every frame equals the plain per-operator path, and one frame of each (size, format) pair
+    equals the CPU oracle."""
+    frames = workloads.c4_batch()
+    assert len(frames) == 96
+    dev = []
+    for pl, raw in frames:
+        d_in = torch.from_numpy(raw).cuda()
+        dev.append((pl, d_in, torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda")))
+    isp.batch_submit(dev, flags=abi.BATCH_GRAPH)
+    isp.batch_submit(dev, flags=abi.BATCH_GRAPH)  # recorded on the first call, replayed here
+    isp.sync_status()
+    fused = [d_out.clone() for _, _, d_out in dev]
+    for _, _, d_out in dev:
+        d_out.zero_()
+    isp.batch_submit(dev, flags=abi.BATCH_PLAIN)
+    isp.sync_status()
+    for k, (f, (pl, _, d_out)) in enumerate(zip(fused, dev)):
+        assert torch.equal(f, d_out), f"frame {k}: {pl.width}x{pl.height} bd {pl.bit_depth} packed {pl.packed}"
+    seen = set()
+    for k, (pl, raw) in enumerate(frames):
+        key = (pl.width, pl.height, pl.bit_depth, pl.packed)
+        if key in seen:
+            continue
+        seen.add(key)
+        ref, _ = O.pipeline(pl, raw)
+        got = fused[k].cpu().numpy().reshape(ref.shape)
+        assert np.array_equal(got, ref), f"frame {k} vs oracle: {key}"
+    assert len(seen) == 15

@@ -59,3 +59,56 @@ def test_noalloc_rejects_beyond_limits():
     cp = pl.to_c()
     assert f(C.byref(cp), 1, 1, None) == abi.ERR_UNSUPPORTED
     assert b"bit depth" in L.imop_last_error_string()
+
+
+def _call(pl, d_in, d_out):
+    L = I.lib()
+    f = L.imop_isp_run_device_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(abi.IspParams), C.c_void_p, C.c_void_p, C.c_void_p]
+    cp = pl.to_c()
+    return f(C.byref(cp), d_in, d_out, None)
+
+
+def test_noalloc_capacity_overflow_then_normal_call():
+    """A frame whose defect chains need more than the array's 16384 seeds reports
+    IMOP_ERR_CAPACITY; the next call, on a normal frame, starts from cleared counters and status
+    and equals the context path."""
+    torch = pytest.importorskip("torch")
+    pl = workloads.c2_pipeline(640, 480)
+    pl.dpc_threshold = 0.05
+    noise = np.random.default_rng(9).integers(0, 4096, (480, 640)).astype(np.uint16)
+    d_noise = torch.from_numpy(I.pack_mipi(noise, 12)).cuda()
+    out = torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+    assert _call(pl, d_noise.data_ptr(), out.data_ptr()) == abi.ERR_CAPACITY
+    pl2 = workloads.c2_pipeline(640, 480)
+    d_in = torch.from_numpy(workloads.c2_frame(pl2, 6)).cuda()
+    got = torch.zeros_like(out)
+    assert _call(pl2, d_in.data_ptr(), got.data_ptr()) == 0, I.lib().imop_last_error_string().decode()
+    ctx = I.Isp()
+    ctx.set_params(pl2)
+    ref = torch.zeros_like(out)
+    ctx.run_device(d_in.data_ptr(), ref.data_ptr())
+    torch.cuda.synchronize()
+    ctx.close()
+    assert torch.equal(got, ref)
+
+
+def test_noalloc_knot_tone_and_polynomial_shading():
+    torch = pytest.importorskip("torch")
+    pl = workloads.c2_pipeline(322, 242)
+    pl.lsc_mode = abi.LSC_POLYNOMIAL
+    pl.lsc_poly = ((0.3, 0.05, 0.0), (0.25, 0.04, 0.01), (0.26, 0.03, 0.0), (0.35, -0.05, 0.1))
+    pl.lsc_center = (0.47, 0.52)
+    pl.tone_mode = abi.TONE_KNOTS
+    pl.tone_knots = tuple(float(v) for v in (np.arange(33) / 32.0) ** 0.45)
+    d_in = torch.from_numpy(workloads.c2_frame(pl, 8)).cuda()
+    got = torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda")
+    assert _call(pl, d_in.data_ptr(), got.data_ptr()) == 0, I.lib().imop_last_error_string().decode()
+    ctx = I.Isp()
+    ctx.set_params(pl)
+    ref = torch.zeros_like(got)
+    ctx.run_device(d_in.data_ptr(), ref.data_ptr())
+    torch.cuda.synchronize()
+    ctx.close()
+    assert torch.equal(got, ref)
