@@ -325,6 +325,12 @@ def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind)
         d_in = torch.from_numpy(workloads.c3_frame(pl, 0)).cuda()
         d_out = torch.empty(pl.output_bytes(), dtype=torch.uint8, device="cuda")
         desc = [(None, d_in.data_ptr(), d_out.data_ptr())]
+        isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+        fused = d_out.clone()
+        isp.batch_submit(desc, flags=abi.BATCH_PLAIN, stream=sh)
+        isp.sync_status(sh)
+        same = bool(torch.equal(fused, d_out))
+        del fused
         for _ in range(max(3, args.warmup)):
             isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
         total = 0.0
@@ -344,12 +350,59 @@ def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind)
         ms = total / steps
         alg = pl.input_bytes() + pl.output_bytes()
         gbs = alg / (ms / 1e3) / 1e9
+        if not same:
+            out[f"{pl.bit_depth}bit"] = {"value": None, "error": "fused frame differs from the plain path"}
+            continue
         out[f"{pl.bit_depth}bit"] = {"ms_per_frame": round(ms, 4), "Mpix/s": round(world * pl.pixels / (ms / 1e3) / 1e6, 1),
                                      "gbs_algorithmic": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
-                                     "bytes_per_frame": alg}
+                                     "bytes_per_frame": alg, "fused_equals_plain": same}
     out["config"] = ("C3: 5320x4600 RGGB, an 8-bit frame and a 12-bit u16 frame, BL, RGB-order WB, HQLI, "
                      "linear tone -> RGB8; L2 flushed between steps; peak " + peak_kind)
     return out
+
+
+def c1_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind, n_frames=64):
+    """C1: 1006x758 RGGB 10-bit u16 frames (BL 64, RGB-order WB, HQLI, linear tone -> RGB8), a
+    batch of n_frames distinct frames per step (244 MB in and out, larger than L2), device-resident,
+    one recorded batch per step; Mpix/s and HBM GB/s against the measured peak.  Every frame is
+    checked against the plain per-operator path before timing."""
+    import imop_gb300 as I
+    from imop_gb300 import abi, workloads
+    pl = workloads.c1_pipeline()
+    isp = I.Isp(pl)
+    d_in = torch.stack([torch.from_numpy(workloads.c1_frame(pl, k)) for k in range(n_frames)]).cuda()
+    d_out = torch.empty((n_frames, pl.output_bytes()), dtype=torch.uint8, device="cuda")
+    sh = stream.cuda_stream
+    desc = [(None, d_in[k].data_ptr(), d_out[k].data_ptr()) for k in range(n_frames)]
+    isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+    fused = d_out.clone()
+    isp.batch_submit(desc, flags=abi.BATCH_PLAIN, stream=sh)
+    isp.sync_status(sh)
+    same = bool(torch.equal(fused, d_out))
+    del fused
+    for _ in range(max(3, args.warmup)):
+        isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(ev0.elapsed_time(ev1)) / args.steps
+    isp.sync_status(sh)
+    isp.close()
+    if not same:
+        return {"value": None, "error": "fused batch differs from the plain path"}
+    px = n_frames * pl.pixels
+    alg = n_frames * (pl.input_bytes() + pl.output_bytes())
+    gbs = alg / (ms / 1e3) / 1e9
+    return {"value": round(world * px / (ms / 1e3) / 1e6, 1), "unit": "Mpix/s", "ms_per_step": round(ms, 4),
+            "frames_per_step": n_frames, "gbs_algorithmic": round(world * gbs, 1), "hbm_frac": round(gbs / peak, 4),
+            "bytes_per_step": alg, "fused_equals_plain": same,
+            "config": f"C1: {n_frames} x 1006x758 RGGB 10-bit u16, BL 64, RGB-order WB, HQLI, linear tone -> RGB8; "
+                      f"peak {peak_kind}"}
 
 
 def adjoint_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
@@ -612,6 +665,7 @@ def main():
     if not args.no_c3:
         pk, pk_kind = peaks()
         c3 = c3_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
+        c3["c1"] = c1_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
 
     adjoint = None
     if not args.no_adjoint:

@@ -308,9 +308,37 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     return true;
 }
 
+// the launch block of frames[0..n) for the light-chain kernel: one rectangle per frame in its tiles
+bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl) {
+    bool fixup = false;
+    if (!make_launch(frames, n, bl, fixup)) return false;
+    int items = 0;
+    for (int f = 0; f < n; f++) {
+        TileRect& R = bl.rects[f];
+        R.tiles_x = tiles_along(R.w, lite_tile_w());
+        R.tiles_y = tiles_along(R.h, lite_tile_h());
+        bl.rect_start[f] = items;
+        items += R.tiles_x * R.tiles_y;
+    }
+    bl.rect_start[bl.n_rects] = items;
+    bl.n_items = items;
+    return true;
+}
+
 cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, const SplitFixup* split = nullptr) {
     BatchLaunch bl;
     bool fixup = false;
+    bool lite = true;
+    for (int f = 0; f < n; f++) lite = lite && lite_eligible(frames[f]);
+    if (lite) {
+        if (!make_lite_launch(frames, n, bl)) return cudaErrorInvalidValue;
+        cudaError_t e = launch_lite(bl, st);
+        // no defect chains to resolve: a split caller's fix-up stream only waits for the tiles
+        if (e == cudaSuccess && split) {
+            if ((e = cudaEventRecord(split->main_done, st)) == cudaSuccess) e = cudaStreamWaitEvent(split->st, split->main_done, 0);
+        }
+        return e;
+    }
     if (!make_launch(frames, n, bl, fixup)) return cudaErrorInvalidValue;
     return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st, split)
                                   : FusedKernels<3>::launch(bl, fixup, st, split);
@@ -346,6 +374,7 @@ static long long instantiation_key(const FrameParams& fp) {
     const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
                         fp.out_format == 0 && fp.out_bpc == 1;
     if (extra) return (long long)fp.out_bpc << 32;
+    if (lite_eligible(fp)) return 1LL << 40;  // the light-chain kernel
     const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
            (lite ? (1 << 12) : 0) | (simple ? fp.fmt + 1 : 0);

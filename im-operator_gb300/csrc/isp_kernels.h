@@ -93,6 +93,14 @@ cudaError_t launch_fused_batch(FrameParams* frames, int n, cudaStream_t st);
 // CTAs of the persistent fused kernel on the current device (SMs x resident CTAs per SM)
 int fused_grid_limit(int out_bpc);
 
+// light-chain kernel (isp_lite.cu): HQLI without defect correction, lens shading, CCM or 3D LUT,
+// RGB8 out, bit depth <= 12, u8 / u16 / MIPI RAW10 / RAW12 input
+bool lite_eligible(const FrameParams& fp);
+int lite_tile_w();
+int lite_tile_h();
+// one persistent launch over the tiles of bl's rectangles (tiles of lite_tile_w() x lite_tile_h())
+cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
+
 // plain per-operator form: one kernel per stage over full frames in device memory.
 // Buffers: bayer_a/bayer_b are w*h u16, rgb is w*h*3 u16.
 struct PlainBuffers {

@@ -158,8 +158,7 @@ int imop_op_rgb_table(imop_isp_t ctx, int width, int height, int bit_depth, cons
     if (!table || !in || !out) return set_error(IMOP_ERR_NULL_INPUT, "null table or frame pointer");
     if (width <= 0 || height <= 0) return set_error(IMOP_ERR_INVALID_DIMENSIONS, "invalid dimensions");
     if (bit_depth < 1 || bit_depth > 16) return set_error(IMOP_ERR_INVALID_BIT_DEPTH, "bit depth must be 1..16");
-    int rc = device_ready();
-    if (rc) return rc;
+    if (!device_ready()) return set_error(IMOP_ERR_NO_DEVICE, "no CUDA device");
     const size_t n = (size_t)width * height * 3;
     const int bps = bit_depth <= 8 ? 1 : 2;
     const size_t tab_bytes = imop_tone_table_entries(bit_depth) * sizeof(uint16_t);

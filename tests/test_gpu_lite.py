@@ -1,0 +1,165 @@
+"""The light-chain kernel (HQLI without defect correction, lens shading or CCM; isp_lite.cuh)
+against the CPU oracle, bit for bit: every input format it takes, bit depths 1-12, both
+white-balance orders, integral and fractional black levels, every tone mode, all Bayer patterns,
+frames from 4x4 up to the 5320x4600 frames of the large-frame workload, widths that are not
+multiples of the tile, unaligned input and output pointers, samples above the bit depth's maximum
+(the reference's MSB-aligned read), and batches that mix it with the general kernel."""
+import numpy as np
+import pytest
+
+import imop_gb300 as I
+from imop_gb300 import abi, workloads
+import oracle_py as O
+
+from helpers import max_abs
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+SIZES = [(6, 6), (7, 6), (6, 9), (9, 7), (8, 9), (33, 17), (131, 70), (255, 129), (256, 16), (257, 20), (259, 19),
+         (260, 23), (520, 300), (771, 37), (1006, 758)]
+
+
+def _pipeline(rng, w, h):
+    fmt = int(rng.integers(0, 4))
+    if fmt == 0:
+        bd, packed = int(rng.integers(1, 9)), False
+    elif fmt == 1:
+        bd, packed = int(rng.integers(9, 13)), False
+    elif fmt == 2:
+        bd, packed = 10, True
+    else:
+        bd, packed = 12, True
+    mv = (1 << bd) - 1
+    stages = 0
+    if rng.random() < 0.8:
+        stages |= abi.STAGE_BLACK_LEVEL
+    if rng.random() < 0.8:
+        stages |= abi.STAGE_WHITE_BALANCE
+    frac = rng.random() < 0.3
+    off = [float(v) if frac else float(round(v)) for v in rng.uniform(0, mv * 0.08, 4)]
+    pl = I.Pipeline(width=w, height=h, bit_depth=bd, packed=packed, pattern=int(rng.integers(0, 4)),
+                    demosaic=abi.HQLI, stages=stages, stage_order=int(rng.integers(0, 2)),
+                    bl_mode=int(rng.integers(0, 2)), bl_offset=tuple(off),
+                    wb_gain=tuple(float(v) for v in rng.uniform(0.6, 2.4, 3)))
+    t = int(rng.integers(0, 3))
+    pl.tone_mode = t
+    if t == abi.TONE_LUT:
+        pl.tone_lut = np.sort(rng.uniform(-0.05, 1.05, mv + 1)).astype(np.float32)
+    elif t == abi.TONE_KNOTS:
+        pl.tone_knots = tuple(float(v) for v in np.sort(rng.uniform(0, 1, 33)))
+    return pl
+
+
+def _frame(rng, pl, over=False):
+    bd = pl.bit_depth
+    mv = (1 << bd) - 1
+    f = I.scene(pl.width, pl.height, bd, pl.pattern, int(rng.integers(0, 2**62)), lo=mv * 0.05, hi=mv * 0.95)
+    if over and not pl.packed:
+        # samples above the bit depth's maximum: u8 frames of depth < 8 carry larger bytes, u16
+        # frames MSB-aligned samples (the reference's get_raw shifts them when nothing clamped)
+        k = rng.integers(0, f.size, max(1, f.size // 7))
+        if bd <= 8:
+            f.reshape(-1)[k] = rng.integers(mv, 256, k.size)
+        else:
+            f.reshape(-1)[k] = (f.reshape(-1)[k].astype(np.uint32) << (16 - bd)).astype(np.uint16)
+    if pl.packed:
+        return I.pack_mipi(f, bd)
+    return f.view(np.uint8).reshape(-1).copy()
+
+
+def _run(isp, pl, raw, in_off=0, out_off=0):
+    buf = torch.zeros(raw.size + 16, dtype=torch.uint8, device="cuda")
+    buf[in_off:in_off + raw.size].copy_(torch.from_numpy(raw))
+    out = torch.full((pl.output_bytes() + 16,), 0x5A, dtype=torch.uint8, device="cuda")
+    isp.set_params(pl)
+    isp.run_device(buf.data_ptr() + in_off, out.data_ptr() + out_off)
+    isp.sync_status()
+    o = out.cpu().numpy()
+    # bytes outside the frame untouched
+    assert (o[:out_off] == 0x5A).all() and (o[out_off + pl.output_bytes():] == 0x5A).all()
+    return o[out_off:out_off + pl.output_bytes()].reshape(pl.output_shape())
+
+
+@pytest.fixture(scope="module")
+def isp():
+    ctx = I.Isp()
+    yield ctx
+    ctx.close()
+
+
+@pytest.mark.parametrize("trial", range(30))
+def test_lite_matches_oracle(isp, trial):
+    rng = np.random.default_rng(9100 + trial)
+    w, h = SIZES[trial % len(SIZES)]
+    pl = _pipeline(rng, w, h)
+    raw = _frame(rng, pl, over=(trial % 3 == 2 and pl.stages == 0))
+    ref, _ = O.pipeline(pl, raw)
+    in_off = int(rng.integers(0, 16)) if trial % 4 == 1 else 0
+    out_off = int(rng.integers(0, 16)) if trial % 2 == 1 else 0
+    got = _run(isp, pl, raw, in_off, out_off)
+    assert max_abs(got, ref) == 0, (w, h, pl.bit_depth, pl.packed, pl.stages, pl.stage_order, in_off, out_off)
+
+
+def test_lite_values_above_max_without_clamping_stages(isp):
+    rng = np.random.default_rng(9200)
+    for bd, packed in ((6, False), (8, False), (10, False), (12, False)):
+        pl = I.Pipeline(width=131, height=70, bit_depth=bd, packed=packed, pattern=abi.GBRG, demosaic=abi.HQLI,
+                        stages=0)
+        raw = _frame(rng, pl, over=True)
+        ref, _ = O.pipeline(pl, raw)
+        assert max_abs(_run(isp, pl, raw), ref) == 0, bd
+
+
+@pytest.mark.parametrize("which", ["c1", "c3_8", "c3_12"])
+def test_lite_full_frames(isp, which):
+    if which == "c1":
+        pl = workloads.c1_pipeline()
+        raw = workloads.c1_frame(pl, 2)
+    else:
+        pl = workloads.c3_pipelines()[0 if which == "c3_8" else 1]
+        raw = workloads.c3_frame(pl, 1)
+    ref, _ = O.pipeline(pl, raw)
+    assert max_abs(_run(isp, pl, raw), ref) == 0
+
+
+def test_lite_in_mixed_batch(isp):
+    """HQLI light-chain frames and general-kernel frames in one batch: both kernels, every frame
+    against the oracle, recorded and replayed."""
+    rng = np.random.default_rng(9300)
+    frames = []
+    for k in range(12):
+        w, h = SIZES[(3 * k + 5) % len(SIZES)]
+        pl = _pipeline(rng, w, h)
+        if k % 3 == 2:
+            pl.demosaic = abi.AMAZE  # general kernel
+        if k % 4 == 3:
+            pl.stages |= abi.STAGE_CCM
+            pl.ccm = workloads.random_ccm(k)
+        raw = _frame(rng, pl)
+        ref, _ = O.pipeline(pl, raw)
+        frames.append((pl, raw, ref))
+    dev = [(pl, torch.from_numpy(raw).cuda(), torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda"))
+           for pl, raw, _ in frames]
+    for flags in (0, abi.BATCH_GRAPH, abi.BATCH_GRAPH):
+        for _, _, d_out in dev:
+            d_out.zero_()
+        isp.batch_submit(dev, flags=flags)
+        isp.sync_status()
+        for k, ((pl, _, ref), (_, _, d_out)) in enumerate(zip(frames, dev)):
+            got = d_out.cpu().numpy().reshape(ref.shape)
+            assert max_abs(got, ref) == 0, (k, pl.width, pl.height, pl.demosaic, flags)
+
+
+def test_lite_host_batch(isp):
+    rng = np.random.default_rng(9400)
+    frames = []
+    for k in range(6):
+        pl = workloads.c1_pipeline(1006 - 2 * k, 758 - k, bit_depth=10)
+        raw = _frame(rng, pl)
+        ref, _ = O.pipeline(pl, raw)
+        frames.append((pl, raw, ref))
+    outs = [np.zeros(ref.shape, ref.dtype) for _, _, ref in frames]
+    isp.run_host_batch([(pl, raw, o) for (pl, raw, _), o in zip(frames, outs)])
+    for (_, _, ref), o in zip(frames, outs):
+        assert max_abs(o, ref) == 0

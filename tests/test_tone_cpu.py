@@ -63,3 +63,15 @@ def test_luminance_curve_and_bad_arguments_refused():
     assert L.imop_tone_table(abi.TONE_CURVE_GAMMA, 12, C.byref(p), t.ctypes.data, 4096) == abi.ERR_INVALID_ARGUMENT
     assert L.imop_tone_table(abi.TONE_CURVE_GAMMA, 12, None, t.ctypes.data, t.size) == abi.ERR_NULL_INPUT
     assert L.imop_tone_table_entries(8) == 256 and L.imop_tone_table_entries(9) == 65536
+
+
+def test_table_stage_reports_no_device_without_gpu():
+    if I.lib().imop_has_cuda() == 1:
+        pytest.skip("a GPU is visible")
+    t = np.zeros(256, np.uint16)
+    img = np.zeros(6 * 6 * 3, np.uint8)
+    # no context can be made without a device; the call checks its arguments and the device before
+    # it touches the handle, so any non-null handle reaches the device check
+    handle = np.zeros(64, np.uint8)
+    rc = I.lib().imop_op_rgb_table(handle.ctypes.data, 6, 6, 8, t.ctypes.data, img.ctypes.data, img.ctypes.data)
+    assert rc == abi.ERR_NO_DEVICE
