@@ -315,8 +315,8 @@ bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl) {
     int items = 0;
     for (int f = 0; f < n; f++) {
         TileRect& R = bl.rects[f];
-        R.tiles_x = tiles_along(R.w, lite_tile_w());
-        R.tiles_y = tiles_along(R.h, lite_tile_h());
+        R.tiles_x = lite_units_x(R.w);
+        R.tiles_y = lite_units_y(R.h);
         bl.rect_start[f] = items;
         items += R.tiles_x * R.tiles_y;
     }
@@ -328,8 +328,11 @@ bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl) {
 cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, const SplitFixup* split = nullptr) {
     BatchLaunch bl;
     bool fixup = false;
+    // the light-chain kernel takes frames of one input format that share their output tables
     bool lite = true;
-    for (int f = 0; f < n; f++) lite = lite && lite_eligible(frames[f]);
+    for (int f = 0; f < n; f++)
+        lite = lite && lite_eligible(frames[f]) && frames[f].fmt == frames[0].fmt &&
+               lite_table_key(frames[f]) == lite_table_key(frames[0]);
     if (lite) {
         if (!make_lite_launch(frames, n, bl)) return cudaErrorInvalidValue;
         cudaError_t e = launch_lite(bl, st);
@@ -374,7 +377,8 @@ static long long instantiation_key(const FrameParams& fp) {
     const bool simple = (!(fp.stages & 2u) || fp.dpc_mode == 0) && (!(fp.stages & 4u) || fp.lsc_mode != 1) &&
                         fp.out_format == 0 && fp.out_bpc == 1;
     if (extra) return (long long)fp.out_bpc << 32;
-    if (lite_eligible(fp)) return 1LL << 40;  // the light-chain kernel
+    // the light-chain kernel: one launch per input format and output table set
+    if (lite_eligible(fp)) return (1LL << 62) | ((long long)fp.fmt << 56) | (lite_table_key(fp) & ((1LL << 56) - 1));
     const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
            (lite ? (1 << 12) : 0) | (simple ? fp.fmt + 1 : 0);

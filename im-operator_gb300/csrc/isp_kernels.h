@@ -96,9 +96,12 @@ int fused_grid_limit(int out_bpc);
 // light-chain kernel (isp_lite.cu): HQLI without defect correction, lens shading, CCM or 3D LUT,
 // RGB8 out, bit depth <= 12, u8 / u16 / MIPI RAW10 / RAW12 input
 bool lite_eligible(const FrameParams& fp);
-int lite_tile_w();
-int lite_tile_h();
-// one persistent launch over the tiles of bl's rectangles (tiles of lite_tile_w() x lite_tile_h())
+// frames of one light-chain launch share this key (their output tables) and the input format
+long long lite_table_key(const FrameParams& fp);
+// units of work of a frame: strips across, bands down (a rectangle's tiles_x / tiles_y)
+int lite_units_x(int w);
+int lite_units_y(int h);
+// one persistent launch over the units of bl's rectangles (bl.fmt: the frames' common format)
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
 
 // plain per-operator form: one kernel per stage over full frames in device memory.

@@ -1,8 +1,9 @@
-// isp_lite.cu - persistent launch of the light-chain tile kernel (isp_lite.cuh) over the tiles of
-// a batch of frames: CTAs claim tiles from a device counter, and warp 0 stages the next claimed
-// tile into the second raw buffer while the CTA computes the current one.
+// isp_lite.cu - the light-chain kernel (isp_lite.cuh): persistent CTAs whose warps each claim bands
+// of frame strips from a device counter and stream them row by row.
 
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "isp_fused_kernel.cuh"
 #include "isp_kernels.h"
@@ -11,86 +12,386 @@
 namespace imop {
 namespace {
 
-constexpr int kLiteTW = 256;
-constexpr int kLiteTH = 16;
 constexpr int kMaxDev = 64;
 
-template <int TW, int TH>
-__device__ void lite_stage_item(LiteSmem<TW, TH>& sm, const BatchLaunch& bl, int item, int b) {
-    const int lane = threadIdx.x & 31;
+// unit `item` of the launch: its rectangle (frame) by binary search, then the band and strip
+__device__ __forceinline__ void unit_of(const BatchLaunch& bl, int item, LiteUnit& U) {
     const int r = item_rect(bl, item);
     const TileRect& R = bl.rects[r];
-    const FrameParams& src = bl.frames[R.frame];
-    const int* s = reinterpret_cast<const int*>(&src);
-    int* d = reinterpret_cast<int*>(&sm.fp[b]);
-    for (int k = lane; k < (int)(sizeof(FrameParams) / 4); k += 32) d[k] = s[k];
     const int t = item - bl.rect_start[r];
     const int ty = t / R.tiles_x, tx = t - ty * R.tiles_x;
-    int x0, tw, y0, th;
-    tile_span(R.w, TW, R.tiles_x, tx, x0, tw);
-    tile_span(R.h, TH, R.tiles_y, ty, y0, th);
-    __syncwarp();
-    lite_stage(sm, b, R.x0 + x0, R.y0 + y0, tw, th);
+    const int sw = lite_strip_w(R.w);
+    U.f = R.frame;
+    U.x0 = R.x0 + tx * sw;
+    U.npx = min(sw, R.w - tx * sw);
+    int y0, bh;
+    tile_span(R.h, kLiteBandH, R.tiles_y, ty, y0, bh);
+    U.y0 = R.y0 + y0;
+    U.bh = bh;
+    U.nrows = bh + 2;
 }
 
-template <int TW, int TH>
+// lane 0: stage row k (y = y0 - 1 + k) of unit U into slot s: the bytes of pixels
+// [x0 - 8, x0 + npx + 8) of the frame, widened to 16-byte boundaries inside the buffer; a row
+// outside the frame (or a frame pointer the copy engine cannot take) completes its barrier phase
+// with no bytes
+template <int FMT>
+__device__ __forceinline__ void stage_row(LiteWarpSmem& ws, const FrameParams& fp, const LiteUnit& U, int k, int s) {
+    const int y = U.y0 - 1 + k;
+    const int W = fp.w;
+    int a0 = 0, len = 0;
+    if (y >= 0 && y < fp.h) {
+        const int xs = max(0, U.x0 - 8), xe = min(W, U.x0 + U.npx + 8);
+        int b0, b1;
+        pixel_bytes(FMT, fp.bd, y * W + xs, y * W + xe, b0, b1);
+        b1 = min(b1, (int)fp.in_bytes);
+        a0 = b0 & ~15;
+        const int a1 = min((b1 + 15) & ~15, (int)(fp.in_bytes & ~(size_t)15));
+        len = max(a1 - a0, 0);
+    }
+    ws.a0[s] = a0;
+    ws.len[s] = len;
+    if (len > 0 && (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0) {
+        ptx::mbar_arrive_expect_tx(&ws.bar[s], (uint32_t)len);
+        ptx::bulk_g2s(ws.raw[s], fp.in + a0, (uint32_t)len, &ws.bar[s]);
+    } else {
+        ptx::mbar_arrive_expect_tx(&ws.bar[s], 0);
+    }
+}
+
+// the 8 raw samples x .. x+7 of staged row y (a0 / len: the slot's window): word loads from the
+// slot where the samples lie whole inside it on a pair / group boundary, else one by one with the
+// packed-tail rule of pixel::get_packed_raw (frame edge, unaligned rows)
+template <int FMT>
+__device__ __forceinline__ void decode_at(const FrameParams& fp, const uint8_t* row, int a0, int len, int y, int x,
+                                          int (&v)[8]) {
+    const int W = fp.w;
+    const int i0 = y * W + x;
+    const int o = lite::byte_of<FMT>(i0) - a0;
+    const bool pair_ok = FMT == FMT_U8 || FMT == FMT_U16 || (FMT == FMT_P12 && (i0 & 1) == 0) ||
+                         (FMT == FMT_P10 && (i0 & 3) == 0);
+    if (x + 8 <= W && pair_ok && o >= 0 && o + lite::bytes8<FMT>() <= len) {
+        lite::decode8<FMT>(row, o, v);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = (x + j < W) ? staged_raw(fp, a0, len, row, i0 + j) : 0;
+    }
+}
+
+template <int FMT>
 __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
-    auto& sm = *reinterpret_cast<LiteSmem<TW, TH>*>(dsm);
+    auto& sm = *reinterpret_cast<LiteSmem*>(dsm);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    LiteWarpSmem& ws = sm.w[warp];
     const int n_items = bl.n_items;
-    if ((int)blockIdx.x >= n_items) return;
-    if (threadIdx.x == 0) {
-        ptx::mbar_init(&sm.bar[0], 1);
-        ptx::mbar_init(&sm.bar[1], 1);
+
+    // tables of the launch (every frame shares them): T_c[v] = tone8[round(v * wb_rgb[c])] when white
+    // balance runs on RGB, else tone8[v]
+    {
+        const FrameParams& f0 = bl.frames[0];
+        const int mv = f0.mv;
+        const bool wb_rgb = (f0.stages & 8u) && f0.stage_order == 1;
+        for (int i = threadIdx.x; i < 3 * (mv + 1); i += kThreads) {
+            const int c = i / (mv + 1), v = i - c * (mv + 1);
+            const int q = wb_rgb ? dev::gain_round(v, f0.wb_rgb[c], mv) : v;
+            sm.tab[c][v] = __ldg(f0.tone8 + q);
+        }
+    }
+    if (lane == 0) {
+        for (int s = 0; s < kLiteRing; s++) ptx::mbar_init(&ws.bar[s], 1);
         ptx::fence_mbar_init();
-        sm.tab_tone = nullptr;
-        sm.tab_mode = -1;
     }
     __syncthreads();
-    uint32_t par0 = 0, par1 = 0;
-    int claimed = 0;
-    if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
-    if (threadIdx.x < 32) lite_stage_item(sm, bl, blockIdx.x, 0);
-    __syncthreads();
-    int b = 0;
-    while (true) {
-        if (threadIdx.x < 32) {
-            const int next = __shfl_sync(0xffffffffu, claimed, 0);
-            if (next < n_items) {
-                if (threadIdx.x == 0) claimed = (int)gridDim.x + atomicAdd(bl.tile_counter, 1);
-                lite_stage_item(sm, bl, next, b ^ 1);
+
+    // The warp's stream of staged rows: the rows of unit `cur`, then those of unit `nxt`, claimed
+    // when staging reaches the end of `cur` (a few rows before `cur` is done, so the claims stay
+    // balanced across warps).  `issued` / `used` count rows over the whole stream: slot = count %
+    // ring, barrier phase = (count / ring) & 1.
+    int cur_item = 0;
+    if (lane == 0) cur_item = atomicAdd(bl.tile_counter, 1);
+    cur_item = __shfl_sync(0xffffffffu, cur_item, 0);
+    if (cur_item >= n_items) return;
+    int nxt_item = -1;  // -1: not claimed yet
+    LiteUnit cur, nxt;
+    unit_of(bl, cur_item, cur);
+    nxt = cur;
+    unsigned issued = 0, used = 0;
+    int iss_unit = 0, iss_k = 0;  // staging position: unit (0 cur, 1 nxt) and row in it
+    // stage the stream's next row (all lanes call it, lane 0 issues); false at the end of the work
+    auto issue_next = [&]() -> bool {
+        if (iss_unit == 0 && iss_k == cur.nrows) {
+            iss_unit = 1;
+            iss_k = 0;
+        }
+        if (iss_unit == 1) {
+            if (nxt_item < 0) {
+                int it = 0;
+                if (lane == 0) it = atomicAdd(bl.tile_counter, 1);
+                nxt_item = __shfl_sync(0xffffffffu, it, 0);
+                if (nxt_item < n_items) unit_of(bl, nxt_item, nxt);
             }
-            if (threadIdx.x == 0) sm.next_item[b ^ 1] = next;
+            if (nxt_item >= n_items || iss_k == nxt.nrows) return false;
         }
-        uint32_t& par = b ? par1 : par0;
-        const bool ok = lite_compute(sm, b, par);
-        const bool more = sm.next_item[b ^ 1] < n_items;
-        if (!ok) {
-            // leave no bulk copy in flight into this CTA's shared memory
-            if (more && (reinterpret_cast<uintptr_t>(sm.fp[b ^ 1].in) & 15) == 0) wait_bar(&sm.bar[b ^ 1], b ? par0 : par1);
-            return;
+        const LiteUnit& U = iss_unit == 0 ? cur : nxt;
+        if (lane == 0) stage_row<FMT>(ws, bl.frames[U.f], U, iss_k, (int)(issued % kLiteRing));
+        issued++;
+        iss_k++;
+        return true;
+    };
+    for (int i = 0; i < kLiteRing; i++)
+        if (!issue_next()) break;
+
+    int U_[10], M[10], D[10];
+    while (true) {
+        const FrameParams& fp = bl.frames[cur.f];
+        const int W = fp.w, H = fp.h, mv = fp.mv;
+        const PatternOffsets po = pattern_offsets(fp.pattern);
+        const bool bl_on = (fp.stages & 1u) != 0;
+        const bool wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
+        const bool need_align = fp.need_align != 0;
+        const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
+        const bool aligned_in = (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0;
+        const int xl = cur.x0 + kLiteLanePx * lane;  // the lane's first column
+        const bool edge_l = cur.x0 == 0, edge_r = cur.x0 + cur.npx == W;
+        for (int k = 0; k < cur.nrows; k++) {
+            const int s = (int)(used % kLiteRing);
+            const uint32_t parity = (used / kLiteRing) & 1u;
+            const bool ok = wait_bar(&ws.bar[s], parity);
+            if (!__all_sync(0xffffffffu, ok)) {
+                // leave no copy in flight into this CTA's shared memory: wait (bounded) for the other
+                // staged rows, then report
+                for (unsigned c = used + 1; c < issued; c++) wait_bar(&ws.bar[c % kLiteRing], (c / kLiteRing) & 1u);
+                if (lane == 0) atomicExch(fp.status, 103 /* IMOP_ERR_TIMEOUT */);
+                return;
+            }
+            const uint8_t* row = ws.raw[s];
+            const int a0 = ws.a0[s], len = ws.len[s];
+            const int y = cur.y0 - 1 + k;
+            if (!aligned_in && len > 0) {
+                // the frame pointer is not 16-byte aligned: the lanes copy the window themselves
+                uint8_t* dst = ws.raw[s];
+                for (int b = lane; b < len; b += 32) dst[b] = __ldg(fp.in + a0 + b);
+                __syncwarp();
+            }
+            // ---- this lane's 8 samples of row y and the strip's outer neighbour (lane 0: column
+            // x0 - 1, lane 31: column x0 + 256), black-levelled and white-balanced ----------------
+            int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            int nb = 0;
+            if (len > 0) {
+                if (xl < W) decode_at<FMT>(fp, row, a0, len, y, xl, v);
+                if (lane == 0 || lane == 31) {
+                    const int xn = lane == 0 ? cur.x0 - 8 : cur.x0 + kLiteStripMax;
+                    if (xn >= 0 && xn < W) {
+                        int t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                        decode_at<FMT>(fp, row, a0, len, y, xn, t);
+                        nb = lane == 0 ? t[7] : t[0];
+                    }
+                }
+                const int p = y & 1;
+                // black level (integral offsets: lite_eligible): (int)((float)v - off) clamped to
+                // [0, mv], one add-min-relu
+                if (bl_on) {
+                    const int bl_e = fp.bl_i[p][0], bl_o = fp.bl_i[p][1];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = __viaddmin_s32_relu(v[j], (j & 1) ? -bl_o : -bl_e, mv);
+                    nb = __viaddmin_s32_relu(nb, lane == 0 ? -bl_o : -bl_e, mv);
+                }
+                if (wb_bayer) {
+                    const float wb_e = fp.wb_cfa[bayer_color(y, 0, po)], wb_o = fp.wb_cfa[bayer_color(y, 1, po)];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = dev::gain_round(v[j], (j & 1) ? wb_o : wb_e, mv);
+                    nb = dev::gain_round(nb, lane == 0 ? wb_o : wb_e, mv);
+                }
+                if (need_align) {
+                    // the demosaic's u16 read of MSB-aligned samples (align_raw_value)
+                    const int sh = 16 - fp.bd;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = v[j] > mv ? v[j] >> sh : v[j];
+                    nb = nb > mv ? nb >> sh : nb;
+                }
+                if (lane == 0 && cur.x0 == 0) nb = 0;
+            }
+            int left = __shfl_up_sync(0xffffffffu, v[7], 1);
+            int right = __shfl_down_sync(0xffffffffu, v[0], 1);
+            if (lane == 0) left = nb;
+            if (lane == 31) right = nb;
+            // the slot is consumed: every lane's reads of it come before the copy that refills it
+            ptx::fence_proxy_async_smem();
+            __syncwarp();
+            used++;
+            issue_next();
+            // slide the window: rows y-2, y-1 (U_, M) and y (D)
+#pragma unroll
+            for (int j = 0; j < 10; j++) {
+                U_[j] = M[j];
+                M[j] = D[j];
+            }
+            D[0] = left;
+#pragma unroll
+            for (int j = 0; j < 8; j++) D[1 + j] = v[j];
+            D[9] = right;
+            if (k < 2) continue;
+
+            // ---- output row yo = y - 1 -------------------------------------------------------------
+            const int yo = y - 1;
+            if (yo < 2 || yo >= H - 2) continue;  // emitted with row 2 / h-3
+            int R[8], G[8], B[8];
+            const bool rrow = (yo & 1) == po.r_row;
+            const int rb = rrow ? po.r_col : po.b_col;
+            if (rb == 0) {
+                if (rrow) lite::hqli8<0, true>(U_, M, D, R, G, B);
+                else lite::hqli8<0, false>(U_, M, D, R, G, B);
+            } else {
+                if (rrow) lite::hqli8<1, true>(U_, M, D, R, G, B);
+                else lite::hqli8<1, false>(U_, M, D, R, G, B);
+            }
+            uint32_t ob[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                // bytes 4q .. 4q+3 of the lane's 24: pixel (4q + b) / 3, channel (4q + b) % 3
+                uint32_t bt[4];
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int n = 4 * q + b, px = n / 3, ch = n % 3;
+                    bt[b] = sm.tab[ch][ch == 0 ? R[px] : ch == 1 ? G[px] : B[px]];
+                }
+                ob[q] = __byte_perm(__byte_perm(bt[0], bt[1], 0x0040), __byte_perm(bt[2], bt[3], 0x0040), 0x5410);
+            }
+            // stage at the output row's 16-byte phase, fix the border columns, store
+            const int g0 = (yo * W + cur.x0) * 3;
+            const int shift = (int)((out_base + (uintptr_t)g0) & 15);
+            const int nbytes = 3 * cur.npx;
+            uint8_t* st = ws.out + shift + 24 * lane;
+            if (xl < cur.x0 + cur.npx) {
+                if ((shift & 7) == 0) {
+                    uint2* q2 = reinterpret_cast<uint2*>(st);
+                    q2[0] = make_uint2(ob[0], ob[1]);
+                    q2[1] = make_uint2(ob[2], ob[3]);
+                    q2[2] = make_uint2(ob[4], ob[5]);
+                } else if ((shift & 3) == 0) {
+                    uint32_t* q4 = reinterpret_cast<uint32_t*>(st);
+#pragma unroll
+                    for (int q = 0; q < 6; q++) q4[q] = ob[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 24; q++) st[q] = (uint8_t)(ob[q >> 2] >> (8 * (q & 3)));
+                }
+            }
+            __syncwarp();
+            uint8_t* so = ws.out + shift;
+            if (edge_l || edge_r) {
+                if (lane < 6) {
+                    // columns 0, 1 <- 2 and w-2, w-1 <- w-3 (lanes 0-2 / 3-5, one byte each)
+                    const int b = lane % 3;
+                    if (lane < 3 && edge_l) so[b] = so[3 + b] = so[6 + b];
+                    if (lane >= 3 && edge_r) {
+                        const int c3 = W - 3 - cur.x0;
+                        so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = so[3 * c3 + b];
+                    }
+                }
+                __syncwarp();
+            }
+            // the row, and rows 0, 1 with row 2 / rows h-2, h-1 with row h-3 (their corner pixels
+            // zero: the tables' bytes of 0)
+            const int copies = (yo == 2 || yo == H - 3) ? 3 : 1;
+            for (int rep = 0; rep < copies; rep++) {
+                const int yt = rep == 0 ? yo : (yo == 2 ? rep - 1 : H - 3 + rep);
+                if (rep == 1) {
+                    if (lane < 6) {
+                        const int b = lane % 3;
+                        const uint8_t z = sm.tab[b][0];
+                        if (lane < 3 && edge_l) so[b] = so[3 + b] = z;
+                        if (lane >= 3 && edge_r) {
+                            const int c3 = W - 3 - cur.x0;
+                            so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = z;
+                        }
+                    }
+                    __syncwarp();
+                }
+                const int gt = (yt * W + cur.x0) * 3;
+                if ((int)((out_base + (uintptr_t)gt) & 15) == shift) {
+                    // staging bytes [A, E) <-> output bytes from gt: whole 16-byte chunks as vector
+                    // stores, the head and tail bytes one per lane
+                    uint8_t* base = fp.out + gt - shift;  // 16-byte aligned
+                    const int A = shift, E = shift + nbytes;
+                    const int F = (A + 15) & ~15, L = E & ~15;
+                    if (F < L) {
+                        for (int c = F / 16 + lane; c < L / 16; c += 32)
+                            ptx::st_global_v4(base + 16 * c, *reinterpret_cast<const uint4*>(ws.out + 16 * c));
+                        if (A + lane < F) base[A + lane] = ws.out[A + lane];
+                        if (L + lane < E) base[L + lane] = ws.out[L + lane];
+                    } else if (A + lane < E) {
+                        base[A + lane] = ws.out[A + lane];
+                    }
+                } else {
+                    uint8_t* d8 = fp.out + gt;
+                    for (int b = lane; b < nbytes; b += 32) d8[b] = so[b];
+                }
+            }
+            __syncwarp();
         }
-        if (!more) return;
-        b ^= 1;
+        // the next unit: `nxt` (claimed while `cur`'s last rows were staged) becomes current
+        if (nxt_item < 0) {
+            int it = 0;
+            if (lane == 0) it = atomicAdd(bl.tile_counter, 1);
+            nxt_item = __shfl_sync(0xffffffffu, it, 0);
+            if (nxt_item < n_items) unit_of(bl, nxt_item, nxt);
+            iss_unit = 1;
+            iss_k = 0;
+        }
+        if (nxt_item >= n_items) return;
+        cur_item = nxt_item;
+        cur = nxt;
+        nxt_item = -1;
+        iss_unit = 0;  // staging continues inside the new `cur` at row iss_k
+        while (issued - used < (unsigned)kLiteRing)
+            if (!issue_next()) break;
     }
 }
 
 int g_lite_grid[kMaxDev];
 
+template <int FMT>
+cudaError_t launch_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
+    lite_batch_kernel<FMT><<<grid, kThreads, smem, st>>>(bl);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 bool lite_eligible(const FrameParams& fp) {
-    const bool fmt_ok = fp.fmt == FMT_U8 || fp.fmt == FMT_U16 || fp.fmt == FMT_P12 || fp.fmt == FMT_P10;
-    return fmt_ok && fp.bd <= 12 && fp.demosaic == DM_HQLI && !(fp.stages & (2u | 4u | 16u | 32u)) &&
-           fp.out_format == 0 && fp.out_bpc == 1 && fp.w >= 4 && fp.h >= 4;
+    const bool fmt_ok = fp.fmt == FMT_U8 || fp.fmt == FMT_U16 || (fp.fmt == FMT_P12 && (fp.w & 1) == 0) ||
+                        (fp.fmt == FMT_P10 && (fp.w & 3) == 0);
+    // integral black levels (one add-min-relu per sample), and samples no larger than the bit depth's
+    // maximum when they reach the demosaic (a stage clamps them, the MSB-aligned u16 read, a packed
+    // format, or full 8-bit bytes), so HQLI needs no clamps
+    const bool bl_ok = !(fp.stages & 1u) || fp.bl_int;
+    const bool bounded =
+        (fp.stages & 1u) || ((fp.stages & 8u) && fp.stage_order == 0) || fp.fmt != FMT_U8 || fp.bd == 8;
+    return fmt_ok && bl_ok && bounded && fp.bd <= 12 && fp.demosaic == DM_HQLI &&
+           !(fp.stages & (2u | 4u | 16u | 32u)) && fp.out_format == 0 && fp.out_bpc == 1 && fp.w >= 6 && fp.h >= 6;
 }
 
-int lite_tile_w() { return kLiteTW; }
-int lite_tile_h() { return kLiteTH; }
+// frames of one launch share their output tables: same tone table, white-balance order and RGB gains
+long long lite_table_key(const FrameParams& fp) {
+    const bool wb_rgb = (fp.stages & 8u) && fp.stage_order == 1;
+    uint64_t h = (uint64_t)reinterpret_cast<uintptr_t>(fp.tone8) * 0x9E3779B97F4A7C15ull;
+    h ^= wb_rgb ? 1u : 0u;
+    if (wb_rgb)
+        for (int c = 0; c < 3; c++) {
+            uint32_t b;
+            std::memcpy(&b, &fp.wb_rgb[c], 4);
+            h = (h ^ b) * 0xBF58476D1CE4E5B9ull;
+        }
+    return (long long)(h >> 8);
+}
+
+int lite_units_x(int w) { return lite_strips(w); }
+int lite_units_y(int h) { return lite_bands(h); }
 
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
-    using K = LiteSmem<kLiteTW, kLiteTH>;
-    const size_t smem = sizeof(K);
+    const size_t smem = sizeof(LiteSmem);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -99,11 +400,12 @@ cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
     {
         std::lock_guard<std::mutex> lock(device_setup_mutex());
         if (!g_lite_grid[dev]) {
-            e = cudaFuncSetAttribute(lite_batch_kernel<kLiteTW, kLiteTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+            void (*ks[4])(BatchLaunch) = {lite_batch_kernel<FMT_U8>, lite_batch_kernel<FMT_U16>,
+                                          lite_batch_kernel<FMT_P10>, lite_batch_kernel<FMT_P12>};
+            for (int k = 0; k < 4 && e == cudaSuccess; k++)
+                e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int n = 0, m = 0;
-            if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lite_batch_kernel<kLiteTW, kLiteTH>, kThreads, smem);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[1], kThreads, smem);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return e;
             g_lite_grid[dev] = m * (n > 0 ? n : 1);
@@ -112,9 +414,16 @@ cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
     }
     if (bl.n_items <= 0) return cudaSuccess;
     if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
-    const int grid = bl.n_items < limit ? bl.n_items : limit;
-    lite_batch_kernel<kLiteTW, kLiteTH><<<grid, kThreads, smem, st>>>(bl);
-    return cudaGetLastError();
+    // enough CTAs that every warp has a unit, at most the resident limit
+    const int want = (bl.n_items + kLiteWarps - 1) / kLiteWarps;
+    const int grid = want < limit ? want : limit;
+    switch (bl.fmt) {
+        case FMT_U8: return launch_fmt<FMT_U8>(bl, grid, smem, st);
+        case FMT_U16: return launch_fmt<FMT_U16>(bl, grid, smem, st);
+        case FMT_P10: return launch_fmt<FMT_P10>(bl, grid, smem, st);
+        case FMT_P12: return launch_fmt<FMT_P12>(bl, grid, smem, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace imop

@@ -1,23 +1,28 @@
 // isp_lite.cuh - the fused RAW->RGB8 pipeline for chains without defect correction and lens
-// shading, demosaiced by HQLI (the workload of the reference's plain per-module composition:
-// black level, white balance, HQLI, tone).
+// shading, demosaiced by HQLI: black level, white balance (Bayer or RGB order), HQLI, tone -> RGB8
+// (the chain of the reference's plain per-module composition).
 //
-// The general tile kernel (isp_tile.cuh) carries every stage's apron: an int plane 5 rows and 6
-// columns wider than the tile for defect correction, a second plane for lens shading and white
-// balance, a float plane for the edge-aware green.  HQLI needs one pixel around each output, so
-// this kernel keeps one u16 plane with a one-row halo and spends its instructions where the
-// measured pipe costs of sm_103a say they are cheap:
-//   * each raw sample is unpacked, black-levelled and (Bayer-order) white-balanced once, eight
-//     samples per thread, into the u16 plane (16-byte shared stores);
-//   * HQLI reads the plane with 16-byte loads, eight outputs per thread, integer sums only;
-//   * RGB-order white balance and the tone LUT fold into one table per output channel
-//     (T_c[v] = tone8[round(v * wb_c)]), built in shared memory by the CTA when the frame's
-//     parameters change, so each output byte is one shared-memory lookup - no float conversion
-//     (the float-to-int conversion runs at an eighth of the FP32 rate on this part);
-//   * output bytes are assembled in shared memory at the output's 16-byte phase and leave as
-//     16-byte vector stores.
-// Tiles touching the frame border compute their border pixels (rows / columns 0, 1, h-2, h-1,
-// w-2, w-1: the reference's fill_rgb_borders copies) in a second pass from the same plane.
+// HQLI reads one pixel around each output, so this kernel needs no shared tile and no CTA-wide
+// barrier in its main loop.  Each warp works alone on a strip of up to 256 columns (8 per lane) of
+// one frame, walking down a band of rows:
+//   * lane 0 stages every raw row's byte window into the warp's ring of shared-memory slots with a
+//     1-D bulk copy (cp.async.bulk, completing on the slot's mbarrier), kLiteRing rows ahead and
+//     across the end of one band into the next band the warp claims, so the next rows are in
+//     flight while the current one is computed;
+//   * each lane unpacks, black-levels and (Bayer-order) white-balances its eight samples of a row
+//     once; the columns to its left and right come from the neighbouring lanes by shuffles;
+//   * three rows live in registers (a sliding window), so HQLI of the middle row is integer sums;
+//   * RGB-order white balance and the tone LUT fold into one shared-memory table per output
+//     channel (T_c[v] = tone8[round(v * wb_c)], built once per launch: the frames of a launch share
+//     their tables), so each output byte is one lookup and no float-to-int conversion (an eighth of
+//     the FP32 rate on this part) is in the loop;
+//   * a row's 24 bytes per lane are assembled at the output's 16-byte phase in the warp's staging
+//     row and leave as 16-byte vector stores.
+// The reference's RGB border copies (fill_rgb_borders, src/algorithms/common.hpp:47-96) copy
+// pixels; the RGB white balance and the tone are per-pixel maps, so copying output bytes gives the
+// same result.  Columns 0, 1 / w-2, w-1 of a row take the bytes of column 2 / w-3 of that row;
+// rows 0, 1 / h-2, h-1 are emitted with row 2 / h-3, their corner pixels (never written by the
+// reference's HQLI, so zero) mapped through the tables.
 #pragma once
 
 #include "isp_device.cuh"
@@ -27,52 +32,54 @@
 
 namespace imop {
 
-template <int TW, int TH>
-struct LiteGeom {
-    static_assert(TW % 8 == 0, "tile width: whole chunks of eight pixels");
-    static constexpr int TWM = TW + 3, THM = TH + 3;          // a last tile absorbs a remainder below 4
-    static constexpr int PR = THM + 2;                          // plane rows: y0-1 .. y0+th
-    static constexpr int PCH = (TWM + 1 + 8 + 7) / 8 + 1;       // plane chunks of 8 samples (x0-8 ...)
-    static constexpr int PW = 8 * PCH;                          // plane samples per row
-    static constexpr int RAW_PITCH = round16(2 * PW + 32);      // staged bytes per raw row (u16 worst case)
-    static constexpr int OCH = (TWM + 7) / 8;                   // output chunks of 8 pixels per row
-    static constexpr int OUT_PITCH = round16(24 * OCH + 16);    // a row's chunks at any 16-byte phase
-    static_assert(PCH >= OCH + 2, "the plane covers the last chunk's right neighbour");
+constexpr int kLiteLanePx = 8;                   // pixels per lane
+constexpr int kLiteStripMax = 32 * kLiteLanePx;  // columns of a strip
+constexpr int kLiteBandH = 16;                   // rows of a band (the last absorbs a remainder below 4)
+constexpr int kLiteRing = 4;                     // staged rows per warp
+constexpr int kLiteWarps = 8;
+
+struct LiteWarpSmem {
+    // byte window of pixels [x0 - 8, x0 + 264) of a row in the widest format (u16), its 16-byte
+    // alignment slack, and readable bytes past it for the unpack's word loads
+    static constexpr int RAW_PITCH = round16(2 * (kLiteStripMax + 16) + 32 + 16);
+    static constexpr int OUT_PITCH = round16(3 * kLiteStripMax + 16);
+    alignas(16) uint8_t raw[kLiteRing][RAW_PITCH];
+    alignas(16) uint8_t out[OUT_PITCH];
+    int a0[kLiteRing];   // first staged byte of each slot's row (offset in the input frame)
+    int len[kLiteRing];  // staged bytes (0: a row outside the frame)
+    alignas(8) uint64_t bar[kLiteRing];
 };
 
-template <int TW, int TH>
 struct LiteSmem {
-    using G = LiteGeom<TW, TH>;
-    alignas(16) uint8_t raw[2][G::PR * G::RAW_PITCH];
-    alignas(16) uint16_t plane[G::PR * G::PW];
-    alignas(16) uint8_t out[G::THM * G::OUT_PITCH];
-    alignas(16) uint8_t tab[3][4096];   // per output channel: RGB-order WB and the tone LUT
-    alignas(16) FrameParams fp[2];
-    int row_a0[2][G::PR];               // staged byte window [a0, a0 + len) of each raw row
-    int row_len[2][G::PR];
-    int tile[2][4];                     // x0, y0, tw, th
-    int next_item[2];
-    // parameters the tables were built for
-    const uint8_t* tab_tone;
-    float tab_wb[3];
-    int tab_mode;
-    alignas(8) uint64_t bar[2];
+    alignas(16) uint8_t tab[3][4096];  // output byte per channel and sample value
+    LiteWarpSmem w[kLiteWarps];
+};
+
+// width of a frame's strips: at most 256 columns, chosen so the last strip holds at least three
+// columns (the right border copies column w-3 into w-2 and w-1 of the same strip)
+__host__ __device__ inline int lite_strip_w(int w) {
+    if (w <= kLiteStripMax) return kLiteStripMax;
+    for (int s = kLiteStripMax; s > 64; s -= 8)
+        if (w % s == 0 || w % s >= 3) return s;
+    return 64;
+}
+__host__ __device__ inline int lite_strips(int w) {
+    const int s = lite_strip_w(w);
+    return (w + s - 1) / s;
+}
+__host__ __device__ inline int lite_bands(int h) { return tiles_along(h, kLiteBandH); }
+
+// geometry of one band of one frame's strip (a warp's unit of work)
+struct LiteUnit {
+    int f;        // frame index in the launch
+    int x0, npx;  // first column and columns of the strip
+    int y0, bh;   // first row and rows of the band
+    int nrows;    // staged rows: y0 - 1 .. y0 + bh
 };
 
 namespace lite {
 
-// byte offset of pixel index i in the input stream (a pair / group boundary for packed formats)
-__device__ __forceinline__ int pixel_byte(int fmt, int i) {
-    switch (fmt) {
-        case FMT_U8: return i;
-        case FMT_U16: return 2 * i;
-        case FMT_P12: return 3 * (i >> 1);
-        default: return 5 * (i >> 2);
-    }
-}
-
-// bytes [o, o + 4k) of a staged row as k words, for any byte offset o (the row buffer has at least
-// four readable bytes past the last word)
+// bytes [o, o + 4K) of a staged row as K words, for any byte offset o
 template <int K>
 __device__ __forceinline__ void load_words(const uint8_t* row, int o, uint32_t (&w)[K]) {
     const uint32_t* p = reinterpret_cast<const uint32_t*>(row + (o & ~3));
@@ -86,14 +93,16 @@ __device__ __forceinline__ void load_words(const uint8_t* row, int o, uint32_t (
     }
 }
 
-// eight raw samples (x, x+1, ..., x+7; x even) of a staged row from byte offset o
-__device__ __forceinline__ void decode8(int fmt, const uint8_t* row, int o, int (&v)[8]) {
-    if (fmt == FMT_U8) {
+// eight raw samples x .. x+7 of a staged row, pixel x at byte offset o (for the MIPI formats x
+// lies on a pair / group boundary); bytes per eight samples: 8, 16, 12, 10
+template <int FMT>
+__device__ __forceinline__ void decode8(const uint8_t* row, int o, int (&v)[8]) {
+    if (FMT == FMT_U8) {
         uint32_t w[2];
         load_words(row, o, w);
 #pragma unroll
         for (int k = 0; k < 8; k++) v[k] = (w[k >> 2] >> (8 * (k & 3))) & 0xFF;
-    } else if (fmt == FMT_U16) {
+    } else if (FMT == FMT_U16) {
         uint32_t w[4];
         load_words(row, o, w);
 #pragma unroll
@@ -101,7 +110,7 @@ __device__ __forceinline__ void decode8(int fmt, const uint8_t* row, int o, int 
             v[2 * k] = w[k] & 0xFFFF;
             v[2 * k + 1] = w[k] >> 16;
         }
-    } else if (fmt == FMT_P12) {
+    } else if (FMT == FMT_P12) {
         uint32_t w[3];
         load_words(row, o, w);
         const uint32_t g[4] = {w[0], __funnelshift_r(w[0], w[1], 24), __funnelshift_r(w[1], w[2], 16), w[2] >> 8};
@@ -111,7 +120,7 @@ __device__ __forceinline__ void decode8(int fmt, const uint8_t* row, int o, int 
             v[2 * k] = p & 0xFFFF;
             v[2 * k + 1] = p >> 16;
         }
-    } else {  // MIPI RAW10: two groups of four samples in five bytes
+    } else {
         uint32_t w[3];
         load_words(row, o, w);
         const uint32_t lo4[2] = {w[0], __funnelshift_r(w[1], w[2], 8)};
@@ -124,310 +133,45 @@ __device__ __forceinline__ void decode8(int fmt, const uint8_t* row, int o, int 
     }
 }
 
-// black level, Bayer-order white balance and the demosaic's u16 read of one sample (the order of
-// the general tile's defect / shading phase without those two stages)
-__device__ __forceinline__ int bay_sample(const FrameParams& fp, int v, int y, int x, PatternOffsets po, bool bl_on,
-                                          bool bl_int, bool wb_bayer, bool need_align) {
-    const int mv = fp.mv;
-    if (bl_on) {
-        if (bl_int) v = __viaddmin_s32_relu(v, -fp.bl_i[y & 1][x & 1], mv);
-        else v = dev::black_level(fp, v, bayer_color(y, x, po));
+template <int FMT>
+__host__ __device__ constexpr int bytes8() {
+    return FMT == FMT_U8 ? 8 : FMT == FMT_U16 ? 16 : FMT == FMT_P12 ? 12 : 10;
+}
+
+// byte offset of pixel index i (on a pair / group boundary for the MIPI formats)
+template <int FMT>
+__device__ __forceinline__ int byte_of(int i) {
+    return FMT == FMT_U8 ? i : FMT == FMT_U16 ? 2 * i : FMT == FMT_P12 ? 3 * (i >> 1) : 5 * (i >> 2);
+}
+
+// RGB of the 8 pixels of a lane's row (m) from the rows above (u) and below (d): detail::hqli_core
+// (src/algorithms/interp_core.hpp:39-65) at interior sites; index 0 / 9 hold the columns left /
+// right of the lane's pixels.  RB: which pixel of each pair is the red / blue site; RR: the row is
+// a red row.  The samples never exceed the bit depth's maximum here (lite_eligible), so the
+// reference's clamps of the averages to that maximum are identities.
+template <int RB, bool RR>
+__device__ __forceinline__ void hqli8(const int (&u)[10], const int (&m)[10], const int (&d)[10], int (&R)[8],
+                                      int (&G)[8], int (&B)[8]) {
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+        const int i = p + 1;
+        if ((p & 1) == RB) {
+            const int own = m[i];
+            const int gq = (m[i - 1] + m[i + 1] + u[i] + d[i] + 2) >> 2;
+            const int oq = (u[i - 1] + u[i + 1] + d[i - 1] + d[i + 1] + 2) >> 2;
+            R[p] = RR ? own : oq;
+            B[p] = RR ? oq : own;
+            G[p] = gq;
+        } else {
+            const int hz = (m[i - 1] + m[i + 1] + 1) >> 1;
+            const int vt = (u[i] + d[i] + 1) >> 1;
+            G[p] = m[i];
+            R[p] = RR ? hz : vt;
+            B[p] = RR ? vt : hz;
+        }
     }
-    if (wb_bayer) v = dev::gain_round(v, fp.wb_cfa[bayer_color(y, x, po)], mv);
-    if (need_align && v > mv) v >>= (16 - fp.bd);
-    return v;
 }
 
 }  // namespace lite
-
-// warp 0: staged byte windows of the tile's raw rows y0-1 .. y0+th into buffer b (bulk copies
-// completing on bar[b]); sm.fp[b] holds the frame's parameters
-template <int TW, int TH>
-__device__ void lite_stage(LiteSmem<TW, TH>& sm, int b, int x0, int y0, int tw, int th) {
-    using G = LiteGeom<TW, TH>;
-    const FrameParams& fp = sm.fp[b];
-    const int lane = threadIdx.x & 31;
-    const int W = fp.w, H = fp.h;
-    const int in16 = (int)(fp.in_bytes & ~(size_t)15);
-    uint32_t bytes = 0;
-    for (int r = lane; r < th + 2; r += 32) {
-        const int y = y0 - 1 + r;
-        int a0 = 0, len = 0;
-        if (y >= 0 && y < H) {
-            const int xs = max(0, x0 - 8), xe = min(W, x0 - 8 + G::PW);
-            int b0, b1;
-            pixel_bytes(fp.fmt, fp.bd, y * W + xs, y * W + xe, b0, b1);
-            b1 = min(b1, (int)fp.in_bytes);
-            a0 = b0 & ~15;
-            const int a1 = min((b1 + 15) & ~15, in16);
-            len = max(a1 - a0, 0);
-        }
-        sm.row_a0[b][r] = a0;
-        sm.row_len[b][r] = len;
-        bytes += (uint32_t)len;
-    }
-    if (lane == 0) {
-        sm.tile[b][0] = x0;
-        sm.tile[b][1] = y0;
-        sm.tile[b][2] = tw;
-        sm.tile[b][3] = th;
-    }
-    if ((reinterpret_cast<uintptr_t>(fp.in) & 15) != 0) return;  // compute copies with plain loads
-    for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
-    if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.bar[b], bytes);
-    __syncwarp();
-    for (int r = lane; r < th + 2; r += 32) {
-        const int n = sm.row_len[b][r];
-        if (n > 0) ptx::bulk_g2s(sm.raw[b] + r * G::RAW_PITCH, fp.in + sm.row_a0[b][r], (uint32_t)n, &sm.bar[b]);
-    }
-}
-
-// one staged tile through the chain (all threads); false when the staged bytes never arrived
-template <int TW, int TH>
-__device__ bool lite_compute(LiteSmem<TW, TH>& sm, int b, uint32_t& parity) {
-    using G = LiteGeom<TW, TH>;
-    const FrameParams& fp = sm.fp[b];
-    const int x0 = sm.tile[b][0], y0 = sm.tile[b][1], tw = sm.tile[b][2], th = sm.tile[b][3];
-    const int W = fp.w, H = fp.h, mv = fp.mv, fmt = fp.fmt;
-    const PatternOffsets po = pattern_offsets(fp.pattern);
-    const int tid = threadIdx.x;
-    const unsigned stages = fp.stages;
-    const bool bl_on = (stages & 1u) != 0, bl_int = fp.bl_int != 0;
-    const bool wb_bayer = (stages & 8u) && fp.stage_order == 0;
-    const bool wb_rgb = (stages & 8u) && fp.stage_order == 1;
-    const bool need_align = fp.need_align != 0;
-
-    // per-channel output tables when the frame's tone table or RGB gains changed
-    const int tmode = wb_rgb ? 1 : 0;
-    const bool rebuild = sm.tab_tone != fp.tone8 || sm.tab_mode != tmode ||
-                         (wb_rgb && (sm.tab_wb[0] != fp.wb_rgb[0] || sm.tab_wb[1] != fp.wb_rgb[1] ||
-                                     sm.tab_wb[2] != fp.wb_rgb[2]));
-    if (rebuild) {
-        for (int i = tid; i < 3 * (mv + 1); i += kThreads) {
-            const int c = i / (mv + 1), v = i - c * (mv + 1);
-            const int q = wb_rgb ? dev::gain_round(v, fp.wb_rgb[c], mv) : v;
-            sm.tab[c][v] = __ldg(fp.tone8 + q);
-        }
-    }
-
-    bool arrived = true;
-    uint8_t* raw = sm.raw[b];
-    if ((reinterpret_cast<uintptr_t>(fp.in) & 15) == 0) {
-        arrived = wait_bar(&sm.bar[b], parity);
-        parity ^= 1u;
-    } else {
-        __syncthreads();
-        for (int r = 0; r < th + 2; r++) {
-            const int n = sm.row_len[b][r];
-            for (int k = tid; k < n; k += kThreads) raw[r * G::RAW_PITCH + k] = __ldg(fp.in + sm.row_a0[b][r] + k);
-        }
-    }
-    if (__syncthreads_or(!arrived)) {
-        if (tid == 0) atomicExch(fp.status, 103 /* IMOP_ERR_TIMEOUT */);
-        return false;
-    }
-    if (rebuild && tid == 0) {
-        sm.tab_tone = fp.tone8;
-        sm.tab_mode = tmode;
-        sm.tab_wb[0] = fp.wb_rgb[0];
-        sm.tab_wb[1] = fp.wb_rgb[1];
-        sm.tab_wb[2] = fp.wb_rgb[2];
-    }
-
-    // ---- A. raw rows -> u16 plane: plane (r, c) is pixel (x0 - 8 + c, y0 - 1 + r) ---------------
-    // chunks 0 .. och + 1 cover plane columns 7 (x0 - 1) .. 8 och + 8 (the last chunk's neighbour)
-    const int nch = ((tw + 7) >> 3) + 2;
-    for (int it = tid; it < (th + 2) * nch; it += kThreads) {
-        const int r = it / nch, k = it - r * nch;
-        const int y = y0 - 1 + r, x = x0 - 8 + 8 * k;
-        int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (y >= 0 && y < H) {
-            const uint8_t* row = raw + r * G::RAW_PITCH;
-            const int len = sm.row_len[b][r], a0 = sm.row_a0[b][r];
-            const int i0 = y * W + x;
-            const bool aligned = fmt == FMT_U8 || fmt == FMT_U16 || (fmt == FMT_P12 && (i0 & 1) == 0) ||
-                                 (fmt == FMT_P10 && (i0 & 3) == 0);
-            const int o = aligned ? lite::pixel_byte(fmt, i0) - a0 : 0;
-            const int nb = fmt == FMT_U8 ? 8 : fmt == FMT_U16 ? 16 : fmt == FMT_P12 ? 12 : 10;
-            if (x >= 0 && x + 8 <= W && aligned && o >= 0 && o + nb <= len) {
-                lite::decode8(fmt, row, o, v);
-#pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = lite::bay_sample(fp, v[j], y, x + j, po, bl_on, bl_int, wb_bayer, need_align);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-                    if (x + j >= 0 && x + j < W)
-                        v[j] = lite::bay_sample(fp, dev::load_raw(fp, x + j, y), y, x + j, po, bl_on, bl_int, wb_bayer,
-                                                need_align);
-            }
-        }
-        uint4 q;
-        q.x = (uint32_t)v[0] | ((uint32_t)v[1] << 16);
-        q.y = (uint32_t)v[2] | ((uint32_t)v[3] << 16);
-        q.z = (uint32_t)v[4] | ((uint32_t)v[5] << 16);
-        q.w = (uint32_t)v[6] | ((uint32_t)v[7] << 16);
-        *reinterpret_cast<uint4*>(sm.plane + r * G::PW + 8 * k) = q;
-    }
-    __syncthreads();
-
-    // ---- B. HQLI (detail::hqli_core, src/algorithms/interp_core.hpp:39-65) + tables -> bytes -----
-    // A warp takes one output row: eight consecutive pixels per lane.
-    const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
-    const int och = (tw + 7) >> 3;
-    auto P = [&](int r, int c) -> int { return sm.plane[r * G::PW + c]; };
-    for (int it = tid; it < th * 32 * ((och + 31) >> 5); it += kThreads) {
-        const int r = it / (32 * ((och + 31) >> 5));
-        const int j = it - r * 32 * ((och + 31) >> 5);
-        if (j >= och) continue;
-        const int y = y0 + r;
-        const int pr = r + 1, pc = 8 * j + 8;
-        int u[10], m[10], d[10];  // columns x-1 .. x+8 of rows y-1, y, y+1
-        {
-            const uint4 qu = *reinterpret_cast<const uint4*>(sm.plane + (pr - 1) * G::PW + pc);
-            const uint4 qm = *reinterpret_cast<const uint4*>(sm.plane + pr * G::PW + pc);
-            const uint4 qd = *reinterpret_cast<const uint4*>(sm.plane + (pr + 1) * G::PW + pc);
-            const uint32_t au[4] = {qu.x, qu.y, qu.z, qu.w}, am[4] = {qm.x, qm.y, qm.z, qm.w},
-                           ad[4] = {qd.x, qd.y, qd.z, qd.w};
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                u[1 + 2 * k] = au[k] & 0xFFFF; u[2 + 2 * k] = au[k] >> 16;
-                m[1 + 2 * k] = am[k] & 0xFFFF; m[2 + 2 * k] = am[k] >> 16;
-                d[1 + 2 * k] = ad[k] & 0xFFFF; d[2 + 2 * k] = ad[k] >> 16;
-            }
-            u[0] = P(pr - 1, pc - 1); m[0] = P(pr, pc - 1); d[0] = P(pr + 1, pc - 1);
-            u[9] = P(pr - 1, pc + 8); m[9] = P(pr, pc + 8); d[9] = P(pr + 1, pc + 8);
-        }
-        const bool rrow = (y & 1) == po.r_row;
-        const int rbh = rrow ? po.r_col : po.b_col;  // sample of each pair at the red / blue site
-        uint32_t ob[6];
-#pragma unroll
-        for (int px = 0; px < 8; px += 2) {
-            int R[2], Gv[2], B[2];
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int i = 1 + px + h;  // column index in u / m / d
-                int own, gq, oq;
-                if (h == rbh) {
-                    own = min(m[i], mv);
-                    gq = min((m[i - 1] + m[i + 1] + u[i] + d[i] + 2) >> 2, mv);
-                    oq = min((u[i - 1] + u[i + 1] + d[i - 1] + d[i + 1] + 2) >> 2, mv);
-                    R[h] = rrow ? own : oq;
-                    B[h] = rrow ? oq : own;
-                    Gv[h] = gq;
-                } else {
-                    const int hz = min((m[i - 1] + m[i + 1] + 1) >> 1, mv);
-                    const int vt = min((u[i] + d[i] + 1) >> 1, mv);
-                    Gv[h] = min(m[i], mv);
-                    R[h] = rrow ? hz : vt;
-                    B[h] = rrow ? vt : hz;
-                }
-            }
-            const uint32_t t0 = sm.tab[0][R[0]], t1 = sm.tab[1][Gv[0]], t2 = sm.tab[2][B[0]];
-            const uint32_t t3 = sm.tab[0][R[1]], t4 = sm.tab[1][Gv[1]], t5 = sm.tab[2][B[1]];
-            // six bytes of this pair at byte 3 * px of the chunk's 24
-            const int bo = 3 * px;
-            const uint32_t bytes6[6] = {t0, t1, t2, t3, t4, t5};
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                const int pos = bo + k;
-                if ((pos & 3) == 0) ob[pos >> 2] = bytes6[k];
-                else ob[pos >> 2] |= bytes6[k] << (8 * (pos & 3));
-            }
-        }
-        // stage the chunk's 24 bytes at the row's 16-byte phase
-        const int g0 = (y * W + x0) * 3;
-        const int shift = (int)((out_base + (uintptr_t)g0) & 15);
-        uint8_t* q = sm.out + r * G::OUT_PITCH + shift + 24 * j;
-        const int qa = shift + 24 * j;
-        if ((qa & 7) == 0) {
-            uint2* q2 = reinterpret_cast<uint2*>(q);
-            q2[0] = make_uint2(ob[0], ob[1]);
-            q2[1] = make_uint2(ob[2], ob[3]);
-            q2[2] = make_uint2(ob[4], ob[5]);
-        } else if ((qa & 3) == 0) {
-            uint32_t* q4 = reinterpret_cast<uint32_t*>(q);
-#pragma unroll
-            for (int k = 0; k < 6; k++) q4[k] = ob[k];
-        } else if ((qa & 1) == 0) {
-            uint16_t* q2 = reinterpret_cast<uint16_t*>(q);
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                q2[2 * k] = (uint16_t)ob[k];
-                q2[2 * k + 1] = (uint16_t)(ob[k] >> 16);
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 24; k++) q[k] = (uint8_t)(ob[k >> 2] >> (8 * (k & 3)));
-        }
-    }
-
-    // ---- border pixels: the reference's border copies, from the same plane -------------------------
-    const bool border = x0 < 2 || y0 < 2 || x0 + tw > W - 2 || y0 + th > H - 2;
-    if (border) {
-        __syncthreads();
-        // rows 0, 1, h-2, h-1 of the tile (whole width), then columns 0, 1, w-2, w-1 of its other rows
-        const int rt = max(0, min(2 - y0, th)), rb = max(0, min(y0 + th - (H - 2), th - rt));
-        const int cl = max(0, min(2 - x0, tw)), cr = max(0, min(x0 + tw - (W - 2), tw - cl));
-        const int mid = th - rt - rb;
-        const int n_rows = (rt + rb) * tw, n_cols = mid * (cl + cr);
-        for (int it = tid; it < n_rows + n_cols; it += kThreads) {
-            int x, y;
-            if (it < n_rows) {
-                const int rr = it / tw, cc = it - rr * tw;
-                y = rr < rt ? y0 + rr : y0 + th - rb + (rr - rt);
-                x = x0 + cc;
-            } else {
-                const int k = it - n_rows, rr = k / (cl + cr), cc = k - rr * (cl + cr);
-                y = y0 + rt + rr;
-                x = cc < cl ? x0 + cc : x0 + tw - cr + (cc - cl);
-            }
-            int sx, sy;
-            dev::border_source(x, y, W, H, fp.border_mode, sx, sy);
-            int R = 0, Gv = 0, B = 0;
-            if (sx >= 2 && sx < W - 2 && sy >= 2 && sy < H - 2) {
-                const int pr = sy - y0 + 1, pc = sx - x0 + 8;
-                const bool at_r = ((sy & 1) == po.r_row) && ((sx & 1) == po.r_col);
-                const bool at_b = ((sy & 1) == po.b_row) && ((sx & 1) == po.b_col);
-                const int n4 = P(pr, pc - 1) + P(pr, pc + 1) + P(pr - 1, pc) + P(pr + 1, pc);
-                const int d4 = P(pr - 1, pc - 1) + P(pr - 1, pc + 1) + P(pr + 1, pc - 1) + P(pr + 1, pc + 1);
-                if (at_r) { R = P(pr, pc); Gv = (n4 + 2) / 4; B = (d4 + 2) / 4; }
-                else if (at_b) { R = (d4 + 2) / 4; Gv = (n4 + 2) / 4; B = P(pr, pc); }
-                else {
-                    Gv = P(pr, pc);
-                    const int hz = (P(pr, pc - 1) + P(pr, pc + 1) + 1) / 2;
-                    const int vt = (P(pr - 1, pc) + P(pr + 1, pc) + 1) / 2;
-                    if ((sy & 1) == po.r_row) { R = hz; B = vt; } else { B = hz; R = vt; }
-                }
-                R = min(R, mv); Gv = min(Gv, mv); B = min(B, mv);
-            }
-            const int g0 = (y * W + x0) * 3;
-            const int shift = (int)((out_base + (uintptr_t)g0) & 15);
-            uint8_t* q = sm.out + (y - y0) * G::OUT_PITCH + shift + 3 * (x - x0);
-            q[0] = sm.tab[0][R];
-            q[1] = sm.tab[1][Gv];
-            q[2] = sm.tab[2][B];
-        }
-    }
-    __syncthreads();
-
-    // ---- C. stores: 16-byte vector stores on the output's own 16-byte grid ---------------------------
-    const int len = tw * 3;
-    constexpr int CH = G::OUT_PITCH / 16;
-    for (int s = tid; s < th * CH; s += kThreads) {
-        const int r = s / CH, k = s - r * CH;
-        const int g0 = ((y0 + r) * W + x0) * 3;
-        const int shift = (int)((out_base + (uintptr_t)g0) & 15);
-        const int lo = 16 * k, hi = lo + 16;
-        if (hi <= shift || lo >= shift + len) continue;
-        const uint8_t* src = sm.out + r * G::OUT_PITCH;
-        uint8_t* dst = fp.out + g0 - shift;
-        if (lo >= shift && hi <= shift + len) ptx::st_global_v4(dst + lo, *reinterpret_cast<const uint4*>(src + lo));
-        else store_piece(dst, src, max(lo, shift), min(hi, shift + len));
-    }
-    // this tile's reads of its raw buffer come before the bulk copy that stages a later tile into it
-    ptx::fence_proxy_async_smem();
-    __syncthreads();
-    return true;
-}
 
 }  // namespace imop
