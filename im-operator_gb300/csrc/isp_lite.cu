@@ -59,22 +59,48 @@ __device__ __forceinline__ void stage_row(LiteWarpSmem& ws, const FrameParams& f
     }
 }
 
-// the 8 raw samples x .. x+7 of staged row y (a0 / len: the slot's window): word loads from the
-// slot where the samples lie whole inside it on a pair / group boundary, else one by one with the
-// packed-tail rule of pixel::get_packed_raw (frame edge, unaligned rows)
+// the 8 raw samples x .. x+7 (x even) of staged row y as packed pairs (a0 / len: the slot's
+// window): word loads from the slot where the samples lie whole inside it on a pair / group
+// boundary, else one by one with the packed-tail rule of pixel::get_packed_raw (frame edge,
+// unaligned rows)
 template <int FMT>
-__device__ __forceinline__ void decode_at(const FrameParams& fp, const uint8_t* row, int a0, int len, int y, int x,
-                                          int (&v)[8]) {
+__device__ __forceinline__ void decode_pairs(const FrameParams& fp, const uint8_t* row, int a0, int len, int y, int x,
+                                             uint32_t (&P)[4]) {
     const int W = fp.w;
     const int i0 = y * W + x;
     const int o = lite::byte_of<FMT>(i0) - a0;
     const bool pair_ok = FMT == FMT_U8 || FMT == FMT_U16 || (FMT == FMT_P12 && (i0 & 1) == 0) ||
                          (FMT == FMT_P10 && (i0 & 3) == 0);
     if (x + 8 <= W && pair_ok && o >= 0 && o + lite::bytes8<FMT>() <= len) {
-        lite::decode8<FMT>(row, o, v);
+        if (FMT == FMT_U8) {
+            uint32_t w[2];
+            lite::load_words(row, o, w);
+            P[0] = __byte_perm(w[0], 0u, 0x4140);
+            P[1] = __byte_perm(w[0], 0u, 0x4342);
+            P[2] = __byte_perm(w[1], 0u, 0x4140);
+            P[3] = __byte_perm(w[1], 0u, 0x4342);
+        } else if (FMT == FMT_U16) {
+            lite::load_words(row, o, P);
+        } else if (FMT == FMT_P12) {
+            uint32_t w[3];
+            lite::load_words(row, o, w);
+            P[0] = unpack12_pair(w[0]);
+            P[1] = unpack12_pair(__funnelshift_r(w[0], w[1], 24));
+            P[2] = unpack12_pair(__funnelshift_r(w[1], w[2], 16));
+            P[3] = unpack12_pair(w[2] >> 8);
+        } else {
+            int v[8];
+            lite::decode8<FMT>(row, o, v);
+#pragma unroll
+            for (int j = 0; j < 4; j++) P[j] = (uint32_t)v[2 * j] | ((uint32_t)v[2 * j + 1] << 16);
+        }
     } else {
 #pragma unroll
-        for (int j = 0; j < 8; j++) v[j] = (x + j < W) ? staged_raw(fp, a0, len, row, i0 + j) : 0;
+        for (int j = 0; j < 4; j++) {
+            const uint32_t lo = (x + 2 * j < W) ? (uint32_t)staged_raw(fp, a0, len, row, i0 + 2 * j) : 0u;
+            const uint32_t hi = (x + 2 * j + 1 < W) ? (uint32_t)staged_raw(fp, a0, len, row, i0 + 2 * j + 1) : 0u;
+            P[j] = lo | (hi << 16);
+        }
     }
 }
 
@@ -142,7 +168,7 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
     for (int i = 0; i < kLiteRing; i++)
         if (!issue_next()) break;
 
-    int U_[10], M[10], D[10];
+    lite::Row Ur, Mr, Dr;  // rows y-2, y-1, y of the lane (packed pairs)
     while (true) {
         const FrameParams& fp = bl.frames[cur.f];
         const int W = fp.w, H = fp.h, mv = fp.mv;
@@ -150,10 +176,13 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
         const bool bl_on = (fp.stages & 1u) != 0;
         const bool wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
         const bool need_align = fp.need_align != 0;
+        // a float stage or the MSB-aligned read take the per-sample path
+        const bool per_sample_frame = wb_bayer || need_align;
         const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
         const bool aligned_in = (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0;
         const int xl = cur.x0 + kLiteLanePx * lane;  // the lane's first column
         const bool edge_l = cur.x0 == 0, edge_r = cur.x0 + cur.npx == W;
+        const bool lane_in = xl + kLiteLanePx <= cur.x0 + cur.npx;  // all 8 pixels in the strip
         for (int k = 0; k < cur.nrows; k++) {
             const int s = (int)(used % kLiteRing);
             const uint32_t parity = (used / kLiteRing) & 1u;
@@ -174,92 +203,94 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
                 for (int b = lane; b < len; b += 32) dst[b] = __ldg(fp.in + a0 + b);
                 __syncwarp();
             }
-            // ---- this lane's 8 samples of row y and the strip's outer neighbour (lane 0: column
-            // x0 - 1, lane 31: column x0 + 256), black-levelled and white-balanced ----------------
-            int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            // ---- this lane's 8 samples of row y (packed pairs) and the strip's outer neighbour
+            // (lane 0: column x0 - 1, lane 31: column x0 + 256), black-levelled and white-balanced --
+            uint32_t P[4] = {0u, 0u, 0u, 0u};
             int nb = 0;
             if (len > 0) {
-                if (xl < W) decode_at<FMT>(fp, row, a0, len, y, xl, v);
+                if (xl < W) decode_pairs<FMT>(fp, row, a0, len, y, xl, P);
                 if (lane == 0 || lane == 31) {
                     const int xn = lane == 0 ? cur.x0 - 8 : cur.x0 + kLiteStripMax;
                     if (xn >= 0 && xn < W) {
-                        int t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                        decode_at<FMT>(fp, row, a0, len, y, xn, t);
-                        nb = lane == 0 ? t[7] : t[0];
+                        uint32_t t[4];
+                        decode_pairs<FMT>(fp, row, a0, len, y, xn, t);
+                        nb = lane == 0 ? (int)(t[3] >> 16) : (int)(t[0] & 0xFFFFu);
                     }
                 }
                 const int p = y & 1;
-                // black level (integral offsets: lite_eligible): (int)((float)v - off) clamped to
-                // [0, mv], one add-min-relu
-                if (bl_on) {
-                    const int bl_e = fp.bl_i[p][0], bl_o = fp.bl_i[p][1];
+                const int bl_e = fp.bl_i[p][0], bl_o = fp.bl_i[p][1];
+                // u16 samples above 32767 (beyond any bit depth here) do not fit the pairs' signed
+                // 16-bit add: those lanes take the per-sample path
+                const bool per_sample =
+                    per_sample_frame || (FMT == FMT_U16 && bl_on && ((P[0] | P[1] | P[2] | P[3]) & 0x80008000u) != 0);
+                if (!per_sample) {
+                    // black level (integral offsets <= the maximum: lite_eligible) on both samples of
+                    // a pair at once: (int)((float)v - off) clamped to [0, mv]
+                    if (bl_on) {
+                        const uint32_t nbl = ((uint32_t)(-bl_e) & 0xFFFFu) | ((uint32_t)(-bl_o) << 16);
+                        const uint32_t mv2 = (uint32_t)mv | ((uint32_t)mv << 16);
 #pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = __viaddmin_s32_relu(v[j], (j & 1) ? -bl_o : -bl_e, mv);
-                    nb = __viaddmin_s32_relu(nb, lane == 0 ? -bl_o : -bl_e, mv);
-                }
-                if (wb_bayer) {
+                        for (int j = 0; j < 4; j++) P[j] = __viaddmin_s16x2_relu(P[j], nbl, mv2);
+                        nb = __viaddmin_s32_relu(nb, lane == 0 ? -bl_o : -bl_e, mv);
+                    }
+                } else {
                     const float wb_e = fp.wb_cfa[bayer_color(y, 0, po)], wb_o = fp.wb_cfa[bayer_color(y, 1, po)];
+                    auto one = [&](int v, bool odd) {
+                        if (bl_on) v = __viaddmin_s32_relu(v, odd ? -bl_o : -bl_e, mv);
+                        if (wb_bayer) v = dev::gain_round(v, odd ? wb_o : wb_e, mv);
+                        if (need_align && v > mv) v >>= (16 - fp.bd);
+                        return v;
+                    };
 #pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = dev::gain_round(v[j], (j & 1) ? wb_o : wb_e, mv);
-                    nb = dev::gain_round(nb, lane == 0 ? wb_o : wb_e, mv);
-                }
-                if (need_align) {
-                    // the demosaic's u16 read of MSB-aligned samples (align_raw_value)
-                    const int sh = 16 - fp.bd;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = v[j] > mv ? v[j] >> sh : v[j];
-                    nb = nb > mv ? nb >> sh : nb;
+                    for (int j = 0; j < 4; j++)
+                        P[j] = (uint32_t)one((int)(P[j] & 0xFFFFu), false) | ((uint32_t)one((int)(P[j] >> 16), true) << 16);
+                    nb = one(nb, lane == 0);
                 }
                 if (lane == 0 && cur.x0 == 0) nb = 0;
             }
-            int left = __shfl_up_sync(0xffffffffu, v[7], 1);
-            int right = __shfl_down_sync(0xffffffffu, v[0], 1);
-            if (lane == 0) left = nb;
-            if (lane == 31) right = nb;
+            uint32_t Lw = __shfl_up_sync(0xffffffffu, P[3], 1) & 0xFFFF0000u;
+            uint32_t Rn = __shfl_down_sync(0xffffffffu, P[0], 1) & 0xFFFFu;
+            if (lane == 0) Lw = (uint32_t)nb << 16;
+            if (lane == 31) Rn = (uint32_t)nb;
             // the slot is consumed: every lane's reads of it come before the copy that refills it
             ptx::fence_proxy_async_smem();
             __syncwarp();
             used++;
             issue_next();
-            // slide the window: rows y-2, y-1 (U_, M) and y (D)
+            // slide the window
+            Ur = Mr;
+            Mr = Dr;
 #pragma unroll
-            for (int j = 0; j < 10; j++) {
-                U_[j] = M[j];
-                M[j] = D[j];
-            }
-            D[0] = left;
-#pragma unroll
-            for (int j = 0; j < 8; j++) D[1 + j] = v[j];
-            D[9] = right;
+            for (int j = 0; j < 4; j++) Dr.P[j] = P[j];
+            Dr.Lw = Lw;
+            Dr.R = Rn;
             if (k < 2) continue;
 
             // ---- output row yo = y - 1 -------------------------------------------------------------
             const int yo = y - 1;
             if (yo < 2 || yo >= H - 2) continue;  // emitted with row 2 / h-3
-            int R[8], G[8], B[8];
+            uint32_t ob[6];
             const bool rrow = (yo & 1) == po.r_row;
             const int rb = rrow ? po.r_col : po.b_col;
             if (rb == 0) {
-                if (rrow) lite::hqli8<0, true>(U_, M, D, R, G, B);
-                else lite::hqli8<0, false>(U_, M, D, R, G, B);
+                if (rrow) lite::hqli_row<0, true>(Ur, Mr, Dr, sm.tab, ob);
+                else lite::hqli_row<0, false>(Ur, Mr, Dr, sm.tab, ob);
             } else {
-                if (rrow) lite::hqli8<1, true>(U_, M, D, R, G, B);
-                else lite::hqli8<1, false>(U_, M, D, R, G, B);
+                if (rrow) lite::hqli_row<1, true>(Ur, Mr, Dr, sm.tab, ob);
+                else lite::hqli_row<1, false>(Ur, Mr, Dr, sm.tab, ob);
             }
-            uint32_t ob[6];
-#pragma unroll
-            for (int q = 0; q < 6; q++) {
-                // bytes 4q .. 4q+3 of the lane's 24: pixel (4q + b) / 3, channel (4q + b) % 3
-                uint32_t bt[4];
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int n = 4 * q + b, px = n / 3, ch = n % 3;
-                    bt[b] = sm.tab[ch][ch == 0 ? R[px] : ch == 1 ? G[px] : B[px]];
-                }
-                ob[q] = __byte_perm(__byte_perm(bt[0], bt[1], 0x0040), __byte_perm(bt[2], bt[3], 0x0040), 0x5410);
-            }
-            // stage at the output row's 16-byte phase, fix the border columns, store
             const int g0 = (yo * W + cur.x0) * 3;
+            // an interior strip whose row starts 8-byte aligned: each lane stores its 24 bytes
+            if (!edge_l && !edge_r && yo != 2 && yo != H - 3 && ((out_base + (uintptr_t)g0) & 7) == 0) {
+                if (lane_in) {
+                    uint2* q = reinterpret_cast<uint2*>(fp.out + g0 + 24 * lane);
+                    q[0] = make_uint2(ob[0], ob[1]);
+                    q[1] = make_uint2(ob[2], ob[3]);
+                    q[2] = make_uint2(ob[4], ob[5]);
+                }
+                continue;
+            }
+            // otherwise: stage at the output row's 16-byte phase, fix the border columns, store
             const int shift = (int)((out_base + (uintptr_t)g0) & 15);
             const int nbytes = 3 * cur.npx;
             uint8_t* st = ws.out + shift + 24 * lane;
@@ -366,7 +397,8 @@ bool lite_eligible(const FrameParams& fp) {
     // integral black levels (one add-min-relu per sample), and samples no larger than the bit depth's
     // maximum when they reach the demosaic (a stage clamps them, the MSB-aligned u16 read, a packed
     // format, or full 8-bit bytes), so HQLI needs no clamps
-    const bool bl_ok = !(fp.stages & 1u) || fp.bl_int;
+    bool bl_ok = !(fp.stages & 1u) || fp.bl_int;
+    for (int c = 0; c < 4; c++) bl_ok = bl_ok && (!(fp.stages & 1u) || fp.bl[c] <= (float)fp.mv);
     const bool bounded =
         (fp.stages & 1u) || ((fp.stages & 8u) && fp.stage_order == 0) || fp.fmt != FMT_U8 || fp.bd == 8;
     return fmt_ok && bl_ok && bounded && fp.bd <= 12 && fp.demosaic == DM_HQLI &&

@@ -144,30 +144,77 @@ __device__ __forceinline__ int byte_of(int i) {
     return FMT == FMT_U8 ? i : FMT == FMT_U16 ? 2 * i : FMT == FMT_P12 ? 3 * (i >> 1) : 5 * (i >> 2);
 }
 
-// RGB of the 8 pixels of a lane's row (m) from the rows above (u) and below (d): detail::hqli_core
-// (src/algorithms/interp_core.hpp:39-65) at interior sites; index 0 / 9 hold the columns left /
-// right of the lane's pixels.  RB: which pixel of each pair is the red / blue site; RR: the row is
-// a red row.  The samples never exceed the bit depth's maximum here (lite_eligible), so the
-// reference's clamps of the averages to that maximum are identities.
+// A row of a lane as packed u16 pairs: P[j] = pixel 2j | pixel 2j+1 << 16 (j = 0..3), Lw = the
+// column left of the lane << 16, R = the column right of it.  Samples are at most 4095 (bit depth
+// <= 12), so sums of up to four of them never carry from one half-word into the other.
+struct Row {
+    uint32_t P[4];
+    uint32_t Lw, R;
+};
+
+// byte k of word w replaced by byte 0 of t
+__device__ __forceinline__ uint32_t put_byte(uint32_t w, uint32_t t, int k) {
+    return __byte_perm(w, t, k == 0 ? 0x3214 : k == 1 ? 0x3240 : k == 2 ? 0x3410 : 0x4210);
+}
+
+// HQLI (detail::hqli_core, src/algorithms/interp_core.hpp:39-65) of the lane's 8 pixels of row m
+// from rows u and d, two pixels per 32-bit operation, each output through its channel's table
+// (tab[c][v]) into 24 bytes (ob, pixel-interleaved RGB).  RB: the pixel of each pair at the red /
+// blue site (0 even, 1 odd); RR: the row holds red sites.  Per pair j (pixels 2j, 2j+1):
+//   Hp = horizontal neighbour sums (m[p-1] + m[p+1]) of both pixels    = Me[j] + Me[j+1]
+//   Vp = vertical sums (u[p] + d[p])                                  = U[j] + D[j]
+//   Dg = diagonal sums (u + d at p-1 plus at p+1)                      = Ve[j] + Ve[j+1]
+// where Me / Ve are the rows shifted by one pixel (pairs 2j-1, 2j).  A red / blue site takes
+// (Hp + Vp + 2) >> 2 for green and (Dg + 2) >> 2 for the other colour; a green site
+// (Hp + 1) >> 1 and (Vp + 1) >> 1 for the horizontal / vertical colour.  The samples never exceed
+// the bit depth's maximum (lite_eligible), so the reference's clamps of these averages are
+// identities.
 template <int RB, bool RR>
-__device__ __forceinline__ void hqli8(const int (&u)[10], const int (&m)[10], const int (&d)[10], int (&R)[8],
-                                      int (&G)[8], int (&B)[8]) {
+__device__ __forceinline__ void hqli_row(const Row& u, const Row& m, const Row& d, const uint8_t (*tab)[4096],
+                                         uint32_t (&ob)[6]) {
+    uint32_t VN[4];
 #pragma unroll
-    for (int p = 0; p < 8; p++) {
-        const int i = p + 1;
-        if ((p & 1) == RB) {
-            const int own = m[i];
-            const int gq = (m[i - 1] + m[i + 1] + u[i] + d[i] + 2) >> 2;
-            const int oq = (u[i - 1] + u[i + 1] + d[i - 1] + d[i + 1] + 2) >> 2;
-            R[p] = RR ? own : oq;
-            B[p] = RR ? oq : own;
-            G[p] = gq;
+    for (int j = 0; j < 4; j++) VN[j] = u.P[j] + d.P[j];
+    const uint32_t VL = u.Lw + d.Lw, VR = u.R + d.R;
+    const uint32_t vs[6] = {VL, VN[0], VN[1], VN[2], VN[3], VR};
+    const uint32_t ms[6] = {m.Lw, m.P[0], m.P[1], m.P[2], m.P[3], m.R};
+    uint32_t Ve[5], Me[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+        Ve[j] = __funnelshift_r(vs[j], vs[j + 1], 16);
+        Me[j] = __funnelshift_r(ms[j], ms[j + 1], 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const uint32_t Hp = Me[j] + Me[j + 1], Dg = Ve[j] + Ve[j + 1], Vp = VN[j], Own = m.P[j];
+        uint32_t gq, hz, vt, oq, own, g;
+        if (RB == 0) {
+            const uint32_t X = Hp + (Vp & 0xFFFFu) + 0x00010002u;
+            gq = (X & 0xFFFFu) >> 2;
+            hz = X >> 17;
+            vt = (Vp + 0x10000u) >> 17;
+            oq = ((Dg + 2u) & 0xFFFFu) >> 2;
+            own = Own & 0xFFFFu;
+            g = Own >> 16;
         } else {
-            const int hz = (m[i - 1] + m[i + 1] + 1) >> 1;
-            const int vt = (u[i] + d[i] + 1) >> 1;
-            G[p] = m[i];
-            R[p] = RR ? hz : vt;
-            B[p] = RR ? vt : hz;
+            const uint32_t X = Hp + (Vp & 0xFFFF0000u) + 0x00020001u;
+            hz = (X & 0xFFFFu) >> 1;
+            gq = X >> 18;
+            vt = ((Vp + 1u) & 0xFFFFu) >> 1;
+            oq = (Dg + 0x20000u) >> 18;
+            own = Own >> 16;
+            g = Own & 0xFFFFu;
+        }
+        // the red / blue site and the green site of the pair
+        const uint32_t rs_r = RR ? own : oq, rs_b = RR ? oq : own;
+        const uint32_t gs_r = RR ? hz : vt, gs_b = RR ? vt : hz;
+        const uint32_t r0 = RB == 0 ? rs_r : gs_r, g0 = RB == 0 ? gq : g, b0 = RB == 0 ? rs_b : gs_b;
+        const uint32_t r1 = RB == 0 ? gs_r : rs_r, g1 = RB == 0 ? g : gq, b1 = RB == 0 ? gs_b : rs_b;
+        const uint32_t t[6] = {tab[0][r0], tab[1][g0], tab[2][b0], tab[0][r1], tab[1][g1], tab[2][b1]};
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            const int n = 6 * j + c;
+            ob[n >> 2] = (n & 3) == 0 ? t[c] : put_byte(ob[n >> 2], t[c], n & 3);
         }
     }
 }

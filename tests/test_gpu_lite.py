@@ -1,7 +1,8 @@
 """The light-chain kernel (HQLI without defect correction, lens shading or CCM; isp_lite.cuh)
 against the CPU oracle, bit for bit: every input format it takes, bit depths 1-12, both
-white-balance orders, integral and fractional black levels, every tone mode, all Bayer patterns,
-frames from 4x4 up to the 5320x4600 frames of the large-frame workload, widths that are not
+white-balance orders, integral and fractional black levels (the latter through the general
+kernel), every tone mode, all Bayer patterns, frames from 6x6 up to the 5320x4600 frames of the
+large-frame workload, widths that are not
 multiples of the tile, unaligned input and output pointers, samples above the bit depth's maximum
 (the reference's MSB-aligned read), and batches that mix it with the general kernel."""
 import numpy as np
@@ -106,6 +107,14 @@ def test_lite_values_above_max_without_clamping_stages(isp):
     for bd, packed in ((6, False), (8, False), (10, False), (12, False)):
         pl = I.Pipeline(width=131, height=70, bit_depth=bd, packed=packed, pattern=abi.GBRG, demosaic=abi.HQLI,
                         stages=0)
+        raw = _frame(rng, pl, over=True)
+        ref, _ = O.pipeline(pl, raw)
+        assert max_abs(_run(isp, pl, raw), ref) == 0, bd
+    # u16 samples above 32767 with black level on (the per-sample path of the lanes holding them)
+    for bd in (10, 12):
+        pl = I.Pipeline(width=300, height=41, bit_depth=bd, packed=False, pattern=abi.RGGB, demosaic=abi.HQLI,
+                        stages=abi.STAGE_BLACK_LEVEL | abi.STAGE_WHITE_BALANCE, stage_order=abi.ORDER_RGB_WB,
+                        bl_offset=(20.0, 21.0, 22.0, 23.0), wb_gain=(1.7, 1.0, 1.4))
         raw = _frame(rng, pl, over=True)
         ref, _ = O.pipeline(pl, raw)
         assert max_abs(_run(isp, pl, raw), ref) == 0, bd
