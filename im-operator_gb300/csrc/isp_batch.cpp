@@ -160,6 +160,7 @@ int resolve_tables(imop_isp_ctx* c, const ImopIspParams* p, FrameParams& fp, con
         fp.gw = p->lsc_mode == IMOP_LSC_FLAT_FIELD ? 32 : p->lsc_grid_w;
         fp.gh = p->lsc_mode == IMOP_LSC_FLAT_FIELD ? 24 : p->lsc_grid_h;
         fp.grid = (const float*)slot->ptr;
+        fp.lsc_bounded = lsc_grid_bounded(p);
     }
     if (p->stages & IMOP_STAGE_LUT3D) {
         Key k;
@@ -272,6 +273,8 @@ int prepare_batch(imop_isp_ctx* c, const ImopFrameDesc* frames, int n, std::vect
         fp.seed_cap = b.cap;
         fp.status = (int*)c->fix.status.ptr;
         fp.tile_counter = (int*)c->fix.tile_counter.ptr;
+        fp.seg_words = (unsigned long long*)c->fix.seg.ptr;
+        fp.seg_cap = c->fix.seg.ptr ? kStreamSegCap : 0;
         fp.fix_heap = (int*)b.heap.ptr + off;
         fp.fix_ov_idx = (int*)b.ov_idx.ptr + off;
         fp.fix_ov_val = (int*)b.ov_val.ptr + off;

@@ -134,6 +134,14 @@ void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan
 
 // Grid construction of lens_shading::process_flat_field (src/lens_shading/flat_field.cpp:30-76):
 // a parameter derivation done once per set_params, 32 x 24 x 4 gains.
+int lsc_grid_bounded(const ImopIspParams* p) {
+    if (!(p->stages & IMOP_STAGE_LENS_SHADING) || p->lsc_mode != IMOP_LSC_GRID || !p->lsc_grid) return 0;
+    const size_t n = (size_t)p->lsc_grid_w * p->lsc_grid_h * 4;
+    for (size_t i = 0; i < n; i++)
+        if (!(p->lsc_grid[i] >= 0.0f && p->lsc_grid[i] <= 15.0f)) return 0;
+    return 1;
+}
+
 int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm) {
     if (!ff) return fail(IMOP_ERR_NULL_INPUT, "flat-field frame is null");
     if (ffw <= 0 || ffh <= 0) return fail(IMOP_ERR_INVALID_DIMENSIONS, "flat-field dimensions");
@@ -352,6 +360,7 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
             }
             if ((e = upload(tabs.grid, g))) return cuda_fail(e, "upload lens-shading grid");
             fp.grid = (const float*)tabs.grid.ptr;
+            fp.lsc_bounded = lsc_grid_bounded(p);
         }
     }
     if (p->stages & IMOP_STAGE_LUT3D) {
@@ -384,7 +393,7 @@ int ensure_fixup(FixupState& fx, int cap) {
     cudaError_t e;
     if (fx.cap >= cap && fx.seed_count.ptr) return IMOP_OK;
     if ((e = fx.seed_count.ensure(sizeof(int))) || (e = fx.status.ensure(sizeof(int))) ||
-        (e = fx.tile_counter.ensure(sizeof(int))) ||
+        (e = fx.tile_counter.ensure(sizeof(int))) || (e = fx.seg.ensure(kStreamSegCap * sizeof(unsigned long long))) ||
         (e = fx.seeds.ensure((size_t)cap * sizeof(int))) || (e = fx.heap.ensure((size_t)cap * sizeof(int))) ||
         (e = fx.ov_idx.ensure((size_t)cap * sizeof(int))) || (e = fx.ov_val.ensure((size_t)cap * sizeof(int))) ||
         (e = fx.n_ov.ensure(sizeof(int))))
@@ -418,6 +427,8 @@ void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs) {
     fp.seed_cap = fx.cap;
     fp.status = (int*)fx.status.ptr;
     fp.tile_counter = (int*)fx.tile_counter.ptr;
+    fp.seg_words = (unsigned long long*)fx.seg.ptr;
+    fp.seg_cap = kStreamSegCap;
     fs.heap = (int*)fx.heap.ptr;
     fs.ov_idx = (int*)fx.ov_idx.ptr;
     fs.ov_val = (int*)fx.ov_val.ptr;

@@ -120,6 +120,8 @@ struct FrameParams {
     int seed_cap;
     int* status;         // sticky error word (IMOP_ERR_*), 0 when fine
     int* tile_counter;   // next-tile counter of the fused launch (one per launch, zeroed before it)
+    unsigned long long* seg_words;  // work-claim words of the streaming kernel (seg_cap of them)
+    int seg_cap;
     // defect-chain fix-up scratch of this frame (heap, sorted override list)
     int* fix_heap;
     int* fix_ov_idx;
@@ -132,6 +134,8 @@ struct FrameParams {
     // optional 3D LUT after the CCM (stage bit 5): size^3 x 3 floats, R-major
     const float* lut3d;
     int lut3d_size;
+    // lens-shading grid gains all finite and within [0, 15] (the streaming kernel's packed halves)
+    int lsc_bounded;
 };
 
 }  // namespace imop

@@ -78,7 +78,7 @@ struct BatchGraph {
 
 // defect-chain scratch (seeds, heap, overrides) and the sticky status word
 struct FixupState {
-    DevBuf seed_count, seeds, heap, ov_idx, ov_val, n_ov, status, tile_counter;
+    DevBuf seed_count, seeds, heap, ov_idx, ov_val, n_ov, status, tile_counter, seg;
     int cap = 0;
 };
 
@@ -123,6 +123,9 @@ int build_frame_params(const ImopIspParams* p, FrameTables& tabs, FrameParams& f
 int upload_map_plan(const ImopIspParams* p, FrameTables& tabs, FrameParams& fp);
 void build_map_plan(const ImopDefectPoint* map, int n, int w, int h, HostMapPlan& P);
 int flat_field_grid(const void* ff, int ffw, int ffh, int pattern, int bd, std::vector<float>& gm);
+// 1 when every gain of an explicit lens-shading grid (ImopIspParams::lsc_grid) is finite and within
+// [0, 15], the range the streaming kernel takes; 0 for the other shading modes
+int lsc_grid_bounded(const ImopIspParams* p);
 int ensure_fixup(FixupState& fx, int cap);
 bool device_mapped_host(const void* p, size_t n);
 void attach_fixup(FixupState& fx, FrameParams& fp, FixupScratch& fs);

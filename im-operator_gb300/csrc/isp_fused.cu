@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "isp_kernels.h"
@@ -223,6 +224,7 @@ struct FusedKernels {
         if (bl.n_items > 0) {
             if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             const int grid = bl.n_items < limit ? bl.n_items : limit;
+            count_launch(0);
             if (OUTB == 3 && bl.simple && !bl.extra && bl.demosaic && bl.fmt >= FMT_U8 && bl.fmt <= FMT_P12) {
                 if ((e = launch_fused_spec(bl.fmt, bl.demosaic, bl.no_dpc_lsc != 0, bl, grid, smem, st)) != cudaSuccess)
                     return e;
@@ -256,15 +258,15 @@ struct FusedKernels {
 template <int OUTB> int FusedKernels<OUTB>::ctas_per_sm[kMaxDevices] = {};
 template <int OUTB> int FusedKernels<OUTB>::sms[kMaxDevices] = {};
 
-void add_rect(BatchLaunch& bl, int frame, int x0, int y0, int w, int h, int& items) {
+void add_rect(BatchLaunch& bl, int frame, int x0, int y0, int w, int h, int& items, int tw = kTileW, int th = kTileH) {
     TileRect& R = bl.rects[bl.n_rects];
     R.frame = frame;
     R.x0 = x0;
     R.y0 = y0;
     R.w = w;
     R.h = h;
-    R.tiles_x = tiles_along(w, kTileW);
-    R.tiles_y = tiles_along(h, kTileH);
+    R.tiles_x = tiles_along(w, tw);
+    R.tiles_y = tiles_along(h, th);
     bl.rect_start[bl.n_rects] = items;
     items += R.tiles_x * R.tiles_y;
     bl.n_rects++;
@@ -342,7 +344,38 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
         }
         return e;
     }
+    // the AMAZE chains: the interior of every frame by the streaming kernel, then the border rows
+    // and columns by the tile kernel (its launch also runs the defect-chain fix-up of the frames)
+    bool stream = true;
+    for (int f = 0; f < n; f++)
+        stream = stream && stream_eligible(frames[f]) && frames[f].fmt == frames[0].fmt &&
+                 frames[f].tone8 == frames[0].tone8 && frames[f].seg_words == frames[0].seg_words;
     if (!make_launch(frames, n, bl, fixup)) return cudaErrorInvalidValue;
+    if (stream) {
+        // interior: the streaming kernel; border columns: the narrow tile; border rows: the nominal
+        // tile, whose launch also runs the fix-up
+        BatchLaunch bs = bl, bn = bl;
+        int items_s = 0, items_n = 0, items_b = 0;
+        bs.n_rects = bn.n_rects = bl.n_rects = 0;
+        for (int f = 0; f < n; f++) {
+            TileRect in, border[4];
+            stream_rects(frames[f], in, border);
+            in.frame = f;
+            bs.rects[bs.n_rects] = in;
+            bs.rect_start[bs.n_rects++] = items_s;
+            items_s += in.tiles_x * in.tiles_y;
+            for (int k = 0; k < 2; k++) add_rect(bl, f, border[k].x0, border[k].y0, border[k].w, border[k].h, items_b);
+            for (int k = 2; k < 4; k++)
+                add_rect(bn, f, border[k].x0, border[k].y0, border[k].w, border[k].h, items_n, kNarrowW, kNarrowH);
+        }
+        bs.rect_start[bs.n_rects] = bs.n_items = items_s;
+        bs.seg_words = frames[0].seg_words;
+        bn.rect_start[bn.n_rects] = bn.n_items = items_n;
+        bl.rect_start[bl.n_rects] = bl.n_items = items_b;
+        cudaError_t e = launch_stream(bs, st);
+        if (e == cudaSuccess) e = launch_fused_narrow(bn, st);
+        if (e != cudaSuccess) return e;
+    }
     return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st, split)
                                   : FusedKernels<3>::launch(bl, fixup, st, split);
 }
@@ -364,6 +397,13 @@ std::mutex& device_setup_mutex() {
     return m;
 }
 
+static std::atomic<long long> g_launches[3];
+void count_launch(int kernel) { g_launches[kernel].fetch_add(1, std::memory_order_relaxed); }
+
+extern "C" long long imop_kernel_launches(int kernel) {
+    return (kernel >= 0 && kernel < 3) ? g_launches[kernel].load(std::memory_order_relaxed) : -1;
+}
+
 int fused_grid_limit(int out_bpc) {
     int limit = 0;
     cudaError_t e = out_bpc == 2 ? FusedKernels<6>::setup(limit) : FusedKernels<3>::setup(limit);
@@ -379,6 +419,8 @@ static long long instantiation_key(const FrameParams& fp) {
     if (extra) return (long long)fp.out_bpc << 32;
     // the light-chain kernel: one launch per input format and output table set
     if (lite_eligible(fp)) return (1LL << 62) | ((long long)fp.fmt << 56) | (lite_table_key(fp) & ((1LL << 56) - 1));
+    // the streaming kernel: one launch per input format and tone table
+    if (stream_eligible(fp)) return (1LL << 61) | ((long long)fp.fmt << 56) | (stream_table_key(fp) & ((1LL << 56) - 1));
     const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
            (lite ? (1 << 12) : 0) | (simple ? fp.fmt + 1 : 0);

@@ -12,13 +12,18 @@ namespace imop {
 // nominal fused tile (the last tile of a row / column absorbs a remainder below 4)
 constexpr int kTileW = 120;
 constexpr int kTileH = 24;
+// work-claim words of one streaming launch (segments of its strips)
+constexpr int kStreamSegCap = 4096;
+// narrow fused tile of the border columns of streamed frames (isp_fused_narrow.cu)
+constexpr int kNarrowW = 16;
+constexpr int kNarrowH = 128;
 
 // Frames of one fused launch, passed by value as the kernel's parameter block.  The kernel walks
 // the tiles of a list of rectangles (one per frame), rectangle after rectangle, tiles in raster
 // order; CTAs claim tiles from a device counter, so border tiles (the general path) and
 // partial tiles do not unbalance the CTAs.
 constexpr int kBatchInline = 16;
-constexpr int kMaxRects = kBatchInline;
+constexpr int kMaxRects = 4 * kBatchInline;  // the border rectangles of a streamed batch
 struct TileRect {
     int frame;
     int x0, y0, w, h;  // x0 even; w, h >= 4
@@ -34,6 +39,8 @@ struct BatchLaunch {
     int simple;                     // every frame has the common stage configuration (per-format kernels)
     int no_dpc_lsc;                 // no frame corrects defects or lens shading
     int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
+    unsigned long long* seg_words;  // streaming kernel: per segment, bands claimed (front | back << 32)
+    int band_h;                     // streaming kernel: rows of a band
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];
@@ -62,6 +69,9 @@ struct MapPlan {
 // reference-named glue gives each host thread its own context, so first calls can come from
 // several threads at once
 std::mutex& device_setup_mutex();
+
+// launches enqueued per fused kernel (IMOP_KERNEL_TILE / _LITE / _STREAM)
+void count_launch(int kernel);
 
 int fused_tile_grid(int w, int h, int& ntx, int& nty);
 cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots, int bd, uint8_t* d_out,
@@ -103,6 +113,23 @@ int lite_units_x(int w);
 int lite_units_y(int h);
 // one persistent launch over the units of bl's rectangles (bl.fmt: the frames' common format)
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
+
+// warp-streamed kernel for the AMAZE chains (isp_stream.cu): black level, adaptive defect
+// correction, grid lens shading, Bayer-order white balance, AMAZE, CCM, tone -> RGB8 on the interior
+// of each frame; u8 / u16 / MIPI RAW10 / RAW12 input, width a multiple of 8, bit depth <= 12
+bool stream_eligible(const FrameParams& fp);
+// frames of one streamed launch share this key (their tone table) and the input format
+long long stream_table_key(const FrameParams& fp);
+// the interior rectangle of a frame (tiles_x / tiles_y: strips and bands) and the four border
+// rectangles (rows 0-6, rows h-7.., columns 0-7 and the right columns of the rows between) that the
+// tile kernel takes
+void stream_rects(const FrameParams& fp, TileRect& interior, TileRect (&border)[4]);
+// the tile kernel over bl's rectangles in the narrow tile (AMAZE frames without a bit stream or
+// 3D LUT; rectangles at most kNarrowW wide, tiles_x / tiles_y in that tile)
+cudaError_t launch_fused_narrow(const BatchLaunch& bl, cudaStream_t st);
+// one persistent launch over bl's interior rectangles (bl.fmt: the frames' common format); the
+// band height, the same for every rectangle, is chosen here
+cudaError_t launch_stream(const BatchLaunch& bl, cudaStream_t st);
 
 // plain per-operator form: one kernel per stage over full frames in device memory.
 // Buffers: bayer_a/bayer_b are w*h u16, rgb is w*h*3 u16.

@@ -449,6 +449,7 @@ cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
     // enough CTAs that every warp has a unit, at most the resident limit
     const int want = (bl.n_items + kLiteWarps - 1) / kLiteWarps;
     const int grid = want < limit ? want : limit;
+    count_launch(1);
     switch (bl.fmt) {
         case FMT_U8: return launch_fmt<FMT_U8>(bl, grid, smem, st);
         case FMT_U16: return launch_fmt<FMT_U16>(bl, grid, smem, st);

@@ -65,6 +65,7 @@ def lib():
             "imop_abi_version": (i, []),
             "imop_has_cuda": (i, []),
             "imop_shim_calls_served": (C.c_longlong, []),
+            "imop_kernel_launches": (C.c_longlong, [i]),
             "imop_tone_table_entries": (sz, [i]),
             "imop_tone_table": (i, [i, i, C.POINTER(abi.ToneParams), vp, sz]),
             "imop_op_rgb_table": (i, [vp, i, i, i, vp, vp, vp]),

@@ -489,6 +489,12 @@ int imop_has_cuda(void);
  * device and that returned Ok: a reference dispatcher linked against this library falls back to
  * its CPU code silently on any other status, so this count tells an integrator which one ran. */
 long long imop_shim_calls_served(void);
+/* Fused-kernel launches this process enqueued, by kernel: the tile kernel (every chain, and the
+ * border rows / columns of streamed frames), the light-chain kernel (HQLI without defect
+ * correction or lens shading) and the streaming kernel (the interior of AMAZE frames).  A launch
+ * recorded into a CUDA graph counts once, when it is recorded. */
+enum { IMOP_KERNEL_TILE = 0, IMOP_KERNEL_LITE = 1, IMOP_KERNEL_STREAM = 2 };
+long long imop_kernel_launches(int kernel);
 
 #ifdef __cplusplus
 }
