@@ -349,9 +349,9 @@ __device__ __forceinline__ void green_row(const uint32_t (&m2)[4], const uint32_
 // ---- output row q: AMAZE colour differences (src/algorithms/common.hpp:142-199), CCM, tone ------
 // cdm / cdc / cdp: colour differences of rows q-1, q, q+1 with the neighbouring lane's value each
 // needs (em / ec / ep: pair -1 or 4); gq: green of row q; bq: bay row q.  RBH: the half at the red /
-// blue site; RROW: the row holds red sites.
-template <int RBH, bool RROW>
-__device__ __forceinline__ void out_row(const float (&cdm)[4], float em, const float (&cdc)[4], float ec,
+// blue site; rrow: the row holds red sites (a row of blue sites is the same with R and B swapped).
+template <int RBH>
+__device__ __forceinline__ void out_row(bool rrow, const float (&cdm)[4], float em, const float (&cdc)[4], float ec,
                                         const float (&cdp)[4], float ep, const float (&gq)[4], const uint32_t (&bq)[4],
                                         const float (&m)[9], bool ccm_on, uint32_t mv2, float2 z2,
                                         const uint8_t* tone, uint32_t (&ob)[6]) {
@@ -370,14 +370,13 @@ __device__ __forceinline__ void out_row(const float (&cdm)[4], float em, const f
         const float2 rb2 = dev::fma2(hv, h5, make_float2(fgg, fgg));
         const uint32_t W1 = round_pack(make_float2(other, gq[j]), mv2);  // (other colour, green) at the R/B site
         const uint32_t W2 = round_pack(rb2, mv2);                           // (horizontal, vertical) at the G site
-        // sources of R, G, B of both pixels: (word, half)
-        // R/B site: R = own / other, G = green, B = other / own; G site: R = hz / vt, G = own, B = vt / hz
+        // sources of R, G, B of both pixels, (word, half), in a row of red sites: R/B site R = own,
+        // G = green, B = other; G site R = horizontal, G = own, B = vertical
         const uint32_t wb = bq[j];
         uint32_t Rw, Gw, Bw;  // (pixel 0, pixel 1) per channel
-        // per pixel: the R/B site's values, the G site's values
-        const uint32_t rs_r = RROW ? wb : W1, rs_b = RROW ? W1 : wb;  // word holding R / B at the R/B site
-        const int rs_rh = RROW ? RBH : 0, rs_bh = RROW ? 0 : RBH;     // its half
-        const int gs_rh = RROW ? 0 : 1, gs_bh = RROW ? 1 : 0;         // halves of W2 holding R / B at the G site
+        const uint32_t rs_r = wb, rs_b = W1;  // word holding R / B at the R/B site
+        const int rs_rh = RBH, rs_bh = 0;     // its half
+        const int gs_rh = 0, gs_bh = 1;       // halves of W2 holding R / B at the G site
         // pixel 0 is the R/B site when RBH == 0
         auto sel = [&](uint32_t w0, int h0, uint32_t w1, int h1) -> uint32_t {
             // (half h0 of w0) | (half h1 of w1) << 16
@@ -391,6 +390,11 @@ __device__ __forceinline__ void out_row(const float (&cdm)[4], float em, const f
             Rw = sel(W2, gs_rh, rs_r, rs_rh);
             Gw = sel(wb, 0, W1, 1);
             Bw = sel(W2, gs_bh, rs_b, rs_bh);
+        }
+        if (!rrow) {
+            const uint32_t t = Rw;
+            Rw = Bw;
+            Bw = t;
         }
         if (ccm_on) {
             const float2 rr = halves_f2(Rw), gg = halves_f2(Gw), bb = halves_f2(Bw);
@@ -644,13 +648,8 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
                     const bool rrow = (q & 1) == po.r_row;
                     const int rbh = rrow ? po.r_col : po.b_col;
                     uint32_t ob[6];
-                    if (rbh == 0) {
-                        if (rrow) out_row<0, true>(cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
-                        else out_row<0, false>(cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
-                    } else {
-                        if (rrow) out_row<1, true>(cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
-                        else out_row<1, false>(cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
-                    }
+                    if (rbh == 0) out_row<0>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
+                    else out_row<1>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
                     if (lane_out) {
                         uint8_t* dst = outp;
                         if ((out_base & 7) == 0) {

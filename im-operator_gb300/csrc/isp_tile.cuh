@@ -593,14 +593,23 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
             }
         }
     } else {
+        // wide regions: a warp takes 32 pair columns of one row; narrow ones (border columns): the
+        // (row, pair) items spread over all threads, so the lanes are not mostly idle
         const int nbk = (bpw + 31) >> 5;
+        const bool flat = bpw <= 16;
         int cache_key = -1;
         float2 A = make_float2(0.f, 0.f), B = A, C = A, D = A, WB = make_float2(1.f, 1.f);
-        for (int item = warp; item < nbk * bh; item += 8) {
-            int blk, r;
-            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
-            int pc = blk * 32 + lane;
-            if (pc >= bpw) continue;
+        for (int item = flat ? tid : warp; item < (flat ? bh * bpw : nbk * bh); item += flat ? kThreads : 8) {
+            int r, pc;
+            if (flat) {
+                r = item / bpw;
+                pc = item - r * bpw;
+            } else {
+                int blk;
+                if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+                pc = blk * 32 + lane;
+                if (pc >= bpw) continue;
+            }
             int y = yb + r, x = xb + 2 * pc;
             const int* o = orig + (r + 2) * G::OW + (x - xo);
             int2 c = *reinterpret_cast<const int2*>(o);
@@ -774,12 +783,19 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         }
     } else if (demosaic != DM_HQLI) {
         const int nbk = (gpw + 31) >> 5;
+        const bool flat = gpw <= 16;
         const bool fast_div = fp.bd <= 12;
-        for (int item = warp; item < nbk * gh; item += 8) {
-            int blk, r;
-            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
-            int pc = blk * 32 + lane;
-            if (pc >= gpw) continue;
+        for (int item = flat ? tid : warp; item < (flat ? gh * gpw : nbk * gh); item += flat ? kThreads : 8) {
+            int r, pc;
+            if (flat) {
+                r = item / gpw;
+                pc = item - r * gpw;
+            } else {
+                int blk;
+                if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+                pc = blk * 32 + lane;
+                if (pc >= gpw) continue;
+            }
             int y = yg0 + r;
             int rbh = ((y & 1) == po.r_row) ? po.r_col : po.b_col;
             int x = xg0 + 2 * pc + rbh;
@@ -1001,11 +1017,18 @@ __device__ bool compute_tile(TileSmem<TW, TH, OUTB>& sm, int b, Overrides ov, bo
         }
     } else {
         const int nbk = FULL ? (G::F_TPW + 31) / 32 : (tpw + 31) >> 5;
-        for (int item = warp; item < nbk * th; item += 8) {
-            int blk, r;
-            if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
-            int pc = blk * 32 + lane;
-            if (pc >= tpw) continue;
+        const bool flat = !FULL && tpw <= 16;
+        for (int item = flat ? tid : warp; item < (flat ? th * tpw : nbk * th); item += flat ? kThreads : 8) {
+            int r, pc;
+            if (flat) {
+                r = item / tpw;
+                pc = item - r * tpw;
+            } else {
+                int blk;
+                if (nbk == 2) { blk = item & 1; r = item >> 1; } else { blk = item % nbk; r = item / nbk; }
+                pc = blk * 32 + lane;
+                if (pc >= tpw) continue;
+            }
             int y = y0 + r, x = x0 + 2 * pc;
             int R0, G0, B0, R1, G1, B1;
             if (!border_tile && demosaic != DM_MG) {
