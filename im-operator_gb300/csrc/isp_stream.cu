@@ -353,7 +353,7 @@ __device__ __forceinline__ void green_row(const uint32_t (&m2)[4], const uint32_
 template <int RBH>
 __device__ __forceinline__ void out_row(bool rrow, const float (&cdm)[4], float em, const float (&cdc)[4], float ec,
                                         const float (&cdp)[4], float ep, const float (&gq)[4], const uint32_t (&bq)[4],
-                                        const float (&m)[9], bool ccm_on, uint32_t mv2, float2 z2,
+                                        const float (&m)[9], bool ccm_on, int mv, uint32_t mv2, float2 z2,
                                         const uint8_t* tone, uint32_t (&ob)[6]) {
     // neighbour pairs: diagonals of rows q +- 1 at pairs j+pa, j+pa+1; horizontals of row q at j+pl, j+pl+1
     auto at = [&](const float (&r)[4], float e, int i) -> float { return i < 0 ? e : (i > 3 ? e : r[i]); };
@@ -396,6 +396,7 @@ __device__ __forceinline__ void out_row(bool rrow, const float (&cdm)[4], float 
             Rw = Bw;
             Bw = t;
         }
+        uint32_t i0[3], i1[3];  // tone indices of pixels 0 and 1, per channel
         if (ccm_on) {
             const float2 rr = halves_f2(Rw), gg = halves_f2(Gw), bb = halves_f2(Bw);
             auto M = [&](int k) { return make_float2(m[k], m[k]); };
@@ -406,12 +407,25 @@ __device__ __forceinline__ void out_row(bool rrow, const float (&cdm)[4], float 
                                                     dev::pmul(M(5), bb, z2)), h5);
             const float2 bo = dev::fadd2(dev::fadd2(dev::fadd2(dev::pmul(M(6), rr, z2), dev::pmul(M(7), gg, z2)),
                                                     dev::pmul(M(8), bb, z2)), h5);
-            Rw = floor_pack_s(ro, mv2);
-            Gw = floor_pack_s(go, mv2);
-            Bw = floor_pack_s(bo, mv2);
+            // clamp((int)t, 0, mv) straight from the bits of t + 1.5 * 2^23 (floor(t) above their
+            // bias; C's truncation differs from floor only below 0, where both clamp to 0)
+            const float2 o[3] = {ro, go, bo};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float2 f = fadd2_rz(o[c], make_float2(kMagic, kMagic));
+                i0[c] = (uint32_t)__viaddmin_s32_relu((int)__float_as_uint(f.x), -(int)kMagicBits, mv);
+                i1[c] = (uint32_t)__viaddmin_s32_relu((int)__float_as_uint(f.y), -(int)kMagicBits, mv);
+            }
+        } else {
+            const uint32_t w[3] = {Rw, Gw, Bw};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                i0[c] = w[c] & 0xFFFFu;
+                i1[c] = w[c] >> 16;
+            }
         }
-        const uint32_t t0 = tone[Rw & 0xFFFFu], t1 = tone[Gw & 0xFFFFu], t2 = tone[Bw & 0xFFFFu];
-        const uint32_t t3 = tone[Rw >> 16], t4 = tone[Gw >> 16], t5 = tone[Bw >> 16];
+        const uint32_t t0 = tone[i0[0]], t1 = tone[i0[1]], t2 = tone[i0[2]];
+        const uint32_t t3 = tone[i1[0]], t4 = tone[i1[1]], t5 = tone[i1[2]];
         // bytes 6j .. 6j+5 of the lane's 24
         const uint32_t lo = t0 | (t1 << 8) | (t2 << 16) | (t3 << 24), hi = t4 | (t5 << 8);
         if ((j & 1) == 0) {
@@ -428,8 +442,10 @@ __device__ __forceinline__ int mod5(int v) { return v >= 5 ? v - 5 : v; }
 __device__ __forceinline__ int mod3(int v) { return v >= 3 ? v - 3 : v; }
 
 // Streams band (y0, bh) of segment G; own: the segment's word when this warp owns it, so that it
-// continues with the segment's next bands while it gets them
-template <int FMT>
+// continues with the segment's next bands while it gets them.  CHAIN: every frame of the launch
+// runs all five stages (black level, adaptive defect correction, grid shading, Bayer white
+// balance, CCM), fixed at compile time; 0: each frame's own stage set.
+template <int FMT, int CHAIN>
 __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamSmem& sm, StreamWarpSmem& ws,
                                             const SSeg& U, int y0, int bh, unsigned long long* own, int lane) {
     const unsigned full = 0xffffffffu;
@@ -438,8 +454,9 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
     const FrameParams& fp = bl.frames[U.f];
     const int W = fp.w, H = fp.h, mv = fp.mv;
     const unsigned stages = fp.stages;
-    const bool bl_on = (stages & 1u) != 0, dpc_on = (stages & 2u) != 0, lsc_on = (stages & 4u) != 0,
-               wb_on = (stages & 8u) != 0, ccm_on = (stages & 16u) != 0;
+    const bool bl_on = CHAIN || (stages & 1u) != 0, dpc_on = CHAIN || (stages & 2u) != 0,
+               lsc_on = CHAIN || (stages & 4u) != 0, wb_on = CHAIN || (stages & 8u) != 0,
+               ccm_on = CHAIN || (stages & 16u) != 0;
     const PatternOffsets po = pattern_offsets(fp.pattern);
     const uint32_t mv2 = fp.mv2;
     const int thr = fp.dpc_thr;
@@ -521,7 +538,9 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
         }
         ws.orig[m5][lane] = make_uint4(P[0], P[1], P[2], P[3]);
 
-        if (k >= 4) {
+        // B and C run from the first row: until their inputs are streamed (k < 4, k < 8) they work
+        // on the rings' earlier contents, and nothing they leave there reaches an output or a seed
+        {
             // ---- B: bay row b = n - 2 ------------------------------------------------------------
             const int b = n - 2;
             const int so0 = mod5(m5 + 1), so2 = mod5(m5 + 3);  // orig rows b-2, b
@@ -617,7 +636,7 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
             const int sb = mod5(m5 + 3);  // kb mod 5
             ws.bay[sb][lane] = make_uint4(Bq[0], Bq[1], Bq[2], Bq[3]);
 
-            if (k >= 8) {
+            {
                 // ---- C: green row g = b - 2 (bay rows g-2 .. g+2 = slots kb-4 .. kb) ------------
                 const int g = b - 2;
                 const uint4 q0 = ws.bay[mod5(sb + 1)][lane], q1 = ws.bay[mod5(sb + 2)][lane];
@@ -648,8 +667,8 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
                     const bool rrow = (q & 1) == po.r_row;
                     const int rbh = rrow ? po.r_col : po.b_col;
                     uint32_t ob[6];
-                    if (rbh == 0) out_row<0>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
-                    else out_row<1>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv2, z2, sm.tone, ob);
+                    if (rbh == 0) out_row<0>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv, mv2, z2, sm.tone, ob);
+                    else out_row<1>(rrow, cdm, em, cdc, ec, cd, ce, gprev, bq, ccm, ccm_on, mv, mv2, z2, sm.tone, ob);
                     if (lane_out) {
                         uint8_t* dst = outp;
                         if ((out_base & 7) == 0) {
@@ -677,15 +696,17 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
     }
 }
 
-template <int FMT>
+template <int FMT, int CHAIN>
 __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<StreamSmem*>(dsm);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
-        // every frame of the launch shares its tone table
+        // every frame of the launch shares its tone table; the rings start zeroed
         const FrameParams& f0 = bl.frames[0];
         for (int i = threadIdx.x; i <= f0.mv; i += kStThreads) sm.tone[i] = __ldg(f0.tone8 + i);
+        uint4* r = reinterpret_cast<uint4*>(&sm.w[warp]);
+        for (int i = lane; i < (int)(sizeof(StreamWarpSmem) / 16); i += 32) r[i] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncthreads();
     const unsigned full = 0xffffffffu;
@@ -701,7 +722,7 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
         if (i >= 0) {
             int y0, bh;
             band_rows(G, i, y0, bh);
-            stream_unit<FMT>(bl, sm, sm.w[warp], G, y0, bh, bl.seg_words + gw, lane);
+            stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], G, y0, bh, bl.seg_words + gw, lane);
         }
     }
     // then single bands from the back of segments that still have unclaimed ones: 32 segments
@@ -731,15 +752,16 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
         seg_of(bl, seg, S);
         int y0, bh;
         band_rows(S, j, y0, bh);
-        stream_unit<FMT>(bl, sm, sm.w[warp], S, y0, bh, nullptr, lane);
+        stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], S, y0, bh, nullptr, lane);
     }
 }
 
 int g_stream_grid[kMaxDev];
 
 template <int FMT>
-cudaError_t launch_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
-    stream_kernel<FMT><<<grid, kStThreads, smem, st>>>(bl);
+cudaError_t launch_fmt(const BatchLaunch& bl, bool chain, int grid, size_t smem, cudaStream_t st) {
+    if (chain) stream_kernel<FMT, 1><<<grid, kStThreads, smem, st>>>(bl);
+    else stream_kernel<FMT, 0><<<grid, kStThreads, smem, st>>>(bl);
     return cudaGetLastError();
 }
 
@@ -827,9 +849,10 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
     {
         std::lock_guard<std::mutex> lock(device_setup_mutex());
         if (!g_stream_grid[dev]) {
-            void (*ks[4])(BatchLaunch) = {stream_kernel<FMT_U8>, stream_kernel<FMT_U16>, stream_kernel<FMT_P10>,
-                                          stream_kernel<FMT_P12>};
-            for (int k = 0; k < 4 && e == cudaSuccess; k++)
+            void (*ks[8])(BatchLaunch) = {stream_kernel<FMT_U8, 0>,  stream_kernel<FMT_U16, 0>, stream_kernel<FMT_P10, 0>,
+                                          stream_kernel<FMT_P12, 0>, stream_kernel<FMT_U8, 1>,  stream_kernel<FMT_U16, 1>,
+                                          stream_kernel<FMT_P10, 1>, stream_kernel<FMT_P12, 1>};
+            for (int k = 0; k < 8 && e == cudaSuccess; k++)
                 e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int n = 0, m = 0;
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[3], kStThreads, smem);
@@ -848,11 +871,14 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
     const int want = (bl.n_items + kStWarps - 1) / kStWarps;
     const int grid = want < limit ? want : limit;
     count_launch(2);
+    // the instantiation with every stage fixed on when each frame runs all five
+    bool chain = true;
+    for (int f = 0; f < bl.n_frames; f++) chain = chain && (bl.frames[f].stages & 31u) == 31u;
     switch (bl.fmt) {
-        case FMT_U8: return launch_fmt<FMT_U8>(bl, grid, smem, st);
-        case FMT_U16: return launch_fmt<FMT_U16>(bl, grid, smem, st);
-        case FMT_P10: return launch_fmt<FMT_P10>(bl, grid, smem, st);
-        case FMT_P12: return launch_fmt<FMT_P12>(bl, grid, smem, st);
+        case FMT_U8: return launch_fmt<FMT_U8>(bl, chain, grid, smem, st);
+        case FMT_U16: return launch_fmt<FMT_U16>(bl, chain, grid, smem, st);
+        case FMT_P10: return launch_fmt<FMT_P10>(bl, chain, grid, smem, st);
+        case FMT_P12: return launch_fmt<FMT_P12>(bl, chain, grid, smem, st);
         default: return cudaErrorInvalidValue;
     }
 }
