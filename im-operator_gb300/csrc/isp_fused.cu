@@ -56,14 +56,18 @@ __global__ void tone_table_kernel(int mode, const float* lut, const float* knots
 // values.
 constexpr int kRenderCtas = 16;
 
+constexpr int kResolveHeap = 6144, kResolveOv = 3072;  // shared-memory entries (48 KB)
+
 __global__ void __launch_bounds__(32) dpc_resolve_kernel(const __grid_constant__ BatchLaunch bl) {
+    __shared__ int heap[kResolveHeap], ov_idx[kResolveOv], ov_val[kResolveOv];
     const FrameParams& fp = bl.frames[blockIdx.x];
     if (!((fp.stages & 2u) && fp.dpc_mode == 0)) return;
     int n_ov = 0;
     if (*fp.seed_count > 0) {
         const FixupScratch fs{fp.fix_heap, fp.fix_ov_idx, fp.fix_ov_val, fp.fix_n_ov, fp.fix_cap};
         GlobalOrig orig{&fp, pattern_offsets(fp.pattern)};
-        n_ov = resolve_chains_warp(fp, orig, fs);
+        n_ov = resolve_chains_warp_smem(fp, orig, fs, heap, kResolveHeap, ov_idx, ov_val, kResolveOv);
+        if (n_ov < 0) n_ov = resolve_chains_warp(fp, orig, fs);  // more chains than shared memory holds
     }
     if (threadIdx.x == 0) *fp.fix_n_ov = n_ov;
 }
@@ -327,6 +331,28 @@ bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl) {
     return true;
 }
 
+// A second stream and two events per host thread and device: the border-column launch of a
+// streamed batch runs beside its border-row launch (both are short and latency-bound), forked
+// from and joined back into the launch stream by events, which a graph capture records as two
+// branches.
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+cudaError_t side_stream(SideStream*& out) {
+    thread_local SideStream side[kMaxDevices];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    SideStream& s = side[dev];
+    if (!s.st && (e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    if (!s.fork && (e = cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if (!s.join && (e = cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    out = &s;
+    return cudaSuccess;
+}
+
 cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, const SplitFixup* split = nullptr) {
     BatchLaunch bl;
     bool fixup = false;
@@ -372,9 +398,26 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
         bs.seg_words = frames[0].seg_words;
         bn.rect_start[bn.n_rects] = bn.n_items = items_n;
         bl.rect_start[bl.n_rects] = bl.n_items = items_b;
+        // the column launch counts its tiles in the last claim word, which the streaming launch
+        // leaves alone
+        bn.tile_counter = reinterpret_cast<int*>(frames[0].seg_words + (kStreamSegCap - 1));
+        SideStream* side = nullptr;
         cudaError_t e = launch_stream(bs, st);
-        if (e == cudaSuccess) e = launch_fused_narrow(bn, st);
+        if (e == cudaSuccess) e = side_stream(side);
+        if (e == cudaSuccess && (e = cudaEventRecord(side->fork, st)) == cudaSuccess &&
+            (e = cudaStreamWaitEvent(side->st, side->fork, 0)) == cudaSuccess &&
+            (e = launch_fused_narrow(bn, side->st)) == cudaSuccess)
+            e = cudaEventRecord(side->join, side->st);
         if (e != cudaSuccess) return e;
+        // the border rows, then (after the columns joined) the fix-up
+        BatchLaunch bf = bl;
+        bf.n_items = 0;
+        if (frames[0].out_bpc == 2) e = FusedKernels<6>::launch(bl, false, st, nullptr);
+        else e = FusedKernels<3>::launch(bl, false, st, nullptr);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, side->join, 0);
+        if (e != cudaSuccess) return e;
+        return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bf, fixup, st, split)
+                                      : FusedKernels<3>::launch(bf, fixup, st, split);
     }
     return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, fixup, st, split)
                                   : FusedKernels<3>::launch(bl, fixup, st, split);

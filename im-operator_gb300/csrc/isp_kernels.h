@@ -12,7 +12,8 @@ namespace imop {
 // nominal fused tile (the last tile of a row / column absorbs a remainder below 4)
 constexpr int kTileW = 120;
 constexpr int kTileH = 24;
-// work-claim words of one streaming launch (segments of its strips)
+// work-claim words of one streaming launch (segments of its strips; the last word counts the tiles
+// of the batch's border-column launch)
 constexpr int kStreamSegCap = 4096;
 // narrow fused tile of the border columns of streamed frames (isp_fused_narrow.cu)
 constexpr int kNarrowW = 16;

@@ -833,8 +833,8 @@ static void choose_segments(BatchLaunch& bl, int warps) {
             items += R.tiles_x * R.tiles_y;
         }
         bl.rect_start[bl.n_rects] = bl.n_items = items;
-        if (items <= kStreamSegCap) break;
-        per *= (double)items / kStreamSegCap;
+        if (items < kStreamSegCap) break;
+        per *= (double)items / (kStreamSegCap - 1);
     }
     bl.band_h = kStBand;
 }
@@ -865,7 +865,7 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
     BatchLaunch bl = bl_in;
     choose_segments(bl, limit * kStWarps);
     if (bl.n_items <= 0) return cudaSuccess;
-    if (bl.n_items > kStreamSegCap || !bl.seg_words) return cudaErrorInvalidValue;
+    if (bl.n_items >= kStreamSegCap || !bl.seg_words) return cudaErrorInvalidValue;  // the last word: the column launch
     if ((e = cudaMemsetAsync(bl.seg_words, 0, sizeof(unsigned long long) * (size_t)bl.n_items, st)) != cudaSuccess)
         return e;
     const int want = (bl.n_items + kStWarps - 1) / kStWarps;

@@ -200,3 +200,15 @@ def test_stream_full_c2_frame(isp):
     got = _run(isp, pl, raw)
     assert _launches() > n0
     assert max_abs(got, ref) == 0
+
+
+def test_defect_chains_beyond_shared_memory(isp):
+    """Thousands of same-colour defect clusters in one frame: more chain overrides than the
+    resolution keeps in shared memory, so it falls back to its global-memory lists; the bytes must
+    still equal the oracle's raster-order result."""
+    rng = np.random.default_rng(12700)
+    pl = _pipeline(rng, 1008, 760, fmt=3, stages=abi.STAGE_ALL & ~abi.STAGE_LUT3D)
+    pl.dpc_threshold = 0.1
+    raw = _frame(rng, pl, defect_frac=0.02, clusters=5000)
+    ref, _ = O.pipeline(pl, raw)
+    assert max_abs(_run(isp, pl, raw), ref) == 0
