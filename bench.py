@@ -7,22 +7,24 @@ CCM, 4096-entry gamma LUT -> RGB8).  The batch is larger than L2 (FRAMES x 55 MB
 is needed between steps.
 
   value       Mpix/s of the fused path with inputs resident in HBM (whole job, all ranks): one
-              recorded batch per step (one persistent launch over all frames' tiles)
+              recorded batch per step (the streaming kernel over all frames' interiors, the
+              border tile launches, the defect-chain fix-up)
   e2e         the same through the host-buffer batch API: pinned frames, copies in / kernels /
-              copies out pipelined over three streams
+              copies out pipelined over four device slots
   roofline    dominant kernel: algorithmic bytes per launch / CUDA-event launch time vs the
               measured HBM copy bandwidth
   plain       the same batch through the plain per-operator kernels (one kernel per stage)
-  cpu_baseline  the CPU oracle (plain-C restatement of the reference's CPU path) on a bounded
-              sample of the same frames on this host's cores
+  cpu_baseline  the reference's own CPU per-module calls (oracle/_ref, compiled from its sources
+              staged beside the oracle) on a bounded sample of the same frames on this host's cores,
+              or the plain-C restatement where those sources were not staged
   c3          one 5320x4600 frame per step (8-bit and 12-bit), per-frame time and HBM GB/s
   jpeg        the step's RGB8 frames encoded to baseline JPEG (quality 90, 4:2:0, the reference's
               JpegParams defaults), byte-identical to the reference's encoder: device-resident
               frames, the host entry point with pinned buffers (e2e), RAW -> JPEG on the device
               (ISP step + encodes), and the CPU restatement of the reference's encoder
 
-`--impl reference` times the reference's CPU algorithm for this path (the oracle port; the
-reference's own sources do not exist on GPU hosts) with all host threads, same metric / config.
+`--impl reference` times the reference's CPU algorithm for this path (its own per-module calls
+compiled from the staged sources, else the oracle port) with all host threads, same metric / config.
 """
 import argparse
 import json
@@ -38,8 +40,12 @@ sys.path.insert(0, os.path.join(REPO, "im-operator_gb300"))
 
 METRIC = "ISP Mpix/s & % HBM peak, fused-batched vs plain (1 GB300, <=1 LSB); adjoint Mpix/s"
 W_C2, H_C2 = 4024, 3032
-# ncu smsp__inst_executed.sum of one fused_batch_kernel launch over 8 C2 frames
-WARP_INST_PER_LAUNCH_8 = 1.002e9
+# ncu smsp__inst_executed.sum of one recorded C2 step over 8 frames: the streaming kernel
+# (377.55e6), the border-column (16.66e6) and border-row (10.51e6) tile launches, the defect-chain
+# resolution (0.02e6) and window re-rendering (0.04e6)
+WARP_INST_PER_STEP_8 = 4.048e8
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the streaming kernel's launch over 8 frames
+STREAM_DRAM_BYTES_8 = 393691392
 
 
 def parse():
@@ -678,7 +684,8 @@ def main():
     mpix = world * args.steps * px_step / (ms / 1e3) / 1e6
     alg_bytes = in_b + out_b + 4096 * 4 + 17 * 13 * 4 * 4  # per frame: RAW12P in, RGB8 out, LUT, grid
     # the launch time of the roofline is the recorded step of the timed region (CUDA events on the
-    # launching stream): the persistent launch plus its two defect fix-up launches
+    # launching stream): the streaming kernel over the frames' interiors (85 % of the step in the
+    # ncu launch list), the border-column and border-row tile launches and the two fix-up launches
     per_launch_ms = ms / args.steps
     achieved = B * alg_bytes / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
@@ -693,24 +700,27 @@ def main():
         "hbm_frac": round(world * args.steps * B * alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
         "fused_equals_plain": parity_ok,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": 382078976, "peak_kind": peak_kind,
-                     "kernel": "fused_batch_kernel: one persistent launch over the step's frames "
-                               "(timed with its seed reset and the two defect fix-up launches)",
+                     "frac": round(achieved / peak, 4), "traffic": int(STREAM_DRAM_BYTES_8 * B / 8),
+                     "peak_kind": peak_kind,
+                     "kernel": "stream_kernel (warp-streamed strips of the frames' interiors, one launch "
+                               "over the step's frames), timed as the recorded step with the border "
+                               "tile launches, the seed reset and the two defect fix-up launches",
                      "bytes_per_launch": B * alg_bytes, "launch_ms": round(per_launch_ms, 4),
-                     "traffic_note": "ncu: 382.1 MB DRAM read+write per launch of 8 frames (profiles/)"},
-        "gpu_launches": 3 * args.steps,
+                     "traffic_note": "ncu: 393.7 MB DRAM read+write of the streaming kernel's launch over "
+                                     "8 frames (the last writes still in L2 when it ends; profiles/)"},
+        "gpu_launches": 5 * args.steps,
         "clocks": clk.summary(),
     }
     # the ceiling that binds this kernel: warp-instruction issue (4 per SM per clock)
     sm_mhz = line["clocks"]["sm_mhz"] or line["clocks"]["sm_max_mhz"] or 2070.0
     n_sm = torch.cuda.get_device_properties(0).multi_processor_count
     issue_peak = n_sm * 4 * sm_mhz * 1e6
-    issue_achieved = WARP_INST_PER_LAUNCH_8 * B / 8 / (per_launch_ms / 1e3)
+    issue_achieved = WARP_INST_PER_STEP_8 * B / 8 / (per_launch_ms / 1e3)
     line["roofline"]["issue"] = {
         "achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
         "unit": "T warp instructions/s", "frac": round(issue_achieved / issue_peak, 4),
-        "warp_instructions_per_launch": int(WARP_INST_PER_LAUNCH_8 * B / 8),
-        "note": f"ncu smsp__inst_executed.sum of one launch over 8 frames (profiles/); peak = {n_sm} SMs x 4 "
+        "warp_instructions_per_launch": int(WARP_INST_PER_STEP_8 * B / 8),
+        "note": f"ncu smsp__inst_executed.sum of the step's five kernels over 8 frames (profiles/); peak = {n_sm} SMs x 4 "
                 f"schedulers x the median SM clock sampled in the timed region"}
     if ms_e2e is not None:
         line["e2e"] = {"value": round(world * args.steps * px_step / (ms_e2e / 1e3) / 1e6, 2), "unit": "Mpix/s",
