@@ -300,6 +300,7 @@ cudaError_t enqueue_batch(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaS
 Key batch_key(const std::vector<PreparedFrame>& pf, cudaStream_t st) {
     Key k;
     k.val(st);
+    k.val(tuning_generation());  // a new tuning table records anew
     int n = (int)pf.size();
     k.val(n);
     for (auto& f : pf) k.bytes(&f.fp, sizeof(FrameParams));

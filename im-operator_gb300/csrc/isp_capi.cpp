@@ -457,6 +457,18 @@ const char* imop_last_error_string(void) { return t_last_error.c_str(); }
 int imop_abi_version(void) { return IMOP_ISP_ABI_VERSION; }
 int imop_has_cuda(void) { return device_ready(); }
 
+const char* imop_device_name(void) {
+    thread_local char name[256];
+    name[0] = 0;
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (device_ready() && cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+        std::strncpy(name, prop.name, sizeof(name) - 1);
+        name[sizeof(name) - 1] = 0;
+    }
+    return name;
+}
+
 void imop_isp_params_default(ImopIspParams* p, int width, int height, int bit_depth, int packed) {
     if (!p) return;
     std::memset(p, 0, sizeof(*p));

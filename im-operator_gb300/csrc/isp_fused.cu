@@ -18,6 +18,7 @@
 #include <atomic>
 #include <vector>
 
+#include "imop_isp.h"
 #include "isp_kernels.h"
 #include "isp_dpc.cuh"
 #include "isp_fused_kernel.cuh"
@@ -314,15 +315,16 @@ bool make_launch(FrameParams* frames, int n, BatchLaunch& bl, bool& fixup) {
     return true;
 }
 
-// the launch block of frames[0..n) for the light-chain kernel: one rectangle per frame in its tiles
-bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl) {
+// the launch block of frames[0..n) for the light-chain kernel: one rectangle per frame in its units
+bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl, int band_rows) {
     bool fixup = false;
     if (!make_launch(frames, n, bl, fixup)) return false;
+    bl.band_h = band_rows;
     int items = 0;
     for (int f = 0; f < n; f++) {
         TileRect& R = bl.rects[f];
         R.tiles_x = lite_units_x(R.w);
-        R.tiles_y = lite_units_y(R.h);
+        R.tiles_y = lite_units_y(R.h, band_rows);
         bl.rect_start[f] = items;
         items += R.tiles_x * R.tiles_y;
     }
@@ -357,12 +359,15 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
     BatchLaunch bl;
     bool fixup = false;
     // the light-chain kernel takes frames of one input format that share their output tables
-    bool lite = true;
+    int wmax = 0;
+    for (int f = 0; f < n; f++) wmax = std::max(wmax, frames[f].w);
+    const TuneParams tl = tuning_for(IMOP_KERNEL_LITE, frames[0].fmt, wmax);
+    bool lite = tl.enabled;
     for (int f = 0; f < n; f++)
         lite = lite && lite_eligible(frames[f]) && frames[f].fmt == frames[0].fmt &&
                lite_table_key(frames[f]) == lite_table_key(frames[0]);
     if (lite) {
-        if (!make_lite_launch(frames, n, bl)) return cudaErrorInvalidValue;
+        if (!make_lite_launch(frames, n, bl, tl.band_rows)) return cudaErrorInvalidValue;
         cudaError_t e = launch_lite(bl, st);
         // no defect chains to resolve: a split caller's fix-up stream only waits for the tiles
         if (e == cudaSuccess && split) {
@@ -372,7 +377,7 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
     }
     // the AMAZE chains: the interior of every frame by the streaming kernel, then the border rows
     // and columns by the tile kernel (its launch also runs the defect-chain fix-up of the frames)
-    bool stream = true;
+    bool stream = tuning_for(IMOP_KERNEL_STREAM, frames[0].fmt, wmax).enabled;
     for (int f = 0; f < n; f++)
         stream = stream && stream_eligible(frames[f]) && frames[f].fmt == frames[0].fmt &&
                  frames[f].tone8 == frames[0].tone8 && frames[f].seg_words == frames[0].seg_words;
@@ -461,9 +466,11 @@ static long long instantiation_key(const FrameParams& fp) {
                         fp.out_format == 0 && fp.out_bpc == 1;
     if (extra) return (long long)fp.out_bpc << 32;
     // the light-chain kernel: one launch per input format and output table set
-    if (lite_eligible(fp)) return (1LL << 62) | ((long long)fp.fmt << 56) | (lite_table_key(fp) & ((1LL << 56) - 1));
+    if (lite_eligible(fp) && tuning_for(IMOP_KERNEL_LITE, fp.fmt, fp.w).enabled)
+        return (1LL << 62) | ((long long)fp.fmt << 56) | (lite_table_key(fp) & ((1LL << 56) - 1));
     // the streaming kernel: one launch per input format and tone table
-    if (stream_eligible(fp)) return (1LL << 61) | ((long long)fp.fmt << 56) | (stream_table_key(fp) & ((1LL << 56) - 1));
+    if (stream_eligible(fp) && tuning_for(IMOP_KERNEL_STREAM, fp.fmt, fp.w).enabled)
+        return (1LL << 61) | ((long long)fp.fmt << 56) | (stream_table_key(fp) & ((1LL << 56) - 1));
     const bool lite = simple && !(fp.stages & 6u);
     return ((long long)fp.out_bpc << 32) | (1LL << 24) | ((long long)fp.demosaic << 16) | (simple ? (1 << 8) : 0) |
            (lite ? (1 << 12) : 0) | (simple ? fp.fmt + 1 : 0);

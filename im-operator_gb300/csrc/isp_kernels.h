@@ -41,7 +41,7 @@ struct BatchLaunch {
     int no_dpc_lsc;                 // no frame corrects defects or lens shading
     int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
     unsigned long long* seg_words;  // streaming kernel: per segment, bands claimed (front | back << 32)
-    int band_h;                     // streaming kernel: rows of a band
+    int band_h;                     // streamed kernels: rows of a band
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];
@@ -73,6 +73,17 @@ std::mutex& device_setup_mutex();
 
 // launches enqueued per fused kernel (IMOP_KERNEL_TILE / _LITE / _STREAM)
 void count_launch(int kernel);
+
+// launch parameters of a streamed kernel (1 light-chain, 2 streaming) for input format fmt and
+// frames up to `width` columns, from the tuning table (imop_tuning_set) or the defaults
+struct TuneParams {
+    bool enabled;
+    int band_rows;
+    int seg_percent;
+};
+TuneParams tuning_for(int kernel, int fmt, int width);
+// changes with every imop_tuning_set (part of the recorded-graph key)
+int tuning_generation();
 
 int fused_tile_grid(int w, int h, int& ntx, int& nty);
 cudaError_t launch_tone_table(int mode, const float* d_lut, const float* d_knots, int bd, uint8_t* d_out,
@@ -111,7 +122,7 @@ bool lite_eligible(const FrameParams& fp);
 long long lite_table_key(const FrameParams& fp);
 // units of work of a frame: strips across, bands down (a rectangle's tiles_x / tiles_y)
 int lite_units_x(int w);
-int lite_units_y(int h);
+int lite_units_y(int h, int band_rows);
 // one persistent launch over the units of bl's rectangles (bl.fmt: the frames' common format)
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
 

@@ -25,7 +25,7 @@ __device__ __forceinline__ void unit_of(const BatchLaunch& bl, int item, LiteUni
     U.x0 = R.x0 + tx * sw;
     U.npx = min(sw, R.w - tx * sw);
     int y0, bh;
-    tile_span(R.h, kLiteBandH, R.tiles_y, ty, y0, bh);
+    tile_span(R.h, bl.band_h, R.tiles_y, ty, y0, bh);
     U.y0 = R.y0 + y0;
     U.bh = bh;
     U.nrows = bh + 2;
@@ -420,7 +420,7 @@ long long lite_table_key(const FrameParams& fp) {
 }
 
 int lite_units_x(int w) { return lite_strips(w); }
-int lite_units_y(int h) { return lite_bands(h); }
+int lite_units_y(int h, int band_rows) { return tiles_along(h, band_rows); }
 
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
     const size_t smem = sizeof(LiteSmem);

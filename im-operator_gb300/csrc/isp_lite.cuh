@@ -34,7 +34,7 @@ namespace imop {
 
 constexpr int kLiteLanePx = 8;                   // pixels per lane
 constexpr int kLiteStripMax = 32 * kLiteLanePx;  // columns of a strip
-constexpr int kLiteBandH = 16;                   // rows of a band (the last absorbs a remainder below 4)
+constexpr int kLiteBandH = 16;                   // default rows of a band (the last absorbs a remainder below 4)
 constexpr int kLiteRing = 4;                     // staged rows per warp
 constexpr int kLiteWarps = 8;
 
@@ -67,7 +67,6 @@ __host__ __device__ inline int lite_strips(int w) {
     const int s = lite_strip_w(w);
     return (w + s - 1) / s;
 }
-__host__ __device__ inline int lite_bands(int h) { return tiles_along(h, kLiteBandH); }
 
 // geometry of one band of one frame's strip (a warp's unit of work)
 struct LiteUnit {

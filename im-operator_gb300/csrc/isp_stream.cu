@@ -30,6 +30,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "imop_isp.h"
 #include "isp_device.cuh"
 #include "isp_fused_kernel.cuh"
 #include "isp_kernels.h"
@@ -43,7 +44,6 @@ constexpr int kStWin = 32 * kStLanePx;          // window columns of a strip
 constexpr int kStOut = kStWin - 2 * kStLanePx;  // output columns of a strip (lanes 1..30)
 constexpr int kStWarps = 12;  // one CTA per SM: every SM streams the same number of units
 constexpr int kStThreads = 32 * kStWarps;
-constexpr int kStBand = 32;  // rows of a band
 constexpr int kMaxDev = 64;
 
 struct StreamWarpSmem {
@@ -817,13 +817,13 @@ void stream_rects(const FrameParams& fp, TileRect& interior, TileRect (&border)[
     border[3] = {0, xe, 7, W - xe, H - 14, 0, 0};
 }
 
-// Segments of the rectangles of a launch: each strip in segments of about the rows that spread the
-// launch's strip rows evenly over the resident warps, bands of kStBand rows inside them (the
-// granule of the end-of-launch balancing, each taken band paying 10 rows of warm-up)
-static void choose_segments(BatchLaunch& bl, int warps) {
+// Segments of the rectangles of a launch: each strip in segments of seg_percent % of the rows that
+// spread the launch's strip rows evenly over the resident warps, bands of band_rows rows inside
+// them (the granule of the end-of-launch balancing, each taken band paying 10 rows of warm-up)
+static void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows) {
     long long strip_rows = 0;
     for (int r = 0; r < bl.n_rects; r++) strip_rows += (long long)bl.rects[r].tiles_x * bl.rects[r].h;
-    double per = std::max(1.0, (double)strip_rows / std::max(1, warps));
+    double per = std::max(1.0, (double)strip_rows / std::max(1, warps) * seg_percent / 100.0);
     for (int pass = 0; pass < 8; pass++) {
         int items = 0;
         for (int r = 0; r < bl.n_rects; r++) {
@@ -836,7 +836,7 @@ static void choose_segments(BatchLaunch& bl, int warps) {
         if (items < kStreamSegCap) break;
         per *= (double)items / (kStreamSegCap - 1);
     }
-    bl.band_h = kStBand;
+    bl.band_h = band_rows;
 }
 
 cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
@@ -863,7 +863,10 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
         limit = g_stream_grid[dev];
     }
     BatchLaunch bl = bl_in;
-    choose_segments(bl, limit * kStWarps);
+    int wmax = 0;
+    for (int f = 0; f < bl.n_frames; f++) wmax = std::max(wmax, bl.frames[f].w);
+    const TuneParams tp = tuning_for(IMOP_KERNEL_STREAM, bl.fmt, wmax);
+    choose_segments(bl, limit * kStWarps, tp.seg_percent, tp.band_rows);
     if (bl.n_items <= 0) return cudaSuccess;
     if (bl.n_items >= kStreamSegCap || !bl.seg_words) return cudaErrorInvalidValue;  // the last word: the column launch
     if ((e = cudaMemsetAsync(bl.seg_words, 0, sizeof(unsigned long long) * (size_t)bl.n_items, st)) != cudaSuccess)

@@ -64,8 +64,11 @@ def lib():
             "imop_last_error_string": (C.c_char_p, []),
             "imop_abi_version": (i, []),
             "imop_has_cuda": (i, []),
+            "imop_device_name": (C.c_char_p, []),
             "imop_shim_calls_served": (C.c_longlong, []),
             "imop_kernel_launches": (C.c_longlong, [i]),
+            "imop_tuning_set": (i, [C.POINTER(abi.TuneEntry), i]),
+            "imop_tuning_get": (i, [C.POINTER(abi.TuneEntry), i]),
             "imop_tone_table_entries": (sz, [i]),
             "imop_tone_table": (i, [i, i, C.POINTER(abi.ToneParams), vp, sz]),
             "imop_op_rgb_table": (i, [vp, i, i, i, vp, vp, vp]),
@@ -97,12 +100,29 @@ def _addr(x):
     raise TypeError(type(x))
 
 
+_tuning_loaded = False
+
+
+def _load_tuning():
+    """Once per process: the measured launch-tuning table beside the package (tuning.py), when it
+    was measured on this device; IMOP_TUNING_FILE names another table, IMOP_TUNING_FILE="" none."""
+    global _tuning_loaded
+    if _tuning_loaded:
+        return
+    _tuning_loaded = True
+    from . import tuning
+    path = os.environ.get("IMOP_TUNING_FILE", tuning.DEFAULT_TABLE)
+    if path:
+        tuning.load(path, device_name=lib().imop_device_name().decode())
+
+
 class Isp:
     """One pipeline context (imop_isp_t)."""
 
     def __init__(self, pipeline=None):
         h = C.c_void_p()
         check(lib().imop_isp_create(C.byref(h)))
+        _load_tuning()
         self.h = h
         self.pipeline = None
         self._cparams = None

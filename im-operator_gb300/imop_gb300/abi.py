@@ -107,3 +107,12 @@ TONE_CURVE_GAMMA, TONE_CURVE_S_CURVE, TONE_CURVE_LEVELS, TONE_CURVE_3POINT, TONE
 class ToneParams(C.Structure):
     _fields_ = [("gamma", C.c_float), ("contrast", C.c_float), ("shadows", C.c_float), ("highlights", C.c_float),
                 ("black_point", C.c_float), ("white_point", C.c_float), ("mid_point", C.c_float)]
+
+
+KERNEL_TILE, KERNEL_LITE, KERNEL_STREAM = 0, 1, 2
+
+
+class TuneEntry(C.Structure):
+    """ImopTuneEntry: launch parameters of a streamed kernel for one (kernel, format, width) class"""
+    _fields_ = [("kernel", C.c_int), ("fmt", C.c_int), ("max_width", C.c_int), ("enabled", C.c_int),
+                ("band_rows", C.c_int), ("seg_percent", C.c_int)]

@@ -485,6 +485,8 @@ const char* imop_last_error_string(void);
 int imop_abi_version(void);
 /* 1 when a CUDA device is visible (cached, like has_cuda_shared in src/gpu_dispatch.cpp:37-43). */
 int imop_has_cuda(void);
+/* the current device's name ("" without a device) */
+const char* imop_device_name(void);
 /* Calls of the reference-named GPU glue (include/imop_ref_shims.hpp) that this process ran on the
  * device and that returned Ok: a reference dispatcher linked against this library falls back to
  * its CPU code silently on any other status, so this count tells an integrator which one ran. */
@@ -495,6 +497,27 @@ long long imop_shim_calls_served(void);
  * recorded into a CUDA graph counts once, when it is recorded. */
 enum { IMOP_KERNEL_TILE = 0, IMOP_KERNEL_LITE = 1, IMOP_KERNEL_STREAM = 2 };
 long long imop_kernel_launches(int kernel);
+
+/* ---- launch tuning ------------------------------------------------------------------ */
+/* Launch parameters of the two streamed kernels per (kernel, input format, width class), measured
+ * by the tuner (imop_gb300.tuning) and loaded by the caller.  For a launch the first entry whose
+ * kernel matches, whose fmt matches (or is -1) and whose max_width is at least the widest frame of
+ * the launch applies; with none, the built-in defaults (enabled, 16-row bands for the light-chain
+ * kernel, 32-row bands and 100 % segments for the streaming kernel).  A launch recorded into a
+ * graph keeps the parameters it was recorded with. */
+typedef struct ImopTuneEntry {
+    int kernel;      /* IMOP_KERNEL_LITE or IMOP_KERNEL_STREAM */
+    int fmt;         /* input format: 0 u8, 1 u16, 2 MIPI RAW10, 3 MIPI RAW12; -1 any */
+    int max_width;   /* frames up to this many columns */
+    int enabled;     /* 0: frames of this class take the tile kernel instead */
+    int band_rows;   /* rows of a band: the light-chain kernel's unit, the streaming kernel's claim */
+    int seg_percent; /* streaming kernel: rows of a segment, in percent of the launch's strip rows
+                        spread evenly over the resident warps */
+} ImopTuneEntry;
+/* replaces the table (n = 0 clears it); IMOP_ERR_INVALID_ARGUMENT for an entry out of range */
+int imop_tuning_set(const ImopTuneEntry* entries, int n);
+/* copies up to cap entries of the table to out; returns the table's length */
+int imop_tuning_get(ImopTuneEntry* out, int cap);
 
 #ifdef __cplusplus
 }

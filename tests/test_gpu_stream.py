@@ -212,3 +212,33 @@ def test_defect_chains_beyond_shared_memory(isp):
     raw = _frame(rng, pl, defect_frac=0.02, clusters=5000)
     ref, _ = O.pipeline(pl, raw)
     assert max_abs(_run(isp, pl, raw), ref) == 0
+
+
+@pytest.mark.parametrize("entry", [
+    {"kernel": abi.KERNEL_STREAM, "enabled": 1, "band_rows": 16, "seg_percent": 50},
+    {"kernel": abi.KERNEL_STREAM, "enabled": 1, "band_rows": 64, "seg_percent": 200},
+    {"kernel": abi.KERNEL_STREAM, "enabled": 0, "band_rows": 32, "seg_percent": 100},
+    {"kernel": abi.KERNEL_LITE, "enabled": 1, "band_rows": 8, "seg_percent": 100},
+    {"kernel": abi.KERNEL_LITE, "enabled": 1, "band_rows": 48, "seg_percent": 100},
+    {"kernel": abi.KERNEL_LITE, "enabled": 0, "band_rows": 16, "seg_percent": 100}])
+def test_tuned_launches_same_bytes(isp, entry):
+    """Every tuning choice (band rows, segment size, the tile kernel instead) leaves the output
+    equal to the oracle's; a disabled class takes the tile kernel."""
+    from imop_gb300 import tuning
+    rng = np.random.default_rng(12800 + entry["band_rows"] + entry["seg_percent"] + 7 * entry["enabled"])
+    saved = tuning.get_table()
+    try:
+        tuning.set_table([dict(entry, fmt=-1, max_width=1 << 30)])
+        if entry["kernel"] == abi.KERNEL_STREAM:
+            pl = _pipeline(rng, 1288, 260, fmt=3, stages=abi.STAGE_ALL & ~abi.STAGE_LUT3D)
+        else:
+            pl = workloads.c1_pipeline(1006, 303)
+        raw = _frame(rng, pl) if entry["kernel"] == abi.KERNEL_STREAM else workloads.c1_frame(pl, 5)
+        ref, _ = O.pipeline(pl, raw)
+        n0 = I.lib().imop_kernel_launches(entry["kernel"])
+        got = _run(isp, pl, raw)
+        ran = I.lib().imop_kernel_launches(entry["kernel"]) > n0
+        assert ran == bool(entry["enabled"])
+        assert max_abs(got, ref) == 0
+    finally:
+        tuning.set_table(saved)
