@@ -486,8 +486,25 @@ def c4_leg(isp, args, torch, stream, barrier, max_over_ranks, world):
     if bad:
         return {"value": None, "error": f"recorded batch differs from the plain path on frames {bad[:8]}",
                 "frames": len(frames)}
+    # the same batch with the built-in launch parameters, and with the tile kernel alone (both
+    # streamed kernels disabled), against the measured table loaded at start-up
+    from imop_gb300 import tuning
+    table = tuning.get_table()
+    try:
+        tuning.set_table([])
+        ms_fixed = run(abi.BATCH_GRAPH)
+        off = {"fmt": -1, "max_width": 1 << 30, "enabled": 0, "band_rows": 16, "seg_percent": 100}
+        tuning.set_table([dict(off, kernel=abi.KERNEL_LITE), dict(off, kernel=abi.KERNEL_STREAM)])
+        ms_tile = run(abi.BATCH_GRAPH)
+    finally:
+        tuning.set_table(table)
+    isp.sync_status(sh)
+    tuned = {"table_entries": len(table), "ms_per_step": round(ms, 3), "fixed_ms_per_step": round(ms_fixed, 3),
+             "tile_kernel_only_ms_per_step": round(ms_tile, 3),
+             "note": "fixed: the built-in launch parameters; tile kernel only: every frame in the general "
+                     "tiled kernel, one launch per instantiation group of up to 16 frames"}
     return {"value": round(world * px / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s", "ms_per_step": round(ms, 3),
-            "fused_equals_plain": True,
+            "fused_equals_plain": True, "tuning": tuned,
             "plain": {"value": round(world * px / (ms_plain / 1e3) / 1e6, 2), "ms_per_step": round(ms_plain, 3)},
             "gbs_algorithmic": round(world * alg / (ms / 1e3) / 1e9, 1), "frames": len(frames),
             "megapixels_per_step": round(px / 1e6, 1), "steps": steps,
