@@ -576,6 +576,7 @@ def run_reference(args):
     rate = args.steps * B * pl.pixels / dt / 1e6
     sample = (f"{args.steps} steps of the step's {B} C2 frames: {ch.describe()}; frames concurrently in "
               f"{min(B, ch.cores)} threads sharing {ch.cores} host cores")
+    ref_cuda = reference_cuda_leg(args, pl, frames, O)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": "Mpix/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -586,8 +587,37 @@ def run_reference(args):
         "cpu_baseline": {"value": round(rate, 3), "unit": "Mpix/s", "cores": ch.cores, "kind": ch.kind,
                          "sample": sample},
         "e2e": {"value": round(rate, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda": ref_cuda,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda_leg(args, pl, frames, O):
+    """The reference's own GPU path on this GB300, timed beside its CPU path: each frame through
+    the calls its dispatchers make on a CUDA host (oracle_py.ref_chain_cuda: its GPU black level,
+    adaptive defect correction and AMAZE, each with its own host copies; its CPU unpack and CCM; the
+    restated grid shading, Bayer WB and LUT), one frame after the other as its synchronous calls
+    run.  Timing only."""
+    if not (O.ref_available() and O.refcuda_available()):
+        return {"value": None, "unavailable": "the reference's sources were not staged on this host"}
+    if O.refcuda().refcuda_has_cuda() != 1:
+        return {"value": None, "unavailable": "no CUDA device"}
+    O.ref_chain_cuda(pl, frames[0])  # context, workspaces
+    n = max(1, min(len(frames), 8))
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 3))):
+        for f in frames[:n]:
+            O.ref_chain_cuda(pl, f)
+    dt = time.perf_counter() - t0
+    done = max(1, min(args.steps, 3)) * n
+    return {"value": round(done * pl.pixels / dt / 1e6, 3), "unit": "Mpix/s", "frames": done,
+            "seconds": round(dt, 3),
+            "on_gpu": "black_level::process_black_level_cuda, defect_correct::process_defect_correct_cuda "
+                      "(adaptive), imop::demosaic_cuda (AMAZE; the reference's GPU demosaic takes no packed input)",
+            "not_run": "ccm::process_ccm_cuda and the reference's other kern_gpu_pipeline stages: their parameter "
+                       "buffer is never allocated on that path (GpuWorkspace::ensure(w, h, bd, 0)), so the kernel "
+                       "would read through a null pointer; the CCM runs on the reference's CPU code",
+            "note": "timing only: the reference's GPU kernels do not reproduce its CPU results"}
 
 
 def main():

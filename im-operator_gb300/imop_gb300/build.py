@@ -81,8 +81,9 @@ def build_library(verbose=False):
 
 
 def build_oracle(verbose=False):
-    """The CPU oracle (test infrastructure), and the reference's own CPU library (and its
-    dispatchers over this library) where the reference's sources exist: the reference tree
+    """The CPU oracle (test infrastructure), and the reference's own CPU library (its dispatchers
+    over this library, and its own GPU glue for the timed reference arm) where the reference's
+    sources exist: the reference tree
     (IMOP_REFERENCE_ROOT, default the checkout beside this one) is first copied into the
     git-ignored oracle/_ref/src, so a host without the tree builds the same files from the copy."""
     oracle = os.path.join(REPO, "oracle")
@@ -97,7 +98,7 @@ def build_oracle(verbose=False):
     staged = os.path.join(oracle, "_ref", "src")
     if os.path.isdir(os.path.join(staged, "src", "algorithms")):
         jobs = str(min(16, os.cpu_count() or 4))
-        r = subprocess.run(["make", "-C", oracle, "ref", "dropin", "-j" + jobs, f"REF_ROOT={staged}"],
+        r = subprocess.run(["make", "-C", oracle, "ref", "dropin", "refcuda", "-j" + jobs, f"REF_ROOT={staged}"],
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")

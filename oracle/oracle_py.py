@@ -356,3 +356,64 @@ def ref_chain(pl, raw):
     L.or_tone_rgb8(rgb2.ctypes.data_as(U16P), out.ctypes.data_as(U8P), w, h, bd, pl.tone_mode,
                    lut.ctypes.data_as(F32P), None)
     return out
+
+
+_refcuda = None
+
+
+def refcuda_available():
+    return os.path.exists(os.path.join(HERE, "_ref", "libimop_refcuda.so"))
+
+
+def refcuda():
+    """the reference's own GPU path (`make -C oracle refcuda`; timing only)"""
+    global _refcuda
+    if _refcuda is None:
+        path = os.path.join(HERE, "_ref", "libimop_refcuda.so")
+        if not os.path.exists(path):
+            raise RuntimeError("reference GPU library not built: run `make -C oracle refcuda`")
+        _refcuda = C.CDLL(path)
+        i, vp = C.c_int, C.c_void_p
+        _refcuda.refcuda_has_cuda.argtypes = []
+        _refcuda.refcuda_black_level.argtypes = [vp, i, i, i, i, F32P]
+        _refcuda.refcuda_defect_adaptive.argtypes = [vp, i, i, i, i, C.c_float]
+        _refcuda.refcuda_demosaic.argtypes = [vp, vp, i, i, i, i, i]
+    return _refcuda
+
+
+def ref_chain_cuda(pl, raw):
+    """RGB8 of one frame through the calls the reference's dispatchers make on a CUDA host: its GPU
+    black level, adaptive defect correction and demosaic (each copying the frame in and out, as the
+    reference's glue does), its CPU unpack and CCM, and the oracle's restatements of the stages the
+    reference has no function for (as ref_chain).  Timing only: the reference's GPU kernels do not
+    reproduce its CPU results.  Raises when a GPU call reports an error."""
+    assert pl.packed and pl.bit_depth in (10, 12) and pl.stage_order == abi.ORDER_BAYER_WB
+    assert pl.bl_mode == abi.BL_PER_CHANNEL and pl.dpc_mode == abi.DPC_ADAPTIVE and pl.lsc_mode == abi.LSC_GRID
+    assert pl.stages == abi.STAGE_ALL and pl.tone_mode == abi.TONE_LUT and pl.out_format == abi.OUT_RGB8
+    R, G, L = _ref_chain_lib(), refcuda(), stages()
+    L.or_tone_rgb8.argtypes = [U16P, U8P, C.c_int, C.c_int, C.c_int, C.c_int, F32P, F32P]
+    w, h, bd, pat = pl.width, pl.height, pl.bit_depth, pl.pattern
+    raw = np.ascontiguousarray(raw, np.uint8)
+    bay = np.empty((h, w), np.uint16)
+    R.ref_unpack_packed(raw.ctypes.data, raw.size, bay.ctypes.data, w, h, bd)
+    off = np.asarray(pl.bl_offset, np.float32)
+    for rc, what in ((G.refcuda_black_level(bay.ctypes.data, w, h, pat, bd, off.ctypes.data_as(F32P)), "black level"),
+                     (G.refcuda_defect_adaptive(bay.ctypes.data, w, h, pat, bd, float(pl.dpc_threshold)), "defects")):
+        if rc != 0:
+            raise RuntimeError(f"reference GPU {what}: status {rc}")
+    grid = np.ascontiguousarray(pl.lsc_grid, np.float32)
+    L.or_lsc_grid(bay.ctypes.data_as(U16P), w, h, pat, bd, grid.ctypes.data_as(F32P), grid.shape[1], grid.shape[0])
+    wb = np.asarray(pl.wb_gain, np.float32)
+    L.or_wb_bayer(bay.ctypes.data_as(U16P), w, h, pat, bd, wb.ctypes.data_as(F32P))
+    rgb = np.empty((h, w, 3), np.uint16)
+    rc = G.refcuda_demosaic(bay.ctypes.data, rgb.ctypes.data, w, h, pat, pl.demosaic, bd)
+    if rc != 0:
+        raise RuntimeError(f"reference GPU demosaic: status {rc}")
+    m = np.asarray(pl.ccm, np.float32)
+    rgb2 = np.empty_like(rgb)
+    R.ref_ccm_store(rgb.ctypes.data, rgb2.ctypes.data, w, h, bd, m.ctypes.data_as(F32P))
+    out = np.empty((h, w, 3), np.uint8)
+    lut = np.ascontiguousarray(pl.tone_lut, np.float32)
+    L.or_tone_rgb8(rgb2.ctypes.data_as(U16P), out.ctypes.data_as(U8P), w, h, bd, pl.tone_mode,
+                   lut.ctypes.data_as(F32P), None)
+    return out
