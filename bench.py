@@ -46,6 +46,8 @@ W_C2, H_C2 = 4024, 3032
 WARP_INST_PER_STEP_8 = 4.048e8
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the streaming kernel's launch over 8 frames
 STREAM_DRAM_BYTES_8 = 393691392
+# HBM bytes per C2 pixel of the plain per-operator chain (planes between its kernels)
+PLAIN_BYTES_PER_PX = 62.5
 
 
 def parse():
@@ -774,8 +776,13 @@ def main():
                        "h2d_bytes_per_step": B * in_b, "d2h_bytes_per_step": B * out_b,
                        "api": "imop_isp_run_host_batch (pinned host frames)"}
     if ms_plain is not None:
+        # the plain path's own HBM traffic: u16 planes between its kernels (bytes per C2 pixel:
+        # unpack 1.5 + 2, black level 2 + 2, Jacobi 2 + 2, seeds 2 + 2, lens shading 2 + 2, white
+        # balance 2 + 2, green 2 + 4, demosaic 2 + 4 + 6, CCM 6 + 6, output 6 + 3)
+        plain_gbs = world * args.steps * px_step * PLAIN_BYTES_PER_PX / (ms_plain / 1e3) / 1e9
         line["plain"] = {"value": round(world * args.steps * px_step / (ms_plain / 1e3) / 1e6, 2), "unit": "Mpix/s",
-                         "ms_per_step": round(ms_plain / args.steps, 4)}
+                         "ms_per_step": round(ms_plain / args.steps, 4), "bytes_per_pixel": PLAIN_BYTES_PER_PX,
+                         "gbs_traffic": round(plain_gbs, 1), "hbm_frac": round(plain_gbs / peak, 4)}
     if adjoint is not None:
         line["adjoint"] = adjoint
     if c4 is not None:

@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "isp_kernels.h"
 #include "isp_dpc.cuh"
 #include "isp_tile.cuh"
@@ -22,19 +24,29 @@ inline int plain_blocks(size_t n) {
 
 #define GRID_STRIDE(i, n) for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (n); i += (size_t)gridDim.x * blockDim.x)
 
+// every pixel (x, y) of a W x H plane, i = y * W + x: rows over the grid's y blocks, columns over
+// its x threads (no division per pixel)
+#define FOR_PIXELS(x, y, i, W, H)                                                                  \
+    for (int y = blockIdx.y; y < (H); y += gridDim.y)                                               \
+        for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < (W); x += gridDim.x * blockDim.x) \
+            if (const size_t i = (size_t)y * (W) + x; true)
+
+// 2-D grid of those loops: enough column blocks for a row, rows up to about 16 CTAs per SM
+inline dim3 pixel_grid(int w, int h) {
+    const int gx = (w + kPlainThreads - 1) / kPlainThreads;
+    const int gy = std::max(1, std::min(h, 152 * 16 / std::max(1, gx)));
+    return dim3((unsigned)gx, (unsigned)gy);
+}
+
 __global__ void unpack_kernel(const __grid_constant__ FrameParams fp, uint16_t* out) {
-    size_t n = (size_t)fp.w * fp.h;
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / fp.w), x = (int)(i % fp.w);
+    FOR_PIXELS(x, y, i, fp.w, fp.h) {
         out[i] = (uint16_t)dev::load_raw(fp, x, y);
     }
 }
 
 __global__ void black_level_kernel(const __grid_constant__ FrameParams fp, uint16_t* d) {
-    size_t n = (size_t)fp.w * fp.h;
     PatternOffsets po = pattern_offsets(fp.pattern);
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / fp.w), x = (int)(i % fp.w);
+    FOR_PIXELS(x, y, i, fp.w, fp.h) {
         d[i] = (uint16_t)dev::black_level(fp, d[i], bayer_color(y, x, po));
     }
 }
@@ -42,9 +54,7 @@ __global__ void black_level_kernel(const __grid_constant__ FrameParams fp, uint1
 // Jacobi defect pass: out = F(in) (adaptive) / in (other pixels)
 __global__ void dpc_jacobi_kernel(const __grid_constant__ FrameParams fp, const uint16_t* in, uint16_t* out) {
     const int W = fp.w, H = fp.h;
-    size_t n = (size_t)W * H;
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / W), x = (int)(i % W);
+    FOR_PIXELS(x, y, i, W, H) {
         int v = in[i];
         if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) {
             int nb[8] = {in[i - 2 * W - 2], in[i - 2 * W], in[i - 2 * W + 2], in[i - 2],
@@ -57,9 +67,7 @@ __global__ void dpc_jacobi_kernel(const __grid_constant__ FrameParams fp, const 
 
 __global__ void dpc_seed_kernel(const __grid_constant__ FrameParams fp, const uint16_t* orig, const uint16_t* jac) {
     const int W = fp.w, H = fp.h;
-    size_t n = (size_t)W * H;
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / W), x = (int)(i % W);
+    FOR_PIXELS(x, y, i, W, H) {
         if (x < 2 || x >= W - 2 || y < 2 || y >= H - 2) continue;
         unsigned m = dev::dpc_valid_mask(x, y, W, H);
         const size_t e[4] = {i - 2 * W - 2, i - 2 * W, i - 2 * W + 2, i - 2};
@@ -96,9 +104,7 @@ __global__ void dpc_fixup_plain_kernel(const __grid_constant__ FrameParams fp, F
 
 __global__ void dpc_map_apply_kernel(const __grid_constant__ FrameParams fp, const uint16_t* in, uint16_t* out) {
     const int W = fp.w, H = fp.h;
-    size_t n = (size_t)W * H;
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / W), x = (int)(i % W);
+    FOR_PIXELS(x, y, i, W, H) {
         int v = in[i];
         if (x >= 2 && x < W - 2 && y >= 2 && y < H - 2) {
             int s = map_lookup(fp, x, y);
@@ -109,10 +115,8 @@ __global__ void dpc_map_apply_kernel(const __grid_constant__ FrameParams fp, con
 }
 
 __global__ void lens_shading_kernel(const __grid_constant__ FrameParams fp, uint16_t* d) {
-    size_t n = (size_t)fp.w * fp.h;
     PatternOffsets po = pattern_offsets(fp.pattern);
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / fp.w), x = (int)(i % fp.w);
+    FOR_PIXELS(x, y, i, fp.w, fp.h) {
         int c = bayer_color(y, x, po);
         d[i] = (uint16_t)((fp.lsc_mode == 1) ? dev::lsc_poly(fp, d[i], x, y, c) : dev::lsc_grid(fp, d[i], x, y, c));
     }
@@ -120,10 +124,8 @@ __global__ void lens_shading_kernel(const __grid_constant__ FrameParams fp, uint
 
 // Bayer WB (spec order) and the demosaic's align_raw_value read
 __global__ void bayer_wb_kernel(const __grid_constant__ FrameParams fp, uint16_t* d, int do_wb) {
-    size_t n = (size_t)fp.w * fp.h;
     PatternOffsets po = pattern_offsets(fp.pattern);
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / fp.w), x = (int)(i % fp.w);
+    FOR_PIXELS(x, y, i, fp.w, fp.h) {
         int v = d[i];
         if (do_wb) v = dev::gain_round(v, fp.wb_cfa[bayer_color(y, x, po)], fp.mv);
         if (fp.bd > 8 && fp.bd < 16 && v > fp.mv) v >>= (16 - fp.bd);
@@ -133,10 +135,8 @@ __global__ void bayer_wb_kernel(const __grid_constant__ FrameParams fp, uint16_t
 
 __global__ void green_kernel(const __grid_constant__ FrameParams fp, const uint16_t* bay, float* green) {
     const int W = fp.w, H = fp.h;
-    size_t n = (size_t)W * H;
     PatternOffsets po = pattern_offsets(fp.pattern);
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / W), x = (int)(i % W);
+    FOR_PIXELS(x, y, i, W, H) {
         bool at_r = ((y & 1) == po.r_row) && ((x & 1) == po.r_col);
         bool at_b = ((y & 1) == po.b_row) && ((x & 1) == po.b_col);
         bool interior = x >= 2 && x < W - 2 && y >= 2 && y < H - 2;
@@ -166,12 +166,10 @@ __global__ void green_kernel(const __grid_constant__ FrameParams fp, const uint1
 __global__ void demosaic_rgb_kernel(const __grid_constant__ FrameParams fp, const uint16_t* bay, const float* green,
                                     uint16_t* rgb) {
     const int W = fp.w, H = fp.h, mv = fp.mv;
-    size_t n = (size_t)W * H;
     PatternOffsets po = pattern_offsets(fp.pattern);
     auto B_ = [&](int x, int y) -> int { return bay[(size_t)y * W + x]; };
     auto G_ = [&](int x, int y) -> float { return green[(size_t)y * W + x]; };
-    GRID_STRIDE(i, n) {
-        int y = (int)(i / W), x = (int)(i % W);
+    FOR_PIXELS(x, y, i, W, H) {
         int sx, sy;
         dev::border_source(x, y, W, H, fp.border_mode, sx, sy);
         bool at_r = ((sy & 1) == po.r_row) && ((sx & 1) == po.r_col);
@@ -293,6 +291,7 @@ cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const Ma
                          const PlainDumps* dumps, cudaStream_t st) {
     const size_t n = (size_t)fp.w * fp.h;
     const int nb = plain_blocks(n), nb3 = plain_blocks(3 * n);
+    const dim3 pg = pixel_grid(fp.w, fp.h);
     auto dump = [&](uint16_t* dst, const uint16_t* src, size_t cnt) -> cudaError_t {
         if (!dst) return cudaSuccess;
         return cudaMemcpyAsync(dst, src, cnt * sizeof(uint16_t), cudaMemcpyDeviceToDevice, st);
@@ -301,31 +300,31 @@ cudaError_t launch_plain(const FrameParams& fp, const FixupScratch& fs, const Ma
     if (!dumps) dumps = &none;
     uint16_t* A = b.bayer_a;
     uint16_t* B = b.bayer_b;
-    unpack_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A);
+    unpack_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A);
     dump(dumps->unpacked, A, n);
-    if (fp.stages & 1u) black_level_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A);
+    if (fp.stages & 1u) black_level_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A);
     dump(dumps->black_level, A, n);
     if (fp.stages & 2u) {
         if (fp.dpc_mode == 0) {
             cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st);
-            dpc_jacobi_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, B);
-            dpc_seed_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, B);
+            dpc_jacobi_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, B);
+            dpc_seed_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, B);
             dpc_fixup_plain_kernel<<<1, 32, 0, st>>>(fp, fs, A, B);
         } else {
             if (plan) launch_map_resolve(fp, *plan, st);
-            dpc_map_apply_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, B);
+            dpc_map_apply_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, B);
         }
         uint16_t* t = A; A = B; B = t;
     }
     dump(dumps->defect, A, n);
-    if (fp.stages & 4u) lens_shading_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A);
+    if (fp.stages & 4u) lens_shading_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A);
     dump(dumps->lens_shading, A, n);
     bool wb = (fp.stages & 8u) != 0;
-    bayer_wb_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, (wb && fp.stage_order == 0) ? 1 : 0);
+    bayer_wb_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, (wb && fp.stage_order == 0) ? 1 : 0);
     if (wb && fp.stage_order == 0) dump(dumps->white_balance, A, n);
     float* green = reinterpret_cast<float*>(B);  // bayer_b is sized for w*h floats
-    if (fp.demosaic != DM_HQLI) green_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, green);
-    demosaic_rgb_kernel<<<nb, kPlainThreads, 0, st>>>(fp, A, green, b.rgb);
+    if (fp.demosaic != DM_HQLI) green_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, green);
+    demosaic_rgb_kernel<<<pg, kPlainThreads, 0, st>>>(fp, A, green, b.rgb);
     dump(dumps->demosaic, b.rgb, 3 * n);
     if (wb && fp.stage_order == 1) {
         rgb_wb_kernel<<<nb3, kPlainThreads, 0, st>>>(fp, b.rgb);
@@ -352,24 +351,24 @@ cudaError_t launch_narrow(const uint16_t* in, uint8_t* out, size_t n, int bytes_
 cudaError_t launch_op_bayer(const FrameParams& fp, unsigned stage, const FixupScratch& fs, const MapPlan* plan,
                             uint16_t* a, uint16_t* b, cudaStream_t st) {
     const size_t n = (size_t)fp.w * fp.h;
-    const int nb = plain_blocks(n);
+    const dim3 pg = pixel_grid(fp.w, fp.h);
     cudaError_t e = cudaSuccess;
     if (stage == 1u) {
-        black_level_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a);
+        black_level_kernel<<<pg, kPlainThreads, 0, st>>>(fp, a);
     } else if (stage == 2u) {
         if (fp.dpc_mode == 0) {
             if ((e = cudaMemsetAsync(fp.seed_count, 0, sizeof(int), st))) return e;
-            dpc_jacobi_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
-            dpc_seed_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
+            dpc_jacobi_kernel<<<pg, kPlainThreads, 0, st>>>(fp, a, b);
+            dpc_seed_kernel<<<pg, kPlainThreads, 0, st>>>(fp, a, b);
             dpc_fixup_plain_kernel<<<1, 32, 0, st>>>(fp, fs, a, b);
         } else {
             if (plan && (e = launch_map_resolve(fp, *plan, st))) return e;
-            dpc_map_apply_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a, b);
+            dpc_map_apply_kernel<<<pg, kPlainThreads, 0, st>>>(fp, a, b);
         }
         if ((e = cudaGetLastError())) return e;
         return cudaMemcpyAsync(a, b, n * sizeof(uint16_t), cudaMemcpyDeviceToDevice, st);
     } else if (stage == 4u) {
-        lens_shading_kernel<<<nb, kPlainThreads, 0, st>>>(fp, a);
+        lens_shading_kernel<<<pg, kPlainThreads, 0, st>>>(fp, a);
     } else {
         return cudaErrorInvalidValue;
     }
