@@ -3,7 +3,7 @@
 // imop_isp_batch_submit: every frame's parameters are expanded into a FrameParams whose table
 // pointers come from the context's TableCache (one device copy per distinct grid / tone table /
 // defect map / bit depth), each frame gets its own defect-chain scratch, and the frames go to the
-// persistent fused kernel together: one launch walks the tiles of up to 16 frames.  With
+// persistent fused kernels together: one launch walks the work of up to 32 frames.  With
 // IMOP_BATCH_GRAPH the launches are recorded once into a CUDA graph and replayed while the
 // descriptors stay the same.
 //

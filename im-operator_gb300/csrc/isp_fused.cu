@@ -445,11 +445,11 @@ std::mutex& device_setup_mutex() {
     return m;
 }
 
-static std::atomic<long long> g_launches[3];
+static std::atomic<long long> g_launches[4];
 void count_launch(int kernel) { g_launches[kernel].fetch_add(1, std::memory_order_relaxed); }
 
 extern "C" long long imop_kernel_launches(int kernel) {
-    return (kernel >= 0 && kernel < 3) ? g_launches[kernel].load(std::memory_order_relaxed) : -1;
+    return (kernel >= 0 && kernel < 4) ? g_launches[kernel].load(std::memory_order_relaxed) : -1;
 }
 
 int fused_grid_limit(int out_bpc) {

@@ -12,9 +12,11 @@ namespace imop {
 // nominal fused tile (the last tile of a row / column absorbs a remainder below 4)
 constexpr int kTileW = 120;
 constexpr int kTileH = 24;
-// work-claim words of one streaming launch (segments of its strips; the last word counts the tiles
-// of the batch's border-column launch)
+// work-claim words of one streamed launch: a word per segment of its strips (at most kSegMax),
+// then the count of segments taken; the last word counts the tiles of a streamed batch's
+// border-column launch
 constexpr int kStreamSegCap = 4096;
+constexpr int kSegMax = kStreamSegCap - 2;
 // narrow fused tile of the border columns of streamed frames (isp_fused_narrow.cu)
 constexpr int kNarrowW = 16;
 constexpr int kNarrowH = 128;
@@ -23,7 +25,7 @@ constexpr int kNarrowH = 128;
 // the tiles of a list of rectangles (one per frame), rectangle after rectangle, tiles in raster
 // order; CTAs claim tiles from a device counter, so border tiles (the general path) and
 // partial tiles do not unbalance the CTAs.
-constexpr int kBatchInline = 16;
+constexpr int kBatchInline = 32;
 constexpr int kMaxRects = 4 * kBatchInline;  // the border rectangles of a streamed batch
 struct TileRect {
     int frame;
@@ -123,8 +125,14 @@ long long lite_table_key(const FrameParams& fp);
 // units of work of a frame: strips across, bands down (a rectangle's tiles_x / tiles_y)
 int lite_units_x(int w);
 int lite_units_y(int h, int band_rows);
-// one persistent launch over the units of bl's rectangles (bl.fmt: the frames' common format)
+// one persistent launch over the units of bl's rectangles (bl.fmt: the frames' common format);
+// frames 16-byte aligned with widths that are multiples of 8 and work-claim words take the
+// direct-read variant, whose segments are chosen here
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
+// Segments of the strips of bl's rectangles (tiles_x strips each): each strip cut into segments
+// of seg_percent % of the rows that spread the launch's strip rows evenly over `warps` warps,
+// at most kSegMax in all; bands of band_rows rows inside them (isp_segments.cuh)
+void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows);
 
 // warp-streamed kernel for the AMAZE chains (isp_stream.cu): black level, adaptive defect
 // correction, grid lens shading, Bayer-order white balance, AMAZE, CCM, tone -> RGB8 on the interior

@@ -1,13 +1,21 @@
-// isp_lite.cu - the light-chain kernel (isp_lite.cuh): persistent CTAs whose warps each claim bands
-// of frame strips from a device counter and stream them row by row.
+// isp_lite.cu - the light-chain kernel (isp_lite.cuh) in two variants.  The staged one: persistent
+// CTAs whose warps each claim bands of frame strips from a device counter and stream them row by
+// row from a ring of bulk-copied rows (any frame).  The direct-read one: frames 16-byte aligned
+// with a width that is a multiple of 8; lanes load their samples with plain coalesced loads two
+// rows ahead, and each warp streams a whole segment of its strip (isp_segments.cuh).
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
+#include <mutex>
 
+#include "imop_isp.h"
 #include "isp_fused_kernel.cuh"
 #include "isp_kernels.h"
 #include "isp_lite.cuh"
+#include "isp_rows.cuh"
+#include "isp_segments.cuh"
 
 namespace imop {
 namespace {
@@ -104,6 +112,192 @@ __device__ __forceinline__ void decode_pairs(const FrameParams& fp, const uint8_
     }
 }
 
+// black level and Bayer-order white balance of a row, its parameters in registers for a unit (the
+// parameter block is read through an indexed constant bank)
+struct LiteLevels {
+    uint32_t nbl0, nbl1, mv2;  // the negated black levels of even / odd rows as pairs; the maximum twice
+    int nbb0, nbb1, mv;        // the negated black level of the lane's outer sample, even / odd rows
+    bool bl_on, per_sample;    // per_sample: Bayer-order white balance or the MSB-aligned read
+};
+__device__ __forceinline__ LiteLevels lite_levels_of(const FrameParams& fp, int lane) {
+    LiteLevels L;
+    const int e0 = fp.bl_i[0][0], o0 = fp.bl_i[0][1], e1 = fp.bl_i[1][0], o1 = fp.bl_i[1][1];
+    L.nbl0 = ((uint32_t)(-e0) & 0xFFFFu) | ((uint32_t)(-o0) << 16);
+    L.nbl1 = ((uint32_t)(-e1) & 0xFFFFu) | ((uint32_t)(-o1) << 16);
+    // lane 0's outer sample (column x0 - 1) is in an odd column, lane 31's (x0 + 256) in an even one
+    L.nbb0 = lane == 0 ? -o0 : -e0;
+    L.nbb1 = lane == 0 ? -o1 : -e1;
+    L.mv = fp.mv;
+    L.mv2 = (uint32_t)fp.mv | ((uint32_t)fp.mv << 16);
+    L.bl_on = (fp.stages & 1u) != 0;
+    L.per_sample = ((fp.stages & 8u) && fp.stage_order == 0) || fp.need_align != 0;
+    return L;
+}
+
+// one sample at a time: black level, Bayer-order white balance, the MSB-aligned read
+__device__ __forceinline__ void lite_levels_each(const FrameParams& fp, PatternOffsets po, int y, int lane,
+                                                 uint32_t (&P)[4], int& nb) {
+    const int mv = fp.mv, p = y & 1;
+    const int bl_e = fp.bl_i[p][0], bl_o = fp.bl_i[p][1];
+    const bool bl_on = (fp.stages & 1u) != 0, wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
+    const bool need_align = fp.need_align != 0;
+    const float wb_e = fp.wb_cfa[bayer_color(y, 0, po)], wb_o = fp.wb_cfa[bayer_color(y, 1, po)];
+    auto one = [&](int v, bool odd) {
+        if (bl_on) v = __viaddmin_s32_relu(v, odd ? -bl_o : -bl_e, mv);
+        if (wb_bayer) v = dev::gain_round(v, odd ? wb_o : wb_e, mv);
+        if (need_align && v > mv) v >>= (16 - fp.bd);
+        return v;
+    };
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        P[j] = (uint32_t)one((int)(P[j] & 0xFFFFu), false) | ((uint32_t)one((int)(P[j] >> 16), true) << 16);
+    nb = one(nb, lane == 0);
+}
+
+// the lane's pairs P and the strip's outer neighbour nb (lane 0: column x0 - 1, lane 31: column
+// x0 + 256) of row y
+template <int FMT>
+__device__ __forceinline__ void lite_levels(const FrameParams& fp, const LiteLevels& L, PatternOffsets po, int y,
+                                            int lane, uint32_t (&P)[4], int& nb) {
+    // u16 samples above 32767 (beyond any bit depth here) do not fit the pairs' signed 16-bit add:
+    // those lanes take the per-sample path
+    const bool per_sample =
+        L.per_sample || (FMT == FMT_U16 && L.bl_on && ((P[0] | P[1] | P[2] | P[3]) & 0x80008000u) != 0);
+    if (!per_sample) {
+        // black level (integral offsets <= the maximum: lite_eligible) on both samples of a pair at
+        // once: (int)((float)v - off) clamped to [0, mv]
+        if (L.bl_on) {
+            const bool odd = (y & 1) != 0;
+            const uint32_t nbl = odd ? L.nbl1 : L.nbl0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) P[j] = __viaddmin_s16x2_relu(P[j], nbl, L.mv2);
+            nb = __viaddmin_s32_relu(nb, odd ? L.nbb1 : L.nbb0, L.mv);
+        }
+    } else {
+        lite_levels_each(fp, po, y, lane, P, nb);
+    }
+}
+
+// the output row from the staging row of the warp: the row's bytes at their 16-byte phase, the
+// border columns fixed, vector stores of the whole 16-byte chunks; rows 0, 1 / h-2, h-1 with row
+// 2 / h-3
+__device__ __forceinline__ void lite_emit_staged(const uint8_t (*tab)[4096], uint8_t* wout, uint8_t* out, int W, int H,
+                                              int x0, int npx, int lane, int yo, uint4 oa, uint2 ob2) {
+    const uint32_t ob[6] = {oa.x, oa.y, oa.z, oa.w, ob2.x, ob2.y};
+    const uintptr_t out_base = reinterpret_cast<uintptr_t>(out);
+    const int xl = x0 + kLiteLanePx * lane;
+    const bool edge_l = x0 == 0, edge_r = x0 + npx == W;
+    const int g0 = (yo * W + x0) * 3;
+    // otherwise: stage at the output row's 16-byte phase, fix the border columns, store
+    const int shift = (int)((out_base + (uintptr_t)g0) & 15);
+    const int nbytes = 3 * npx;
+    uint8_t* st = wout + shift + 24 * lane;
+    if (xl < x0 + npx) {
+        if ((shift & 7) == 0) {
+            uint2* q2 = reinterpret_cast<uint2*>(st);
+            q2[0] = make_uint2(ob[0], ob[1]);
+            q2[1] = make_uint2(ob[2], ob[3]);
+            q2[2] = make_uint2(ob[4], ob[5]);
+        } else if ((shift & 3) == 0) {
+            uint32_t* q4 = reinterpret_cast<uint32_t*>(st);
+#pragma unroll
+            for (int q = 0; q < 6; q++) q4[q] = ob[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 24; q++) st[q] = (uint8_t)(ob[q >> 2] >> (8 * (q & 3)));
+        }
+    }
+    __syncwarp();
+    uint8_t* so = wout + shift;
+    if (edge_l || edge_r) {
+        if (lane < 6) {
+            // columns 0, 1 <- 2 and w-2, w-1 <- w-3 (lanes 0-2 / 3-5, one byte each)
+            const int b = lane % 3;
+            if (lane < 3 && edge_l) so[b] = so[3 + b] = so[6 + b];
+            if (lane >= 3 && edge_r) {
+                const int c3 = W - 3 - x0;
+                so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = so[3 * c3 + b];
+            }
+        }
+        __syncwarp();
+    }
+    // the row, and rows 0, 1 with row 2 / rows h-2, h-1 with row h-3 (their corner pixels
+    // zero: the tables' bytes of 0)
+    const int copies = (yo == 2 || yo == H - 3) ? 3 : 1;
+    for (int rep = 0; rep < copies; rep++) {
+        const int yt = rep == 0 ? yo : (yo == 2 ? rep - 1 : H - 3 + rep);
+        if (rep == 1) {
+            if (lane < 6) {
+                const int b = lane % 3;
+                const uint8_t z = tab[b][0];
+                if (lane < 3 && edge_l) so[b] = so[3 + b] = z;
+                if (lane >= 3 && edge_r) {
+                    const int c3 = W - 3 - x0;
+                    so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = z;
+                }
+            }
+            __syncwarp();
+        }
+        const int gt = (yt * W + x0) * 3;
+        if ((int)((out_base + (uintptr_t)gt) & 15) == shift) {
+            // staging bytes [A, E) <-> output bytes from gt: whole 16-byte chunks as vector
+            // stores, the head and tail bytes one per lane
+            uint8_t* base = out + gt - shift;  // 16-byte aligned
+            const int A = shift, E = shift + nbytes;
+            const int F = (A + 15) & ~15, L = E & ~15;
+            if (F < L) {
+                for (int c = F / 16 + lane; c < L / 16; c += 32)
+                    ptx::st_global_v4(base + 16 * c, *reinterpret_cast<const uint4*>(wout + 16 * c));
+                if (A + lane < F) base[A + lane] = wout[A + lane];
+                if (L + lane < E) base[L + lane] = wout[L + lane];
+            } else if (A + lane < E) {
+                base[A + lane] = wout[A + lane];
+            }
+        } else {
+            uint8_t* d8 = out + gt;
+            for (int b = lane; b < nbytes; b += 32) d8[b] = so[b];
+        }
+    }
+    __syncwarp();
+}
+
+// output row y - 1 from rows u, m, d (y - 2 .. y) of the strip at x0 (npx columns): HQLI through
+// the output tables, the reference's border copies, 24-byte stores per lane or staged rows
+__device__ __forceinline__ void lite_emit(const uint8_t (*tab)[4096], uint8_t* wout, int W, int H, uint8_t* out,
+                                          PatternOffsets po, int x0, int npx, int lane, int y, const lite::Row& Ur,
+                                          const lite::Row& Mr, const lite::Row& Dr) {
+    const uintptr_t out_base = reinterpret_cast<uintptr_t>(out);
+    const int xl = x0 + kLiteLanePx * lane;
+    const bool edge_l = x0 == 0, edge_r = x0 + npx == W;
+    const bool lane_in = xl + kLiteLanePx <= x0 + npx;
+    // ---- output row yo = y - 1 -------------------------------------------------------------
+    const int yo = y - 1;
+    if (yo < 2 || yo >= H - 2) return;  // emitted with row 2 / h-3
+    uint32_t ob[6];
+    const bool rrow = (yo & 1) == po.r_row;
+    const int rb = rrow ? po.r_col : po.b_col;
+    if (rb == 0) {
+        if (rrow) lite::hqli_row<0, true>(Ur, Mr, Dr, tab, ob);
+        else lite::hqli_row<0, false>(Ur, Mr, Dr, tab, ob);
+    } else {
+        if (rrow) lite::hqli_row<1, true>(Ur, Mr, Dr, tab, ob);
+        else lite::hqli_row<1, false>(Ur, Mr, Dr, tab, ob);
+    }
+    const int g0 = (yo * W + x0) * 3;
+    // an interior strip whose row starts 8-byte aligned: each lane stores its 24 bytes
+    if (!edge_l && !edge_r && yo != 2 && yo != H - 3 && ((out_base + (uintptr_t)g0) & 7) == 0) {
+        if (lane_in) {
+            uint2* q = reinterpret_cast<uint2*>(out + g0 + 24 * lane);
+            q[0] = make_uint2(ob[0], ob[1]);
+            q[1] = make_uint2(ob[2], ob[3]);
+            q[2] = make_uint2(ob[4], ob[5]);
+        }
+        return;
+    }
+    lite_emit_staged(tab, wout, out, W, H, x0, npx, lane, yo, make_uint4(ob[0], ob[1], ob[2], ob[3]),
+                     make_uint2(ob[4], ob[5]));
+}
+
 template <int FMT>
 __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
@@ -171,18 +365,11 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
     lite::Row Ur, Mr, Dr;  // rows y-2, y-1, y of the lane (packed pairs)
     while (true) {
         const FrameParams& fp = bl.frames[cur.f];
-        const int W = fp.w, H = fp.h, mv = fp.mv;
+        const int W = fp.w;
         const PatternOffsets po = pattern_offsets(fp.pattern);
-        const bool bl_on = (fp.stages & 1u) != 0;
-        const bool wb_bayer = (fp.stages & 8u) && fp.stage_order == 0;
-        const bool need_align = fp.need_align != 0;
-        // a float stage or the MSB-aligned read take the per-sample path
-        const bool per_sample_frame = wb_bayer || need_align;
-        const uintptr_t out_base = reinterpret_cast<uintptr_t>(fp.out);
+        const LiteLevels L = lite_levels_of(fp, lane);
         const bool aligned_in = (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0;
         const int xl = cur.x0 + kLiteLanePx * lane;  // the lane's first column
-        const bool edge_l = cur.x0 == 0, edge_r = cur.x0 + cur.npx == W;
-        const bool lane_in = xl + kLiteLanePx <= cur.x0 + cur.npx;  // all 8 pixels in the strip
         for (int k = 0; k < cur.nrows; k++) {
             const int s = (int)(used % kLiteRing);
             const uint32_t parity = (used / kLiteRing) & 1u;
@@ -217,35 +404,7 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
                         nb = lane == 0 ? (int)(t[3] >> 16) : (int)(t[0] & 0xFFFFu);
                     }
                 }
-                const int p = y & 1;
-                const int bl_e = fp.bl_i[p][0], bl_o = fp.bl_i[p][1];
-                // u16 samples above 32767 (beyond any bit depth here) do not fit the pairs' signed
-                // 16-bit add: those lanes take the per-sample path
-                const bool per_sample =
-                    per_sample_frame || (FMT == FMT_U16 && bl_on && ((P[0] | P[1] | P[2] | P[3]) & 0x80008000u) != 0);
-                if (!per_sample) {
-                    // black level (integral offsets <= the maximum: lite_eligible) on both samples of
-                    // a pair at once: (int)((float)v - off) clamped to [0, mv]
-                    if (bl_on) {
-                        const uint32_t nbl = ((uint32_t)(-bl_e) & 0xFFFFu) | ((uint32_t)(-bl_o) << 16);
-                        const uint32_t mv2 = (uint32_t)mv | ((uint32_t)mv << 16);
-#pragma unroll
-                        for (int j = 0; j < 4; j++) P[j] = __viaddmin_s16x2_relu(P[j], nbl, mv2);
-                        nb = __viaddmin_s32_relu(nb, lane == 0 ? -bl_o : -bl_e, mv);
-                    }
-                } else {
-                    const float wb_e = fp.wb_cfa[bayer_color(y, 0, po)], wb_o = fp.wb_cfa[bayer_color(y, 1, po)];
-                    auto one = [&](int v, bool odd) {
-                        if (bl_on) v = __viaddmin_s32_relu(v, odd ? -bl_o : -bl_e, mv);
-                        if (wb_bayer) v = dev::gain_round(v, odd ? wb_o : wb_e, mv);
-                        if (need_align && v > mv) v >>= (16 - fp.bd);
-                        return v;
-                    };
-#pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        P[j] = (uint32_t)one((int)(P[j] & 0xFFFFu), false) | ((uint32_t)one((int)(P[j] >> 16), true) << 16);
-                    nb = one(nb, lane == 0);
-                }
+                lite_levels<FMT>(fp, L, po, y, lane, P, nb);
                 if (lane == 0 && cur.x0 == 0) nb = 0;
             }
             uint32_t Lw = __shfl_up_sync(0xffffffffu, P[3], 1) & 0xFFFF0000u;
@@ -266,101 +425,7 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
             Dr.R = Rn;
             if (k < 2) continue;
 
-            // ---- output row yo = y - 1 -------------------------------------------------------------
-            const int yo = y - 1;
-            if (yo < 2 || yo >= H - 2) continue;  // emitted with row 2 / h-3
-            uint32_t ob[6];
-            const bool rrow = (yo & 1) == po.r_row;
-            const int rb = rrow ? po.r_col : po.b_col;
-            if (rb == 0) {
-                if (rrow) lite::hqli_row<0, true>(Ur, Mr, Dr, sm.tab, ob);
-                else lite::hqli_row<0, false>(Ur, Mr, Dr, sm.tab, ob);
-            } else {
-                if (rrow) lite::hqli_row<1, true>(Ur, Mr, Dr, sm.tab, ob);
-                else lite::hqli_row<1, false>(Ur, Mr, Dr, sm.tab, ob);
-            }
-            const int g0 = (yo * W + cur.x0) * 3;
-            // an interior strip whose row starts 8-byte aligned: each lane stores its 24 bytes
-            if (!edge_l && !edge_r && yo != 2 && yo != H - 3 && ((out_base + (uintptr_t)g0) & 7) == 0) {
-                if (lane_in) {
-                    uint2* q = reinterpret_cast<uint2*>(fp.out + g0 + 24 * lane);
-                    q[0] = make_uint2(ob[0], ob[1]);
-                    q[1] = make_uint2(ob[2], ob[3]);
-                    q[2] = make_uint2(ob[4], ob[5]);
-                }
-                continue;
-            }
-            // otherwise: stage at the output row's 16-byte phase, fix the border columns, store
-            const int shift = (int)((out_base + (uintptr_t)g0) & 15);
-            const int nbytes = 3 * cur.npx;
-            uint8_t* st = ws.out + shift + 24 * lane;
-            if (xl < cur.x0 + cur.npx) {
-                if ((shift & 7) == 0) {
-                    uint2* q2 = reinterpret_cast<uint2*>(st);
-                    q2[0] = make_uint2(ob[0], ob[1]);
-                    q2[1] = make_uint2(ob[2], ob[3]);
-                    q2[2] = make_uint2(ob[4], ob[5]);
-                } else if ((shift & 3) == 0) {
-                    uint32_t* q4 = reinterpret_cast<uint32_t*>(st);
-#pragma unroll
-                    for (int q = 0; q < 6; q++) q4[q] = ob[q];
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 24; q++) st[q] = (uint8_t)(ob[q >> 2] >> (8 * (q & 3)));
-                }
-            }
-            __syncwarp();
-            uint8_t* so = ws.out + shift;
-            if (edge_l || edge_r) {
-                if (lane < 6) {
-                    // columns 0, 1 <- 2 and w-2, w-1 <- w-3 (lanes 0-2 / 3-5, one byte each)
-                    const int b = lane % 3;
-                    if (lane < 3 && edge_l) so[b] = so[3 + b] = so[6 + b];
-                    if (lane >= 3 && edge_r) {
-                        const int c3 = W - 3 - cur.x0;
-                        so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = so[3 * c3 + b];
-                    }
-                }
-                __syncwarp();
-            }
-            // the row, and rows 0, 1 with row 2 / rows h-2, h-1 with row h-3 (their corner pixels
-            // zero: the tables' bytes of 0)
-            const int copies = (yo == 2 || yo == H - 3) ? 3 : 1;
-            for (int rep = 0; rep < copies; rep++) {
-                const int yt = rep == 0 ? yo : (yo == 2 ? rep - 1 : H - 3 + rep);
-                if (rep == 1) {
-                    if (lane < 6) {
-                        const int b = lane % 3;
-                        const uint8_t z = sm.tab[b][0];
-                        if (lane < 3 && edge_l) so[b] = so[3 + b] = z;
-                        if (lane >= 3 && edge_r) {
-                            const int c3 = W - 3 - cur.x0;
-                            so[3 * (c3 + 1) + b] = so[3 * (c3 + 2) + b] = z;
-                        }
-                    }
-                    __syncwarp();
-                }
-                const int gt = (yt * W + cur.x0) * 3;
-                if ((int)((out_base + (uintptr_t)gt) & 15) == shift) {
-                    // staging bytes [A, E) <-> output bytes from gt: whole 16-byte chunks as vector
-                    // stores, the head and tail bytes one per lane
-                    uint8_t* base = fp.out + gt - shift;  // 16-byte aligned
-                    const int A = shift, E = shift + nbytes;
-                    const int F = (A + 15) & ~15, L = E & ~15;
-                    if (F < L) {
-                        for (int c = F / 16 + lane; c < L / 16; c += 32)
-                            ptx::st_global_v4(base + 16 * c, *reinterpret_cast<const uint4*>(ws.out + 16 * c));
-                        if (A + lane < F) base[A + lane] = ws.out[A + lane];
-                        if (L + lane < E) base[L + lane] = ws.out[L + lane];
-                    } else if (A + lane < E) {
-                        base[A + lane] = ws.out[A + lane];
-                    }
-                } else {
-                    uint8_t* d8 = fp.out + gt;
-                    for (int b = lane; b < nbytes; b += 32) d8[b] = so[b];
-                }
-            }
-            __syncwarp();
+            lite_emit(sm.tab, ws.out, W, fp.h, fp.out, po, cur.x0, cur.npx, lane, y, Ur, Mr, Dr);
         }
         // the next unit: `nxt` (claimed while `cur`'s last rows were staged) becomes current
         if (nxt_item < 0) {
@@ -379,6 +444,178 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
         while (issued - used < (unsigned)kLiteRing)
             if (!issue_next()) break;
     }
+}
+
+// ---- the direct-read variant ---------------------------------------------------------------
+// Frames 16-byte aligned with a width that is a multiple of 8 skip the staging ring: each lane
+// reads its 8 samples of a row with plain coalesced loads two rows ahead of their use (lanes 0 and
+// 31 also the groups left and right of the strip), and a warp streams a whole segment of its strip
+// band after band, so only bands taken from the back of another warp's segment (the end-of-launch
+// balancing) re-read the two rows above them.  One CTA per SM builds the output tables once.
+constexpr int kDirWarps = 16;
+constexpr int kDirThreads = 32 * kDirWarps;
+
+struct LiteDirectSmem {
+    alignas(16) uint8_t tab[3][4096];
+    alignas(16) uint8_t out[kDirWarps][LiteWarpSmem::OUT_PITCH];
+};
+static_assert(kDirWarps * LiteWarpSmem::OUT_PITCH >= 4096, "the staging rows hold the tone table at start");
+
+// a segment of a strip (isp_segments.cuh): columns [x0, x0 + npx), output rows [s0, s0 + len)
+struct LSeg {
+    int f, x0, npx, s0, len, nb;
+};
+
+__device__ __forceinline__ void lseg_of(const BatchLaunch& bl, int seg, LSeg& G) {
+    const int r = item_rect(bl, seg);
+    const TileRect& R = bl.rects[r];
+    const int t = seg - bl.rect_start[r];
+    const int ty = t / R.tiles_x, tx = t - ty * R.tiles_x;
+    const int sw = lite_strip_w(R.w);
+    G.f = R.frame;
+    G.x0 = R.x0 + tx * sw;
+    G.npx = min(sw, R.w - tx * sw);
+    segs::split_rows(R.y0, R.h, R.tiles_y, ty, G.s0, G.len);
+    G.nb = max(1, (G.len + bl.band_h - 1) / bl.band_h);
+}
+
+// output rows [y0, y0 + bh) of segment U and, while `own` is set, the segment's next bands from
+// the front: input rows y0 - 1 .. (the row below the last output row)
+template <int FMT>
+__device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t (*tab)[4096], uint8_t* wout,
+                                            const LSeg& U, int y0, int bh, unsigned long long* own, int lane) {
+    const unsigned full = 0xffffffffu;
+    const FrameParams& fp = bl.frames[U.f];
+    const int W = fp.w, H = fp.h;
+    const uint8_t* const in = fp.in;
+    uint8_t* const out = fp.out;
+    const PatternOffsets po = pattern_offsets(fp.pattern);
+    const LiteLevels L = lite_levels_of(fp, lane);
+    const int xl = U.x0 + kLiteLanePx * lane;
+    const bool lane_in = xl < W;  // the width is a multiple of 8
+    // lane 0: the sample left of the strip (column x0 - 1); lane 31: the one right of it (x0 + 256)
+    const int xe = lane == 0 ? U.x0 - 1 : U.x0 + kLiteStripMax;
+    const bool edge_in = (lane == 0 || lane == 31) && xe >= 0 && xe < W;
+    const int lane_byte = xl * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+    const int edge_byte = !edge_in ? 0 : lane == 0 ? rows::edge_byte<FMT, true>(xe) : rows::edge_byte<FMT, false>(xe);
+    const int pitch = W * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+    const int n0 = y0 - 1;
+    int nrows = bh + 2;
+    auto fetch = [&](int n, uint32_t (&w)[4], rows::Edge<FMT>& e) {
+        const bool row_in = (unsigned)n < (unsigned)H;
+        const uint8_t* rp = in + (row_in ? (long long)n * pitch : 0ll);
+        rows::load8<FMT>(rp, lane_byte, row_in && lane_in, w);
+        rows::load_edge<FMT>(rp, edge_byte, row_in && edge_in, e);
+    };
+    // two row buffers, each refilled with the row two below as soon as it is decoded, so every
+    // load has two rows of work to arrive in (the loop is unrolled by two: no buffer is copied)
+    uint32_t wa[4], wb[4];
+    rows::Edge<FMT> ea, eb;
+    fetch(n0, wa, ea);
+    fetch(n0 + 1, wb, eb);
+    lite::Row Ur, Mr, Dr;  // rows n - 2, n - 1, n of the lane
+    // the owner's claim of the segment's next band is in flight a band ahead of its use (lane 0
+    // holds the counter's old value), so the warp never waits for the atomic
+    unsigned long long pend = 0;
+    if (own && lane == 0) pend = atomicAdd(own, segs::kFrontOne);
+    int k = 0;
+    auto step = [&](uint32_t (&w)[4], rows::Edge<FMT>& e) -> bool {
+        if (k >= nrows) return false;
+        const int n = n0 + k;
+        uint32_t P[4];
+        rows::decode8<FMT>(w, P);
+        int nb = lane == 0 ? rows::decode_edge<FMT, true>(e) : rows::decode_edge<FMT, false>(e);
+        if (own && k + 2 == nrows) {
+            // the segment's next band continues this stream
+            int j = 0;
+            if (lane == 0) j = segs::settle_front(pend, bl.seg_words + bl.n_items);
+            j = __shfl_sync(full, j, 0);
+            if (j >= 0) {
+                int yb, hb;
+                segs::band_of(U.s0, U.len, U.nb, j, yb, hb);
+                nrows += hb;
+                if (lane == 0) pend = atomicAdd(own, segs::kFrontOne);
+            } else {
+                own = nullptr;
+            }
+        }
+        if (k + 2 < nrows) fetch(n + 2, w, e);
+        lite_levels<FMT>(fp, L, po, n, lane, P, nb);
+        uint32_t Lw = __shfl_up_sync(full, P[3], 1) & 0xFFFF0000u;
+        uint32_t Rn = __shfl_down_sync(full, P[0], 1) & 0xFFFFu;
+        if (lane == 0) Lw = (uint32_t)nb << 16;
+        if (lane == 31) Rn = (uint32_t)nb;
+        Ur = Mr;
+        Mr = Dr;
+#pragma unroll
+        for (int j = 0; j < 4; j++) Dr.P[j] = P[j];
+        Dr.Lw = Lw;
+        Dr.R = Rn;
+        if (k >= 2) lite_emit(tab, wout, W, H, out, po, U.x0, U.npx, lane, n, Ur, Mr, Dr);
+        k++;
+        return true;
+    };
+#pragma unroll 1
+    while (step(wa, ea) && step(wb, eb)) {
+    }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __grid_constant__ BatchLaunch bl) {
+    extern __shared__ __align__(16) uint8_t dsm[];
+    auto& sm = *reinterpret_cast<LiteDirectSmem*>(dsm);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    {
+        // tables of the launch, as in the staged variant; the tone table first comes into the
+        // warps' staging rows by 16-byte loads (its buffer holds at least 4096 bytes)
+        const FrameParams& f0 = bl.frames[0];
+        const int mv = f0.mv, nv = mv + 1;
+        const bool wb_rgb = (f0.stages & 8u) && f0.stage_order == 1;
+        uint8_t* tone_s = &sm.out[0][0];
+        for (int i = threadIdx.x; i < (nv + 15) / 16; i += kDirThreads)
+            reinterpret_cast<uint4*>(tone_s)[i] = __ldg(reinterpret_cast<const uint4*>(f0.tone8) + i);
+        __syncthreads();
+#pragma unroll 1
+        for (int c = 0; c < 3; c++) {
+            const float g = f0.wb_rgb[c];
+            for (int v = threadIdx.x; v < nv; v += kDirThreads) sm.tab[c][v] = tone_s[wb_rgb ? dev::gain_round(v, g, mv) : v];
+        }
+    }
+    __syncthreads();
+    const int nseg = bl.n_items;
+    const int gw = (int)blockIdx.x * kDirWarps + warp;
+    uint8_t* wout = sm.out[warp];
+    // the warp's own segment, band after band from the front, then bands from the back of others
+    segs::Walk walk(gw, nseg);
+    int seg, band;
+    bool own;
+    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
+        LSeg S;
+        lseg_of(bl, seg, S);
+        int y0, bh;
+        segs::band_of(S.s0, S.len, S.nb, band, y0, bh);
+        direct_unit<FMT>(bl, sm.tab, wout, S, y0, bh, own ? bl.seg_words + seg : nullptr, lane);
+    }
+}
+
+// the launch's claim words: each segment's band count with zero claims, then the taken count
+__global__ void lite_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < bl.n_items) {
+        LSeg G;
+        lseg_of(bl, i, G);
+        bl.seg_words[i] = segs::initial_word(G.nb);
+    } else if (i == bl.n_items) {
+        bl.seg_words[i] = 0ull;
+    }
+}
+
+int g_direct_grid[kMaxDev];
+
+template <int FMT>
+cudaError_t launch_direct_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
+    lite_direct_kernel<FMT><<<grid, kDirThreads, smem, st>>>(bl);
+    return cudaGetLastError();
 }
 
 int g_lite_grid[kMaxDev];
@@ -422,7 +659,63 @@ long long lite_table_key(const FrameParams& fp) {
 int lite_units_x(int w) { return lite_strips(w); }
 int lite_units_y(int h, int band_rows) { return tiles_along(h, band_rows); }
 
+// frames the direct-read variant takes: whole lane groups, word-aligned rows, claim words
+static bool direct_ok(const FrameParams& fp) {
+    return fp.w % 8 == 0 && (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0 && fp.seg_words &&
+           fp.seg_cap >= kStreamSegCap;
+}
+
+static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
+    const size_t smem = sizeof(LiteDirectSmem);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    int limit;
+    {
+        std::lock_guard<std::mutex> lock(device_setup_mutex());
+        if (!g_direct_grid[dev]) {
+            void (*ks[4])(BatchLaunch) = {lite_direct_kernel<FMT_U8>, lite_direct_kernel<FMT_U16>,
+                                          lite_direct_kernel<FMT_P10>, lite_direct_kernel<FMT_P12>};
+            for (int k = 0; k < 4 && e == cudaSuccess; k++)
+                e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int n = 0, m = 0;
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[1], kDirThreads, smem);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            g_direct_grid[dev] = m * (n > 0 ? n : 1);
+        }
+        limit = g_direct_grid[dev];
+    }
+    BatchLaunch bl = bl_in;
+    int wmax = 0;
+    for (int f = 0; f < bl.n_frames; f++) wmax = std::max(wmax, bl.frames[f].w);
+    const TuneParams tp = tuning_for(IMOP_KERNEL_LITE, bl.fmt, wmax);
+    choose_segments(bl, limit * kDirWarps, tp.seg_percent, tp.band_rows);
+    if (bl.n_items <= 0) return cudaSuccess;
+    if (bl.n_items > kSegMax) return cudaErrorInvalidValue;
+    unsigned long long* words = bl.frames[0].seg_words;
+    bl.seg_words = words;
+    lite_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int want = (bl.n_items + kDirWarps - 1) / kDirWarps;
+    const int grid = want < limit ? want : limit;
+    count_launch(IMOP_KERNEL_LITE);
+    count_launch(IMOP_KERNEL_LITE_DIRECT);
+    switch (bl.fmt) {
+        case FMT_U8: return launch_direct_fmt<FMT_U8>(bl, grid, smem, st);
+        case FMT_U16: return launch_direct_fmt<FMT_U16>(bl, grid, smem, st);
+        case FMT_P10: return launch_direct_fmt<FMT_P10>(bl, grid, smem, st);
+        case FMT_P12: return launch_direct_fmt<FMT_P12>(bl, grid, smem, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
+    bool direct = bl.n_frames > 0;
+    for (int f = 0; f < bl.n_frames; f++)
+        direct = direct && direct_ok(bl.frames[f]) && bl.frames[f].seg_words == bl.frames[0].seg_words;
+    if (direct) return launch_direct(bl, st);
     const size_t smem = sizeof(LiteSmem);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -34,6 +34,8 @@
 #include "isp_device.cuh"
 #include "isp_fused_kernel.cuh"
 #include "isp_kernels.h"
+#include "isp_rows.cuh"
+#include "isp_segments.cuh"
 #include "isp_tile.cuh"
 
 namespace imop {
@@ -59,11 +61,7 @@ struct StreamSmem {
     StreamWarpSmem w[kStWarps];
 };
 
-// Work: each strip of a frame is cut into segments (about one per resident warp), each segment
-// into bands.  A warp streams its own segment's bands from the front, one after the other without
-// re-warming its rings; a warp whose segment is done takes single bands from the back of other
-// segments.  Per segment one 64-bit word counts the bands claimed from the front (low half) and
-// from the back (high half): a claim is valid while their sum is below the segment's band count.
+// Work claiming (isp_segments.cuh): a segment of a strip, its output columns and rows
 struct SSeg {
     int f;
     int xw;        // first window column (output columns start 8 later)
@@ -81,27 +79,11 @@ __device__ __forceinline__ void seg_of(const BatchLaunch& bl, int seg, SSeg& G) 
     G.ox0 = R.x0 + kStOut * tx;
     G.ox1 = min(G.ox0 + kStOut, R.x0 + R.w);
     G.xw = G.ox0 - kStLanePx;
-    // R.h rows in R.tiles_y segments, the first R.h % R.tiles_y of them one row taller
-    const int n = R.tiles_y, q = R.h / n, rem = R.h - q * n;
-    G.s0 = R.y0 + ty * q + min(ty, rem);
-    G.len = q + (ty < rem ? 1 : 0);
+    segs::split_rows(R.y0, R.h, R.tiles_y, ty, G.s0, G.len);
     G.nb = max(1, (G.len + bl.band_h - 1) / bl.band_h);
 }
 __device__ __forceinline__ void band_rows(const SSeg& G, int i, int& y0, int& bh) {
-    const int q = G.len / G.nb, rem = G.len - q * G.nb;
-    y0 = G.s0 + i * q + min(i, rem);
-    bh = q + (i < rem ? 1 : 0);
-}
-// lane 0: the next band from the front (the segment's own warp) / back (another warp), or -1
-__device__ __forceinline__ int claim_front(unsigned long long* w, int nb) {
-    const unsigned long long old = atomicAdd(w, 1ull);
-    const unsigned f = (unsigned)old, b = (unsigned)(old >> 32);
-    return f + b < (unsigned)nb ? (int)f : -1;
-}
-__device__ __forceinline__ int claim_back(unsigned long long* w, int nb) {
-    const unsigned long long old = atomicAdd(w, 1ull << 32);
-    const unsigned f = (unsigned)old, b = (unsigned)(old >> 32);
-    return f + b < (unsigned)nb ? nb - 1 - (int)b : -1;
+    segs::band_of(G.s0, G.len, G.nb, i, y0, bh);
 }
 
 // ---- packed helpers ------------------------------------------------------------------------
@@ -140,73 +122,6 @@ __device__ __forceinline__ uint32_t floor_pack_s(float2 t, uint32_t mv2) {
 // round_plane of both components: clamp((int)(v + 0.5f), 0, mv)
 __device__ __forceinline__ uint32_t round_pack(float2 v, uint32_t mv2) {
     return floor_pack_s(dev::fadd2(v, make_float2(0.5f, 0.5f)), mv2);
-}
-
-// ---- input rows ------------------------------------------------------------------------------
-template <int FMT>
-__host__ __device__ constexpr int row_bytes_num() { return FMT == FMT_U8 ? 1 : FMT == FMT_U16 ? 2 : FMT == FMT_P12 ? 3 : 5; }
-template <int FMT>
-__host__ __device__ constexpr int row_bytes_den() { return FMT == FMT_P12 ? 2 : FMT == FMT_P10 ? 4 : 1; }
-
-// the words holding the lane's 8 samples of a row (the frame is 16-byte aligned and its width a
-// multiple of 8, so they start on a word: on the sample for u8 / u16 / RAW12, on the sample or two
-// bytes before it for RAW10)
-template <int FMT>
-__device__ __forceinline__ void load_words(const uint8_t* row, int lane_byte, bool in, uint32_t (&w)[4]) {
-    w[0] = w[1] = w[2] = w[3] = 0u;
-    if (!in) return;
-    const uint8_t* p = row + lane_byte;
-    if (FMT == FMT_U8) {
-        const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-        w[0] = v.x;
-        w[1] = v.y;
-    } else if (FMT == FMT_U16) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-        w[0] = v.x;
-        w[1] = v.y;
-        w[2] = v.z;
-        w[3] = v.w;
-    } else {
-        const uint32_t* q = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
-        w[0] = __ldg(q);
-        w[1] = __ldg(q + 1);
-        w[2] = __ldg(q + 2);
-        w[3] = (uint32_t)(reinterpret_cast<uintptr_t>(p) & 3);  // RAW10: byte offset in the first word
-    }
-}
-
-template <int FMT>
-__device__ __forceinline__ void decode(const uint32_t (&w)[4], uint32_t (&P)[4]) {
-    if (FMT == FMT_U8) {
-        P[0] = __byte_perm(w[0], 0u, 0x4140);
-        P[1] = __byte_perm(w[0], 0u, 0x4342);
-        P[2] = __byte_perm(w[1], 0u, 0x4140);
-        P[3] = __byte_perm(w[1], 0u, 0x4342);
-    } else if (FMT == FMT_U16) {
-        P[0] = w[0];
-        P[1] = w[1];
-        P[2] = w[2];
-        P[3] = w[3];
-    } else if (FMT == FMT_P12) {
-        P[0] = unpack12_pair(w[0]);
-        P[1] = unpack12_pair(__funnelshift_r(w[0], w[1], 24));
-        P[2] = unpack12_pair(__funnelshift_r(w[1], w[2], 16));
-        P[3] = unpack12_pair(w[2] >> 8);
-    } else {
-        // RAW10: two 5-byte groups, each four high bytes then the four 2-bit remainders
-        const int sh = 8 * (int)w[3];
-        const uint32_t a = __funnelshift_r(w[0], w[1], sh), b = __funnelshift_r(w[1], w[2], sh), c = w[2] >> sh;
-        const uint32_t hi[2] = {a, __funnelshift_r(b, c, 8)};
-        const uint32_t lo[2] = {b & 0xFFu, (c >> 8) & 0xFFu};
-#pragma unroll
-        for (int g = 0; g < 2; g++)
-#pragma unroll
-            for (int s = 0; s < 2; s++) {
-                const uint32_t h2 = __byte_perm(hi[g], 0u, s ? 0x4342 : 0x4140);  // two high bytes as halves
-                const uint32_t l2 = ((lo[g] >> (4 * s)) & 3u) | (((lo[g] >> (4 * s + 2)) & 3u) << 16);
-                P[2 * g + s] = (h2 << 2) | l2;
-            }
-    }
 }
 
 // ---- defect correction: the median of the flagged samples, and defect-chain seeds --------------
@@ -482,8 +397,8 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
 #pragma unroll
     for (int i = 0; i < kStLanePx; i++)
         need |= (xl + i >= U.ox0 - 5 && xl + i < U.ox1 + 5) ? 1u << i : 0u;
-    const int lane_byte = xl * row_bytes_num<FMT>() / row_bytes_den<FMT>();
-    const size_t pitch = (size_t)W * row_bytes_num<FMT>() / row_bytes_den<FMT>();
+    const int lane_byte = xl * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+    const size_t pitch = (size_t)W * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
     uint8_t* const out = fp.out;
     const uintptr_t out_base = reinterpret_cast<uintptr_t>(out);
     const int n0 = y0 - 5;
@@ -492,7 +407,7 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
     const uint8_t* rowp = fp.in + (size_t)n0 * pitch;  // input row n (then n + 1 once loaded)
     uint8_t* outp = out + ((size_t)y0 * W + xl) * 3;  // the lane's bytes of output row q
     uint32_t rw[4];
-    load_words<FMT>(rowp, lane_byte, lane_in, rw);
+    rows::load8<FMT>(rowp, lane_byte, lane_in, rw);
     int m5 = 0, m3 = 0;           // k mod 5, k mod 3
     unsigned modrows = 0;         // bit i: jac row b - i differs from orig row b - i in the warp
     int lsc_gy = -1;              // cell row of the lens-shading table
@@ -505,11 +420,11 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
         const int n = n0 + k;
         // ---- A: samples of row n -------------------------------------------------------------
         uint32_t P[4];
-        decode<FMT>(rw, P);
+        rows::decode8<FMT>(rw, P);
         if (own && k + 1 == nrows) {
             // the segment's next band continues this stream
             int j = 0;
-            if (lane == 0) j = claim_front(own, U.nb);
+            if (lane == 0) j = segs::claim_front(own, bl.seg_words + bl.n_items);
             j = __shfl_sync(full, j, 0);
             if (j >= 0) {
                 int yb, hb;
@@ -521,7 +436,7 @@ __device__ __forceinline__ void stream_unit(const BatchLaunch& bl, const StreamS
             }
         }
         rowp += pitch;
-        if (k + 1 < nrows) load_words<FMT>(rowp, lane_byte, lane_in, rw);
+        if (k + 1 < nrows) rows::load8<FMT>(rowp, lane_byte, lane_in, rw);
         if (bl_on) {
             const int par = n & 1;
             const int bl_e = par ? bl_e1 : bl_e0, bl_o = par ? bl_o1 : bl_o0;
@@ -709,50 +624,30 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
         for (int i = lane; i < (int)(sizeof(StreamWarpSmem) / 16); i += 32) r[i] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncthreads();
-    const unsigned full = 0xffffffffu;
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kStWarps + warp;
-    // the warp's own segment, band after band from the front
-    if (gw < nseg) {
-        SSeg G;
-        seg_of(bl, gw, G);
-        int i = 0;
-        if (lane == 0) i = claim_front(bl.seg_words + gw, G.nb);
-        i = __shfl_sync(full, i, 0);
-        if (i >= 0) {
-            int y0, bh;
-            band_rows(G, i, y0, bh);
-            stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], G, y0, bh, bl.seg_words + gw, lane);
-        }
-    }
-    // then single bands from the back of segments that still have unclaimed ones: 32 segments
-    // tested at a time, from the warp's own onwards, until a pass over all of them finds none
-    int base = gw % nseg, scanned = 0;
-    while (scanned < nseg) {
-        const int cand = (base + lane) % nseg;
-        SSeg G;
-        seg_of(bl, cand, G);
-        const unsigned long long wv = *reinterpret_cast<volatile unsigned long long*>(bl.seg_words + cand);
-        const bool open = lane < nseg && (unsigned)wv + (unsigned)(wv >> 32) < (unsigned)G.nb;
-        const unsigned m = __ballot_sync(full, open);
-        if (!m) {
-            base = (base + 32) % nseg;
-            scanned += 32;
-            continue;
-        }
-        const int src = __ffs(m) - 1;
-        const int seg = __shfl_sync(full, cand, src);
-        int j = 0;
-        if (lane == src) j = claim_back(bl.seg_words + seg, G.nb);
-        j = __shfl_sync(full, j, src);
-        base = seg;  // the segment may hold more
-        scanned = 0;
-        if (j < 0) continue;
+    // the warp's own segment, band after band from the front, then bands from the back of others
+    segs::Walk walk(gw, nseg);
+    int seg, band;
+    bool own;
+    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
         SSeg S;
         seg_of(bl, seg, S);
         int y0, bh;
-        band_rows(S, j, y0, bh);
-        stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], S, y0, bh, nullptr, lane);
+        band_rows(S, band, y0, bh);
+        stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], S, y0, bh, own ? bl.seg_words + seg : nullptr, lane);
+    }
+}
+
+// the launch's claim words: each segment's band count with zero claims, then the taken count
+__global__ void stream_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < bl.n_items) {
+        SSeg G;
+        seg_of(bl, i, G);
+        bl.seg_words[i] = segs::initial_word(G.nb);
+    } else if (i == bl.n_items) {
+        bl.seg_words[i] = 0ull;
     }
 }
 
@@ -817,10 +712,7 @@ void stream_rects(const FrameParams& fp, TileRect& interior, TileRect (&border)[
     border[3] = {0, xe, 7, W - xe, H - 14, 0, 0};
 }
 
-// Segments of the rectangles of a launch: each strip in segments of seg_percent % of the rows that
-// spread the launch's strip rows evenly over the resident warps, bands of band_rows rows inside
-// them (the granule of the end-of-launch balancing, each taken band paying 10 rows of warm-up)
-static void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows) {
+void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows) {
     long long strip_rows = 0;
     for (int r = 0; r < bl.n_rects; r++) strip_rows += (long long)bl.rects[r].tiles_x * bl.rects[r].h;
     double per = std::max(1.0, (double)strip_rows / std::max(1, warps) * seg_percent / 100.0);
@@ -833,10 +725,14 @@ static void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int ban
             items += R.tiles_x * R.tiles_y;
         }
         bl.rect_start[bl.n_rects] = bl.n_items = items;
-        if (items < kStreamSegCap) break;
-        per *= (double)items / (kStreamSegCap - 1);
+        if (items <= kSegMax) break;
+        per *= (double)items / kSegMax;
     }
-    bl.band_h = band_rows;
+    // at most segs::kMaxBands bands per segment (the claim word's band count field)
+    int longest = 0;
+    for (int r = 0; r < bl.n_rects; r++)
+        longest = std::max(longest, (bl.rects[r].h + bl.rects[r].tiles_y - 1) / bl.rects[r].tiles_y);
+    bl.band_h = std::max(band_rows, (longest + segs::kMaxBands - 1) / segs::kMaxBands);
 }
 
 cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
@@ -868,9 +764,9 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
     const TuneParams tp = tuning_for(IMOP_KERNEL_STREAM, bl.fmt, wmax);
     choose_segments(bl, limit * kStWarps, tp.seg_percent, tp.band_rows);
     if (bl.n_items <= 0) return cudaSuccess;
-    if (bl.n_items >= kStreamSegCap || !bl.seg_words) return cudaErrorInvalidValue;  // the last word: the column launch
-    if ((e = cudaMemsetAsync(bl.seg_words, 0, sizeof(unsigned long long) * (size_t)bl.n_items, st)) != cudaSuccess)
-        return e;
+    if (bl.n_items > kSegMax || !bl.seg_words) return cudaErrorInvalidValue;
+    stream_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int want = (bl.n_items + kStWarps - 1) / kStWarps;
     const int grid = want < limit ? want : limit;
     count_launch(2);

@@ -109,7 +109,7 @@ class ToneParams(C.Structure):
                 ("black_point", C.c_float), ("white_point", C.c_float), ("mid_point", C.c_float)]
 
 
-KERNEL_TILE, KERNEL_LITE, KERNEL_STREAM = 0, 1, 2
+KERNEL_TILE, KERNEL_LITE, KERNEL_STREAM, KERNEL_LITE_DIRECT = 0, 1, 2, 3
 
 
 class TuneEntry(C.Structure):

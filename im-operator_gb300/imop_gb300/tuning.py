@@ -88,7 +88,8 @@ def _classes():
 
 def _candidates(kernel):
     if kernel == abi.KERNEL_LITE:
-        return [(1, b, 100) for b in (8, 16, 24, 32, 48)] + [(0, 16, 100)]
+        # the staged variant takes only the band; the direct-read one also the segment spread
+        return [(1, b, s) for b in (8, 16, 32) for s in (50, 100, 200)] + [(0, 16, 100)]
     return [(1, b, s) for b in (16, 32, 64) for s in (50, 100, 200)] + [(0, 32, 100)]
 
 

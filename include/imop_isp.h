@@ -218,7 +218,7 @@ enum {
     IMOP_BATCH_PLAIN = 2  /* one plain per-operator pipeline per frame (the comparator) */
 };
 
-/* All frames through the persistent fused kernel: one launch per run of up to 16 frames with
+/* All frames through the persistent fused kernels: one launch per run of up to 32 frames with
  * the same output channel width, tiles of every frame pulled by the same CTAs, and one defect
  * fix-up launch.  Parameter tables are uploaded once per distinct content and cached in the
  * context.  Asynchronous on `stream`; device frames must stay valid until it completes. */
@@ -493,9 +493,11 @@ const char* imop_device_name(void);
 long long imop_shim_calls_served(void);
 /* Fused-kernel launches this process enqueued, by kernel: the tile kernel (every chain, and the
  * border rows / columns of streamed frames), the light-chain kernel (HQLI without defect
- * correction or lens shading) and the streaming kernel (the interior of AMAZE frames).  A launch
- * recorded into a CUDA graph counts once, when it is recorded. */
-enum { IMOP_KERNEL_TILE = 0, IMOP_KERNEL_LITE = 1, IMOP_KERNEL_STREAM = 2 };
+ * correction or lens shading; both of its variants), the streaming kernel (the interior of AMAZE
+ * frames) and, counted again on its own, the light-chain kernel's direct-read variant (aligned
+ * frames whose width is a multiple of 8).  A launch recorded into a CUDA graph counts once, when
+ * it is recorded. */
+enum { IMOP_KERNEL_TILE = 0, IMOP_KERNEL_LITE = 1, IMOP_KERNEL_STREAM = 2, IMOP_KERNEL_LITE_DIRECT = 3 };
 long long imop_kernel_launches(int kernel);
 
 /* ---- launch tuning ------------------------------------------------------------------ */

@@ -4,7 +4,12 @@ white-balance orders, integral and fractional black levels (the latter through t
 kernel), every tone mode, all Bayer patterns, frames from 6x6 up to the 5320x4600 frames of the
 large-frame workload, widths that are not
 multiples of the tile, unaligned input and output pointers, samples above the bit depth's maximum
-(the reference's MSB-aligned read), and batches that mix it with the general kernel."""
+(the reference's MSB-aligned read), and batches that mix it with the general kernel.  The
+direct-read variant (aligned frames whose width is a multiple of 8) separately: its launches
+counted, segments continued and bands taken from the back under extreme tuning entries, and
+batches of frames of several widths in one launch."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -21,7 +26,7 @@ SIZES = [(6, 6), (7, 6), (6, 9), (9, 7), (8, 9), (33, 17), (131, 70), (255, 129)
          (260, 23), (520, 300), (771, 37), (1006, 758)]
 
 
-def _pipeline(rng, w, h):
+def _pipeline(rng, w, h, allow_frac=True):
     fmt = int(rng.integers(0, 4))
     if fmt == 0:
         bd, packed = int(rng.integers(1, 9)), False
@@ -37,7 +42,7 @@ def _pipeline(rng, w, h):
         stages |= abi.STAGE_BLACK_LEVEL
     if rng.random() < 0.8:
         stages |= abi.STAGE_WHITE_BALANCE
-    frac = rng.random() < 0.3
+    frac = allow_frac and rng.random() < 0.3
     off = [float(v) if frac else float(round(v)) for v in rng.uniform(0, mv * 0.08, 4)]
     pl = I.Pipeline(width=w, height=h, bit_depth=bd, packed=packed, pattern=int(rng.integers(0, 4)),
                     demosaic=abi.HQLI, stages=stages, stage_order=int(rng.integers(0, 2)),
@@ -172,3 +177,93 @@ def test_lite_host_batch(isp):
     isp.run_host_batch([(pl, raw, o) for (pl, raw, _), o in zip(frames, outs)])
     for (_, _, ref), o in zip(frames, outs):
         assert max_abs(o, ref) == 0
+
+
+# widths that are multiples of 8: one strip and several, a last strip narrower than 256, up to the
+# large-frame width
+DIRECT_SIZES = [(8, 6), (16, 9), (64, 33), (248, 40), (256, 17), (264, 31), (512, 64), (520, 300), (1000, 77),
+                (2048, 129), (5320, 57), (776, 6)]
+
+
+def _direct_launches():
+    return I.lib().imop_kernel_launches(abi.KERNEL_LITE_DIRECT)
+
+
+def _bounded(pl):
+    """the light-chain kernel's condition on the samples reaching HQLI: a clamping stage (black
+    level, Bayer-order white balance), a format without spare bits, or full 8-bit bytes"""
+    return bool(pl.stages & abi.STAGE_BLACK_LEVEL or (pl.stages & abi.STAGE_WHITE_BALANCE and pl.stage_order == 0)
+                or pl.packed or pl.bit_depth >= 8)
+
+
+@pytest.mark.parametrize("trial", range(24))
+def test_direct_matches_oracle(isp, trial):
+    rng = np.random.default_rng(9500 + trial)
+    w, h = DIRECT_SIZES[trial % len(DIRECT_SIZES)]
+    pl = _pipeline(rng, w, h, allow_frac=False)
+    raw = _frame(rng, pl, over=(trial % 3 == 2 and pl.stages == 0))
+    ref, _ = O.pipeline(pl, raw)
+    out_off = int(rng.integers(0, 16)) if trial % 2 == 1 else 0
+    n0 = _direct_launches()
+    got = _run(isp, pl, raw, 0, out_off)
+    assert (_direct_launches() > n0) == _bounded(pl), (w, h)
+    assert max_abs(got, ref) == 0, (w, h, pl.bit_depth, pl.packed, pl.stages, pl.stage_order, out_off)
+
+
+def test_direct_unaligned_input_takes_staged_kernel(isp):
+    rng = np.random.default_rng(9600)
+    pl = _pipeline(rng, 520, 40, allow_frac=False)
+    raw = _frame(rng, pl)
+    ref, _ = O.pipeline(pl, raw)
+    n0 = _direct_launches()
+    got = _run(isp, pl, raw, 3, 0)
+    assert _direct_launches() == n0
+    assert max_abs(got, ref) == 0
+
+
+@pytest.mark.parametrize("band,seg", [(4, 10), (4, 1000), (1024, 100), (8, 50)])
+def test_direct_segments_and_stolen_bands(isp, band, seg):
+    """segments much shorter than a warp's share (most bands taken from the back by warps that
+    own none), much longer (warps without a segment steal), one band per segment, and the default
+    spread: every frame against the oracle"""
+    from imop_gb300 import tuning
+    old = tuning.get_table()
+    try:
+        tuning.set_table([{"kernel": abi.KERNEL_LITE, "fmt": -1, "max_width": 1 << 30, "enabled": 1,
+                           "band_rows": band, "seg_percent": seg}])
+        rng = np.random.default_rng(9700 + band + seg)
+        for w, h in ((2048, 300), (264, 1001), (5320, 97)):
+            pl = _pipeline(rng, w, h, allow_frac=False)
+            pl.stages |= abi.STAGE_BLACK_LEVEL
+            raw = _frame(rng, pl)
+            ref, _ = O.pipeline(pl, raw)
+            n0 = _direct_launches()
+            got = _run(isp, pl, raw)
+            assert _direct_launches() > n0
+            assert max_abs(got, ref) == 0, (w, h, band, seg)
+    finally:
+        tuning.set_table(old)
+
+
+def test_direct_batch_of_widths(isp):
+    """frames of six widths in one recorded direct-read launch (one rectangle each), replayed"""
+    rng = np.random.default_rng(9800)
+    base = _pipeline(rng, 64, 64, allow_frac=False)
+    base.stages |= abi.STAGE_BLACK_LEVEL
+    frames = []
+    for k, (w, h) in enumerate(((64, 40), (256, 77), (520, 33), (1000, 64), (2048, 19), (264, 150))):
+        pl = dataclasses.replace(base, width=w, height=h)
+        raw = _frame(rng, pl)
+        ref, _ = O.pipeline(pl, raw)
+        frames.append((pl, raw, ref))
+    dev = [(pl, torch.from_numpy(raw).cuda(), torch.zeros(pl.output_bytes(), dtype=torch.uint8, device="cuda"))
+           for pl, raw, _ in frames]
+    n0 = _direct_launches()
+    for flags in (0, abi.BATCH_GRAPH, abi.BATCH_GRAPH):
+        for _, _, d_out in dev:
+            d_out.zero_()
+        isp.batch_submit(dev, flags=flags)
+        isp.sync_status()
+        for k, ((pl, _, ref), (_, _, d_out)) in enumerate(zip(frames, dev)):
+            assert max_abs(d_out.cpu().numpy().reshape(ref.shape), ref) == 0, (k, pl.width, pl.height, flags)
+    assert _direct_launches() > n0
