@@ -288,8 +288,11 @@ int prepare_batch(imop_isp_ctx* c, const ImopFrameDesc* frames, int n, std::vect
 // the batch's device work, in stream order
 cudaError_t enqueue_batch(imop_isp_ctx* c, std::vector<PreparedFrame>& pf, cudaStream_t st) {
     const int n = (int)pf.size();
-    cudaError_t e = cudaMemsetAsync(c->batch.seed_count.ptr, 0, n * sizeof(int), st);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
+    // the defect-chain seed counters, when a frame runs adaptive defect correction
+    bool seeds = false;
+    for (auto& f : pf) seeds = seeds || ((f.fp.stages & 2u) && f.fp.dpc_mode == 0);
+    if (seeds && (e = cudaMemsetAsync(c->batch.seed_count.ptr, 0, n * sizeof(int), st)) != cudaSuccess) return e;
     for (auto& f : pf)
         if (f.map_tabs && (e = launch_map_resolve(f.fp, f.map_tabs->plan, st))) return e;
     std::vector<FrameParams> fps(n);

@@ -501,6 +501,16 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
     const int pitch = W * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
     const int n0 = y0 - 1;
     int nrows = bh + 2;
+    // output: the rows of a frame whose width is a multiple of 8 all start at the same 8-byte
+    // phase, so whether the lanes store their 24 bytes straight (an interior strip at phase 0) is
+    // decided once; the lane's bytes of output row n - 1 lie at out + ooff
+    const bool lane_st = xl + kLiteLanePx <= U.x0 + U.npx;
+    const bool fast = U.x0 != 0 && U.x0 + U.npx != W && ((reinterpret_cast<uintptr_t>(out) + 3u * U.x0) & 7) == 0;
+    long long ooff = ((long long)(n0 - 1) * W + xl) * 3;
+    // the HQLI variant (red / blue site column, red row) of even and odd output rows
+    const bool rr_e = po.r_row == 0;
+    const int v_e = 2 * (rr_e ? po.r_col : po.b_col) + (rr_e ? 1 : 0);
+    const int v_o = 2 * (rr_e ? po.b_col : po.r_col) + (rr_e ? 0 : 1);
     auto fetch = [&](int n, uint32_t (&w)[4], rows::Edge<FMT>& e) {
         const bool row_in = (unsigned)n < (unsigned)H;
         const uint8_t* rp = in + (row_in ? (long long)n * pitch : 0ll);
@@ -551,7 +561,27 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
         for (int j = 0; j < 4; j++) Dr.P[j] = P[j];
         Dr.Lw = Lw;
         Dr.R = Rn;
-        if (k >= 2) lite_emit(tab, wout, W, H, out, po, U.x0, U.npx, lane, n, Ur, Mr, Dr);
+        const int yo = n - 1;  // rows 0, 1 / h-2, h-1 are emitted with row 2 / h-3
+        if (k >= 2 && yo >= 2 && yo <= H - 3) {
+            uint32_t ob[6];
+            const int v = (yo & 1) ? v_o : v_e;
+            if (v == 0) lite::hqli_row<0, false>(Ur, Mr, Dr, tab, ob);
+            else if (v == 1) lite::hqli_row<0, true>(Ur, Mr, Dr, tab, ob);
+            else if (v == 2) lite::hqli_row<1, false>(Ur, Mr, Dr, tab, ob);
+            else lite::hqli_row<1, true>(Ur, Mr, Dr, tab, ob);
+            if (fast && yo != 2 && yo != H - 3) {
+                if (lane_st) {
+                    uint2* q = reinterpret_cast<uint2*>(out + ooff);
+                    q[0] = make_uint2(ob[0], ob[1]);
+                    q[1] = make_uint2(ob[2], ob[3]);
+                    q[2] = make_uint2(ob[4], ob[5]);
+                }
+            } else {
+                lite_emit_staged(tab, wout, out, W, H, U.x0, U.npx, lane, yo, make_uint4(ob[0], ob[1], ob[2], ob[3]),
+                                 make_uint2(ob[4], ob[5]));
+            }
+        }
+        ooff += 3 * W;
         k++;
         return true;
     };
@@ -582,11 +612,12 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
         }
     }
     __syncthreads();
+    segs::wait_init();
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kDirWarps + warp;
     uint8_t* wout = sm.out[warp];
     // the warp's own segment, band after band from the front, then bands from the back of others
-    segs::Walk walk(gw, nseg);
+    segs::Walk walk(gw, nseg, (int)gridDim.x * kDirWarps);
     int seg, band;
     bool own;
     while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
@@ -600,6 +631,7 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
 
 // the launch's claim words: each segment's band count with zero claims, then the taken count
 __global__ void lite_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
+    segs::release_dependents();
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < bl.n_items) {
         LSeg G;
@@ -614,8 +646,7 @@ int g_direct_grid[kMaxDev];
 
 template <int FMT>
 cudaError_t launch_direct_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
-    lite_direct_kernel<FMT><<<grid, kDirThreads, smem, st>>>(bl);
-    return cudaGetLastError();
+    return launch_dependent(lite_direct_kernel<FMT>, grid, kDirThreads, smem, st, bl);
 }
 
 int g_lite_grid[kMaxDev];

@@ -3,27 +3,38 @@
 // segment's bands from the front, one after the other without re-reading warm-up rows; a warp
 // whose segment is done takes single bands from the back of other segments.
 //
-// Per segment one 64-bit word: the claims made from the front (bits 0-23) and from the back
-// (bits 24-47) and the segment's band count (bits 48-63, written with zero counts by the launch's
-// init kernel before the streamed kernel runs).  A claim is valid while the two counts before it
-// sum to less than the band count, so a warp looking for work reads everything it needs from the
-// word.  The claim that takes a segment's last band counts the segment in the word after the
-// launch's last segment word; a warp looking for work stops once that count reaches the number of
-// segments.
+// Per segment one 64-bit word: the claims made from the front (bits 0-22) and from the back
+// (bits 23-45), whether a warp adopted the segment (bit 46) and the segment's band count (bits
+// 48-63, written with zero counts by the launch's init kernel before the streamed kernel runs).
+// A claim is valid while the two counts before it sum to less than the band count, so a warp
+// looking for work reads everything it needs from the word.  Segments beyond the launch's warps
+// start without an owner: the first warp that finds one sets its adopted bit and streams it from
+// the front like an owner.  The claim that takes a segment's last band counts the segment in the
+// word after the launch's last segment word; a warp looking for work stops once that count
+// reaches the number of segments.
 #pragma once
+
+#include <cuda_runtime.h>
 
 namespace imop {
 namespace segs {
 
 constexpr unsigned long long kFrontOne = 1ull;
-constexpr unsigned long long kBackOne = 1ull << 24;
+constexpr unsigned long long kBackOne = 1ull << 23;
+constexpr unsigned long long kAdopted = 1ull << 46;
 constexpr int kMaxBands = 65535;
 
 __host__ __device__ inline unsigned long long initial_word(int nb) { return (unsigned long long)nb << 48; }
-__device__ __forceinline__ unsigned front_of(unsigned long long w) { return (unsigned)w & 0xFFFFFFu; }
-__device__ __forceinline__ unsigned back_of(unsigned long long w) { return (unsigned)(w >> 24) & 0xFFFFFFu; }
+__device__ __forceinline__ unsigned front_of(unsigned long long w) { return (unsigned)w & 0x7FFFFFu; }
+__device__ __forceinline__ unsigned back_of(unsigned long long w) { return (unsigned)(w >> 23) & 0x7FFFFFu; }
 __device__ __forceinline__ unsigned bands_of(unsigned long long w) { return (unsigned)(w >> 48); }
 __device__ __forceinline__ bool open(unsigned long long w) { return front_of(w) + back_of(w) < bands_of(w); }
+
+// The streamed kernels are launched as programmatic dependents of their init kernel: they may
+// start while it runs (their table prologue overlaps it) and wait for its writes before the
+// first claim.  Both are no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void release_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void wait_init() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // rows [s0, s0 + len) of a segment in nb bands: band i
 __device__ __forceinline__ void band_of(int s0, int len, int nb, int i, int& y0, int& bh) {
@@ -59,27 +70,30 @@ __device__ __forceinline__ int claim_back(unsigned long long* w, unsigned long l
     return (int)(nb - 1 - b);
 }
 
-// The work of one warp over the nseg segments of `words` (the taken count at words[nseg]): first
-// its own segment gw from the front (the caller continues it band after band), then single bands
-// from the back of others: 128 segments tested per pass, from the last one that held work on, a
-// band taken from the first one still open.  next() gives the segment and band to do and whether
-// it is the warp's own; it returns false when every segment is taken, or when a whole pass finds
-// none open.
+// The work of one warp gw of nwarps over the nseg segments of `words` (the taken count at
+// words[nseg]): first its own segments from the front (the caller continues each band after
+// band): segment gw, then gw + nwarps, gw + 2 nwarps, ... (those beyond the launch's warps are
+// adopted first, so that a warp looking for work may take one over); then, 128 segments tested
+// per pass from the last one that held work on, one still open: adopted and streamed from the
+// front if no warp has begun it, else a single band from its back.  next() gives the segment and
+// band to do and whether the warp streams on from it; it returns false when every segment is
+// taken, or when a whole pass finds none open.
 struct Walk {
-    int base, scanned;
-    bool own_pending;
-    __device__ __forceinline__ Walk(int gw, int nseg) : base(gw % nseg), scanned(0), own_pending(gw < nseg) {}
+    int base, scanned, nwarps, next_own;
+    __device__ __forceinline__ Walk(int gw, int nseg, int nw) : base(gw % nseg), scanned(0), nwarps(nw), next_own(gw) {}
 
     __device__ __forceinline__ bool next(unsigned long long* words, int nseg, int gw, int lane, int& seg, int& band,
                                          bool& own) {
         const unsigned full = 0xffffffffu;
-        if (own_pending) {
-            own_pending = false;
-            int i = 0;
-            if (lane == 0) i = claim_front(words + gw, words + nseg);
+        while (next_own < nseg) {
+            const int s = next_own;
+            next_own += nwarps;
+            int i = -1;
+            if (lane == 0 && (s < nwarps || !(atomicOr(words + s, kAdopted) & kAdopted)))
+                i = claim_front(words + s, words + nseg);
             i = __shfl_sync(full, i, 0);
             if (i >= 0) {
-                seg = gw;
+                seg = s;
                 band = i;
                 own = true;
                 return true;
@@ -88,22 +102,34 @@ struct Walk {
         own = false;
         const volatile unsigned long long* vw = words;
         while (scanned < nseg) {
-            unsigned long long wv[4];
-            int cand[4];
+            unsigned long long wv[4];  // segment base + lane + 32 i (wrapped), or nothing open
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 int c = base + lane + 32 * i;  // base < nseg
                 if (c >= nseg) c -= nseg;
                 if (c >= nseg) c %= nseg;  // fewer than 128 segments
-                cand[i] = c;
                 wv[i] = lane + 32 * i < nseg ? vw[c] : 0ull;
             }
             if (vw[nseg] >= (unsigned long long)nseg) return false;  // every segment taken
+            unsigned m[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) m[i] = __ballot_sync(full, open(wv[i]));
+            // an open segment of the window, chosen from a place that depends on the warp, so the
+            // warps looking for work spread over the open segments instead of all claiming the
+            // first one
+            const int rot = gw & 31, grot = (gw >> 5) & 3;
             int s = -1;
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const unsigned m = __ballot_sync(full, open(wv[i]));
-                if (s < 0 && m) s = __shfl_sync(full, cand[i], __ffs(m) - 1);
+            for (int t = 0; t < 4; t++) {
+                const int i = (t + grot) & 3;
+                const unsigned mm = i == 0 ? m[0] : i == 1 ? m[1] : i == 2 ? m[2] : m[3];
+                if (s < 0 && mm) {
+                    const int bit = (__ffs(__funnelshift_r(mm, mm, rot)) - 1 + rot) & 31;
+                    int c = base + bit + 32 * i;
+                    if (c >= nseg) c -= nseg;
+                    if (c >= nseg) c %= nseg;
+                    s = c;
+                }
             }
             if (s < 0) {
                 base += 128;
@@ -112,13 +138,23 @@ struct Walk {
                 continue;
             }
             int j = 0;
-            if (lane == 0) j = claim_back(words + s, words + nseg);
+            bool adopt = false;
+            if (lane == 0) {
+                if (s >= nwarps && !(atomicOr(words + s, kAdopted) & kAdopted)) {
+                    adopt = true;
+                    j = claim_front(words + s, words + nseg);
+                } else {
+                    j = claim_back(words + s, words + nseg);
+                }
+            }
             j = __shfl_sync(full, j, 0);
+            adopt = __shfl_sync(full, adopt, 0);
             base = s;  // the segment may hold more
             scanned = 0;
             if (j >= 0) {
                 seg = s;
                 band = j;
+                own = adopt;
                 return true;
             }
         }
@@ -126,5 +162,28 @@ struct Walk {
     }
 };
 
+// host: launch kernel k as a programmatic dependent of the kernel before it in stream st
+inline cudaError_t launch_dependent_impl(const void* k, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                         void** args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, k, args);
+}
+
 }  // namespace segs
+
+template <class Arg>
+inline cudaError_t launch_dependent(void (*k)(Arg), int grid, int block, size_t smem, cudaStream_t st, const Arg& a) {
+    void* args[1] = {const_cast<Arg*>(&a)};
+    return segs::launch_dependent_impl(reinterpret_cast<const void*>(k), dim3(grid), dim3(block), smem, st, args);
+}
+
 }  // namespace imop

@@ -624,10 +624,11 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
         for (int i = lane; i < (int)(sizeof(StreamWarpSmem) / 16); i += 32) r[i] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncthreads();
+    segs::wait_init();
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kStWarps + warp;
     // the warp's own segment, band after band from the front, then bands from the back of others
-    segs::Walk walk(gw, nseg);
+    segs::Walk walk(gw, nseg, (int)gridDim.x * kStWarps);
     int seg, band;
     bool own;
     while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
@@ -641,6 +642,7 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
 
 // the launch's claim words: each segment's band count with zero claims, then the taken count
 __global__ void stream_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
+    segs::release_dependents();
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < bl.n_items) {
         SSeg G;
@@ -655,9 +657,8 @@ int g_stream_grid[kMaxDev];
 
 template <int FMT>
 cudaError_t launch_fmt(const BatchLaunch& bl, bool chain, int grid, size_t smem, cudaStream_t st) {
-    if (chain) stream_kernel<FMT, 1><<<grid, kStThreads, smem, st>>>(bl);
-    else stream_kernel<FMT, 0><<<grid, kStThreads, smem, st>>>(bl);
-    return cudaGetLastError();
+    return chain ? launch_dependent(stream_kernel<FMT, 1>, grid, kStThreads, smem, st, bl)
+                 : launch_dependent(stream_kernel<FMT, 0>, grid, kStThreads, smem, st, bl);
 }
 
 }  // namespace

@@ -5,6 +5,7 @@ kernel at all (otherwise the general tile kernel), the rows of a band (the light
 unit of work, the streaming kernel's claim granule) and the streaming kernel's segment size.
 
     python -m imop_gb300.tuning --out tuning_gb300.json    # measure on this GPU, write the table
+    python -m imop_gb300.tuning --kernels lite             # re-measure one kernel's classes
 
 measures every candidate of every class on the device (CUDA events over replayed batch graphs)
 and writes the best entry per class together with every timing, the built-in default's among
@@ -89,18 +90,29 @@ def _classes():
 def _candidates(kernel):
     if kernel == abi.KERNEL_LITE:
         # the staged variant takes only the band; the direct-read one also the segment spread
-        return [(1, b, s) for b in (8, 16, 32) for s in (50, 100, 200)] + [(0, 16, 100)]
+        return [(1, b, s) for b in (4, 8, 16, 32) for s in (50, 100, 200)] + [(0, 16, 100)]
     return [(1, b, s) for b in (16, 32, 64) for s in (50, 100, 200)] + [(0, 32, 100)]
 
 
-def tune(out_path, steps=5, warmup=2, verbose=True):
-    """Measure every candidate of every class on the current device; write and apply the table."""
+def tune(out_path, steps=5, warmup=2, verbose=True, kernels=None):
+    """Measure every candidate of every class on the current device; write and apply the table.
+    kernels: the kernels whose classes are measured (default both); the entries and measurements
+    of the others are kept from the table at out_path."""
     import torch
     from . import Isp
     dev = torch.cuda.get_device_name(0)
     isp = Isp()
     rows, entries = [], []
+    if kernels is not None and os.path.exists(out_path):
+        with open(out_path) as f:
+            old = json.load(f)
+        if old.get("device") == dev:
+            entries = [e for e in old["entries"] if e["kernel"] not in kernels]
+            names = {abi.KERNEL_LITE: "lite", abi.KERNEL_STREAM: "stream"}
+            rows = [r for r in old.get("measurements", []) if r["kernel"] not in {names[k] for k in kernels}]
     for kernel, fmt, wc, frames in _classes():
+        if kernels is not None and kernel not in kernels:
+            continue
         d = [(pl, torch.from_numpy(raw).cuda(), torch.empty(pl.output_bytes(), dtype=torch.uint8, device="cuda"))
              for pl, raw in frames]
         px = sum(pl.width * pl.height for pl, _ in frames)
@@ -149,8 +161,11 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--out", default=DEFAULT_TABLE)
     ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--kernels", choices=["lite", "stream"], nargs="*",
+                    help="measure these kernels' classes only (the others' entries are kept)")
     args = ap.parse_args()
-    tune(args.out, steps=args.steps)
+    ks = None if not args.kernels else [abi.KERNEL_LITE if k == "lite" else abi.KERNEL_STREAM for k in args.kernels]
+    tune(args.out, steps=args.steps, kernels=ks)
 
 
 if __name__ == "__main__":

@@ -89,8 +89,14 @@ def _run(isp, pl, raw, in_off=0, out_off=0):
 
 @pytest.fixture(scope="module")
 def isp():
+    """a context, with the built-in launch parameters while the module runs (the measured table
+    may send a class to the tile kernel; the tests that change the table restore these)"""
+    from imop_gb300 import tuning
     ctx = I.Isp()
+    saved = tuning.get_table()
+    tuning.set_table([])
     yield ctx
+    tuning.set_table(saved)
     ctx.close()
 
 
