@@ -44,6 +44,7 @@ struct BatchLaunch {
     int* tile_counter;              // claims beyond the first gridDim.x items; zero at launch
     unsigned long long* seg_words;  // streaming kernel: per segment, bands claimed (front | back << 32)
     int band_h;                     // streamed kernels: rows of a band
+    int owners = 0;                 // streamed kernels: segments below this start with band 0 claimed by their warp
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];
@@ -131,8 +132,9 @@ int lite_units_y(int h, int band_rows);
 cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st);
 // Segments of the strips of bl's rectangles (tiles_x strips each): each strip cut into segments
 // of seg_percent % of the rows that spread the launch's strip rows evenly over `warps` warps,
-// at most kSegMax in all; bands of band_rows rows inside them (isp_segments.cuh)
-void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows);
+// at most kSegMax in all; bands of band_rows rows inside them (isp_segments.cuh).  False when
+// the launch has more strips than kSegMax.
+bool choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows);
 
 // warp-streamed kernel for the AMAZE chains (isp_stream.cu): black level, adaptive defect
 // correction, grid lens shading, Bayer-order white balance, AMAZE, CCM, tone -> RGB8 on the interior

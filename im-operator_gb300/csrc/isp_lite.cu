@@ -447,17 +447,23 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
 }
 
 // ---- the direct-read variant ---------------------------------------------------------------
-// Frames 16-byte aligned with a width that is a multiple of 8 skip the staging ring: each lane
-// reads its 8 samples of a row with plain coalesced loads two rows ahead of their use (lanes 0 and
-// 31 also the groups left and right of the strip), and a warp streams a whole segment of its strip
-// band after band, so only bands taken from the back of another warp's segment (the end-of-launch
-// balancing) re-read the two rows above them.  One CTA per SM builds the output tables once.
-constexpr int kDirWarps = 16;
+// Frames 16-byte aligned with a width that is a multiple of 8 skip the shared staging of whole
+// rows: each lane copies the words of its own 8 samples of a row (lanes 0 and 31 also the sample
+// beside the strip) into its slot of a ring of kDirRing rows with per-thread asynchronous copies,
+// kDirRing - 1 rows ahead of their use, and reads them back itself: no lane waits for another,
+// no barrier, and the rows in flight hold no registers.  A warp streams a whole segment of its
+// strip band after band, so only bands taken from the back of another warp's segment (the
+// end-of-launch balancing) re-read the two rows above them.  One CTA per SM builds the output
+// tables once.
+constexpr int kDirWarps = 24;
 constexpr int kDirThreads = 32 * kDirWarps;
+constexpr int kDirRing = 4;
 
 struct LiteDirectSmem {
     alignas(16) uint8_t tab[3][4096];
     alignas(16) uint8_t out[kDirWarps][LiteWarpSmem::OUT_PITCH];
+    uint4 ring[kDirWarps][kDirRing][32];   // the lanes' words of each row in flight
+    uint2 ring_e[kDirWarps][kDirRing][32];  // the words of the sample beside the strip (lanes 0, 31)
 };
 static_assert(kDirWarps * LiteWarpSmem::OUT_PITCH >= 4096, "the staging rows hold the tone table at start");
 
@@ -479,26 +485,64 @@ __device__ __forceinline__ void lseg_of(const BatchLaunch& bl, int seg, LSeg& G)
     G.nb = max(1, (G.len + bl.band_h - 1) / bl.band_h);
 }
 
+// where a lane's samples of strip U's rows are: its 8 samples and (lanes 0 and 31) the sample
+// beside the strip
+template <int FMT>
+struct DirectRows {
+    int pitch, lane_byte, edge_byte;
+    bool lane_in, edge_in;
+    __device__ __forceinline__ DirectRows(const FrameParams& fp, const LSeg& U, int lane) {
+        const int W = fp.w;
+        const int xl = U.x0 + kLiteLanePx * lane;
+        lane_in = xl < W;  // the width is a multiple of 8
+        // lane 0: the sample left of the strip (column x0 - 1); lane 31: the one right of it
+        const int xe = lane == 0 ? U.x0 - 1 : U.x0 + kLiteStripMax;
+        edge_in = (lane == 0 || lane == 31) && xe >= 0 && xe < W;
+        lane_byte = xl * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+        edge_byte = !edge_in ? 0 : lane == 0 ? rows::edge_byte<FMT, true>(xe) : rows::edge_byte<FMT, false>(xe);
+        pitch = W * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+    }
+    // row n of frame fp into the lane's ring slots (zeros outside the frame)
+    __device__ __forceinline__ void issue(const FrameParams& fp, int n, uint32_t main, uint32_t edge) const {
+        const bool row_in = (unsigned)n < (unsigned)fp.h;
+        const uint8_t* rp = fp.in + (row_in ? (long long)n * pitch : 0ll);
+        rows::ring_load8<FMT>(main, rp, lane_byte, row_in && lane_in, fp.in);
+        rows::ring_load_edge<FMT>(edge, rp, edge_byte, row_in && edge_in, fp.in);
+    }
+    // row n back from the slots (after its copies completed): the lane's words and the edge words
+    __device__ __forceinline__ void read(const FrameParams& fp, int n, const uint4& main, const uint2& edge,
+                                         uint32_t (&w)[4], rows::Edge<FMT>& e) const {
+        const uint4 m = main;
+        w[0] = m.x;
+        w[1] = m.y;
+        w[2] = m.z;
+        w[3] = m.w;
+        e.g[0] = edge.x;
+        if (FMT == FMT_P10) {
+            // the byte offsets of the samples in the first copied words
+            const bool row_in = (unsigned)n < (unsigned)fp.h;
+            const uint8_t* rp = fp.in + (row_in ? (long long)n * pitch : 0ll);
+            w[3] = rows::ring_offset(rp, lane_byte);
+            e.g[1] = edge.y;
+            e.g[2] = rows::ring_offset(rp, edge_byte);
+        }
+    }
+};
+
 // output rows [y0, y0 + bh) of segment U and, while `own` is set, the segment's next bands from
 // the front: input rows y0 - 1 .. (the row below the last output row)
 template <int FMT>
 __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t (*tab)[4096], uint8_t* wout,
-                                            const LSeg& U, int y0, int bh, unsigned long long* own, int lane) {
+                                            uint4 (*ring)[32], uint2 (*ring_e)[32], const LSeg& U, int y0, int bh,
+                                            unsigned long long* own, int lane) {
     const unsigned full = 0xffffffffu;
     const FrameParams& fp = bl.frames[U.f];
     const int W = fp.w, H = fp.h;
-    const uint8_t* const in = fp.in;
     uint8_t* const out = fp.out;
     const PatternOffsets po = pattern_offsets(fp.pattern);
     const LiteLevels L = lite_levels_of(fp, lane);
     const int xl = U.x0 + kLiteLanePx * lane;
-    const bool lane_in = xl < W;  // the width is a multiple of 8
-    // lane 0: the sample left of the strip (column x0 - 1); lane 31: the one right of it (x0 + 256)
-    const int xe = lane == 0 ? U.x0 - 1 : U.x0 + kLiteStripMax;
-    const bool edge_in = (lane == 0 || lane == 31) && xe >= 0 && xe < W;
-    const int lane_byte = xl * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
-    const int edge_byte = !edge_in ? 0 : lane == 0 ? rows::edge_byte<FMT, true>(xe) : rows::edge_byte<FMT, false>(xe);
-    const int pitch = W * rows::bytes_num<FMT>() / rows::bytes_den<FMT>();
+    const DirectRows<FMT> src(fp, U, lane);
     const int n0 = y0 - 1;
     int nrows = bh + 2;
     // output: the rows of a frame whose width is a multiple of 8 all start at the same 8-byte
@@ -511,31 +555,24 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
     const bool rr_e = po.r_row == 0;
     const int v_e = 2 * (rr_e ? po.r_col : po.b_col) + (rr_e ? 1 : 0);
     const int v_o = 2 * (rr_e ? po.b_col : po.r_col) + (rr_e ? 0 : 1);
-    auto fetch = [&](int n, uint32_t (&w)[4], rows::Edge<FMT>& e) {
-        const bool row_in = (unsigned)n < (unsigned)H;
-        const uint8_t* rp = in + (row_in ? (long long)n * pitch : 0ll);
-        rows::load8<FMT>(rp, lane_byte, row_in && lane_in, w);
-        rows::load_edge<FMT>(rp, edge_byte, row_in && edge_in, e);
-    };
-    // two row buffers, each refilled with the row two below as soon as it is decoded, so every
-    // load has two rows of work to arrive in (the loop is unrolled by two: no buffer is copied)
-    uint32_t wa[4], wb[4];
-    rows::Edge<FMT> ea, eb;
-    fetch(n0, wa, ea);
-    fetch(n0 + 1, wb, eb);
+    // rows n0 .. n0 + kDirRing - 2 on their way (one commit group per row, empty past the unit's
+    // rows, so that the group of row k is always kDirRing - 1 groups before the newest)
+    const uint32_t main0 = ptx::smem_u32(&ring[0][lane]), edge0 = ptx::smem_u32(&ring_e[0][lane]);
+    constexpr uint32_t kMainStep = sizeof(ring[0]), kEdgeStep = sizeof(ring_e[0]);
+#pragma unroll
+    for (int r = 0; r < kDirRing - 1; r++) {
+        if (r < nrows) src.issue(fp, n0 + r, main0 + r * kMainStep, edge0 + r * kEdgeStep);
+        ptx::cp_async_commit();
+    }
     lite::Row Ur, Mr, Dr;  // rows n - 2, n - 1, n of the lane
     // the owner's claim of the segment's next band is in flight a band ahead of its use (lane 0
     // holds the counter's old value), so the warp never waits for the atomic
     unsigned long long pend = 0;
     if (own && lane == 0) pend = atomicAdd(own, segs::kFrontOne);
-    int k = 0;
-    auto step = [&](uint32_t (&w)[4], rows::Edge<FMT>& e) -> bool {
-        if (k >= nrows) return false;
+#pragma unroll 1
+    for (int k = 0; k < nrows; k++) {
         const int n = n0 + k;
-        uint32_t P[4];
-        rows::decode8<FMT>(w, P);
-        int nb = lane == 0 ? rows::decode_edge<FMT, true>(e) : rows::decode_edge<FMT, false>(e);
-        if (own && k + 2 == nrows) {
+        if (own && k + kDirRing - 1 == nrows) {
             // the segment's next band continues this stream
             int j = 0;
             if (lane == 0) j = segs::settle_front(pend, bl.seg_words + bl.n_items);
@@ -549,7 +586,18 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
                 own = nullptr;
             }
         }
-        if (k + 2 < nrows) fetch(n + 2, w, e);
+        // row n + kDirRing - 1 into the slot row n - 1 left, then row n's copies complete
+        const int ahead = (k + kDirRing - 1) & (kDirRing - 1);
+        if (k + kDirRing - 1 < nrows) src.issue(fp, n + kDirRing - 1, main0 + ahead * kMainStep, edge0 + ahead * kEdgeStep);
+        ptx::cp_async_commit();
+        ptx::cp_async_wait<kDirRing - 1>();
+        const int slot = k & (kDirRing - 1);
+        uint32_t w[4];
+        rows::Edge<FMT> e;
+        src.read(fp, n, ring[slot][lane], ring_e[slot][lane], w, e);
+        uint32_t P[4];
+        rows::decode8<FMT>(w, P);
+        int nb = lane == 0 ? rows::decode_edge<FMT, true>(e) : rows::decode_edge<FMT, false>(e);
         lite_levels<FMT>(fp, L, po, n, lane, P, nb);
         uint32_t Lw = __shfl_up_sync(full, P[3], 1) & 0xFFFF0000u;
         uint32_t Rn = __shfl_down_sync(full, P[0], 1) & 0xFFFFu;
@@ -582,11 +630,6 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
             }
         }
         ooff += 3 * W;
-        k++;
-        return true;
-    };
-#pragma unroll 1
-    while (step(wa, ea) && step(wb, eb)) {
     }
 }
 
@@ -595,6 +638,8 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<LiteDirectSmem*>(dsm);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nseg = bl.n_items;
+    const int gw = (int)blockIdx.x * kDirWarps + warp;
     {
         // tables of the launch, as in the staged variant; the tone table first comes into the
         // warps' staging rows by 16-byte loads (its buffer holds at least 4096 bytes)
@@ -613,19 +658,24 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
     }
     __syncthreads();
     segs::wait_init();
-    const int nseg = bl.n_items;
-    const int gw = (int)blockIdx.x * kDirWarps + warp;
     uint8_t* wout = sm.out[warp];
-    // the warp's own segment, band after band from the front, then bands from the back of others
-    segs::Walk walk(gw, nseg, (int)gridDim.x * kDirWarps);
-    int seg, band;
+    // the warp's own segment (its band 0 claimed for it by the init kernel), band after band from
+    // the front, then bands from the back of others
+    segs::Walk walk(gw, nseg, (int)gridDim.x * kDirWarps, bl.owners);
+    int seg, band, nbands;
     bool own;
-    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
+    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, nbands, own)) {
         LSeg S;
         lseg_of(bl, seg, S);
-        int y0, bh;
+        // a segment of one band is taken with the claim made for its warp
+        if (seg < bl.owners && band == 0 && S.nb == 1 && lane == 0) atomicAdd(bl.seg_words + nseg, 1ull);
+        // bands band .. band + nbands - 1: contiguous rows
+        int y0, bh, yl, hl;
         segs::band_of(S.s0, S.len, S.nb, band, y0, bh);
-        direct_unit<FMT>(bl, sm.tab, wout, S, y0, bh, own ? bl.seg_words + seg : nullptr, lane);
+        segs::band_of(S.s0, S.len, S.nb, band + nbands - 1, yl, hl);
+        bh = yl + hl - y0;
+        direct_unit<FMT>(bl, sm.tab, wout, sm.ring[warp], sm.ring_e[warp], S, y0, bh, own ? bl.seg_words + seg : nullptr,
+                         lane);
     }
 }
 
@@ -636,7 +686,7 @@ __global__ void lite_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
     if (i < bl.n_items) {
         LSeg G;
         lseg_of(bl, i, G);
-        bl.seg_words[i] = segs::initial_word(G.nb);
+        bl.seg_words[i] = segs::initial_word(G.nb) + (i < bl.owners ? segs::kFrontOne : 0ull);
     } else if (i == bl.n_items) {
         bl.seg_words[i] = 0ull;
     }
@@ -722,15 +772,16 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     int wmax = 0;
     for (int f = 0; f < bl.n_frames; f++) wmax = std::max(wmax, bl.frames[f].w);
     const TuneParams tp = tuning_for(IMOP_KERNEL_LITE, bl.fmt, wmax);
-    choose_segments(bl, limit * kDirWarps, tp.seg_percent, tp.band_rows);
+    if (!choose_segments(bl, limit * kDirWarps, tp.seg_percent, tp.band_rows)) return cudaErrorNotSupported;
     if (bl.n_items <= 0) return cudaSuccess;
     if (bl.n_items > kSegMax) return cudaErrorInvalidValue;
     unsigned long long* words = bl.frames[0].seg_words;
     bl.seg_words = words;
-    lite_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int want = (bl.n_items + kDirWarps - 1) / kDirWarps;
     const int grid = want < limit ? want : limit;
+    bl.owners = grid * kDirWarps;  // every warp starts on its own segment's band 0
+    lite_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     count_launch(IMOP_KERNEL_LITE);
     count_launch(IMOP_KERNEL_LITE_DIRECT);
     switch (bl.fmt) {
@@ -746,7 +797,10 @@ cudaError_t launch_lite(const BatchLaunch& bl, cudaStream_t st) {
     bool direct = bl.n_frames > 0;
     for (int f = 0; f < bl.n_frames; f++)
         direct = direct && direct_ok(bl.frames[f]) && bl.frames[f].seg_words == bl.frames[0].seg_words;
-    if (direct) return launch_direct(bl, st);
+    if (direct) {
+        const cudaError_t e = launch_direct(bl, st);
+        if (e != cudaErrorNotSupported) return e;  // else more strips than claim words: the staged variant
+    }
     const size_t smem = sizeof(LiteSmem);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -1,4 +1,5 @@
-// isp_ptx.cuh - inline PTX for the sm_103a tile pipeline: mbarriers and 1-D bulk (TMA) copies.
+// isp_ptx.cuh - inline PTX for the sm_103a pipelines: per-thread asynchronous copies, mbarriers and
+// 1-D bulk (TMA) copies.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -9,6 +10,25 @@ namespace ptx {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// per-thread asynchronous copies global -> shared of 4, 8 or 16 bytes (both addresses aligned to
+// the size); `bytes` of them are read, the rest of the destination is zero-filled (0: nothing is
+// read).  A thread's copies complete in commit groups: wait_group<N> waits until at most N of its
+// newest groups are pending.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {

@@ -12,6 +12,7 @@
 #include <cstdint>
 
 #include "isp_common.h"
+#include "isp_ptx.cuh"
 #include "isp_tile.cuh"
 
 namespace imop {
@@ -126,6 +127,35 @@ __device__ __forceinline__ int decode_edge(const Edge<FMT>& e) {
         return (int)(((v & 0xFFu) << 2) | ((v >> 14) & 3u));
     }
     return (int)((((w >> sh) & 0xFFu) << 2) | ((e.g[1] >> sh) & 3u));
+}
+
+// The same words brought into shared memory by the lane itself (ptx::cp_async*), for a ring of
+// rows: main = the lane's 16-byte slot, edge = its 8-byte slot for the sample beside the strip.
+// Rows outside the frame (in false) fill the slots with zeros and read nothing; `any` stands in
+// for the source address then.  The RAW10 byte offsets are not copied: ring_offset gives them.
+template <int FMT>
+__device__ __forceinline__ void ring_load8(uint32_t main, const uint8_t* row, int lane_byte, bool in, const void* any) {
+    const uint8_t* p = row + lane_byte;
+    if (FMT == FMT_U8) {
+        ptx::cp_async8(main, in ? (const void*)p : any, in ? 8u : 0u);
+    } else if (FMT == FMT_U16) {
+        ptx::cp_async16(main, in ? (const void*)p : any, in ? 16u : 0u);
+    } else {
+        const uint8_t* q = reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
+#pragma unroll
+        for (int k = 0; k < 3; k++) ptx::cp_async4(main + 4 * k, in ? (const void*)(q + 4 * k) : any, in ? 4u : 0u);
+    }
+}
+template <int FMT>
+__device__ __forceinline__ void ring_load_edge(uint32_t edge, const uint8_t* row, int byte, bool in, const void* any) {
+    const uint8_t* q =
+        reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(row + byte) & ~(uintptr_t)3);
+    ptx::cp_async4(edge, in ? (const void*)q : any, in ? 4u : 0u);
+    if (FMT == FMT_P10) ptx::cp_async4(edge + 4, in ? (const void*)(q + 4) : any, in ? 4u : 0u);
+}
+// the byte offset of a RAW10 lane's samples (or edge sample) in its first copied word
+__device__ __forceinline__ uint32_t ring_offset(const uint8_t* row, int byte) {
+    return (uint32_t)(reinterpret_cast<uintptr_t>(row + byte) & 3);
 }
 
 }  // namespace rows

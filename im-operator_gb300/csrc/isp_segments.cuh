@@ -5,7 +5,8 @@
 //
 // Per segment one 64-bit word: the claims made from the front (bits 0-22) and from the back
 // (bits 23-45), whether a warp adopted the segment (bit 46) and the segment's band count (bits
-// 48-63, written with zero counts by the launch's init kernel before the streamed kernel runs).
+// 48-63), written by the launch's init kernel before the streamed kernel runs: zero claims, or
+// band 0 already claimed for the segment's warp (which then starts on it with no atomic).
 // A claim is valid while the two counts before it sum to less than the band count, so a warp
 // looking for work reads everything it needs from the word.  Segments beyond the launch's warps
 // start without an owner: the first warp that finds one sets its adopted bit and streams it from
@@ -62,12 +63,19 @@ __device__ __forceinline__ int settle_front(unsigned long long old, unsigned lon
 __device__ __forceinline__ int claim_front(unsigned long long* w, unsigned long long* taken) {
     return settle_front(atomicAdd(w, kFrontOne), taken);
 }
-__device__ __forceinline__ int claim_back(unsigned long long* w, unsigned long long* taken) {
-    const unsigned long long old = atomicAdd(w, kBackOne);
+// up to k bands from the back in one claim: the first of them (-1 if none was left) and, in n,
+// how many (contiguous; fewer than k when the front claims reached them)
+__device__ __forceinline__ int claim_back(unsigned long long* w, unsigned long long* taken, unsigned k, int& n) {
+    const unsigned long long old = atomicAdd(w, kBackOne * k);
     const unsigned f = front_of(old), b = back_of(old), nb = bands_of(old);
+    n = 0;
     if (f + b >= nb) return -1;
-    if (f + b + 1 == nb) atomicAdd(taken, 1ull);
-    return (int)(nb - 1 - b);
+    if (f + b + k >= nb) atomicAdd(taken, 1ull);
+    // bands [f, nb - b) were unclaimed; this claim took the last k of them (k may exceed their
+    // number when other claims came between the read that chose k and this one)
+    const int last = (int)nb - 1 - (int)b, first = max((int)f, (int)nb - (int)b - (int)k);
+    n = last - first + 1;
+    return first;
 }
 
 // The work of one warp gw of nwarps over the nseg segments of `words` (the taken count at
@@ -75,19 +83,28 @@ __device__ __forceinline__ int claim_back(unsigned long long* w, unsigned long l
 // band): segment gw, then gw + nwarps, gw + 2 nwarps, ... (those beyond the launch's warps are
 // adopted first, so that a warp looking for work may take one over); then, 128 segments tested
 // per pass from the last one that held work on, one still open: adopted and streamed from the
-// front if no warp has begun it, else a single band from its back.  next() gives the segment and
-// band to do and whether the warp streams on from it; it returns false when every segment is
-// taken, or when a whole pass finds none open.
+// front if no warp has begun it, else its last unclaimed band.  next() gives the
+// segment, its first band and band count to do and whether the warp streams on from them; it
+// returns false when every segment is taken, or when a whole pass finds none open.
 struct Walk {
-    int base, scanned, nwarps, next_own;
-    __device__ __forceinline__ Walk(int gw, int nseg, int nw) : base(gw % nseg), scanned(0), nwarps(nw), next_own(gw) {}
+    int base, scanned, nwarps, next_own, owners;
+    // owners: segments below it start with band 0 claimed for their warp by the init kernel
+    __device__ __forceinline__ Walk(int gw, int nseg, int nw, int own_claimed)
+        : base(gw % nseg), scanned(0), nwarps(nw), next_own(gw), owners(own_claimed) {}
 
     __device__ __forceinline__ bool next(unsigned long long* words, int nseg, int gw, int lane, int& seg, int& band,
-                                         bool& own) {
+                                         int& nbands, bool& own) {
+        nbands = 1;
         const unsigned full = 0xffffffffu;
         while (next_own < nseg) {
             const int s = next_own;
             next_own += nwarps;
+            if (s < owners) {
+                seg = s;
+                band = 0;
+                own = true;
+                return true;
+            }
             int i = -1;
             if (lane == 0 && (s < nwarps || !(atomicOr(words + s, kAdopted) & kAdopted)))
                 i = claim_front(words + s, words + nseg);
@@ -137,23 +154,26 @@ struct Walk {
                 scanned += 128;
                 continue;
             }
-            int j = 0;
+            int j = 0, n = 1;
             bool adopt = false;
             if (lane == 0) {
                 if (s >= nwarps && !(atomicOr(words + s, kAdopted) & kAdopted)) {
                     adopt = true;
                     j = claim_front(words + s, words + nseg);
                 } else {
-                    j = claim_back(words + s, words + nseg);
+                    // one band: a range taken from the back could not be taken over in turn
+                    j = claim_back(words + s, words + nseg, 1u, n);
                 }
             }
             j = __shfl_sync(full, j, 0);
+            n = __shfl_sync(full, n, 0);
             adopt = __shfl_sync(full, adopt, 0);
             base = s;  // the segment may hold more
             scanned = 0;
             if (j >= 0) {
                 seg = s;
                 band = j;
+                nbands = adopt ? 1 : n;
                 own = adopt;
                 return true;
             }

@@ -628,14 +628,17 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kStWarps + warp;
     // the warp's own segment, band after band from the front, then bands from the back of others
-    segs::Walk walk(gw, nseg, (int)gridDim.x * kStWarps);
-    int seg, band;
+    segs::Walk walk(gw, nseg, (int)gridDim.x * kStWarps, bl.owners);
+    int seg, band, nbands;
     bool own;
-    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, own)) {
+    while (walk.next(bl.seg_words, nseg, gw, lane, seg, band, nbands, own)) {
         SSeg S;
         seg_of(bl, seg, S);
-        int y0, bh;
+        // bands band .. band + nbands - 1: contiguous rows
+        int y0, bh, yl, hl;
         band_rows(S, band, y0, bh);
+        band_rows(S, band + nbands - 1, yl, hl);
+        bh = yl + hl - y0;
         stream_unit<FMT, CHAIN>(bl, sm, sm.w[warp], S, y0, bh, own ? bl.seg_words + seg : nullptr, lane);
     }
 }
@@ -713,27 +716,35 @@ void stream_rects(const FrameParams& fp, TileRect& interior, TileRect (&border)[
     border[3] = {0, xe, 7, W - xe, H - 14, 0, 0};
 }
 
-void choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows) {
-    long long strip_rows = 0;
-    for (int r = 0; r < bl.n_rects; r++) strip_rows += (long long)bl.rects[r].tiles_x * bl.rects[r].h;
+bool choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows) {
+    long long strip_rows = 0, strips = 0;
+    for (int r = 0; r < bl.n_rects; r++) {
+        strip_rows += (long long)bl.rects[r].tiles_x * bl.rects[r].h;
+        strips += bl.rects[r].tiles_x;
+    }
+    if (strips > kSegMax) return false;  // one segment per strip is the fewest
     double per = std::max(1.0, (double)strip_rows / std::max(1, warps) * seg_percent / 100.0);
-    for (int pass = 0; pass < 8; pass++) {
-        int items = 0;
+    // rounded to the nearest count first; above the cap, longer segments rounded down until the
+    // count fits (it shrinks with every pass and reaches one per strip)
+    for (int pass = 0;; pass++) {
+        long long items = 0;
         for (int r = 0; r < bl.n_rects; r++) {
             TileRect& R = bl.rects[r];
-            R.tiles_y = std::max(1, std::min(R.h, (int)std::lround(R.h / per)));
-            bl.rect_start[r] = items;
-            items += R.tiles_x * R.tiles_y;
+            const double t = R.h / per;
+            R.tiles_y = std::max(1, std::min(R.h, (int)(pass == 0 ? std::lround(t) : std::floor(t))));
+            bl.rect_start[r] = (int)items;
+            items += (long long)R.tiles_x * R.tiles_y;
         }
-        bl.rect_start[bl.n_rects] = bl.n_items = items;
+        bl.rect_start[bl.n_rects] = bl.n_items = (int)std::min<long long>(items, 1 << 30);
         if (items <= kSegMax) break;
-        per *= (double)items / kSegMax;
+        per *= (double)items / kSegMax * 1.01;
     }
     // at most segs::kMaxBands bands per segment (the claim word's band count field)
     int longest = 0;
     for (int r = 0; r < bl.n_rects; r++)
         longest = std::max(longest, (bl.rects[r].h + bl.rects[r].tiles_y - 1) / bl.rects[r].tiles_y);
     bl.band_h = std::max(band_rows, (longest + segs::kMaxBands - 1) / segs::kMaxBands);
+    return true;
 }
 
 cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
@@ -760,10 +771,11 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
         limit = g_stream_grid[dev];
     }
     BatchLaunch bl = bl_in;
+    bl.owners = 0;
     int wmax = 0;
     for (int f = 0; f < bl.n_frames; f++) wmax = std::max(wmax, bl.frames[f].w);
     const TuneParams tp = tuning_for(IMOP_KERNEL_STREAM, bl.fmt, wmax);
-    choose_segments(bl, limit * kStWarps, tp.seg_percent, tp.band_rows);
+    if (!choose_segments(bl, limit * kStWarps, tp.seg_percent, tp.band_rows)) return cudaErrorInvalidValue;
     if (bl.n_items <= 0) return cudaSuccess;
     if (bl.n_items > kSegMax || !bl.seg_words) return cudaErrorInvalidValue;
     stream_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
