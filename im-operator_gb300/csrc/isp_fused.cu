@@ -227,12 +227,14 @@ struct FusedKernels {
         cudaError_t e = setup(limit);
         if (e != cudaSuccess) return e;
         if (bl.n_items > 0) {
-            if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
+            if (!bl.dependent && (e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
             const int grid = bl.n_items < limit ? bl.n_items : limit;
             count_launch(0);
             if (OUTB == 3 && bl.simple && !bl.extra && bl.demosaic && bl.fmt >= FMT_U8 && bl.fmt <= FMT_P12) {
                 if ((e = launch_fused_spec(bl.fmt, bl.demosaic, bl.no_dpc_lsc != 0, bl, grid, smem, st)) != cudaSuccess)
                     return e;
+            } else if (bl.dependent) {
+                if ((e = launch_dependent(kernel(variant(bl)), grid, kThreads, smem, st, bl)) != cudaSuccess) return e;
             } else {
                 kernel(variant(bl))<<<grid, kThreads, smem, st>>>(bl);
             }
@@ -333,28 +335,6 @@ bool make_lite_launch(FrameParams* frames, int n, BatchLaunch& bl, int band_rows
     return true;
 }
 
-// A second stream and two events per host thread and device: the border-column launch of a
-// streamed batch runs beside its border-row launch (both are short and latency-bound), forked
-// from and joined back into the launch stream by events, which a graph capture records as two
-// branches.
-struct SideStream {
-    cudaStream_t st = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-};
-cudaError_t side_stream(SideStream*& out) {
-    thread_local SideStream side[kMaxDevices];
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    SideStream& s = side[dev];
-    if (!s.st && (e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking)) != cudaSuccess) return e;
-    if (!s.fork && (e = cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
-    if (!s.join && (e = cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming)) != cudaSuccess) return e;
-    out = &s;
-    return cudaSuccess;
-}
-
 cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, const SplitFixup* split = nullptr) {
     BatchLaunch bl;
     bool fixup = false;
@@ -384,7 +364,7 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
     if (!make_launch(frames, n, bl, fixup)) return cudaErrorInvalidValue;
     if (stream) {
         // interior: the streaming kernel; border columns: the narrow tile; border rows: the nominal
-        // tile, whose launch also runs the fix-up
+        // tile; then the fix-up
         BatchLaunch bs = bl, bn = bl;
         int items_s = 0, items_n = 0, items_b = 0;
         bs.n_rects = bn.n_rects = bl.n_rects = 0;
@@ -404,23 +384,21 @@ cudaError_t launch_batch_group(FrameParams* frames, int n, cudaStream_t st, cons
         bn.rect_start[bn.n_rects] = bn.n_items = items_n;
         bl.rect_start[bl.n_rects] = bl.n_items = items_b;
         // the column launch counts its tiles in the last claim word, which the streaming launch
-        // leaves alone
+        // leaves alone; the streaming launch's init kernel zeroes both border counters, and the
+        // border launches are programmatic dependents in the same stream: they start beside the
+        // streaming kernel once its CTAs run (and the init kernel is complete), on the SMs its
+        // CTAs leave at the end.  The fix-up, launched the ordinary way, waits for all three.
         bn.tile_counter = reinterpret_cast<int*>(frames[0].seg_words + (kStreamSegCap - 1));
-        SideStream* side = nullptr;
+        bn.dependent = bl.dependent = 1;
         cudaError_t e = launch_stream(bs, st);
-        if (e == cudaSuccess) e = side_stream(side);
-        if (e == cudaSuccess && (e = cudaEventRecord(side->fork, st)) == cudaSuccess &&
-            (e = cudaStreamWaitEvent(side->st, side->fork, 0)) == cudaSuccess &&
-            (e = launch_fused_narrow(bn, side->st)) == cudaSuccess)
-            e = cudaEventRecord(side->join, side->st);
+        if (e == cudaSuccess) e = launch_fused_narrow(bn, st);
+        if (e == cudaSuccess)
+            e = frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bl, false, st, nullptr)
+                                       : FusedKernels<3>::launch(bl, false, st, nullptr);
         if (e != cudaSuccess) return e;
-        // the border rows, then (after the columns joined) the fix-up
         BatchLaunch bf = bl;
         bf.n_items = 0;
-        if (frames[0].out_bpc == 2) e = FusedKernels<6>::launch(bl, false, st, nullptr);
-        else e = FusedKernels<3>::launch(bl, false, st, nullptr);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, side->join, 0);
-        if (e != cudaSuccess) return e;
+        bf.dependent = 0;
         return frames[0].out_bpc == 2 ? FusedKernels<6>::launch(bf, fixup, st, split)
                                       : FusedKernels<3>::launch(bf, fixup, st, split);
     }

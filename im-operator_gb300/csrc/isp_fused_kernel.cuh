@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "isp_kernels.h"
+#include "isp_segments.cuh"
 #include "isp_tile.cuh"
 
 namespace imop {
@@ -50,6 +51,7 @@ __device__ void stage_item(TileSmem<TW, TH, OUTB>& sm, const BatchLaunch& bl, in
 
 template <int TW, int TH, int OUTB, bool EXTRA, int DM, int SPEC>
 __global__ void __launch_bounds__(kThreads, 3) fused_batch_kernel(const __grid_constant__ BatchLaunch bl) {
+    segs::release_dependents();  // a tile launch after this one may start beside it
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<TileSmem<TW, TH, OUTB>*>(dsm);
     const int n_items = bl.n_items;
@@ -109,6 +111,7 @@ cudaError_t launch_fused_variant(const BatchLaunch& bl, int grid, size_t smem, c
             attr_done[dev] = true;
         }
     }
+    if (bl.dependent) return launch_dependent(fused_batch_kernel<TW, TH, OUTB, EXTRA, DM, SPEC>, grid, kThreads, smem, st, bl);
     fused_batch_kernel<TW, TH, OUTB, EXTRA, DM, SPEC><<<grid, kThreads, smem, st>>>(bl);
     return cudaGetLastError();
 }

@@ -41,9 +41,11 @@ cudaError_t launch_fused_narrow(const BatchLaunch& bl, cudaStream_t st) {
         limit = g_narrow_grid[dev];
     }
     if (bl.n_items <= 0) return cudaSuccess;
-    if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
+    const int grid = bl.n_items < limit ? bl.n_items : limit;
     count_launch(0);
-    narrow_kernel()<<<bl.n_items < limit ? bl.n_items : limit, kThreads, smem, st>>>(bl);
+    if (bl.dependent) return launch_dependent(narrow_kernel(), grid, kThreads, smem, st, bl);
+    if ((e = cudaMemsetAsync(bl.tile_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
+    narrow_kernel()<<<grid, kThreads, smem, st>>>(bl);
     return cudaGetLastError();
 }
 

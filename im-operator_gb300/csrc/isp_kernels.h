@@ -45,6 +45,7 @@ struct BatchLaunch {
     unsigned long long* seg_words;  // streaming kernel: per segment, bands claimed (front | back << 32)
     int band_h;                     // streamed kernels: rows of a band
     int owners = 0;                 // streamed kernels: segments below this start with band 0 claimed by their warp
+    int dependent = 0;              // tile kernel: launched as a programmatic dependent, its counter already zero
     int rect_start[kMaxRects + 1];  // first item of each rectangle; rect_start[n_rects] = n_items
     TileRect rects[kMaxRects];
     FrameParams frames[kBatchInline];

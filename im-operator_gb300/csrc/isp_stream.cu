@@ -625,6 +625,9 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
     }
     __syncthreads();
     segs::wait_init();
+    // the border tile launches may start now (the init kernel, which zeroed their counters, is
+    // complete); their CTAs take the SMs this kernel's CTAs leave
+    segs::release_dependents();
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kStWarps + warp;
     // the warp's own segment, band after band from the front, then bands from the back of others
@@ -643,7 +646,8 @@ __global__ void __launch_bounds__(kStThreads, 1) stream_kernel(const __grid_cons
     }
 }
 
-// the launch's claim words: each segment's band count with zero claims, then the taken count
+// the launch's claim words: each segment's band count with zero claims, then the taken count (and
+// the border launches' tile counters)
 __global__ void stream_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
     segs::release_dependents();
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -653,6 +657,9 @@ __global__ void stream_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
         bl.seg_words[i] = segs::initial_word(G.nb);
     } else if (i == bl.n_items) {
         bl.seg_words[i] = 0ull;
+        // the tile counters of the batch's border-row and border-column launches
+        if (bl.tile_counter) *bl.tile_counter = 0;
+        bl.seg_words[kStreamSegCap - 1] = 0ull;
     }
 }
 
