@@ -40,12 +40,12 @@ sys.path.insert(0, os.path.join(REPO, "im-operator_gb300"))
 
 METRIC = "ISP Mpix/s & % HBM peak, fused-batched vs plain (1 GB300, <=1 LSB); adjoint Mpix/s"
 W_C2, H_C2 = 4024, 3032
-# ncu smsp__inst_executed.sum of one recorded C2 step over 8 frames: the streaming kernel
-# (377.55e6), the border-column (16.66e6) and border-row (10.51e6) tile launches, the defect-chain
-# resolution (0.02e6) and window re-rendering (0.04e6)
-WARP_INST_PER_STEP_8 = 4.048e8
+# ncu smsp__inst_executed.sum of one recorded C2 step over 8 frames: the claim-word init kernel
+# (0.01e6), the streaming kernel (363.24e6), the border-column (16.66e6) and border-row (10.51e6)
+# tile launches, the defect-chain resolution (0.01e6) and window re-rendering (0.04e6)
+WARP_INST_PER_STEP_8 = 3.905e8
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the streaming kernel's launch over 8 frames
-STREAM_DRAM_BYTES_8 = 393691392
+STREAM_DRAM_BYTES_8 = 391222528
 # HBM bytes per C2 pixel of the plain per-operator chain (planes between its kernels)
 PLAIN_BYTES_PER_PX = 62.5
 
@@ -658,8 +658,9 @@ def main():
     host_batch = [(None, h_in[i].data_ptr(), h_out[i].data_ptr()) for i in range(B)]
 
     def step_device():
-        # one recorded graph per step: seed-counter reset, one persistent launch over all B
-        # frames' tiles, the defect-chain resolution and window re-rendering launches
+        # one recorded graph per step: seed-counter reset, the claim-word init, the streaming
+        # launch over all B frames' interiors with the two border tile launches beside it, the
+        # defect-chain resolution and window re-rendering launches
         isp.batch_submit(dev_frames, flags=abi.BATCH_GRAPH, stream=sh)
 
     def step_plain():
@@ -757,12 +758,12 @@ def main():
                      "frac": round(achieved / peak, 4), "traffic": int(STREAM_DRAM_BYTES_8 * B / 8),
                      "peak_kind": peak_kind,
                      "kernel": "stream_kernel (warp-streamed strips of the frames' interiors, one launch "
-                               "over the step's frames), timed as the recorded step with the border "
-                               "tile launches, the seed reset and the two defect fix-up launches",
+                               "over the step's frames), timed as the recorded step with its claim-word "
+                               "init, the border tile launches beside it and the two defect fix-up launches",
                      "bytes_per_launch": B * alg_bytes, "launch_ms": round(per_launch_ms, 4),
-                     "traffic_note": "ncu: 393.7 MB DRAM read+write of the streaming kernel's launch over "
+                     "traffic_note": "ncu: 391.2 MB DRAM read+write of the streaming kernel's launch over "
                                      "8 frames (the last writes still in L2 when it ends; profiles/)"},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 6 * args.steps,
         "clocks": clk.summary(),
     }
     # the ceiling that binds this kernel: warp-instruction issue (4 per SM per clock)
@@ -774,7 +775,7 @@ def main():
         "achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
         "unit": "T warp instructions/s", "frac": round(issue_achieved / issue_peak, 4),
         "warp_instructions_per_launch": int(WARP_INST_PER_STEP_8 * B / 8),
-        "note": f"ncu smsp__inst_executed.sum of the step's five kernels over 8 frames (profiles/); peak = {n_sm} SMs x 4 "
+        "note": f"ncu smsp__inst_executed.sum of the step's six kernels over 8 frames (profiles/); peak = {n_sm} SMs x 4 "
                 f"schedulers x the median SM clock sampled in the timed region"}
     if ms_e2e is not None:
         line["e2e"] = {"value": round(world * args.steps * px_step / (ms_e2e / 1e3) / 1e6, 2), "unit": "Mpix/s",

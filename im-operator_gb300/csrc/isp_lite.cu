@@ -777,8 +777,10 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     if (bl.n_items > kSegMax) return cudaErrorInvalidValue;
     unsigned long long* words = bl.frames[0].seg_words;
     bl.seg_words = words;
+    // every SM once the launch has work for half of them (warps without a segment of their own
+    // take bands from the others from the start); fewer CTAs for a small launch
     const int want = (bl.n_items + kDirWarps - 1) / kDirWarps;
-    const int grid = want < limit ? want : limit;
+    const int grid = want >= limit / 2 ? limit : want;
     bl.owners = grid * kDirWarps;  // every warp starts on its own segment's band 0
     lite_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

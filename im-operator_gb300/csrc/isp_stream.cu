@@ -787,6 +787,8 @@ cudaError_t launch_stream(const BatchLaunch& bl_in, cudaStream_t st) {
     if (bl.n_items > kSegMax || !bl.seg_words) return cudaErrorInvalidValue;
     stream_seg_init_kernel<<<(bl.n_items + 256) / 256, 256, 0, st>>>(bl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // one CTA per 12 segments (a warp that starts without a segment of its own would take bands
+    // from the others from the start, each with 10 warm-up rows: slower than the idle SMs)
     const int want = (bl.n_items + kStWarps - 1) / kStWarps;
     const int grid = want < limit ? want : limit;
     count_launch(2);
