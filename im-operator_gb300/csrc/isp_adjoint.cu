@@ -65,6 +65,26 @@ struct AdjSmem {
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
+// (row, column) of element s = r * w + c of a w-wide region, for a loop whose s starts at s0 and
+// steps by kAdjThreads: one division at the start, then a carry per step
+struct Walk2D {
+    int r, c, dr, dc, w;
+    __device__ __forceinline__ Walk2D(int s0, int w_) : w(w_) {
+        r = s0 / w;
+        c = s0 - r * w;
+        dr = kAdjThreads / w;
+        dc = kAdjThreads - dr * w;
+    }
+    __device__ __forceinline__ void step() {
+        r += dr;
+        c += dc;
+        if (c >= w) {
+            c -= w;
+            r++;
+        }
+    }
+};
+
 
 __device__ __forceinline__ float inside(float v, float lo, float hi) { return (v > lo && v < hi) ? 1.0f : 0.0f; }
 __device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : (v < 0.0f ? -1.0f : 0.0f); }
@@ -163,8 +183,9 @@ __device__ void demosaic_gather(AdjSmem& sm, const TileCtx& t) {
     const float* V2 = sm.gV[2];
     const bool hqli = DM == DM_HQLI;
     const int lo = hqli ? 2 : 1;  // sources with colour interpolation: [lo, w - lo) x [lo, h - lo)
-    for (int s = threadIdx.x; s < gw * gh; s += kAdjThreads) {
-        const int r = s / gw, c = s - r * gw;
+    Walk2D wk(threadIdx.x, gw);
+    for (int s = threadIdx.x; s < gw * gh; s += kAdjThreads, wk.step()) {
+        const int r = wk.r, c = wk.c;
         const int x = t.xg + c, y = t.yg + r;
         const int v = t.vi(x, y), i = t.ui(x, y), j = r * kGW + c;
         auto in_lo = [&](int xx, int yy) { return xx >= lo && xx < f.w - lo && yy >= lo && yy < f.h - lo; };
@@ -235,6 +256,8 @@ __device__ __forceinline__ void tile_of(const AdjLaunch& L, int item, int& fi, T
 
 // one raw sample of frame f (pixel formats of the product path)
 __device__ __forceinline__ int adj_raw(const AdjFrame& f, const uint8_t* in, int x, int y) {
+    // u16 frames (2-byte aligned: every frame of a launch is 2 w h bytes): one 16-bit load
+    if (f.fmt == FMT_U16) return (int)__ldg(reinterpret_cast<const uint16_t*>(in) + (size_t)y * f.w + x);
     FrameParams fp;
     fp.w = f.w;
     fp.bd = f.bd;
@@ -269,8 +292,9 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
     }
     __syncthreads();
     const float* grid = sm.th + 16;
-    for (int s = tid; s < uw * uh; s += kAdjThreads) {
-        int r = s / uw, c = s - r * uw;
+    Walk2D wk(tid, uw);
+    for (int s = tid; s < uw * uh; s += kAdjThreads, wk.step()) {
+        const int r = wk.r, c = wk.c;
         int x = t.xu + c, y = t.yu + r;
         int i = r * kUW + c;
         float rv = 0.0f, uv = 0.0f;
@@ -295,16 +319,24 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
     }
     __syncthreads();
     if (DM == DM_AMAZE || BACKWARD) {
+        // by Bayer pairs (frame columns 2k, 2k + 1): every lane takes the pair's red / blue site
+        // (AMAZE's weighted green) and its green site (a copy), so no lane idles beside another
         const int gw = t.tw + 2, gh = t.th + 2;
-        for (int s = tid; s < gw * gh; s += kAdjThreads) {
-            int r = s / gw, c = s - r * gw;
-            int x = t.xg + c, y = t.yg + r;
-            int j = r * kGW + c;
-            float g = -1.0f;
-            if (DM == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
-                g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
-            sm.G[j] = g;
-            if (BACKWARD) sm.gG[j] = 0.0f;
+        const int xp0 = t.xg & ~1, np = (((t.xg + gw - 1) & ~1) - xp0) / 2 + 1;
+        Walk2D wg(tid, np);
+        for (int s = tid; s < np * gh; s += kAdjThreads, wg.step()) {
+            const int r = wg.r, y = t.yg + r, xp = xp0 + 2 * wg.c;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int x = xp + h, c = x - t.xg;
+                if (c < 0 || c >= gw) continue;
+                const int j = r * kGW + c;
+                float g = -1.0f;
+                if (DM == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
+                    g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
+                sm.G[j] = g;
+                if (BACKWARD) sm.gG[j] = 0.0f;
+            }
         }
         __syncthreads();
     }
@@ -339,10 +371,14 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
     const bool border_tile = t.x0 < 2 || t.x0 + t.tw > f.w - 2 || t.y0 < 2 || t.y0 + t.th > f.h - 2;
     // whole warps iterate together (the knot sums are warp-wide); lanes past the end repeat the
     // last pixel with zero weight
-    for (int s0 = threadIdx.x & ~31; s0 < n_own; s0 += kAdjThreads) {
+    Walk2D wp(threadIdx.x, t.tw);
+    for (int s0 = threadIdx.x & ~31; s0 < n_own; s0 += kAdjThreads, wp.step()) {
         const bool valid = s0 + (int)(threadIdx.x & 31) < n_own;
-        const int s = valid ? s0 + (int)(threadIdx.x & 31) : n_own - 1;
-        int r = s / t.tw, c = s - r * t.tw;
+        int r = wp.r, c = wp.c;
+        if (!valid) {
+            r = t.th - 1;  // the last pixel, with zero weight
+            c = t.tw - 1;
+        }
         int x = t.x0 + c, y = t.y0 + r;
         int sx, sy;
         dev::border_source(x, y, f.w, f.h, f.border_mode, sx, sy);
@@ -418,17 +454,28 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     const float mvf = (float)f.mv;
     __syncthreads();
     if (DM == DM_AMAZE) {
+        // by Bayer pairs, as the forward green loop: each lane the pair's green site (one add)
+        // and its red / blue site (AMAZE's adjoint)
         const int gw = t.tw + 2, gh = t.th + 2;
-        for (int s = tid; s < gw * gh; s += kAdjThreads) {
-            int r = s / gw, c = s - r * gw;
-            int x = t.xg + c, y = t.yg + r;
+        const int xp0 = t.xg & ~1, np = (((t.xg + gw - 1) & ~1) - xp0) / 2 + 1;
+        Walk2D wg(tid, np);
+        for (int s = tid; s < np * gh; s += kAdjThreads, wg.step()) {
+          const int r = wg.r, y = t.yg + r, xp = xp0 + 2 * wg.c;
+          const int rbh = t.rb(xp, y) ? 0 : 1;  // the red / blue site of the pair
+          // the green site first
+          {
+              const int x = xp + 1 - rbh, c = x - t.xg;
+              if (c >= 0 && c < gw && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2) {
+                  const float g = sm.gG[r * kGW + c];
+                  if (g != 0.0f) atomicAdd(&sm.gu[t.ui(x, y)], g);
+              }
+          }
+          {
+            const int x = xp + rbh, c = x - t.xg;
+            if (c < 0 || c >= gw) continue;
             float g = sm.gG[r * kGW + c];
             if (g == 0.0f || x < 2 || x >= f.w - 2 || y < 2 || y >= f.h - 2) continue;
             int i = t.ui(x, y);
-            if (!t.rb(x, y)) {
-                atomicAdd(&sm.gu[i], g);
-                continue;
-            }
             float P[10];
             amaze_df(sm, t, x, y, P);
             float a = P[0], b = P[1], wh = P[2], wv = P[3], gh_ = P[4], gv_ = P[5];
@@ -447,6 +494,7 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
             atomicAdd(&sm.gu[i - 2 * kUW], -tV);
             atomicAdd(&sm.gu[i + 2 * kUW], -tV);
             atomicAdd(&sm.gu[i], 2.0f * (tH + tV));
+          }
         }
         __syncthreads();
     }
@@ -458,8 +506,9 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     const int gnode[4] = {0, 4, 4 * f.gw, 4 * f.gw + 4};
     const int lnode[4] = {0, 4 * 32, 4 * kLNX * 32, (4 * kLNX + 4) * 32};
     float* node_lane = sm.node_lane + (tid & 31);
-    for (int s = tid; s < nu; s += kAdjThreads) {
-        int r = s / uw, c = s - r * uw;
+    Walk2D wu(tid, uw);
+    for (int s = tid; s < nu; s += kAdjThreads, wu.step()) {
+        const int r = wu.r, c = wu.c;
         int i = r * kUW + c;
         float g = sm.gu[i];
         int x = t.xu + c, y = t.yu + r;
