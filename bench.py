@@ -341,7 +341,7 @@ def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind)
         del fused
         for _ in range(max(3, args.warmup)):
             isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
-        steps = max(1, min(args.steps, 5))
+        steps = max(1, min(2 * args.steps, 20))  # short steps: more of them for a steadier mean
         # per step, in one stream: the L2 flush, then the frame's graph between two events; the
         # steps are queued without host waits, so the events bracket the frame's device work alone
         # (the host-side submission overlaps the flush before it)

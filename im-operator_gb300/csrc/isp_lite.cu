@@ -490,9 +490,10 @@ __device__ __forceinline__ void lseg_of(const BatchLaunch& bl, int seg, LSeg& G)
 template <int FMT>
 struct DirectRows {
     int pitch, lane_byte, edge_byte;
-    bool lane_in, edge_in;
+    bool lane_in, edge_in, edge_lane;
     __device__ __forceinline__ DirectRows(const FrameParams& fp, const LSeg& U, int lane) {
         const int W = fp.w;
+        edge_lane = lane == 0 || lane == 31;
         const int xl = U.x0 + kLiteLanePx * lane;
         lane_in = xl < W;  // the width is a multiple of 8
         // lane 0: the sample left of the strip (column x0 - 1); lane 31: the one right of it
@@ -507,16 +508,24 @@ struct DirectRows {
         const bool row_in = (unsigned)n < (unsigned)fp.h;
         const uint8_t* rp = fp.in + (row_in ? (long long)n * pitch : 0ll);
         rows::ring_load8<FMT>(main, rp, lane_byte, row_in && lane_in, fp.in);
-        rows::ring_load_edge<FMT>(edge, rp, edge_byte, row_in && edge_in, fp.in);
+        // only lanes 0 and 31 use the sample beside the strip
+        if (edge_lane) rows::ring_load_edge<FMT>(edge, rp, edge_byte, row_in && edge_in, fp.in);
     }
     // row n back from the slots (after its copies completed): the lane's words and the edge words
     __device__ __forceinline__ void read(const FrameParams& fp, int n, const uint4& main, const uint2& edge,
                                          uint32_t (&w)[4], rows::Edge<FMT>& e) const {
-        const uint4 m = main;
-        w[0] = m.x;
-        w[1] = m.y;
-        w[2] = m.z;
-        w[3] = m.w;
+        if (FMT == FMT_U8) {
+            const uint2 m = *reinterpret_cast<const uint2*>(&main);  // 8 bytes hold the 8 samples
+            w[0] = m.x;
+            w[1] = m.y;
+            w[2] = w[3] = 0u;
+        } else {
+            const uint4 m = main;
+            w[0] = m.x;
+            w[1] = m.y;
+            w[2] = m.z;
+            w[3] = m.w;
+        }
         e.g[0] = edge.x;
         if (FMT == FMT_P10) {
             // the byte offsets of the samples in the first copied words
