@@ -86,8 +86,8 @@ __device__ __forceinline__ void decode8(const uint32_t (&w)[4], uint32_t (&P)[4]
 }
 
 // The sample beside a strip: its last column's right neighbour or its first column's left one,
-// as few words as hold it (the strip's first column x0 is a multiple of 8).  edge_byte is the
-// byte of the row where the sample's bytes start:
+// in as few words as hold it (the strip's first column x0 is a multiple of 8; ring_load_edge
+// brings them).  edge_byte is the byte of the row where the sample's bytes start:
 //   LAST (the sample x0 - 1, the last of its group)     u8 x, u16 2x, RAW12 3(x >> 1), RAW10 5(x >> 2) + 3
 //   first (the sample x0 + 256, the first of its group) u8 x, u16 2x, RAW12 3(x >> 1), RAW10 5(x >> 2)
 template <int FMT>
@@ -98,19 +98,6 @@ struct Edge {
 template <int FMT, bool LAST>
 __host__ __device__ constexpr int edge_byte(int x) {
     return FMT == FMT_U8 ? x : FMT == FMT_U16 ? 2 * x : FMT == FMT_P12 ? 3 * (x >> 1) : 5 * (x >> 2) + (LAST ? 3 : 0);
-}
-template <int FMT>
-__device__ __forceinline__ void load_edge(const uint8_t* row, int byte, bool in, Edge<FMT>& e) {
-#pragma unroll
-    for (int k = 0; k < Edge<FMT>::N; k++) e.g[k] = 0u;
-    if (!in) return;
-    const uintptr_t a = reinterpret_cast<uintptr_t>(row + byte);
-    const uint32_t* q = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
-    e.g[0] = __ldg(q);
-    if (FMT == FMT_P10) {
-        e.g[1] = __ldg(q + 1);
-        e.g[2] = (uint32_t)(a & 3);
-    }
 }
 template <int FMT, bool LAST>
 __device__ __forceinline__ int decode_edge(const Edge<FMT>& e) {
