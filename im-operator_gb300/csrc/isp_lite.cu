@@ -447,8 +447,7 @@ __global__ void __launch_bounds__(kThreads, 3) lite_batch_kernel(const __grid_co
 }
 
 // ---- the direct-read variant ---------------------------------------------------------------
-// Frames 16-byte aligned with a width that is a multiple of 8 skip the shared staging of whole
-// rows: each lane copies the words of its own 8 samples of a row (lanes 0 and 31 also the sample
+// Frames whose rows start on a word (direct_ok) skip the shared staging of whole rows: each lane copies the words of its own 8 samples of a row (lanes 0 and 31 also the sample
 // beside the strip) into its slot of a ring of kDirRing rows with per-thread asynchronous copies,
 // kDirRing - 1 rows ahead of their use, and reads them back itself: no lane waits for another,
 // no barrier, and the rows in flight hold no registers.  A warp streams a whole segment of its
@@ -487,7 +486,9 @@ __device__ __forceinline__ void lseg_of(const BatchLaunch& bl, int seg, LSeg& G)
 
 // where a lane's samples of strip U's rows are: its 8 samples and (lanes 0 and 31) the sample
 // beside the strip
-template <int FMT>
+// WORDS: u8 / u16 rows that start on a word but not on the lanes' 8- / 16-byte loads (a width
+// that is not a multiple of 8, or an input that is not 16-byte aligned)
+template <int FMT, bool WORDS>
 struct DirectRows {
     int pitch, lane_byte, edge_byte;
     bool lane_in, edge_in, edge_lane;
@@ -507,7 +508,10 @@ struct DirectRows {
     __device__ __forceinline__ void issue(const FrameParams& fp, int n, uint32_t main, uint32_t edge) const {
         const bool row_in = (unsigned)n < (unsigned)fp.h;
         const uint8_t* rp = fp.in + (row_in ? (long long)n * pitch : 0ll);
-        rows::ring_load8<FMT>(main, rp, lane_byte, row_in && lane_in, fp.in);
+        if (WORDS)
+            rows::ring_load8_words<FMT>(main, rp, lane_byte, pitch - lane_byte, row_in && lane_in, fp.in);
+        else
+            rows::ring_load8<FMT>(main, rp, lane_byte, row_in && lane_in, fp.in);
         // only lanes 0 and 31 use the sample beside the strip
         if (edge_lane) rows::ring_load_edge<FMT>(edge, rp, edge_byte, row_in && edge_in, fp.in);
     }
@@ -540,7 +544,7 @@ struct DirectRows {
 
 // output rows [y0, y0 + bh) of segment U and, while `own` is set, the segment's next bands from
 // the front: input rows y0 - 1 .. (the row below the last output row)
-template <int FMT>
+template <int FMT, bool WORDS>
 __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t (*tab)[4096], uint8_t* wout,
                                             uint4 (*ring)[32], uint2 (*ring_e)[32], const LSeg& U, int y0, int bh,
                                             unsigned long long* own, int lane) {
@@ -551,14 +555,15 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
     const PatternOffsets po = pattern_offsets(fp.pattern);
     const LiteLevels L = lite_levels_of(fp, lane);
     const int xl = U.x0 + kLiteLanePx * lane;
-    const DirectRows<FMT> src(fp, U, lane);
+    const DirectRows<FMT, WORDS> src(fp, U, lane);
     const int n0 = y0 - 1;
     int nrows = bh + 2;
-    // output: the rows of a frame whose width is a multiple of 8 all start at the same 8-byte
-    // phase, so whether the lanes store their 24 bytes straight (an interior strip at phase 0) is
-    // decided once; the lane's bytes of output row n - 1 lie at out + ooff
+    // output: on an interior strip every lane stores its 24 bytes straight, in words as wide as the
+    // row's 8-byte phase allows (the same for every lane of a row; one phase for all rows of a
+    // frame whose width is a multiple of 8); the lane's bytes of output row n - 1 lie at out + ooff
     const bool lane_st = xl + kLiteLanePx <= U.x0 + U.npx;
-    const bool fast = U.x0 != 0 && U.x0 + U.npx != W && ((reinterpret_cast<uintptr_t>(out) + 3u * U.x0) & 7) == 0;
+    const bool interior = U.x0 != 0 && U.x0 + U.npx != W;
+    const bool fast = interior && ((reinterpret_cast<uintptr_t>(out) + 3u * U.x0) & 7) == 0;  // !WORDS
     long long ooff = ((long long)(n0 - 1) * W + xl) * 3;
     // the HQLI variant (red / blue site column, red row) of even and odd output rows
     const bool rr_e = po.r_row == 0;
@@ -626,12 +631,28 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
             else if (v == 1) lite::hqli_row<0, true>(Ur, Mr, Dr, tab, ob);
             else if (v == 2) lite::hqli_row<1, false>(Ur, Mr, Dr, tab, ob);
             else lite::hqli_row<1, true>(Ur, Mr, Dr, tab, ob);
-            if (fast && yo != 2 && yo != H - 3) {
+            // one phase for all rows unless WORDS
+            const int phase = WORDS ? (int)((reinterpret_cast<uintptr_t>(out) + (uintptr_t)ooff) & 7) : 0;
+            if ((WORDS ? interior && (phase & 1) == 0 : fast) && yo != 2 && yo != H - 3) {
                 if (lane_st) {
-                    uint2* q = reinterpret_cast<uint2*>(out + ooff);
-                    q[0] = make_uint2(ob[0], ob[1]);
-                    q[1] = make_uint2(ob[2], ob[3]);
-                    q[2] = make_uint2(ob[4], ob[5]);
+                    uint8_t* q = out + ooff;
+                    if (!WORDS || phase == 0) {
+                        uint2* q2 = reinterpret_cast<uint2*>(q);
+                        q2[0] = make_uint2(ob[0], ob[1]);
+                        q2[1] = make_uint2(ob[2], ob[3]);
+                        q2[2] = make_uint2(ob[4], ob[5]);
+                    } else if (phase == 4) {
+                        uint32_t* q4 = reinterpret_cast<uint32_t*>(q);
+#pragma unroll
+                        for (int w = 0; w < 6; w++) q4[w] = ob[w];
+                    } else {
+                        // two bytes, five words from the next word boundary on, two bytes
+                        reinterpret_cast<uint16_t*>(q)[0] = (uint16_t)(ob[0] & 0xFFFFu);
+                        uint32_t* q4 = reinterpret_cast<uint32_t*>(q + 2);
+#pragma unroll
+                        for (int w = 0; w < 5; w++) q4[w] = __funnelshift_r(ob[w], ob[w + 1], 16);
+                        reinterpret_cast<uint16_t*>(q + 22)[0] = (uint16_t)(ob[5] >> 16);
+                    }
                 }
             } else {
                 lite_emit_staged(tab, wout, out, W, H, U.x0, U.npx, lane, yo, make_uint4(ob[0], ob[1], ob[2], ob[3]),
@@ -642,7 +663,7 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
     }
 }
 
-template <int FMT>
+template <int FMT, bool WORDS>
 __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
     auto& sm = *reinterpret_cast<LiteDirectSmem*>(dsm);
@@ -683,7 +704,8 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
         segs::band_of(S.s0, S.len, S.nb, band, y0, bh);
         segs::band_of(S.s0, S.len, S.nb, band + nbands - 1, yl, hl);
         bh = yl + hl - y0;
-        direct_unit<FMT>(bl, sm.tab, wout, sm.ring[warp], sm.ring_e[warp], S, y0, bh, own ? bl.seg_words + seg : nullptr,
+        direct_unit<FMT, WORDS>(bl, sm.tab, wout, sm.ring[warp], sm.ring_e[warp], S, y0, bh,
+                                own ? bl.seg_words + seg : nullptr,
                          lane);
     }
 }
@@ -703,9 +725,9 @@ __global__ void lite_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
 
 int g_direct_grid[kMaxDev];
 
-template <int FMT>
+template <int FMT, bool WORDS>
 cudaError_t launch_direct_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
-    return launch_dependent(lite_direct_kernel<FMT>, grid, kDirThreads, smem, st, bl);
+    return launch_dependent(lite_direct_kernel<FMT, WORDS>, grid, kDirThreads, smem, st, bl);
 }
 
 int g_lite_grid[kMaxDev];
@@ -749,10 +771,17 @@ long long lite_table_key(const FrameParams& fp) {
 int lite_units_x(int w) { return lite_strips(w); }
 int lite_units_y(int h, int band_rows) { return tiles_along(h, band_rows); }
 
-// frames the direct-read variant takes: whole lane groups, word-aligned rows, claim words
+// frames the direct-read variant takes: rows that start on a word (the input word-aligned, and a
+// width that is a multiple of 8 for the MIPI formats, even for u16, a multiple of 4 for u8), claim
+// words
 static bool direct_ok(const FrameParams& fp) {
-    return fp.w % 8 == 0 && (reinterpret_cast<uintptr_t>(fp.in) & 15) == 0 && fp.seg_words &&
+    const int wmul = fp.fmt == FMT_U16 ? 2 : fp.fmt == FMT_U8 ? 4 : 8;
+    return fp.w % wmul == 0 && (reinterpret_cast<uintptr_t>(fp.in) & 3) == 0 && fp.seg_words &&
            fp.seg_cap >= kStreamSegCap;
+}
+// u8 / u16 frames whose lanes' 8- / 16-byte loads do not all start on their size: word copies
+static bool needs_words(const FrameParams& fp) {
+    return (fp.fmt == FMT_U8 || fp.fmt == FMT_U16) && (fp.w % 8 != 0 || (reinterpret_cast<uintptr_t>(fp.in) & 15) != 0);
 }
 
 static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
@@ -765,9 +794,10 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     {
         std::lock_guard<std::mutex> lock(device_setup_mutex());
         if (!g_direct_grid[dev]) {
-            void (*ks[4])(BatchLaunch) = {lite_direct_kernel<FMT_U8>, lite_direct_kernel<FMT_U16>,
-                                          lite_direct_kernel<FMT_P10>, lite_direct_kernel<FMT_P12>};
-            for (int k = 0; k < 4 && e == cudaSuccess; k++)
+            void (*ks[6])(BatchLaunch) = {lite_direct_kernel<FMT_U8, false>,  lite_direct_kernel<FMT_U16, false>,
+                                          lite_direct_kernel<FMT_P10, false>, lite_direct_kernel<FMT_P12, false>,
+                                          lite_direct_kernel<FMT_U8, true>,   lite_direct_kernel<FMT_U16, true>};
+            for (int k = 0; k < 6 && e == cudaSuccess; k++)
                 e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int n = 0, m = 0;
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[1], kDirThreads, smem);
@@ -784,8 +814,7 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     if (!choose_segments(bl, limit * kDirWarps, tp.seg_percent, tp.band_rows)) return cudaErrorNotSupported;
     if (bl.n_items <= 0) return cudaSuccess;
     if (bl.n_items > kSegMax) return cudaErrorInvalidValue;
-    unsigned long long* words = bl.frames[0].seg_words;
-    bl.seg_words = words;
+    bl.seg_words = bl.frames[0].seg_words;
     // every SM once the launch has work for half of them (warps without a segment of their own
     // take bands from the others from the start); fewer CTAs for a small launch
     const int want = (bl.n_items + kDirWarps - 1) / kDirWarps;
@@ -795,11 +824,15 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     count_launch(IMOP_KERNEL_LITE);
     count_launch(IMOP_KERNEL_LITE_DIRECT);
+    bool words = false;  // word copies, stores by the rows' phases
+    for (int f = 0; f < bl.n_frames; f++) words = words || needs_words(bl.frames[f]);
     switch (bl.fmt) {
-        case FMT_U8: return launch_direct_fmt<FMT_U8>(bl, grid, smem, st);
-        case FMT_U16: return launch_direct_fmt<FMT_U16>(bl, grid, smem, st);
-        case FMT_P10: return launch_direct_fmt<FMT_P10>(bl, grid, smem, st);
-        case FMT_P12: return launch_direct_fmt<FMT_P12>(bl, grid, smem, st);
+        case FMT_U8: return words ? launch_direct_fmt<FMT_U8, true>(bl, grid, smem, st)
+                                  : launch_direct_fmt<FMT_U8, false>(bl, grid, smem, st);
+        case FMT_U16: return words ? launch_direct_fmt<FMT_U16, true>(bl, grid, smem, st)
+                                   : launch_direct_fmt<FMT_U16, false>(bl, grid, smem, st);
+        case FMT_P10: return launch_direct_fmt<FMT_P10, false>(bl, grid, smem, st);
+        case FMT_P12: return launch_direct_fmt<FMT_P12, false>(bl, grid, smem, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -133,6 +133,20 @@ __device__ __forceinline__ void ring_load8(uint32_t main, const uint8_t* row, in
         for (int k = 0; k < 3; k++) ptx::cp_async4(main + 4 * k, in ? (const void*)(q + 4 * k) : any, in ? 4u : 0u);
     }
 }
+// the same for u8 / u16 rows that start on a word but not on the lane's 8- / 16-byte load:
+// word copies, each limited to the `left` bytes of the row from the lane's first sample on (the
+// samples past the row's end read as zeros)
+template <int FMT>
+__device__ __forceinline__ void ring_load8_words(uint32_t main, const uint8_t* row, int lane_byte, int left, bool in,
+                                                 const void* any) {
+    const uint8_t* p = row + lane_byte;
+    constexpr int kWords = FMT == FMT_U8 ? 2 : 4;
+#pragma unroll
+    for (int k = 0; k < kWords; k++) {
+        const int n = in ? min(max(left - 4 * k, 0), 4) : 0;
+        ptx::cp_async4(main + 4 * k, n ? (const void*)(p + 4 * k) : any, (uint32_t)n);
+    }
+}
 template <int FMT>
 __device__ __forceinline__ void ring_load_edge(uint32_t edge, const uint8_t* row, int byte, bool in, const void* any) {
     const uint8_t* q =

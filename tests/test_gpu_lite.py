@@ -5,9 +5,10 @@ kernel), every tone mode, all Bayer patterns, frames from 6x6 up to the 5320x460
 large-frame workload, widths that are not
 multiples of the tile, unaligned input and output pointers, samples above the bit depth's maximum
 (the reference's MSB-aligned read), and batches that mix it with the general kernel.  The
-direct-read variant (aligned frames whose width is a multiple of 8) separately: its launches
-counted, segments continued and bands taken from the back under extreme tuning entries, and
-batches of frames of several widths in one launch."""
+direct-read variant (aligned frames whose rows start on a word) separately: its launches
+counted, widths that are not multiples of 8 with every output phase, segments continued and bands
+taken from the back under extreme tuning entries, and batches of frames of several widths in one
+launch."""
 import dataclasses
 
 import numpy as np
@@ -195,6 +196,12 @@ def _direct_launches():
     return I.lib().imop_kernel_launches(abi.KERNEL_LITE_DIRECT)
 
 
+def _word_rows(pl):
+    """rows that start on a word: the direct-read variant's condition on the width"""
+    return pl.width % 8 == 0 or (not pl.packed and pl.bit_depth > 8 and pl.width % 2 == 0) or \
+        (not pl.packed and pl.bit_depth <= 8 and pl.width % 4 == 0)
+
+
 def _bounded(pl):
     """the light-chain kernel's condition on the samples reaching HQLI: a clamping stage (black
     level, Bayer-order white balance), a format without spare bits, or full 8-bit bytes"""
@@ -212,8 +219,35 @@ def test_direct_matches_oracle(isp, trial):
     out_off = int(rng.integers(0, 16)) if trial % 2 == 1 else 0
     n0 = _direct_launches()
     got = _run(isp, pl, raw, 0, out_off)
-    assert (_direct_launches() > n0) == _bounded(pl), (w, h)
+    assert (_direct_launches() > n0) == (_bounded(pl) and _word_rows(pl)), (w, h)
     assert max_abs(got, ref) == 0, (w, h, pl.bit_depth, pl.packed, pl.stages, pl.stage_order, out_off)
+
+
+# widths that are not multiples of 8: rows that start on a word (u8: multiples of 4, u16: even)
+WORD_SIZES = [(12, 7), (20, 9), (268, 31), (1004, 40), (6, 6), (10, 11), (262, 33), (1006, 758), (2054, 19)]
+
+
+@pytest.mark.parametrize("trial", range(18))
+def test_direct_word_rows_matches_oracle(isp, trial):
+    """the direct-read variant on rows that start on a word: word copies of each lane's samples
+    limited to the row, output rows stored by their 8-byte phase (odd phases, from odd output
+    offsets, through the staging row)"""
+    rng = np.random.default_rng(9900 + trial)
+    w, h = WORD_SIZES[trial % len(WORD_SIZES)]
+    u8 = w % 4 == 0 and trial % 2 == 0
+    bd = int(rng.integers(1, 9)) if u8 else int(rng.integers(9, 13))
+    pl = I.Pipeline(width=w, height=h, bit_depth=bd, packed=False, pattern=int(rng.integers(0, 4)), demosaic=abi.HQLI,
+                    stages=abi.STAGE_BLACK_LEVEL | (abi.STAGE_WHITE_BALANCE if rng.random() < 0.8 else 0),
+                    stage_order=int(rng.integers(0, 2)),
+                    bl_offset=tuple(float(round(v)) for v in rng.uniform(0, ((1 << bd) - 1) * 0.08, 4)),
+                    wb_gain=tuple(float(v) for v in rng.uniform(0.6, 2.4, 3)))
+    raw = _frame(rng, pl)
+    ref, _ = O.pipeline(pl, raw)
+    out_off = int(rng.integers(0, 16))
+    n0 = _direct_launches()
+    got = _run(isp, pl, raw, 0, out_off)
+    assert _direct_launches() > n0, (w, h, bd)
+    assert max_abs(got, ref) == 0, (w, h, bd, pl.stages, pl.stage_order, out_off)
 
 
 def test_direct_unaligned_input_takes_staged_kernel(isp):
