@@ -77,6 +77,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def warm_up(step, warmup, torch, seconds=0.3):
+    """at least max(3, warmup) steps and `seconds` of them, for the short legs: the host-side set-up
+    before a leg leaves the GPU idle long enough for its clocks to drop, and a timed region of a
+    few milliseconds would otherwise begin before they are back"""
+    n, t0 = 0, time.perf_counter()
+    while n < max(3, warmup) or time.perf_counter() - t0 < seconds:
+        step()
+        n += 1
+        if n % 8 == 0:
+            torch.cuda.synchronize()
+    torch.cuda.synchronize()
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -339,8 +352,7 @@ def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind)
         isp.sync_status(sh)
         same = bool(torch.equal(fused, d_out))
         del fused
-        for _ in range(max(3, args.warmup)):
-            isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+        warm_up(lambda: isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh), args.warmup, torch)
         steps = max(1, min(2 * args.steps, 20))  # short steps: more of them for a steadier mean
         # per step, in one stream: the L2 flush, then the frame's graph between two events; the
         # steps are queued without host waits, so the events bracket the frame's device work alone
@@ -393,8 +405,7 @@ def c1_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind,
     isp.sync_status(sh)
     same = bool(torch.equal(fused, d_out))
     del fused
-    for _ in range(max(3, args.warmup)):
-        isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh)
+    warm_up(lambda: isp.batch_submit(desc, flags=abi.BATCH_GRAPH, stream=sh), args.warmup, torch)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
@@ -725,8 +736,10 @@ def main():
     c3 = None
     if not args.no_c3:
         pk, pk_kind = peaks()
-        c3 = c3_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
-        c3["c1"] = c1_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
+        with ClockSampler(local) as clk3:
+            c3 = c3_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
+            c3["c1"] = c1_leg(args, torch, stream, barrier, max_over_ranks, world, pk, pk_kind)
+        c3["clocks"] = clk3.summary()
 
     adjoint = None
     if not args.no_adjoint:
