@@ -6,7 +6,7 @@
 // Demosaic is HQLI or AMAZE (gradient-weighted green at red/blue sites, colour differences with
 // the -1 green sentinel outside [2,w-2)x[2,h-2), border copies from rows / columns 2 and -3).
 //
-// The adjoint recomputes the forward per tile (64 x 16 output pixels; the last tile of a row or
+// The adjoint recomputes the forward per tile (32 x 32 output pixels; the last tile of a row or
 // column absorbs a remainder below 4 so that every border copy source lies inside its tile) into
 // shared planes: u with a 3-pixel apron, green with a 1-pixel apron.  It back-propagates dL/dt
 // of the tile's own pixels into gradient planes of the same extent (shared atomics), then the
@@ -29,7 +29,7 @@ namespace imop {
 namespace {
 
 constexpr int kAdjThreads = 256;
-constexpr int kTX = 64, kTY = 16;
+constexpr int kTX = 32, kTY = 32;  // 64 x 16 measured 1 % slower, 64 x 32 (2 CTAs / SM) 9 %
 constexpr int kUW = kTX + 3 + 6, kUH = kTY + 3 + 6;  // u region: tile (merged) +- 3
 constexpr int kGW = kTX + 3 + 2, kGH = kTY + 3 + 2;  // green region: tile +- 1
 constexpr int kVW = kTX + 3 + 4, kVH = kTY + 3 + 4;  // demosaic-output gradients: tile +- 2
