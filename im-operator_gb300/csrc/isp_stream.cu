@@ -731,21 +731,54 @@ bool choose_segments(BatchLaunch& bl, int warps, int seg_percent, int band_rows)
     }
     if (strips > kSegMax) return false;  // one segment per strip is the fewest
     double per = std::max(1.0, (double)strip_rows / std::max(1, warps) * seg_percent / 100.0);
-    // rounded to the nearest count first; above the cap, longer segments rounded down until the
-    // count fits (it shrinks with every pass and reaches one per strip)
-    for (int pass = 0;; pass++) {
+    // the segment count the spread aims at (one per warp at 100 %), within the cap
+    const long long target = std::min<long long>(kSegMax, std::max<long long>(strips, std::llround(warps * 100.0 / seg_percent)));
+    // each rectangle's count rounded down, then one more for the rectangles of the height with the
+    // largest remainder — all rectangles of that height at once, so their segments stay equal — while
+    // the total stays within the target (at 100 % every segment has its warp and no warp starts with
+    // two); above the cap, longer segments until the count fits (it shrinks with every pass and
+    // reaches one per strip)
+    for (;;) {
         long long items = 0;
+        double rem[kMaxRects];
         for (int r = 0; r < bl.n_rects; r++) {
             TileRect& R = bl.rects[r];
             const double t = R.h / per;
-            R.tiles_y = std::max(1, std::min(R.h, (int)(pass == 0 ? std::lround(t) : std::floor(t))));
-            bl.rect_start[r] = (int)items;
+            R.tiles_y = std::max(1, std::min(R.h, (int)std::floor(t)));
+            rem[r] = R.tiles_y < R.h ? t - R.tiles_y : -1.0;
             items += (long long)R.tiles_x * R.tiles_y;
         }
-        bl.rect_start[bl.n_rects] = bl.n_items = (int)std::min<long long>(items, 1 << 30);
+        for (;;) {
+            int best = -1;
+            long long add_best = 0;
+            for (int r = 0; r < bl.n_rects; r++) {
+                if (rem[r] <= 0.0 || (best >= 0 && rem[r] <= rem[best])) continue;
+                long long add = 0;  // one more segment per strip of every rectangle of this height
+                for (int q = 0; q < bl.n_rects; q++)
+                    if (bl.rects[q].h == bl.rects[r].h && rem[q] > 0.0) add += bl.rects[q].tiles_x;
+                if (items + add <= target) {
+                    best = r;
+                    add_best = add;
+                }
+            }
+            if (best < 0) break;
+            const int h = bl.rects[best].h;
+            for (int q = 0; q < bl.n_rects; q++)
+                if (bl.rects[q].h == h && rem[q] > 0.0) {
+                    bl.rects[q].tiles_y++;
+                    rem[q] = -1.0;
+                }
+            items += add_best;
+        }
         if (items <= kSegMax) break;
         per *= (double)items / kSegMax * 1.01;
     }
+    int items = 0;
+    for (int r = 0; r < bl.n_rects; r++) {
+        bl.rect_start[r] = items;
+        items += bl.rects[r].tiles_x * bl.rects[r].tiles_y;
+    }
+    bl.rect_start[bl.n_rects] = bl.n_items = items;
     // at most segs::kMaxBands bands per segment (the claim word's band count field)
     int longest = 0;
     for (int r = 0; r < bl.n_rects; r++)
