@@ -339,6 +339,10 @@ def c3_leg(args, torch, stream, barrier, max_over_ranks, world, peak, peak_kind)
     import imop_gb300 as I
     from imop_gb300 import abi, workloads
     out = {}
+    # the earlier legs' cached blocks go back to the device first, so this leg's frames are
+    # fresh allocations rather than pieces of blocks split by other legs
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     sh = stream.cuda_stream
     for pl in workloads.c3_pipelines():
