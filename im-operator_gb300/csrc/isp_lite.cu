@@ -458,13 +458,19 @@ constexpr int kDirWarps = 24;
 constexpr int kDirThreads = 32 * kDirWarps;
 constexpr int kDirRing = 4;
 
+// u8 frames (samples of at most 8 bits) use the replicated output tables (lite::hqli_row_t): fewer
+// integer-pipe instructions per pixel, which binds this kernel; for the others (4096-entry tables)
+// the larger tables measured slower
+template <int FMT>
 struct LiteDirectSmem {
-    alignas(16) uint8_t tab[3][4096];
+    lite::LiteTables<FMT == FMT_U8 ? 256 : 1> tab;
     alignas(16) uint8_t out[kDirWarps][LiteWarpSmem::OUT_PITCH];
     uint4 ring[kDirWarps][kDirRing][32];   // the lanes' words of each row in flight
     uint2 ring_e[kDirWarps][kDirRing][32];  // the words of the sample beside the strip (lanes 0, 31)
 };
 static_assert(kDirWarps * LiteWarpSmem::OUT_PITCH >= 4096, "the staging rows hold the tone table at start");
+template <int FMT>
+constexpr size_t direct_smem() { return sizeof(LiteDirectSmem<FMT>); }
 
 // a segment of a strip (isp_segments.cuh): columns [x0, x0 + npx), output rows [s0, s0 + len)
 struct LSeg {
@@ -545,7 +551,8 @@ struct DirectRows {
 // output rows [y0, y0 + bh) of segment U and, while `own` is set, the segment's next bands from
 // the front: input rows y0 - 1 .. (the row below the last output row)
 template <int FMT, bool WORDS>
-__device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t (*tab)[4096], uint8_t* wout,
+__device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const lite::LiteTables<FMT == FMT_U8 ? 256 : 1>& tab,
+                                            uint8_t* wout,
                                             uint4 (*ring)[32], uint2 (*ring_e)[32], const LSeg& U, int y0, int bh,
                                             unsigned long long* own, int lane) {
     const unsigned full = 0xffffffffu;
@@ -627,10 +634,17 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
         if (k >= 2 && yo >= 2 && yo <= H - 3) {
             uint32_t ob[6];
             const int v = (yo & 1) ? v_o : v_e;
-            if (v == 0) lite::hqli_row<0, false>(Ur, Mr, Dr, tab, ob);
-            else if (v == 1) lite::hqli_row<0, true>(Ur, Mr, Dr, tab, ob);
-            else if (v == 2) lite::hqli_row<1, false>(Ur, Mr, Dr, tab, ob);
-            else lite::hqli_row<1, true>(Ur, Mr, Dr, tab, ob);
+            if (FMT == FMT_U8) {
+                if (v == 0) lite::hqli_row_t<0, false>(Ur, Mr, Dr, tab, ob);
+                else if (v == 1) lite::hqli_row_t<0, true>(Ur, Mr, Dr, tab, ob);
+                else if (v == 2) lite::hqli_row_t<1, false>(Ur, Mr, Dr, tab, ob);
+                else lite::hqli_row_t<1, true>(Ur, Mr, Dr, tab, ob);
+            } else {
+                if (v == 0) lite::hqli_row<0, false>(Ur, Mr, Dr, tab.t1, ob);
+                else if (v == 1) lite::hqli_row<0, true>(Ur, Mr, Dr, tab.t1, ob);
+                else if (v == 2) lite::hqli_row<1, false>(Ur, Mr, Dr, tab.t1, ob);
+                else lite::hqli_row<1, true>(Ur, Mr, Dr, tab.t1, ob);
+            }
             // one phase for all rows unless WORDS
             const int phase = WORDS ? (int)((reinterpret_cast<uintptr_t>(out) + (uintptr_t)ooff) & 7) : 0;
             if ((WORDS ? interior && (phase & 1) == 0 : fast) && yo != 2 && yo != H - 3) {
@@ -655,7 +669,7 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
                     }
                 }
             } else {
-                lite_emit_staged(tab, wout, out, W, H, U.x0, U.npx, lane, yo, make_uint4(ob[0], ob[1], ob[2], ob[3]),
+                lite_emit_staged(tab.t1, wout, out, W, H, U.x0, U.npx, lane, yo, make_uint4(ob[0], ob[1], ob[2], ob[3]),
                                  make_uint2(ob[4], ob[5]));
             }
         }
@@ -666,7 +680,7 @@ __device__ __forceinline__ void direct_unit(const BatchLaunch& bl, const uint8_t
 template <int FMT, bool WORDS>
 __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __grid_constant__ BatchLaunch bl) {
     extern __shared__ __align__(16) uint8_t dsm[];
-    auto& sm = *reinterpret_cast<LiteDirectSmem*>(dsm);
+    auto& sm = *reinterpret_cast<LiteDirectSmem<FMT>*>(dsm);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nseg = bl.n_items;
     const int gw = (int)blockIdx.x * kDirWarps + warp;
@@ -683,7 +697,18 @@ __global__ void __launch_bounds__(kDirThreads, 1) lite_direct_kernel(const __gri
 #pragma unroll 1
         for (int c = 0; c < 3; c++) {
             const float g = f0.wb_rgb[c];
-            for (int v = threadIdx.x; v < nv; v += kDirThreads) sm.tab[c][v] = tone_s[wb_rgb ? dev::gain_round(v, g, mv) : v];
+            for (int v = threadIdx.x; v < nv; v += kDirThreads) sm.tab.t1[c][v] = tone_s[wb_rgb ? dev::gain_round(v, g, mv) : v];
+        }
+        __syncthreads();
+        // the replicated tables (u8), four entries per word: t2 words hold t1[2w], t1[2w], t1[2w+1],
+        // t1[2w+1]; t4 words four copies of t1[w] (nv is a power of two, 2 to 256)
+#pragma unroll 1
+        for (int c = 0; c < (FMT == FMT_U8 ? 3 : 0); c++) {
+            uint32_t* t2 = reinterpret_cast<uint32_t*>(sm.tab.t2[c]);
+            uint32_t* t4 = reinterpret_cast<uint32_t*>(sm.tab.t4[c]);
+            for (int w = threadIdx.x; w < nv / 2; w += kDirThreads)
+                t2[w] = (uint32_t)sm.tab.t1[c][2 * w] * 0x0101u | (uint32_t)sm.tab.t1[c][2 * w + 1] * 0x01010000u;
+            for (int w = threadIdx.x; w < nv; w += kDirThreads) t4[w] = (uint32_t)sm.tab.t1[c][w] * 0x01010101u;
         }
     }
     __syncthreads();
@@ -726,8 +751,8 @@ __global__ void lite_seg_init_kernel(const __grid_constant__ BatchLaunch bl) {
 int g_direct_grid[kMaxDev];
 
 template <int FMT, bool WORDS>
-cudaError_t launch_direct_fmt(const BatchLaunch& bl, int grid, size_t smem, cudaStream_t st) {
-    return launch_dependent(lite_direct_kernel<FMT, WORDS>, grid, kDirThreads, smem, st, bl);
+cudaError_t launch_direct_fmt(const BatchLaunch& bl, int grid, cudaStream_t st) {
+    return launch_dependent(lite_direct_kernel<FMT, WORDS>, grid, kDirThreads, direct_smem<FMT>(), st, bl);
 }
 
 int g_lite_grid[kMaxDev];
@@ -785,7 +810,6 @@ static bool needs_words(const FrameParams& fp) {
 }
 
 static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
-    const size_t smem = sizeof(LiteDirectSmem);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -797,10 +821,13 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
             void (*ks[6])(BatchLaunch) = {lite_direct_kernel<FMT_U8, false>,  lite_direct_kernel<FMT_U16, false>,
                                           lite_direct_kernel<FMT_P10, false>, lite_direct_kernel<FMT_P12, false>,
                                           lite_direct_kernel<FMT_U8, true>,   lite_direct_kernel<FMT_U16, true>};
+            const size_t sm[6] = {direct_smem<FMT_U8>(),  direct_smem<FMT_U16>(), direct_smem<FMT_P10>(),
+                                  direct_smem<FMT_P12>(), direct_smem<FMT_U8>(),  direct_smem<FMT_U16>()};
             for (int k = 0; k < 6 && e == cudaSuccess; k++)
-                e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                e = cudaFuncSetAttribute(ks[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm[k]);
+            // every variant holds one CTA per SM (24 warps at 80 registers); the largest sets the grid
             int n = 0, m = 0;
-            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[1], kDirThreads, smem);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[0], kDirThreads, sm[0]);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return e;
             g_direct_grid[dev] = m * (n > 0 ? n : 1);
@@ -827,12 +854,12 @@ static cudaError_t launch_direct(const BatchLaunch& bl_in, cudaStream_t st) {
     bool words = false;  // word copies, stores by the rows' phases
     for (int f = 0; f < bl.n_frames; f++) words = words || needs_words(bl.frames[f]);
     switch (bl.fmt) {
-        case FMT_U8: return words ? launch_direct_fmt<FMT_U8, true>(bl, grid, smem, st)
-                                  : launch_direct_fmt<FMT_U8, false>(bl, grid, smem, st);
-        case FMT_U16: return words ? launch_direct_fmt<FMT_U16, true>(bl, grid, smem, st)
-                                   : launch_direct_fmt<FMT_U16, false>(bl, grid, smem, st);
-        case FMT_P10: return launch_direct_fmt<FMT_P10, false>(bl, grid, smem, st);
-        case FMT_P12: return launch_direct_fmt<FMT_P12, false>(bl, grid, smem, st);
+        case FMT_U8: return words ? launch_direct_fmt<FMT_U8, true>(bl, grid, st)
+                                  : launch_direct_fmt<FMT_U8, false>(bl, grid, st);
+        case FMT_U16: return words ? launch_direct_fmt<FMT_U16, true>(bl, grid, st)
+                                   : launch_direct_fmt<FMT_U16, false>(bl, grid, st);
+        case FMT_P10: return launch_direct_fmt<FMT_P10, false>(bl, grid, st);
+        case FMT_P12: return launch_direct_fmt<FMT_P12, false>(bl, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }

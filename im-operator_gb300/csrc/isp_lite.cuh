@@ -218,6 +218,65 @@ __device__ __forceinline__ void hqli_row(const Row& u, const Row& m, const Row& 
     }
 }
 
+// The output tables replicated per rounding, for HQLI on the packed sums without the shifts:
+// t1[c][v] is the output byte of channel c for sample value v, t2[c][k] = t1[c][k >> 1] and
+// t4[c][k] = t1[c][k >> 2], so a half or quarter sum indexes t2 / t4 directly and the rounding
+// constant (+1 / +2) is part of the load's address.
+template <int N>  // entries of t1 per channel (the samples' range)
+struct LiteTables {
+    alignas(16) uint8_t t1[3][4096];
+    alignas(16) uint8_t t2[3][2 * N];
+    alignas(16) uint8_t t4[3][4 * N];
+};
+
+// hqli_row through the replicated tables: per pair j, S = Hp + Vp holds the red / blue site's four
+// neighbours in the site's half, Dg its diagonals, Hp and Vp the green site's horizontal and
+// vertical pairs in the other half (no half of a sum of four 12-bit samples carries into the
+// other).  Same bytes as hqli_row, with fewer integer-pipe instructions.
+template <int RB, bool RR, int N>
+__device__ __forceinline__ void hqli_row_t(const Row& u, const Row& m, const Row& d, const LiteTables<N>& T,
+                                           uint32_t (&ob)[6]) {
+    uint32_t VN[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) VN[j] = u.P[j] + d.P[j];
+    const uint32_t VL = u.Lw + d.Lw, VR = u.R + d.R;
+    const uint32_t vs[6] = {VL, VN[0], VN[1], VN[2], VN[3], VR};
+    const uint32_t ms[6] = {m.Lw, m.P[0], m.P[1], m.P[2], m.P[3], m.R};
+    uint32_t Ve[5], Me[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+        Ve[j] = __funnelshift_r(vs[j], vs[j + 1], 16);
+        Me[j] = __funnelshift_r(ms[j], ms[j + 1], 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const uint32_t Hp = Me[j] + Me[j + 1], Dg = Ve[j] + Ve[j + 1], Vp = VN[j], Own = m.P[j];
+        const uint32_t S = Hp + Vp;
+        // the site's half (RB 0: low, 1: high) and the green site's half
+        const uint32_t i_q = RB == 0 ? (S & 0xFFFFu) : (S >> 16);    // four neighbours: green at the site
+        const uint32_t i_d = RB == 0 ? (Dg & 0xFFFFu) : (Dg >> 16);  // four diagonals: the other colour
+        const uint32_t i_h = RB == 0 ? (Hp >> 16) : (Hp & 0xFFFFu);  // horizontal pair at the green site
+        const uint32_t i_v = RB == 0 ? (Vp >> 16) : (Vp & 0xFFFFu);  // vertical pair at the green site
+        const uint32_t own = RB == 0 ? (Own & 0xFFFFu) : (Own >> 16);
+        const uint32_t g = RB == 0 ? (Own >> 16) : (Own & 0xFFFFu);
+        // the red / blue site: its own colour, green, the other colour
+        const uint32_t s_r = RR ? T.t1[0][own] : T.t4[0][i_d + 2];
+        const uint32_t s_g = T.t4[1][i_q + 2];
+        const uint32_t s_b = RR ? T.t4[2][i_d + 2] : T.t1[2][own];
+        // the green site: the row's colour horizontally, the other vertically
+        const uint32_t g_r = RR ? T.t2[0][i_h + 1] : T.t2[0][i_v + 1];
+        const uint32_t g_g = T.t1[1][g];
+        const uint32_t g_b = RR ? T.t2[2][i_v + 1] : T.t2[2][i_h + 1];
+        const uint32_t t[6] = {RB == 0 ? s_r : g_r, RB == 0 ? s_g : g_g, RB == 0 ? s_b : g_b,
+                               RB == 0 ? g_r : s_r, RB == 0 ? g_g : s_g, RB == 0 ? g_b : s_b};
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            const int n = 6 * j + c;
+            ob[n >> 2] = (n & 3) == 0 ? t[c] : put_byte(ob[n >> 2], t[c], n & 3);
+        }
+    }
+}
+
 }  // namespace lite
 
 }  // namespace imop
