@@ -494,8 +494,8 @@ long long imop_shim_calls_served(void);
 /* Fused-kernel launches this process enqueued, by kernel: the tile kernel (every chain, and the
  * border rows / columns of streamed frames), the light-chain kernel (HQLI without defect
  * correction or lens shading; both of its variants), the streaming kernel (the interior of AMAZE
- * frames) and, counted again on its own, the light-chain kernel's direct-read variant (aligned
- * frames whose width is a multiple of 8).  A launch recorded into a CUDA graph counts once, when
+ * frames) and, counted again on its own, the light-chain kernel's direct-read variant (frames
+ * whose rows start on a 4-byte word).  A launch recorded into a CUDA graph counts once, when
  * it is recorded. */
 enum { IMOP_KERNEL_TILE = 0, IMOP_KERNEL_LITE = 1, IMOP_KERNEL_STREAM = 2, IMOP_KERNEL_LITE_DIRECT = 3 };
 long long imop_kernel_launches(int kernel);
