@@ -14,9 +14,9 @@
 // holds only the contributions of this tile's outputs; its parameter terms are linear in those
 // contributions, so each tile adds its share and no tile needs another tile's gradients.
 //
-// Parameter gradients: BL, WB, CCM and the loss in registers, tone knots and the lens-shading grid
-// in shared accumulators; each CTA of the persistent grid writes one partial vector and a second
-// kernel adds the partials in CTA order.
+// Parameter gradients: BL, WB, CCM and the loss in registers, tone knots in shared accumulators,
+// the lens-shading grid in the CTA's partial vector; each CTA of the persistent grid writes one
+// partial vector and a second kernel adds the partials in CTA order.
 
 #include <cuda_runtime.h>
 
@@ -39,20 +39,24 @@ constexpr int kMaxParams = 16 + 4 * kAdjMaxGridNodes + 33;
 // local table (wider spans fall back to the CTA table)
 constexpr int kLNX = 4, kLNY = 3, kLocalNodes = 4 * kLNX * kLNY;
 
+// Under 56 KB, so that four CTAs share an SM: the lens-shading grid's sums live in the CTA's
+// partial vector in global memory (a tile adds its local nodes there once), raw samples are kept
+// as u16, and the green plane's adjoint reuses the green plane, which nothing reads once the pixel
+// pass is done.
 struct AdjSmem {
     float th[kMaxParams];
-    float acc_grid[4 * kAdjMaxGridNodes];
     float acc_knots[33];
     // Accumulators with one column per lane index, entry [k][lane]: the lanes of a warp never meet
     // on an address (and hit 32 different banks); only warps with the same lane index can, so the
     // shared atomics here rarely retry.
     float knot_lane[33 * 32];
     float node_lane[kLocalNodes * 32];
-    float raw[kUH * kUW];
     float u[kUH * kUW];
     float gu[kUH * kUW];
-    float G[kGH * kGW];
-    float gG[kGH * kGW];
+    union {
+        float G[kGH * kGW];   // forward and pixel pass
+        float gG[kGH * kGW];  // demosaic adjoint
+    };
     // dL/d(demosaic output) per channel, summed at each output's source pixel (border copies add
     // into their source); zero outside the tile's own pixels
     float gV[3][kVH * kVW];
@@ -61,6 +65,7 @@ struct AdjSmem {
     int row_gy[kUH];
     float row_fy[kUH];
     float red[kAdjThreads / 32][18];
+    uint16_t raw[kUH * kUW];
 };
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
@@ -297,10 +302,12 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
         const int r = wk.r, c = wk.c;
         int x = t.xu + c, y = t.yu + r;
         int i = r * kUW + c;
-        float rv = 0.0f, uv = 0.0f;
+        int ri = 0;
+        float uv = 0.0f;
         if (x >= 0 && x < f.w && y >= 0 && y < f.h) {
             int cc = t.cfa(x, y);
-            rv = (float)adj_raw(f, in, x, y);
+            ri = adj_raw(f, in, x, y);
+            const float rv = (float)ri;
             float b = clampf(rv - sm.th[cc], 0.0f, mvf);
             int gx = sm.col_gx[c], gy = sm.row_gy[r];
             float fx = sm.col_fx[c], fy = sm.row_fy[r];
@@ -310,7 +317,7 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
             float l = clampf(b * gain, 0.0f, mvf);
             uv = clampf(l * wb_of(sm.th, cc), 0.0f, mvf);
         }
-        sm.raw[i] = rv;
+        sm.raw[i] = (uint16_t)ri;  // samples of at most 16 bits
         sm.u[i] = uv;
         if (BACKWARD) sm.gu[i] = 0.0f;
     }
@@ -318,9 +325,10 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
         for (int s = tid; s < 3 * kVH * kVW; s += kAdjThreads) (&sm.gV[0][0])[s] = 0.0f;
     }
     __syncthreads();
-    if (DM == DM_AMAZE || BACKWARD) {
+    if (DM == DM_AMAZE) {
         // by Bayer pairs (frame columns 2k, 2k + 1): every lane takes the pair's red / blue site
-        // (AMAZE's weighted green) and its green site (a copy), so no lane idles beside another
+        // (AMAZE's weighted green) and its green site (a copy), so no lane idles beside another.
+        // (The demosaic adjoint writes every gG of the green region, so gG needs no clearing.)
         const int gw = t.tw + 2, gh = t.th + 2;
         const int xp0 = t.xg & ~1, np = (((t.xg + gw - 1) & ~1) - xp0) / 2 + 1;
         Walk2D wg(tid, np);
@@ -332,10 +340,9 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
                 if (c < 0 || c >= gw) continue;
                 const int j = r * kGW + c;
                 float g = -1.0f;
-                if (DM == DM_AMAZE && x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
+                if (x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
                     g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
                 sm.G[j] = g;
-                if (BACKWARD) sm.gG[j] = 0.0f;
             }
         }
         __syncthreads();
@@ -446,9 +453,10 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
     }
 }
 
-// adjoint of the green plane into u, then of u into the per-pixel parameters
+// adjoint of the green plane into u, then of u into the per-pixel parameters; acc_grid: the
+// CTA's lens-shading sums (global memory, written by this CTA alone)
 template <int DM>
-__device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
+__device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc, float* acc_grid) {
     const AdjFrame& f = *t.f;
     const int tid = threadIdx.x;
     const float mvf = (float)f.mv;
@@ -515,7 +523,7 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
         float gw4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (g != 0.0f && x >= 0 && x < f.w && y >= 0 && y < f.h) {
             int cc = t.cfa(x, y);
-            float rv = sm.raw[i];
+            float rv = (float)sm.raw[i];
             float b = clampf(rv - sm.th[cc], 0.0f, mvf);
             int gx = sm.col_gx[c], gy = sm.row_gy[r];
             float fx = sm.col_fx[c], fy = sm.row_fy[r];
@@ -541,7 +549,7 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
                         for (int k = 0; k < 4; k++) atomicAdd(q + lnode[k], gw4[k]);
                     } else {
 #pragma unroll
-                        for (int k = 0; k < 4; k++) atomicAdd(&sm.acc_grid[n0 + gnode[k]], gw4[k]);
+                        for (int k = 0; k < 4; k++) atomicAdd(acc_grid + n0 + gnode[k], gw4[k]);
                     }
                     float v = rv - sm.th[cc];
                     if (v > 0.0f && v < mvf) {
@@ -554,7 +562,9 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
     }
     __syncthreads();
     if (local) {
-        // local nodes into the CTA table, lanes in order; the table is cleared for the next tile
+        // local nodes into the CTA's sums, lanes in order, one thread per node (the barriers
+        // between tiles order a node's additions; the read goes to L2, where the sums of a
+        // tile without a local table arrive); the table is cleared for the next tile
         for (int e = tid; e < kLocalNodes; e += kAdjThreads) {
             float v = 0.0f;
             for (int l = 0; l < 32; l++) {
@@ -562,7 +572,10 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
                 sm.node_lane[e * 32 + l] = 0.0f;
             }
             const int lx = (e >> 2) % kLNX, ly = (e >> 2) / kLNX;
-            if (v != 0.0f && gx_lo + lx < f.gw && gy_lo + ly < f.gh) sm.acc_grid[((gy_lo + ly) * f.gw + gx_lo + lx) * 4 + (e & 3)] += v;
+            if (v != 0.0f && gx_lo + lx < f.gw && gy_lo + ly < f.gh) {
+                float* q = acc_grid + ((gy_lo + ly) * f.gw + gx_lo + lx) * 4 + (e & 3);
+                *q = __ldcg(q) + v;
+            }
         }
         __syncthreads();
     }
@@ -570,13 +583,16 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc) {
 
 // DM: the launch's demosaic algorithm (every frame of a launch shares the descriptor)
 template <bool BACKWARD, int DM>
-__global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
+__global__ void __launch_bounds__(kAdjThreads, 4) adjoint_kernel(const __grid_constant__ AdjLaunch L) {
     extern __shared__ __align__(16) uint8_t dsm[];
     AdjSmem& sm = *reinterpret_cast<AdjSmem*>(dsm);
     const int tid = threadIdx.x;
+    const int ng = 4 * L.f.gw * L.f.gh;
+    // this CTA's partial vector: BL, WB, CCM, the lens-shading grid (summed in place), the knots
+    float* part = BACKWARD ? L.partials + (size_t)blockIdx.x * (L.n_params + 1) : nullptr;
     for (int k = tid; k < L.n_params; k += kAdjThreads) sm.th[k] = L.theta[k];
     if (BACKWARD) {
-        for (int k = tid; k < 4 * kAdjMaxGridNodes; k += kAdjThreads) sm.acc_grid[k] = 0.0f;
+        for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = 0.0f;
         for (int k = tid; k < 33; k += kAdjThreads) sm.acc_knots[k] = 0.0f;
         for (int k = tid; k < 33 * 32; k += kAdjThreads) sm.knot_lane[k] = 0.0f;
         for (int k = tid; k < kLocalNodes * 32; k += kAdjThreads) sm.node_lane[k] = 0.0f;
@@ -600,7 +616,7 @@ __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_co
         if (BACKWARD) {
             __syncthreads();
             demosaic_gather<DM>(sm, t);
-            tile_back_planes<DM>(sm, t, acc);
+            tile_back_planes<DM>(sm, t, acc, part + 16);
         }
         else __syncthreads();
     }
@@ -622,15 +638,12 @@ __global__ void __launch_bounds__(kAdjThreads, 3) adjoint_kernel(const __grid_co
             if (lane == 0) sm.red[warp][k] = v;
         }
         __syncthreads();
-        float* part = L.partials + (size_t)blockIdx.x * (L.n_params + 1);
         if (tid < 17) {
             float v = 0.0f;
             for (int w = 0; w < kAdjThreads / 32; w++) v += sm.red[w][tid];
             if (tid < 16) part[tid] = v;
             else part[L.n_params] = v;
         }
-        const int ng = 4 * L.f.gw * L.f.gh;
-        for (int k = tid; k < ng; k += kAdjThreads) part[16 + k] = sm.acc_grid[k];
         for (int k = tid; k < 33; k += kAdjThreads) {
             float v = sm.acc_knots[k];
             for (int l = 0; l < 32; l++) v += sm.knot_lane[k * 32 + l];
