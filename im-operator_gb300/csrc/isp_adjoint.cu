@@ -157,17 +157,79 @@ __device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, f
     float g = G[j];
     v[1] = g;
     if (x < 1 || x >= f.w - 1 || y < 1 || y >= f.h - 1) return;
-    if (ar || ab) {
-        float s = (u[i - kUW - 1] - G[j - kGW - 1]) + (u[i - kUW + 1] - G[j - kGW + 1]) +
-                  (u[i + kUW - 1] - G[j + kGW - 1]) + (u[i + kUW + 1] - G[j + kGW + 1]);
-        float other = g + s * 0.25f;
-        if (ar) { v[0] = u[i]; v[2] = other; } else { v[2] = u[i]; v[0] = other; }
+    // colour differences d = u - G at four neighbours, chosen by the site so that the lanes of a
+    // warp (alternating sites along a row) run one path: at a red / blue site the diagonals, the
+    // other channel g + (d1 + d2 + d3 + d4) / 4; at a G site the horizontal pair d1 + d2 and the
+    // vertical pair d3 + d4, the row's colour from the first, the other colour from the second
+    const bool rbs = ar || ab;
+    const int u1 = rbs ? -kUW - 1 : -1, u2 = rbs ? -kUW + 1 : 1, u3 = rbs ? kUW - 1 : -kUW, u4 = rbs ? kUW + 1 : kUW;
+    const int g1 = rbs ? -kGW - 1 : -1, g2 = rbs ? -kGW + 1 : 1, g3 = rbs ? kGW - 1 : -kGW, g4 = rbs ? kGW + 1 : kGW;
+    const float d12 = (u[i + u1] - G[j + g1]) + (u[i + u2] - G[j + g2]);
+    const float d3 = u[i + u3] - G[j + g3], d4 = u[i + u4] - G[j + g4];
+    const float other = g + ((d12 + d3) + d4) * 0.25f;
+    const float d34 = d3 + d4;
+    const float own = u[i];
+    v[0] = ar ? own : (ab ? other : g + (rrow ? d12 : d34) * 0.5f);
+    v[2] = ab ? own : (ar ? other : g + (rrow ? d34 : d12) * 0.5f);
+}
+
+// one pixel (x, y) of the green region, at region row r, column c; rbs: a red / blue site
+template <int DM>
+__device__ __forceinline__ void gather_site(AdjSmem& sm, const TileCtx& t, int x, int y, int r, int c, bool rbs) {
+    const AdjFrame& f = *t.f;
+    const float* V0 = sm.gV[0];
+    const float* V1 = sm.gV[1];
+    const float* V2 = sm.gV[2];
+    const bool hqli = DM == DM_HQLI;
+    const int lo = hqli ? 2 : 1;  // sources with colour interpolation: [lo, w - lo) x [lo, h - lo)
+    const int v = t.vi(x, y), i = t.ui(x, y), j = r * kGW + c;
+    auto in_lo = [&](int xx, int yy) { return xx >= lo && xx < f.w - lo && yy >= lo && yy < f.h - lo; };
+    float gu = 0.0f, gG = 0.0f;
+    if (rbs) {
+        const bool ar = t.at_r(x, y);
+        // own source: the own channel reads u(q); AMAZE's green and other channel read G(q)
+        if (in_lo(x, y)) {
+            gu += ar ? V0[v] : V2[v];
+            if (!hqli) gG += V1[v] + (ar ? V2[v] : V0[v]);
+        } else if (!hqli) {
+            gG += V1[v];
+        }
+        // diagonals: R/B sites of the other colour, whose other channel is this colour
+        const float* Vd = ar ? V0 : V2;  // at a blue diagonal the other channel is red, and back
+        float nb = 0.0f;
+        if (in_lo(x - 1, y - 1)) nb += 0.25f * Vd[v - kVW - 1];
+        if (in_lo(x + 1, y - 1)) nb += 0.25f * Vd[v - kVW + 1];
+        if (in_lo(x - 1, y + 1)) nb += 0.25f * Vd[v + kVW - 1];
+        if (in_lo(x + 1, y + 1)) nb += 0.25f * Vd[v + kVW + 1];
+        // horizontal / vertical neighbours: G sites; a G site in a red row interpolates red
+        // horizontally and blue vertically
+        const bool rrow = (y & 1) == t.po.r_row;  // the neighbours x +- 1 share this row
+        // (the horizontal pair feeds the row's colour, the vertical pair the other row's other
+        // colour: both are this site's colour)
+        const float* Vn = rrow ? V0 : V2;
+        if (in_lo(x - 1, y)) nb += 0.5f * Vn[v - 1];
+        if (in_lo(x + 1, y)) nb += 0.5f * Vn[v + 1];
+        if (in_lo(x, y - 1)) nb += 0.5f * Vn[v - kVW];
+        if (in_lo(x, y + 1)) nb += 0.5f * Vn[v + kVW];
+        gu += nb;
+        if (!hqli) gG -= nb;
     } else {
-        float hz = (u[i - 1] - G[j - 1]) + (u[i + 1] - G[j + 1]);
-        float vt = (u[i - kUW] - G[j - kGW]) + (u[i + kUW] - G[j + kGW]);
-        v[0] = g + (rrow ? hz : vt) * 0.5f;
-        v[2] = g + (rrow ? vt : hz) * 0.5f;
+        // G site: its own green channel
+        if (hqli) {
+            if (in_lo(x, y)) gu += V1[v];
+            // the green of each horizontal / vertical R/B neighbour reads 1/4 of u(q)
+            float nb = 0.0f;
+            if (in_lo(x - 1, y)) nb += V1[v - 1];
+            if (in_lo(x + 1, y)) nb += V1[v + 1];
+            if (in_lo(x, y - 1)) nb += V1[v - kVW];
+            if (in_lo(x, y + 1)) nb += V1[v + kVW];
+            gu += 0.25f * nb;
+        } else {
+            gG += in_lo(x, y) ? V0[v] + V1[v] + V2[v] : V1[v];
+        }
     }
+    sm.gu[i] = gu;
+    if (!hqli) sm.gG[j] = gG;
 }
 
 // Adjoint of the demosaic as a gather: every pixel q of the green region (own pixels +- 1) adds up
@@ -179,67 +241,21 @@ __device__ void demosaic_df(const AdjSmem& sm, const TileCtx& t, int x, int y, f
 //   AMAZE, source p in [1,w-1)^2 (else only green <- G(p)): green <- G(p); R/B site: own <- u(p),
 //     other <- G(p) + 1/4 sum over diagonals d of (u(d) - G(d)); G site: R, B <- G(p) + 1/2 sum of
 //     (u - G) over the horizontal or the vertical pair.
+// By Bayer pairs (frame columns 2k, 2k + 1): every lane takes its pair's red / blue site, then its
+// green site, so the lanes of a warp run the same path.
 template <int DM>
 __device__ void demosaic_gather(AdjSmem& sm, const TileCtx& t) {
-    const AdjFrame& f = *t.f;
     const int gw = t.tw + 2, gh = t.th + 2;
-    const float* V0 = sm.gV[0];
-    const float* V1 = sm.gV[1];
-    const float* V2 = sm.gV[2];
-    const bool hqli = DM == DM_HQLI;
-    const int lo = hqli ? 2 : 1;  // sources with colour interpolation: [lo, w - lo) x [lo, h - lo)
-    Walk2D wk(threadIdx.x, gw);
-    for (int s = threadIdx.x; s < gw * gh; s += kAdjThreads, wk.step()) {
-        const int r = wk.r, c = wk.c;
-        const int x = t.xg + c, y = t.yg + r;
-        const int v = t.vi(x, y), i = t.ui(x, y), j = r * kGW + c;
-        auto in_lo = [&](int xx, int yy) { return xx >= lo && xx < f.w - lo && yy >= lo && yy < f.h - lo; };
-        float gu = 0.0f, gG = 0.0f;
-        if (t.rb(x, y)) {
-            const bool ar = t.at_r(x, y);
-            // own source: the own channel reads u(q); AMAZE's green and other channel read G(q)
-            if (in_lo(x, y)) {
-                gu += ar ? V0[v] : V2[v];
-                if (!hqli) gG += V1[v] + (ar ? V2[v] : V0[v]);
-            } else if (!hqli) {
-                gG += V1[v];
-            }
-            // diagonals: R/B sites of the other colour, whose other channel is this colour
-            const float* Vd = ar ? V0 : V2;  // at a blue diagonal the other channel is red, and back
-            float nb = 0.0f;
-            if (in_lo(x - 1, y - 1)) nb += 0.25f * Vd[v - kVW - 1];
-            if (in_lo(x + 1, y - 1)) nb += 0.25f * Vd[v - kVW + 1];
-            if (in_lo(x - 1, y + 1)) nb += 0.25f * Vd[v + kVW - 1];
-            if (in_lo(x + 1, y + 1)) nb += 0.25f * Vd[v + kVW + 1];
-            // horizontal / vertical neighbours: G sites; a G site in a red row interpolates red
-            // horizontally and blue vertically
-            const bool rrow = (y & 1) == t.po.r_row;  // the neighbours x +- 1 share this row
-            // (the horizontal pair feeds the row's colour, the vertical pair the other row's other
-            // colour: both are this site's colour)
-            const float* Vn = rrow ? V0 : V2;
-            if (in_lo(x - 1, y)) nb += 0.5f * Vn[v - 1];
-            if (in_lo(x + 1, y)) nb += 0.5f * Vn[v + 1];
-            if (in_lo(x, y - 1)) nb += 0.5f * Vn[v - kVW];
-            if (in_lo(x, y + 1)) nb += 0.5f * Vn[v + kVW];
-            gu += nb;
-            if (!hqli) gG -= nb;
-        } else {
-            // G site: its own green channel
-            if (hqli) {
-                if (in_lo(x, y)) gu += V1[v];
-                // the green of each horizontal / vertical R/B neighbour reads 1/4 of u(q)
-                float nb = 0.0f;
-                if (in_lo(x - 1, y)) nb += V1[v - 1];
-                if (in_lo(x + 1, y)) nb += V1[v + 1];
-                if (in_lo(x, y - 1)) nb += V1[v - kVW];
-                if (in_lo(x, y + 1)) nb += V1[v + kVW];
-                gu += 0.25f * nb;
-            } else {
-                gG += in_lo(x, y) ? V0[v] + V1[v] + V2[v] : V1[v];
-            }
-        }
-        sm.gu[i] = gu;
-        if (!hqli) sm.gG[j] = gG;
+    const int xp0 = t.xg & ~1, np = (((t.xg + gw - 1) & ~1) - xp0) / 2 + 1;
+    Walk2D wg(threadIdx.x, np);
+    for (int s = threadIdx.x; s < np * gh; s += kAdjThreads, wg.step()) {
+        const int r = wg.r, y = t.yg + r, xp = xp0 + 2 * wg.c;
+        const int rbh = t.rb(xp, y) ? 0 : 1;  // the red / blue site of the pair
+        int x = xp + rbh, c = x - t.xg;
+        if (c >= 0 && c < gw) gather_site<DM>(sm, t, x, y, r, c, true);
+        x = xp + 1 - rbh;
+        c = x - t.xg;
+        if (c >= 0 && c < gw) gather_site<DM>(sm, t, x, y, r, c, false);
     }
 }
 
@@ -334,16 +350,14 @@ __device__ void tile_forward(AdjSmem& sm, const TileCtx& t, const uint8_t* in) {
         Walk2D wg(tid, np);
         for (int s = tid; s < np * gh; s += kAdjThreads, wg.step()) {
             const int r = wg.r, y = t.yg + r, xp = xp0 + 2 * wg.c;
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int x = xp + h, c = x - t.xg;
-                if (c < 0 || c >= gw) continue;
-                const int j = r * kGW + c;
-                float g = -1.0f;
-                if (x >= 2 && x < f.w - 2 && y >= 2 && y < f.h - 2)
-                    g = t.rb(x, y) ? amaze_df(sm, t, x, y, nullptr) : sm.u[t.ui(x, y)];
-                sm.G[j] = g;
-            }
+            const int rbh = t.rb(xp, y) ? 0 : 1;  // the red / blue site of the pair
+            const bool rows_in = y >= 2 && y < f.h - 2;
+            int x = xp + rbh, c = x - t.xg;
+            if (c >= 0 && c < gw)
+                sm.G[r * kGW + c] = rows_in && x >= 2 && x < f.w - 2 ? amaze_df(sm, t, x, y, nullptr) : -1.0f;
+            x = xp + 1 - rbh;
+            c = x - t.xg;
+            if (c >= 0 && c < gw) sm.G[r * kGW + c] = rows_in && x >= 2 && x < f.w - 2 ? sm.u[t.ui(x, y)] : -1.0f;
         }
         __syncthreads();
     }
