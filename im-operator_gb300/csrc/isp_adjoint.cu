@@ -16,7 +16,7 @@
 //
 // Parameter gradients: BL, WB, CCM and the loss in registers, tone knots in shared accumulators,
 // the lens-shading grid in the CTA's partial vector; each CTA of the persistent grid writes one
-// partial vector and a second kernel adds the partials in CTA order.
+// partial vector and a second kernel adds the partials in a fixed order.
 
 #include <cuda_runtime.h>
 
@@ -36,7 +36,7 @@ constexpr int kVW = kTX + 3 + 4, kVH = kTY + 3 + 4;  // demosaic-output gradient
 constexpr int kMaxParams = 16 + 4 * kAdjMaxGridNodes + 33;
 
 // tile-local lens-shading nodes: a tile's u region spans at most kLNX x kLNY grid nodes in the
-// local table (wider spans fall back to the CTA table)
+// local table (wider spans add straight into the CTA's partial vector)
 constexpr int kLNX = 4, kLNY = 3, kLocalNodes = 4 * kLNX * kLNY;
 
 // Under 56 KB, so that four CTAs share an SM: the lens-shading grid's sums live in the CTA's
@@ -65,6 +65,7 @@ struct AdjSmem {
     int row_gy[kUH];
     float row_fy[kUH];
     float red[kAdjThreads / 32][18];
+    int next_item[2];  // the tile claimed during tile k, in slot k & 1
     uint16_t raw[kUH * kUW];
 };
 
@@ -576,20 +577,19 @@ __device__ void tile_back_planes(AdjSmem& sm, const TileCtx& t, RegAcc& acc, flo
     }
     __syncthreads();
     if (local) {
-        // local nodes into the CTA's sums, lanes in order, one thread per node (the barriers
-        // between tiles order a node's additions; the read goes to L2, where the sums of a
-        // tile without a local table arrive); the table is cleared for the next tile
-        for (int e = tid; e < kLocalNodes; e += kAdjThreads) {
-            float v = 0.0f;
-            for (int l = 0; l < 32; l++) {
-                v += sm.node_lane[e * 32 + l];
-                sm.node_lane[e * 32 + l] = 0.0f;
-            }
+        // local nodes into the CTA's sums: warp w takes nodes w, w + 8, ...; its lanes add the
+        // node's 32 lane columns by a fixed butterfly and lane 0 adds the sum to the partial
+        // vector (a reduction in global memory: the barriers between tiles order a node's
+        // additions).  The table is cleared for the next tile.
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int e = warp; e < kLocalNodes; e += kAdjThreads / 32) {
+            float v = sm.node_lane[e * 32 + lane];
+            sm.node_lane[e * 32 + lane] = 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             const int lx = (e >> 2) % kLNX, ly = (e >> 2) / kLNX;
-            if (v != 0.0f && gx_lo + lx < f.gw && gy_lo + ly < f.gh) {
-                float* q = acc_grid + ((gy_lo + ly) * f.gw + gx_lo + lx) * 4 + (e & 3);
-                *q = __ldcg(q) + v;
-            }
+            if (lane == 0 && v != 0.0f && gx_lo + lx < f.gw && gy_lo + ly < f.gh)
+                atomicAdd(acc_grid + ((gy_lo + ly) * f.gw + gx_lo + lx) * 4 + (e & 3), v);
         }
         __syncthreads();
     }
@@ -620,7 +620,15 @@ __global__ void __launch_bounds__(kAdjThreads, 4) adjoint_kernel(const __grid_co
 #pragma unroll
     for (int k = 0; k < 9; k++) acc.ccm[k] = 0.0f;
     acc.loss = 0.0f;
-    for (int item = blockIdx.x; item < L.n_items; item += gridDim.x) {
+    // Tiles: the first wave by CTA index, then (backward) claimed from the launch's counter one
+    // tile ahead, so that CTAs given costlier tiles (frame borders, wider last columns) take fewer
+    // of them; the render launch keeps the fixed stride.  Thread 0 writes slot k & 1 at the start
+    // of tile k and every thread reads it after the tile's barriers; the slot is written again at
+    // tile k + 2, after tile k + 1's barriers.
+    unsigned* const counter = BACKWARD ? L.tile_counter : nullptr;
+    int item = blockIdx.x;
+    for (int k = 0; item < L.n_items; k++) {
+        if (counter && tid == 0) sm.next_item[k & 1] = (int)gridDim.x + (int)atomicAdd(counter, 1u);
         int fi;
         TileCtx t;
         tile_of(L, item, fi, t);
@@ -633,6 +641,7 @@ __global__ void __launch_bounds__(kAdjThreads, 4) adjoint_kernel(const __grid_co
             tile_back_planes<DM>(sm, t, acc, part + 16);
         }
         else __syncthreads();
+        item = counter ? sm.next_item[k & 1] : item + (int)gridDim.x;
     }
     if constexpr (BACKWARD) {
         // block reduction of the register accumulators, warps in order
@@ -666,14 +675,25 @@ __global__ void __launch_bounds__(kAdjThreads, 4) adjoint_kernel(const __grid_co
     }
 }
 
-// grad[k] = sum over CTAs of partial[cta][k], in CTA order; loss likewise
-__global__ void reduce_partials_kernel(const float* partials, int n_parts, int n_params, float* grad, float* loss) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k > n_params) return;
+// grad[k] = sum over CTAs of partial[cta][k]; loss likewise (index n_params).  32 parameters per
+// block of 32 x kRedRows threads: row j adds CTAs j, j + kRedRows, ... in order (coalesced over
+// the parameters), then the rows are added in order, so the sum is the same in every run.
+constexpr int kRedRows = 16;
+__global__ void __launch_bounds__(32 * kRedRows) reduce_partials_kernel(const float* partials, int n_parts,
+                                                                       int n_params, float* grad, float* loss) {
+    __shared__ float rows[kRedRows][33];
+    const int k = blockIdx.x * 32 + threadIdx.x;
     float s = 0.0f;
-    for (int c = 0; c < n_parts; c++) s += partials[(size_t)c * (n_params + 1) + k];
-    if (k < n_params) grad[k] = s;
-    else if (loss) *loss = s;
+    if (k <= n_params)
+        for (int c = threadIdx.y; c < n_parts; c += kRedRows) s += partials[(size_t)c * (n_params + 1) + k];
+    rows[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && k <= n_params) {
+        float t = 0.0f;
+        for (int j = 0; j < kRedRows; j++) t += rows[j][threadIdx.x];
+        if (k < n_params) grad[k] = t;
+        else if (loss) *loss = t;
+    }
 }
 
 }  // namespace
@@ -718,8 +738,8 @@ cudaError_t launch_adjoint(const AdjLaunch& L, bool backward, int grid, float* d
             adjoint_kernel<true, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
         else
             adjoint_kernel<true, DM_AMAZE><<<grid, kAdjThreads, smem, st>>>(L);
-        reduce_partials_kernel<<<(L.n_params + 1 + 255) / 256, 256, 0, st>>>(L.partials, grid, L.n_params, d_grad,
-                                                                            d_loss);
+        reduce_partials_kernel<<<(L.n_params + 1 + 31) / 32, dim3(32, kRedRows), 0, st>>>(L.partials, grid,
+                                                                                        L.n_params, d_grad, d_loss);
     } else if (hqli) {
         adjoint_kernel<false, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
     } else {

@@ -27,6 +27,7 @@ struct AdjLaunch {
     int mode;           // 0 target, 1 upstream gradient
     float* rgb_out;     // forward output
     float* partials;    // per CTA: n_params + 1 (loss last)
+    unsigned* tile_counter;  // backward: tiles claimed past the first wave (zero at launch)
 };
 
 int adj_tile_grid(int w, int h, int& tx, int& ty);

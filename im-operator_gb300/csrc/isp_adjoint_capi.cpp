@@ -50,6 +50,7 @@ int make_launch(const ImopAdjointDesc* d, AdjLaunch& L) {
     L.ref = nullptr;
     L.rgb_out = nullptr;
     L.partials = nullptr;
+    L.tile_counter = nullptr;
     return IMOP_OK;
 }
 
@@ -97,13 +98,18 @@ extern "C" int imop_isp_backward_device(imop_isp_t ctx, const ImopAdjointDesc* d
     cudaError_t e = adj_grid_limit(limit);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint set-up");
     const int grid = std::min(limit, L.n_items);
-    const size_t need = (size_t)grid * (L.n_params + 1) * sizeof(float);
+    // the partial vectors, then the tile counter
+    const size_t part_bytes = (size_t)grid * (L.n_params + 1) * sizeof(float);
+    const size_t need = part_bytes + sizeof(unsigned);
     if (ctx->adj_partials.size < need) {
         // the buffer may be read by an adjoint still running on another stream
         if ((e = cudaDeviceSynchronize())) return cuda_fail(e, "sync before partials growth");
         if ((e = ctx->adj_partials.ensure(need))) return cuda_fail(e, "alloc partials");
     }
     L.partials = static_cast<float*>(ctx->adj_partials.ptr);
+    L.tile_counter = reinterpret_cast<unsigned*>(static_cast<uint8_t*>(ctx->adj_partials.ptr) + part_bytes);
+    if ((e = cudaMemsetAsync(L.tile_counter, 0, sizeof(unsigned), (cudaStream_t)stream)))
+        return cuda_fail(e, "tile counter reset");
     if ((e = launch_adjoint(L, true, grid, d_grad, d_loss, (cudaStream_t)stream))) return cuda_fail(e, "adjoint launch");
     return IMOP_OK;
 }
