@@ -402,8 +402,8 @@ __device__ void tile_pixels(AdjSmem& sm, const TileCtx& t, int fi, const AdjLaun
             c = t.tw - 1;
         }
         int x = t.x0 + c, y = t.y0 + r;
-        int sx, sy;
-        dev::border_source(x, y, f.w, f.h, f.border_mode, sx, sy);
+        int sx = x, sy = y;  // the source is the pixel itself away from the frame's border
+        if (border_tile) dev::border_source(x, y, f.w, f.h, f.border_mode, sx, sy);
         float v[3], rgb[3], pre[3], o[3], tt[3], fr[3];
         int idx[3];
         demosaic_df<DM>(sm, t, sx, sy, v);
@@ -644,6 +644,19 @@ __global__ void __launch_bounds__(kAdjThreads, 4) adjoint_kernel(const __grid_co
         item = counter ? sm.next_item[k & 1] : item + (int)gridDim.x;
     }
     if constexpr (BACKWARD) {
+        // the partial reduction may start once every CTA is here (it waits for this grid's end)
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+        // the last CTA to finish (counter[1]) clears both words for the next launch: every other
+        // CTA made its last claim before counting itself
+        if (tid == 0) {
+            __threadfence();
+            if (atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+                counter[0] = 0u;
+                counter[1] = 0u;
+            }
+        }
+    }
+    if constexpr (BACKWARD) {
         // block reduction of the register accumulators, warps in order
         float vals[17];
 #pragma unroll
@@ -682,6 +695,7 @@ constexpr int kRedRows = 16;
 __global__ void __launch_bounds__(32 * kRedRows) reduce_partials_kernel(const float* partials, int n_parts,
                                                                        int n_params, float* grad, float* loss) {
     __shared__ float rows[kRedRows][33];
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // launched as the adjoint's dependent
     const int k = blockIdx.x * 32 + threadIdx.x;
     float s = 0.0f;
     if (k <= n_params)
@@ -738,8 +752,18 @@ cudaError_t launch_adjoint(const AdjLaunch& L, bool backward, int grid, float* d
             adjoint_kernel<true, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
         else
             adjoint_kernel<true, DM_AMAZE><<<grid, kAdjThreads, smem, st>>>(L);
-        reduce_partials_kernel<<<(L.n_params + 1 + 31) / 32, dim3(32, kRedRows), 0, st>>>(L.partials, grid,
-                                                                                        L.n_params, d_grad, d_loss);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((L.n_params + 1 + 31) / 32);
+        cfg.blockDim = dim3(32, kRedRows);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const float* parts = L.partials;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, reduce_partials_kernel, parts, grid, L.n_params, d_grad, d_loss);
+        if (e != cudaSuccess) return e;
     } else if (hqli) {
         adjoint_kernel<false, DM_HQLI><<<grid, kAdjThreads, smem, st>>>(L);
     } else {

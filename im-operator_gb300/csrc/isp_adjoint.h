@@ -27,7 +27,8 @@ struct AdjLaunch {
     int mode;           // 0 target, 1 upstream gradient
     float* rgb_out;     // forward output
     float* partials;    // per CTA: n_params + 1 (loss last)
-    unsigned* tile_counter;  // backward: tiles claimed past the first wave (zero at launch)
+    unsigned* tile_counter;  // backward: [0] tiles claimed past the first wave, [1] CTAs done; zero at
+                             // launch, cleared again by the launch's last CTA
 };
 
 int adj_tile_grid(int w, int h, int& tx, int& ty);

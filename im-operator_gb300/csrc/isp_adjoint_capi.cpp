@@ -98,18 +98,17 @@ extern "C" int imop_isp_backward_device(imop_isp_t ctx, const ImopAdjointDesc* d
     cudaError_t e = adj_grid_limit(limit);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint set-up");
     const int grid = std::min(limit, L.n_items);
-    // the partial vectors, then the tile counter
-    const size_t part_bytes = (size_t)grid * (L.n_params + 1) * sizeof(float);
-    const size_t need = part_bytes + sizeof(unsigned);
+    // the tile counter's two words (16 bytes kept), then the partial vectors; the counter is zeroed
+    // when the buffer is made and each launch's last CTA clears it again
+    const size_t need = 16 + (size_t)grid * (L.n_params + 1) * sizeof(float);
     if (ctx->adj_partials.size < need) {
         // the buffer may be read by an adjoint still running on another stream
         if ((e = cudaDeviceSynchronize())) return cuda_fail(e, "sync before partials growth");
         if ((e = ctx->adj_partials.ensure(need))) return cuda_fail(e, "alloc partials");
+        if ((e = cudaMemset(ctx->adj_partials.ptr, 0, 16))) return cuda_fail(e, "tile counter");
     }
-    L.partials = static_cast<float*>(ctx->adj_partials.ptr);
-    L.tile_counter = reinterpret_cast<unsigned*>(static_cast<uint8_t*>(ctx->adj_partials.ptr) + part_bytes);
-    if ((e = cudaMemsetAsync(L.tile_counter, 0, sizeof(unsigned), (cudaStream_t)stream)))
-        return cuda_fail(e, "tile counter reset");
+    L.tile_counter = static_cast<unsigned*>(ctx->adj_partials.ptr);
+    L.partials = reinterpret_cast<float*>(static_cast<uint8_t*>(ctx->adj_partials.ptr) + 16);
     if ((e = launch_adjoint(L, true, grid, d_grad, d_loss, (cudaStream_t)stream))) return cuda_fail(e, "adjoint launch");
     return IMOP_OK;
 }
