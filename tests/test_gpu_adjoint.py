@@ -123,6 +123,25 @@ def test_c5_gradient_vs_finite_differences(isp, c5):
     assert np.max(rel) <= TOL, f"parameter {idx[int(np.argmax(rel))]}: {g[idx][np.argmax(rel)]} vs {fd[np.argmax(rel)]}"
 
 
+def test_repeated_launches_of_different_sizes(isp, c5):
+    """Tiles past the first wave of a launch are claimed from a counter that the launch's last CTA
+    clears: C5 launches (more tiles than CTAs) alternating with a 16-tile launch give the
+    gradients of their first runs every time (to the rounding of the shared-memory sums)."""
+    d, _, th0, raw, target = c5
+    ds, raws, ths, tgts, _ = _setup(CASES[2], 5)
+    big = (d, torch.from_numpy(th0).cuda(), torch.from_numpy(raw).cuda(), torch.from_numpy(target).cuda())
+    small = (ds, torch.tensor(ths, dtype=torch.float32, device="cuda"), torch.from_numpy(raws).cuda(),
+             torch.from_numpy(tgts).cuda())
+
+    def grads():
+        return [A.backward(isp, *a, abi.ADJ_TARGET)[1].cpu().numpy() for a in (big, small)]
+
+    first = grads()
+    for _ in range(3):
+        for g, f in zip(grads(), first):
+            assert np.allclose(g, f, rtol=1e-5, atol=1e-6 * float(np.abs(f).max()))
+
+
 def test_autograd_wrappers(isp):
     d, raw, th, target, rng = _setup(CASES[2], 4)
     theta = torch.tensor(th, dtype=torch.float32, device="cuda", requires_grad=True)
