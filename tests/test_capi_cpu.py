@@ -70,6 +70,43 @@ def test_raw_to_jpeg_argument_checks_without_device():
     assert f(fake, fake, None, 2) == abi.ERR_NULL_INPUT
 
 
+def test_adjoint_argument_checks_without_device():
+    """The adjoint's host checks (context, descriptor, pointers, mode) come before any device
+    work, with the library's status codes; the parameter vector holds 16 + 4 x grid nodes + 33."""
+    L = I.lib()
+    d = abi.AdjointDesc(1006, 758, 12, 0, abi.RGGB, abi.AMAZE, 17, 13, 16)
+    assert L.imop_adjoint_param_count(C.byref(d)) == 933
+    assert L.imop_adjoint_param_count(None) == 0
+    fake = C.c_void_p(1)  # never dereferenced: the checks fail first
+
+    def backward(desc, ctx=fake, ptr=fake, mode=abi.ADJ_TARGET):
+        return L.imop_isp_backward_device(ctx, None if desc is None else C.byref(desc), ptr, ptr, ptr, mode, None,
+                                          ptr, None)
+
+    def render(desc, ctx=fake, ptr=fake):
+        return L.imop_isp_render_device(ctx, None if desc is None else C.byref(desc), ptr, ptr, ptr, None)
+
+    for call in (backward, render):
+        assert call(d, ctx=None) == abi.ERR_NULL_INPUT
+        assert call(None) == abi.ERR_NULL_INPUT
+        assert call(d, ptr=None) == abi.ERR_NULL_INPUT
+        for field, value, code in [("width", 0, abi.ERR_INVALID_DIMENSIONS),
+                                   ("bit_depth", 17, abi.ERR_INVALID_BIT_DEPTH),
+                                   ("pattern", 4, abi.ERR_INVALID_PATTERN),
+                                   ("height", 5, abi.ERR_IMAGE_TOO_SMALL),
+                                   ("demosaic", abi.MG, abi.ERR_UNSUPPORTED),
+                                   ("grid_w", 1, abi.ERR_INVALID_ARGUMENT),
+                                   ("grid_h", 33, abi.ERR_INVALID_ARGUMENT),
+                                   ("n_frames", 0, abi.ERR_INVALID_ARGUMENT)]:
+            bad = abi.AdjointDesc(*(getattr(d, n) for n, _ in abi.AdjointDesc._fields_))
+            setattr(bad, field, value)
+            assert call(bad) == code, (call.__name__, field)
+        big = abi.AdjointDesc(*(getattr(d, n) for n, _ in abi.AdjointDesc._fields_))
+        big.grid_w, big.grid_h = 17, 17  # 289 nodes: more than the 256 the kernels hold
+        assert call(big) == abi.ERR_INVALID_ARGUMENT
+    assert backward(d, mode=2) == abi.ERR_INVALID_ARGUMENT
+
+
 def test_params_default_and_sizes():
     L = I.lib()
     p = abi.IspParams()
